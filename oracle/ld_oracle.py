@@ -1,0 +1,688 @@
+"""CPU oracle for the two-locus LD path -- TEST INFRASTRUCTURE ONLY.
+
+This module restates, in plain numpy, the arithmetic of the reference
+pg_gpu LD path (kr-colab/pg_gpu).  It is the checker the CUDA library is
+compared against; nothing in the shipped package imports it.  Only
+``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` leg of
+``bench.py`` may use it.
+
+Every statistic is formed as an exact integer numerator over an exact
+integer denominator (numpy int64) and divided once in float64, which is
+exactly what the reference's float64 kernels compute whenever their
+intermediate terms stay below 2**53 (they do for the sample sizes here).
+
+Parity is pinned by ``tests/test_oracle_golden.py`` against fixtures that
+``tests/golden/make_golden.py`` produced by running the reference's own code,
+and against the moments result shipped with the reference's tests.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+I64 = np.int64
+
+
+# ---------------------------------------------------------------------------
+# pair enumeration  (ld_pipeline.py:57-122)
+# ---------------------------------------------------------------------------
+def pairs_within_distance(positions, max_dist):
+    """All (i<j) with pos[j]-pos[i] <= max_dist, i-major then j ascending.
+
+    Same pair set and order as concatenating every chunk yielded by
+    ``ld_pipeline.iter_pairs_within_distance`` (ld_pipeline.py:57-122).
+    """
+    pos = np.asarray(positions)
+    n = len(pos)
+    if n < 2:
+        return np.zeros(0, np.int32), np.zeros(0, np.int32)
+    jmax = np.searchsorted(pos, pos + max_dist, side="right")
+    per = np.maximum(0, jmax - np.arange(n) - 1)
+    total = int(per.sum())
+    idx_i = np.repeat(np.arange(n, dtype=np.int64), per)
+    start = np.cumsum(per) - per
+    within = np.arange(total, dtype=np.int64) - np.repeat(start, per)
+    idx_j = idx_i + 1 + within
+    return idx_i.astype(np.int32), idx_j.astype(np.int32)
+
+
+def chunk_bounds(positions, max_dist, chunk_size):
+    """Anchor-block chunking of the pair list (ld_pipeline.py:94-122).
+
+    Returns a list of (v_lo, v_hi, n_pairs) for the non-empty chunks: chunk k
+    holds every pair whose first index lies in [v_lo, v_hi).
+    """
+    pos = np.asarray(positions)
+    n = len(pos)
+    if n < 2:
+        return []
+    jmax = np.searchsorted(pos, pos + max_dist, side="right")
+    per = np.maximum(0, jmax - np.arange(n) - 1)
+    cum = np.cumsum(per)
+    total = int(cum[-1])
+    if total == 0:
+        return []
+    chunk_size = max(1, int(chunk_size))
+    n_chunks = (total + chunk_size - 1) // chunk_size
+    targets = np.minimum(np.arange(1, n_chunks + 1, dtype=np.int64) * chunk_size, total)
+    v_his = np.minimum(np.searchsorted(cum, targets, side="left") + 1, n)
+    out = []
+    v_lo = 0
+    for v_hi in v_his:
+        v_hi = int(v_hi)
+        if v_hi <= v_lo:
+            continue
+        npairs = int(per[v_lo:v_hi].sum())
+        if npairs:
+            out.append((v_lo, v_hi, npairs))
+        v_lo = v_hi
+    return out
+
+
+# ---------------------------------------------------------------------------
+# joint counts  (ld_pipeline.py:130-175, 183-263)
+# ---------------------------------------------------------------------------
+def counts_for_pairs(hap, idx_i, idx_j, rows=None):
+    """[n11, n10, n01, n00] int32 per pair, plus n_valid (or None).
+
+    ``==1`` / ``==0`` allele semantics and ``>=0`` validity; n_valid is None
+    unless the (row-subset) matrix holds a -1 somewhere (ld_pipeline.py:158).
+    """
+    h = np.asarray(hap)
+    if rows is not None:
+        h = h[np.asarray(rows), :]
+    hi = h[:, idx_i]
+    hj = h[:, idx_j]
+    has_missing = bool(np.any(h == -1))
+    v = (hi >= 0) & (hj >= 0)
+    c = np.stack([
+        np.sum((hi == 1) & (hj == 1) & v, axis=0, dtype=np.int32),
+        np.sum((hi == 1) & (hj == 0) & v, axis=0, dtype=np.int32),
+        np.sum((hi == 0) & (hj == 1) & v, axis=0, dtype=np.int32),
+        np.sum((hi == 0) & (hj == 0) & v, axis=0, dtype=np.int32),
+    ], axis=1)
+    nv = np.sum(v, axis=0, dtype=np.int32) if has_missing else None
+    return c, nv
+
+
+def genotype_counts_for_pairs(geno, idx_i, idx_j, rows=None):
+    """9-way counts ordered n00,n01,n02,n10,...,n22 plus n_valid (or None).
+
+    Follows the reference counting kernel (ld_pipeline.py:183-217): an
+    individual contributes when both dosages are >= 0; n_valid is returned
+    only when the matrix holds a negative entry (ld_pipeline.py:253).
+    """
+    g = np.asarray(geno).astype(np.int8)
+    if rows is not None:
+        g = g[np.asarray(rows), :]
+    gi = g[:, idx_i].astype(np.int32)
+    gj = g[:, idx_j].astype(np.int32)
+    ok = (gi >= 0) & (gj >= 0)
+    combo = gi * 3 + gj
+    out = np.zeros((len(idx_i), 9), np.int32)
+    for k in range(9):
+        out[:, k] = np.sum(ok & (combo == k), axis=0)
+    nv = np.sum(ok, axis=0, dtype=np.int32)
+    return out, (nv if bool(np.any(g < 0)) else None)
+
+
+# ---------------------------------------------------------------------------
+# per-population integer features
+# ---------------------------------------------------------------------------
+class Pop:
+    """Integer per-pair features of one population (cf. ld_pipeline.py:465-482)."""
+
+    def __init__(self, c4, n):
+        c = np.asarray(c4).astype(I64)
+        self.c1, self.c2, self.c3, self.c4 = c[:, 0], c[:, 1], c[:, 2], c[:, 3]
+        self.n = np.asarray(n).astype(I64)
+        self.pA = self.c1 + self.c2
+        self.qA = self.c3 + self.c4
+        self.pB = self.c1 + self.c3
+        self.qB = self.c2 + self.c4
+        # x = c1*c4 - c2*c3 is minus the reference's D (ld_pipeline.py:478)
+        self.x = self.c1 * self.c4 - self.c2 * self.c3
+
+
+def _q(num, den):
+    """num/den in float64 where den > 0, else 0 (the kernels' convention)."""
+    num = np.asarray(num)
+    den = np.asarray(den)
+    out = np.zeros(np.broadcast(num, den).shape, np.float64)
+    ok = den > 0
+    out[ok] = num[ok].astype(np.float64) / den[ok].astype(np.float64)
+    return out
+
+
+def _d4(n):
+    return n * (n - 1) * (n - 2) * (n - 3)
+
+
+# --- DD (ld_statistics.py:1116-1169, haplotype_kernels.py:69-89) ----------
+def dd_ii(p):
+    c1, c2, c3, c4 = p.c1, p.c2, p.c3, p.c4
+    num = c1 * (c1 - 1) * c4 * (c4 - 1) + c2 * (c2 - 1) * c3 * (c3 - 1) - 2 * c1 * c2 * c3 * c4
+    return num, _d4(p.n)
+
+
+def dd_ij(a, b):
+    return a.x * b.x, a.n * (a.n - 1) * b.n * (b.n - 1)
+
+
+# --- Dz (ld_statistics.py:1172-1272, haplotype_kernels.py:95-160) ---------
+def dz_iii(p):
+    c1, c2, c3, c4 = p.c1, p.c2, p.c3, p.c4
+    num = (p.x * (p.qA - p.pA) * (p.qB - p.pB) + p.x * ((c2 + c3) - (c1 + c4))
+           + 2 * (c2 * c3 + c1 * c4))
+    return num, _d4(p.n)
+
+
+def dz_iij(i, j):
+    return (i.qA - i.pA) * i.x * (j.qB - j.pB), j.n * i.n * (i.n - 1) * (i.n - 2)
+
+
+def dz_iji(i, j):
+    return (i.qB - i.pB) * i.x * (j.qA - j.pA), j.n * i.n * (i.n - 1) * (i.n - 2)
+
+
+def dz_ijj(i, j):
+    num = i.x * ((j.c2 + j.c3) - (j.c1 + j.c4)) + i.x * (j.qB - j.pB) * (j.qA - j.pA)
+    return num, i.n * (i.n - 1) * j.n * (j.n - 1)
+
+
+def dz_ijk(i, j, k):
+    return i.x * (j.pA - j.qA) * (k.pB - k.qB), i.n * (i.n - 1) * j.n * k.n
+
+
+# --- pi2 (ld_statistics.py:1275-1617, haplotype_kernels.py:167-304) -------
+def pi2_iiii(p):
+    c1, c2, c3, c4 = p.c1, p.c2, p.c3, p.c4
+    num = (p.pA * p.pB * p.qB * p.qA - c1 * c4 * (-1 + c1 + 3 * c2 + 3 * c3 + c4)
+           - c2 * c3 * (-1 + 3 * c1 + c2 + c3 + 3 * c4))
+    return num, _d4(p.n)
+
+
+def pi2_triple(t, s):
+    """pi2 with population t three times and s once; value = num / den."""
+    num2 = (t.pA * t.qA * (t.qB * s.pB + t.pB * s.qB - 2 * s.qB)
+            + (t.pA * t.c4 + t.c2 * t.qA) * (s.qB - s.pB))
+    return num2, 2 * s.n * t.n * (t.n - 1) * (t.n - 2)
+
+
+def pi2_iikk(i, k):
+    """Kernel form (haplotype_kernels.py:180-190): not symmetrised."""
+    return i.pA * i.qA * k.pB * k.qB, i.n * (i.n - 1) * k.n * (k.n - 1)
+
+
+def pi2_iikk_sym(i, k):
+    """ld_statistics form (ld_statistics.py:1327-1339): symmetrised."""
+    num2 = i.pA * i.qA * k.pB * k.qB + k.pA * k.qA * i.pB * i.qB
+    return num2, 2 * i.n * (i.n - 1) * k.n * (k.n - 1)
+
+
+def pi2_iikl(i, k, l):
+    num2 = i.pA * i.qA * (k.pB * l.qB + k.qB * l.pB)
+    return num2, 2 * i.n * (i.n - 1) * k.n * l.n
+
+
+def pi2_ijkk(i, j, k):
+    num2 = k.pB * k.qB * (i.pA * j.qA + i.qA * j.pA)
+    return num2, 2 * k.n * (k.n - 1) * i.n * j.n
+
+
+def pi2_ijij(a, b):
+    a1, a2, a3, a4 = a.c1, a.c2, a.c3, a.c4
+    b1, b2, b3, b4 = b.c1, b.c2, b.c3, b.c4
+    quart = (a.qB * a.qA * b.pA * b.pB + a.pB * a.qA * b.pA * b.qB
+             + a.pA * a.qB * b.pB * b.qA + a.pA * a.pB * b.qB * b.qA)
+    # cubic correction, grouped by the count of b it multiplies
+    cub = (b1 * (a4 - a2 * a3 - a2 * a4 - a3 * a4 - a4 * a4 - a4 * b1)
+           + b2 * (a3 - a1 * a3 - a3 * a3 - a1 * a4 - a3 * a4 - a3 * b1 - a4 * b1 - a3 * b2)
+           + b3 * (a2 - a1 * a2 - a2 * a2 - a1 * a4 - a2 * a4 - a2 * b1 - a4 * b1
+                   - a1 * b2 - a4 * b2 - a2 * b3)
+           + b4 * (a1 - a1 * a1 - a1 * a2 - a1 * a3 - a2 * a3 - a2 * b1 - a3 * b1
+                   - a1 * b2 - a3 * b2 - a1 * b3 - a2 * b3 - a1 * b4))
+    return quart + cub, 4 * a.n * (a.n - 1) * b.n * (b.n - 1)
+
+
+def pi2_shared(s, a, b):
+    """s appears in both pairs, a in the first, b in the second (ld_statistics.py:1519-1589)."""
+    s1, s2, s3, s4 = s.c1, s.c2, s.c3, s.c4
+    a1, a2 = a.c1, a.c2
+    b1, b2, b3, b4 = b.c1, b.c2, b.c3, b.c4
+    inner = (s3 - 1) * b1 + s3 * b2 - b3 + s3 * b3 + s3 * b4 + s1 * b.qB
+    num4 = (s4 * s4 * a.pA * b.pB + s2 * s2 * a.qA * b.pB
+            + (s1 + s3 - 1) * (s3 * a.pA + s1 * a.qA) * b.qB
+            + s4 * (s1 * a.qA * b.pB + (a1 + a2) * inner)
+            + s2 * (s4 * (a.pA + a.qA) * b.pB + s3 * (a.pA * b.pB + a.qA * b.qB)
+                    + a.qA * ((s1 - 1) * b1 - b3 + s1 * (b2 + b3 + b4))))
+    return num4, 4 * s.n * (s.n - 1) * a.n * b.n
+
+
+def pi2_alldiff(i, j, k, l):
+    num4 = (i.qA * j.pA + i.pA * j.qA) * (k.qB * l.pB + k.pB * l.qB)
+    return num4, 4 * i.n * j.n * k.n * l.n
+
+
+# ---------------------------------------------------------------------------
+# public-API dispatch  (ld_statistics.py:13-129, 1082-1113)
+# ---------------------------------------------------------------------------
+def _pop_n(counts, n_valid, p):
+    """Valid n of population p, following _get_pop_data (ld_statistics.py:1082-1113)."""
+    c = np.asarray(counts)[:, 4 * p:4 * p + 4].astype(I64)
+    if n_valid is None:
+        return c.sum(axis=1)
+    if isinstance(n_valid, tuple):
+        if p < len(n_valid) and n_valid[p] is not None:
+            return np.asarray(n_valid[p]).astype(I64)
+        return c.sum(axis=1)
+    nv = np.asarray(n_valid)
+    if nv.ndim == 2:
+        return nv[:, p].astype(I64)
+    return nv.astype(I64)
+
+
+def _pop(counts, n_valid, p):
+    return Pop(np.asarray(counts)[:, 4 * p:4 * p + 4], _pop_n(counts, n_valid, p))
+
+
+def dd(counts, populations=None, n_valid=None):
+    c = np.asarray(counts)
+    if populations is None or populations[0] == populations[1]:
+        p = 0 if populations is None else populations[0]
+        if populations is None and isinstance(n_valid, np.ndarray) and n_valid.ndim == 2:
+            n_valid = n_valid[:, 0]
+        if populations is None and c.shape[1] == 4:
+            return _q(*dd_ii(Pop(c, _pop_n(c, n_valid, 0))))
+        return _q(*dd_ii(_pop(c, n_valid, p)))
+    a, b = populations
+    if isinstance(n_valid, np.ndarray) and n_valid.ndim == 1:
+        na = nb = n_valid.astype(I64)
+        pa = Pop(c[:, 4 * a:4 * a + 4], na)
+        pb = Pop(c[:, 4 * b:4 * b + 4], nb)
+    elif isinstance(n_valid, tuple):
+        # _dd_between reads the tuple by position (0, 1), not by pop index
+        pa = Pop(c[:, 4 * a:4 * a + 4], _pop_n(c[:, 4 * a:4 * a + 4], (n_valid[0],), 0))
+        pb = Pop(c[:, 4 * b:4 * b + 4], _pop_n(c[:, 4 * b:4 * b + 4], (n_valid[1],), 0))
+    else:
+        pa = _pop(c, n_valid, a)
+        pb = _pop(c, n_valid, b)
+    return _q(*dd_ij(pa, pb))
+
+
+def dz(counts, populations=None, n_valid=None):
+    c = np.asarray(counts)
+    if populations is None:
+        if c.shape[1] == 4:
+            return _q(*dz_iii(Pop(c, _pop_n(c, n_valid, 0))))
+        populations = (0, 0, 0)
+    i, j, k = populations
+    P = lambda p: _pop(c, n_valid, p)  # noqa: E731
+    if i == j == k:
+        return _q(*dz_iii(P(i)))
+    if i == j:
+        return _q(*dz_iij(P(i), P(k)))
+    if i == k:
+        return _q(*dz_iji(P(i), P(j)))
+    if j == k:
+        return _q(*dz_ijj(P(i), P(j)))
+    return _q(*dz_ijk(P(i), P(j), P(k)))
+
+
+def pi2(counts, populations=None, n_valid=None):
+    c = np.asarray(counts)
+    if populations is None:
+        if c.shape[1] == 4:
+            return _q(*pi2_iiii(Pop(c, _pop_n(c, n_valid, 0))))
+        populations = (0, 0, 0, 0)
+    i, j, k, l = populations
+    P = lambda p: _pop(c, n_valid, p)  # noqa: E731
+    cnt = {}
+    for p in populations:
+        cnt[p] = cnt.get(p, 0) + 1
+    nu, mc = len(cnt), max(cnt.values())
+    if nu == 1:
+        return _q(*pi2_iiii(P(i)))
+    if mc == 3:
+        t = [p for p, v in cnt.items() if v == 3][0]
+        s = [p for p, v in cnt.items() if v == 1][0]
+        return _q(*pi2_triple(P(t), P(s)))
+    if i == j and k == l:
+        return _q(*pi2_iikk_sym(P(i), P(k)))
+    if i == j:
+        return _q(*pi2_iikl(P(i), P(k), P(l)))
+    if k == l:
+        return _q(*pi2_ijkk(P(i), P(j), P(k)))
+    if (i == k and j == l) or (i == l and j == k):
+        return _q(*pi2_ijij(P(i), P(j)))
+    if nu == 4:
+        return _q(*pi2_alldiff(P(i), P(j), P(k), P(l)))
+    s, a, b = _shared_roles(i, j, k, l)
+    return _q(*pi2_shared(P(s), P(a), P(b)))
+
+
+def _shared_roles(i, j, k, l):
+    if i == k:
+        return i, j, l
+    if i == l:
+        return i, j, k
+    if j == k:
+        return j, i, l
+    return j, i, k
+
+
+# ---------------------------------------------------------------------------
+# r, r^2, D'  (haplotype_kernels.py:20-62, ld_statistics.py:153-246)
+# ---------------------------------------------------------------------------
+def _rsq_parts(counts, n_valid):
+    c = np.asarray(counts).astype(I64)
+    a, b, cc, d = c[:, 0], c[:, 1], c[:, 2], c[:, 3]
+    n = c.sum(axis=1) if n_valid is None else np.asarray(n_valid).astype(I64)
+    return a, b, cc, d, n
+
+
+def r(counts, n_valid=None):
+    a, b, c, d, n = _rsq_parts(counts, n_valid)
+    den = (a + b) * (n - a - b) * (a + c) * (n - a - c)
+    out = np.full(len(a), np.nan)
+    ok = den > 0
+    out[ok] = (a * d - b * c)[ok].astype(np.float64) / np.sqrt(den[ok].astype(np.float64))
+    return out
+
+
+def r_squared(counts, n_valid=None):
+    a, b, c, d, n = _rsq_parts(counts, n_valid)
+    den = (a + b) * (n - a - b) * (a + c) * (n - a - c)
+    num = (a * d - b * c) ** 2
+    out = np.full(len(a), np.nan)
+    ok = den > 0
+    out[ok] = num[ok].astype(np.float64) / den[ok].astype(np.float64)
+    return out
+
+
+def d_prime(counts, n_valid=None):
+    a, b, c, d, n = _rsq_parts(counts, n_valid)
+    x = a * d - b * c
+    pos = np.minimum((a + b) * (n - a - c), (n - a - b) * (a + c))
+    neg = np.minimum((a + b) * (a + c), (n - a - b) * (n - a - c))
+    dmax = np.where(x >= 0, pos, neg)
+    out = np.full(len(a), np.nan)
+    ok = dmax > 0
+    out[ok] = x[ok].astype(np.float64) / dmax[ok].astype(np.float64)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# moments statistic names / specs  (ld_pipeline.py:357-457)
+# ---------------------------------------------------------------------------
+def ld_names(P):
+    names = [f"DD_{i}_{j}" for i in range(P) for j in range(i, P)]
+    names += [f"Dz_{i}_{j}_{k}" for i in range(P) for j in range(P) for k in range(j, P)]
+    for i in range(P):
+        for j in range(i, P):
+            for k in range(i, P):
+                for l in range(k, P):
+                    if k == i == l and j != i:
+                        continue
+                    if i == k and l < j:
+                        continue
+                    names.append(f"pi2_{i}_{j}_{k}_{l}")
+    return names
+
+
+def het_names(P):
+    return [f"H_{i}_{j}" for i in range(P) for j in range(i, P)]
+
+
+def stat_specs(P):
+    """(name, [(weight, kind, pops)]) exactly as generate_stat_specs."""
+    specs = []
+    for name in ld_names(P):
+        parts = name.split("_")
+        kind, pp = parts[0], tuple(int(v) for v in parts[1:])
+        if kind == "DD":
+            specs.append((name, [(1.0, "dd", pp)]))
+        elif kind == "Dz":
+            i, j, k = pp
+            if j == k:
+                specs.append((name, [(1.0, "dz", pp)]))
+            else:
+                specs.append((name, [(0.5, "dz", (i, j, k)), (0.5, "dz", (i, k, j))]))
+        else:
+            i, j, k, l = pp
+            if i == j and k == l:
+                if i == k:
+                    specs.append((name, [(1.0, "pi2", pp)]))
+                else:
+                    specs.append((name, [(0.5, "pi2", (i, j, k, l)), (0.5, "pi2", (k, l, i, j))]))
+            elif i == j:
+                specs.append((name, [(0.25, "pi2", t) for t in
+                                     ((i, j, k, l), (i, j, l, k), (k, l, i, j), (l, k, i, j))]))
+            elif k == l:
+                specs.append((name, [(0.25, "pi2", t) for t in
+                                     ((i, j, k, l), (j, i, k, l), (k, l, i, j), (k, l, j, i))]))
+            else:
+                specs.append((name, [(0.125, "pi2", t) for t in
+                                     ((i, j, k, l), (i, j, l, k), (j, i, k, l), (j, i, l, k),
+                                      (k, l, i, j), (l, k, i, j), (k, l, j, i), (l, k, j, i))]))
+    return specs
+
+
+def kernel_case_value(kind, pp, pops):
+    """One case of the fused kernels (haplotype_kernels.py:335-581)."""
+    if kind == "dd":
+        a, b = pp
+        return _q(*(dd_ii(pops[a]) if a == b else dd_ij(pops[a], pops[b])))
+    if kind == "dz":
+        i, j, k = pp
+        if i == j == k:
+            return _q(*dz_iii(pops[i]))
+        if i == j:
+            return _q(*dz_iij(pops[i], pops[k]))
+        if i == k:
+            return _q(*dz_iji(pops[i], pops[j]))
+        if j == k:
+            return _q(*dz_ijj(pops[i], pops[j]))
+        return _q(*dz_ijk(pops[i], pops[j], pops[k]))
+    i, j, k, l = pp
+    cnt = {}
+    for p in pp:
+        cnt[p] = cnt.get(p, 0) + 1
+    nu, mc = len(cnt), max(cnt.values())
+    if nu == 1:
+        return _q(*pi2_iiii(pops[i]))
+    if mc == 3:
+        t = [p for p, v in cnt.items() if v == 3][0]
+        s = [p for p, v in cnt.items() if v == 1][0]
+        return _q(*pi2_triple(pops[t], pops[s]))
+    if i == j and k == l:
+        return _q(*pi2_iikk(pops[i], pops[k]))
+    if i == j:
+        return _q(*pi2_iikl(pops[i], pops[k], pops[l]))
+    if k == l:
+        return _q(*pi2_ijkk(pops[i], pops[j], pops[k]))
+    if (i == k and j == l) or (i == l and j == k):
+        return _q(*pi2_ijij(pops[i], pops[j]))
+    if nu == 3:
+        s, a, b = _shared_roles(i, j, k, l)
+        return _q(*pi2_shared(pops[s], pops[a], pops[b]))
+    return _q(*pi2_alldiff(pops[i], pops[j], pops[k], pops[l]))
+
+
+def multi_pop_stats(counts_per_pop, n_valid_per_pop, specs=None):
+    """(N, n_stats) float64 as compute_multi_pop_statistics_batch_hap."""
+    P = len(counts_per_pop)
+    specs = stat_specs(P) if specs is None else specs
+    pops = []
+    for c, nv in zip(counts_per_pop, n_valid_per_pop):
+        c = np.asarray(c)
+        pops.append(Pop(c, c.astype(I64).sum(axis=1) if nv is None else nv))
+    cache = {}
+    out = np.zeros((len(np.asarray(counts_per_pop[0])), len(specs)), np.float64)
+    for s, (_, calls) in enumerate(specs):
+        acc = 0.0
+        for w, kind, pp in calls:
+            key = (kind, pp)
+            if key not in cache:
+                cache[key] = kernel_case_value(kind, pp, pops)
+            acc = acc + (cache[key] if (w == 1.0 and len(calls) == 1) else w * cache[key])
+        out[:, s] = acc
+    return out
+
+
+def two_pop_stats(c1, c2, nv1, nv2):
+    """(N, 15) as ld_pipeline.compute_two_pop_statistics_batch, exact arithmetic."""
+    return multi_pop_stats([c1, c2], [nv1, nv2])
+
+
+def single_pop_stats(c, nv):
+    """(N, 3) DD, Dz, pi2 as ld_pipeline.compute_single_pop_statistics_batch."""
+    return np.stack([dd(c, n_valid=nv), dz(c, n_valid=nv), pi2(c, n_valid=nv)], axis=1)
+
+
+# ---------------------------------------------------------------------------
+# distance-binned sums  (moments_ld.py:248-343, haplotype_matrix.py:1592-1866)
+# ---------------------------------------------------------------------------
+def bin_index(distances, bins):
+    """digitize(d, bins) - 1 with right-open bins; -1 / n_bins mark 'outside'."""
+    return np.digitize(distances, np.asarray(bins, np.float64)) - 1
+
+
+def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
+                pair_block=2_000_000, abs_sums=False):
+    """(n_bins, n_stats) float64 sums of the per-pair statistics, plus pair counts.
+
+    ``pop_rows``: list of row-index arrays, one per population (1..4).
+    ``coords``: per-SNP coordinate used for the distance (positions when None;
+    a genetic map in Morgans for the recombination-distance mode).
+    With ``abs_sums`` the sums of |stat| are returned as a third value
+    (the scale that bounds the float32 rounding of the GPU sums).
+    """
+    pos = np.asarray(positions)
+    coord = pos.astype(np.float64) if coords is None else np.asarray(coords, np.float64)
+    bins = np.asarray(bins, np.float64)
+    n_bins = len(bins) - 1
+    P = len(pop_rows)
+    if max_dist is None:
+        max_dist = float(bins[-1])
+    ii, jj = pairs_within_distance(pos, max_dist)
+    specs = stat_specs(P)
+    sums = np.zeros((n_bins, len(specs)))
+    asums = np.zeros((n_bins, len(specs)))
+    npairs = np.zeros(n_bins, np.int64)
+    h = np.asarray(hap)
+    subs = [h[np.asarray(r), :] for r in pop_rows]
+    miss = [bool(np.any(s == -1)) for s in subs]
+    for s0 in range(0, len(ii), pair_block):
+        ci, cj = ii[s0:s0 + pair_block], jj[s0:s0 + pair_block]
+        d = np.abs(coord[cj] - coord[ci]) if coords is not None else (coord[cj] - coord[ci])
+        b = bin_index(d, bins)
+        keep = (b >= 0) & (b < n_bins)
+        if not np.any(keep):
+            continue
+        ci, cj, b = ci[keep], cj[keep], b[keep]
+        cs, nvs = [], []
+        for sub, m in zip(subs, miss):
+            c, nv = counts_for_pairs(sub, ci, cj)
+            cs.append(c)
+            nvs.append(nv if m else None)
+        st = multi_pop_stats(cs, nvs, specs)
+        for k in range(len(specs)):
+            sums[:, k] += np.bincount(b, weights=st[:, k], minlength=n_bins)
+            if abs_sums:
+                asums[:, k] += np.bincount(b, weights=np.abs(st[:, k]), minlength=n_bins)
+        npairs += np.bincount(b, minlength=n_bins)
+    if abs_sums:
+        return sums, npairs, asums
+    return sums, npairs
+
+
+def heterozygosity(hap, pop_rows):
+    """H_i_j statistics (moments_ld.py:346-388), haplotype mode."""
+    h = np.asarray(hap)
+    alt, ref, size = [], [], []
+    for rws in pop_rows:
+        sub = h[np.asarray(rws), :]
+        a = np.sum(np.maximum(sub, 0).astype(np.int64), axis=0).astype(np.float64)
+        nh = float(len(rws)) * np.ones_like(a)
+        alt.append(a)
+        ref.append(nh - a)
+        size.append(nh)
+    out = {}
+    P = len(pop_rows)
+    for i in range(P):
+        for j in range(i, P):
+            if i == j:
+                out[f"H_{i}_{j}"] = float(np.sum(2.0 * ref[i] * alt[i] / (size[i] * (size[i] - 1))))
+            else:
+                out[f"H_{i}_{j}"] = float(np.sum((ref[i] * alt[j] + alt[i] * ref[j])
+                                                 / (size[i] * size[j])))
+    return out
+
+
+def biallelic_keep(hap):
+    """Columns kept by HaplotypeMatrix.apply_biallelic_filter (haplotype_matrix.py:724-789)."""
+    h = np.asarray(hap)
+    return (np.sum(h >= 2, axis=0) == 0) & (np.sum(h == 0, axis=0) > 0) & (np.sum(h == 1, axis=0) > 0)
+
+
+# ---------------------------------------------------------------------------
+# all-pairs tally  (haplotype_matrix.py:1320-1589) -- correct at any H
+# ---------------------------------------------------------------------------
+def tally(hap, rows=None):
+    h = np.asarray(hap)
+    if rows is not None:
+        h = h[np.asarray(rows), :]
+    m = h.shape[1]
+    ii, jj = np.triu_indices(m, k=1)
+    c, _ = counts_for_pairs(h, ii, jj)
+    if bool(np.any(h == -1)):
+        valid = h != -1
+        nv = np.sum(valid[:, ii] & valid[:, jj], axis=0, dtype=np.int32)
+        return c, nv
+    return c, None
+
+
+# ---------------------------------------------------------------------------
+# Rogers-Huff r  (ld_statistics.py:410-531)
+# ---------------------------------------------------------------------------
+def rogers_huff_r(geno):
+    """Condensed upper-triangle Rogers-Huff r on a complete dosage matrix."""
+    g = np.asarray(geno).astype(np.float64)
+    if np.any(g < 0):
+        raise ValueError("rogers_huff_r: missing values")
+    n = g.shape[0]
+    mu = g.mean(axis=0)
+    ssd = ((g - mu) ** 2).sum(axis=0)
+    cov = g.T @ g - n * np.outer(mu, mu)
+    den = np.sqrt(np.outer(ssd, ssd))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rr = np.where(den > 0, cov / den, np.nan)
+    iu = np.triu_indices(g.shape[1], k=1)
+    return rr[iu]
+
+
+def rogers_huff_r_pairs(geno, idx_i, idx_j):
+    """Rogers-Huff r per listed pair with pairwise-complete individuals.
+
+    With no missing dosage this equals the reference's rogers_huff_r on the
+    same pairs; with missing data (where the reference raises) each pair
+    uses the individuals valid at both loci -- the definition the CUDA
+    path implements.  Exact integer moments, one float64 division.
+    """
+    g = np.asarray(geno).astype(np.int64)
+    gi = g[:, idx_i]
+    gj = g[:, idx_j]
+    v = (gi >= 0) & (gj >= 0)
+    gi = np.where(v, gi, 0)
+    gj = np.where(v, gj, 0)
+    n = v.sum(axis=0)
+    si, sj = gi.sum(axis=0), gj.sum(axis=0)
+    sii, sjj, sij = (gi * gi).sum(axis=0), (gj * gj).sum(axis=0), (gi * gj).sum(axis=0)
+    cov = n * sij - si * sj
+    vi = n * sii - si * si
+    vj = n * sjj - sj * sj
+    den = vi * vj
+    out = np.full(len(idx_i), np.nan)
+    ok = den > 0
+    out[ok] = cov[ok].astype(np.float64) / np.sqrt(den[ok].astype(np.float64))
+    return out

@@ -1,0 +1,299 @@
+"""Generate the golden fixtures in this folder from the reference pg_gpu.
+
+Run here, where the reference checkout exists:
+
+    python tests/golden/make_golden.py        # PGLD_REFERENCE=<checkout> to override
+
+Every expected value is produced by the reference's own code (through the
+numpy stand-in for CuPy in ``_ref_shim.py``; RawKernel bodies compiled as
+host C++), or read from data the reference ships:
+
+* ``hap_counts.npz``  -- ld_pipeline.iter_pairs_within_distance chunks and
+  compute_counts_for_pairs on a seeded matrix with missing data and
+  population subsets (ld_pipeline.py:57-175).
+* ``hap_stats.npz``   -- ld_statistics.dd/dz/pi2 for every population tuple
+  of a 4-population count table, compute_multi_pop_statistics_batch_hap for
+  1..4 populations, compute_two_pop_statistics_batch,
+  compute_single_pop_statistics_batch and r / r_squared / d_prime.
+* ``binned.npz``      -- the binned-sum loop of moments_ld._compute_ld_sums
+  (moments_ld.py:306-343) driven by the reference's own pair iterator,
+  counter and statistics, for 1 and 2 populations.
+* ``moments_im.npz``  -- the haplotypes of examples/data/im-parsing-example.vcf
+  (parsed as text, from_vcf layout haplotype_matrix.py:324-328), the deme
+  rows of im_pop.txt, and the moments binned sums cached by the reference in
+  tests/cache/moments_ld_test_im_4bins_deme0-deme1.pkl (read with a
+  restricted unpickler that only accepts numpy array reconstruction).
+* ``geno.npz``        -- 9-way genotype counts from the reference counting
+  kernel (ld_pipeline.py:183-217), single-population genotype DD from
+  _DD_GENO_SINGLE_KERN (genotype_kernels.py:27-71), sigma_D^2 from
+  _SIGMA_D2_GENO_KERN (genotype_kernels.py:91-169) and Rogers-Huff r from
+  ld_statistics._tile_rogers_huff_r (ld_statistics.py:410-443).
+"""
+import io
+import itertools
+import os
+import pickle
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import _ref_shim as S  # noqa: E402
+
+
+def copying_model(rng, n_hap, n_snp, n_founders, switch, flip=1e-3, missing=0.0):
+    p = rng.beta(0.3, 0.3, size=n_snp)
+    founders = (rng.random((n_founders, n_snp)) < p).astype(np.int8)
+    out = np.empty((n_hap, n_snp), np.int8)
+    for h in range(n_hap):
+        f = rng.integers(n_founders)
+        sw = rng.random(n_snp) < switch
+        seg = np.cumsum(sw)
+        choice = rng.integers(0, n_founders, size=seg[-1] + 1)
+        choice[0] = f
+        out[h] = founders[choice[seg], np.arange(n_snp)]
+    out ^= (rng.random(out.shape) < flip).astype(np.int8)
+    if missing > 0:
+        out[rng.random(out.shape) < missing] = -1
+    return out
+
+
+def gen_hap_counts(M):
+    lp = M["ld_pipeline"]
+    rng = np.random.default_rng(20261203)
+    hap = copying_model(rng, 70, 120, 8, 0.05, missing=0.04)
+    pos = np.sort(rng.choice(60_000, 120, replace=False)).astype(np.int64)
+    max_dist = 9_000.0
+    chunks = list(lp.iter_pairs_within_distance(S.garr(pos), max_dist, 97))
+    ci = np.concatenate([np.asarray(c[0]) for c in chunks])
+    cj = np.concatenate([np.asarray(c[1]) for c in chunks])
+    chunk_len = np.array([len(c[0]) for c in chunks])
+    rows_a = np.arange(0, 33)
+    rows_b = np.arange(33, 70)[::2]
+    out = dict(hap=hap, pos=pos, max_dist=max_dist, chunk_size=97, idx_i=ci, idx_j=cj,
+               chunk_len=chunk_len, rows_a=rows_a, rows_b=rows_b)
+    for tag, rows in (("all", None), ("a", rows_a), ("b", rows_b)):
+        c, nv = lp.compute_counts_for_pairs(S.garr(hap), S.garr(ci), S.garr(cj),
+                                            None if rows is None else list(rows))
+        out[f"counts_{tag}"] = np.asarray(c)
+        out[f"nvalid_{tag}"] = np.asarray(nv)
+    # no-missing matrix: n_valid must come back as None
+    hap0 = np.where(hap < 0, 0, hap).astype(np.int8)
+    c0, nv0 = lp.compute_counts_for_pairs(S.garr(hap0), S.garr(ci), S.garr(cj))
+    assert nv0 is None
+    out["hap_nomiss"] = hap0
+    out["counts_nomiss"] = np.asarray(c0)
+    # pair chunking for other chunk sizes / distances
+    for cs, md in ((1, 2000.0), (10_000, 60_000.0), (50, 0.0)):
+        ch = list(lp.iter_pairs_within_distance(S.garr(pos), md, cs))
+        out[f"chunks_{cs}_{int(md)}_len"] = np.array([len(c[0]) for c in ch], np.int64)
+        if ch:
+            out[f"chunks_{cs}_{int(md)}_i"] = np.concatenate([np.asarray(c[0]) for c in ch])
+            out[f"chunks_{cs}_{int(md)}_j"] = np.concatenate([np.asarray(c[1]) for c in ch])
+        else:
+            out[f"chunks_{cs}_{int(md)}_i"] = np.zeros(0, np.int32)
+            out[f"chunks_{cs}_{int(md)}_j"] = np.zeros(0, np.int32)
+    np.savez_compressed(os.path.join(HERE, "hap_counts.npz"), **out)
+
+
+def gen_hap_stats(M):
+    lp, ls, hk = M["ld_pipeline"], M["ld_statistics"], M["haplotype_kernels"]
+    rng = np.random.default_rng(20261204)
+    N, P = 150, 4
+    counts = rng.integers(0, 24, size=(N, 4 * P)).astype(np.int32)
+    counts[:7, :4] = [[0, 0, 5, 5], [5, 5, 0, 0], [3, 0, 0, 3], [0, 4, 4, 0],
+                      [1, 0, 0, 1], [2, 0, 1, 0], [0, 0, 0, 0]]
+    nv = np.stack([counts[:, 4 * p:4 * p + 4].sum(1) + rng.integers(0, 3, N)
+                   for p in range(P)], 1).astype(np.int32)
+    out = dict(counts=counts, nvalid=nv)
+    for pp in itertools.product(range(P), repeat=2):
+        out["dd_" + "".join(map(str, pp))] = np.asarray(ls.dd(S.garr(counts), pp, S.garr(nv)))
+    for pp in itertools.product(range(P), repeat=3):
+        out["dz_" + "".join(map(str, pp))] = np.asarray(ls.dz(S.garr(counts), pp, S.garr(nv)))
+    for pp in itertools.product(range(P), repeat=4):
+        out["pi2_" + "".join(map(str, pp))] = np.asarray(ls.pi2(S.garr(counts), pp, S.garr(nv)))
+    c4 = counts[:, :4]
+    out["dd_single_nonv"] = np.asarray(ls.dd(S.garr(c4)))
+    out["dz_single_nonv"] = np.asarray(ls.dz(S.garr(c4)))
+    out["pi2_single_nonv"] = np.asarray(ls.pi2(S.garr(c4)))
+    for f in ("r", "r_squared", "d_prime"):
+        out[f + "_nv"] = np.asarray(getattr(ls, f)(S.garr(c4), S.garr(nv[:, 0])))
+        out[f + "_nonv"] = np.asarray(getattr(ls, f)(S.garr(c4)))
+    for p in range(1, P + 1):
+        cs = [S.garr(counts[:, 4 * q:4 * q + 4]) for q in range(p)]
+        nvs = [S.garr(nv[:, q]) for q in range(p)]
+        out[f"multi_{p}"] = np.asarray(hk.compute_multi_pop_statistics_batch_hap(
+            cs, nvs, ls, lp.generate_stat_specs(p)))
+        out[f"multi_{p}_nonv"] = np.asarray(hk.compute_multi_pop_statistics_batch_hap(
+            cs, [None] * p, ls, lp.generate_stat_specs(p)))
+    out["two_pop"] = np.asarray(lp.compute_two_pop_statistics_batch(
+        S.garr(counts[:, :4]), S.garr(counts[:, 4:8]), S.garr(nv[:, 0]), S.garr(nv[:, 1]), ls))
+    out["two_pop_nonv"] = np.asarray(lp.compute_two_pop_statistics_batch(
+        S.garr(counts[:, :4]), S.garr(counts[:, 4:8]), None, None, ls))
+    out["single_pop"] = np.asarray(lp.compute_single_pop_statistics_batch(
+        S.garr(c4), S.garr(nv[:, 0]), ls))
+    np.savez_compressed(os.path.join(HERE, "hap_stats.npz"), **out)
+    names = {p: lp.ld_names(p) for p in range(1, 5)}
+    with open(os.path.join(HERE, "ld_names.txt"), "w") as f:
+        for p in range(1, 5):
+            f.write(f"{p} " + " ".join(names[p]) + "\n")
+            f.write(f"H{p} " + " ".join(lp.het_names(p)) + "\n")
+
+
+def ref_binned_sums(M, hap, pos, pop_rows, bins, chunk):
+    """moments_ld._compute_ld_sums (moments_ld.py:306-343), haplotype mode."""
+    lp, ls, hk = M["ld_pipeline"], M["ld_statistics"], M["haplotype_kernels"]
+    n_bins = len(bins) - 1
+    P = len(pop_rows)
+    n_ld = len(lp.ld_names(P))
+    sums = np.zeros((n_bins, n_ld))
+    specs = lp.generate_stat_specs(P) if P != 2 else None
+    for ci, cj in lp.iter_pairs_within_distance(S.garr(pos), float(bins[-1]), chunk):
+        d = pos[np.asarray(cj)] - pos[np.asarray(ci)]
+        cb = np.digitize(d, bins) - 1
+        cl, nl = [], []
+        for rows in pop_rows:
+            c, nv = lp.compute_counts_for_pairs(S.garr(hap), ci, cj, list(rows))
+            cl.append(c)
+            nl.append(nv)
+        if P == 2:
+            st = lp.compute_two_pop_statistics_batch(cl[0], cl[1], nl[0], nl[1], ls)
+        else:
+            st = hk.compute_multi_pop_statistics_batch_hap(cl, nl, ls, specs)
+        st = np.asarray(st)
+        ok = (cb >= 0) & (cb < n_bins)
+        flat = cb[ok][:, None] * n_ld + np.arange(n_ld)[None, :]
+        np.add.at(sums.ravel(), flat.ravel(), st[ok].ravel())
+    return sums
+
+
+def gen_binned(M):
+    rng = np.random.default_rng(20261205)
+    hap = copying_model(rng, 48, 400, 10, 0.01, missing=0.02)
+    pos = np.sort(rng.choice(200_000, 400, replace=False)).astype(np.int64)
+    bins = np.logspace(2, np.log10(50_000), 9)
+    pops = [np.arange(0, 24), np.arange(24, 48)]
+    out = dict(hap=hap, pos=pos, bins=bins, rows0=pops[0], rows1=pops[1])
+    out["sums_2pop"] = ref_binned_sums(M, hap, pos, pops, bins, 5000)
+    out["sums_1pop"] = ref_binned_sums(M, hap, pos, pops[:1], bins, 5000)
+    out["sums_3pop"] = ref_binned_sums(M, hap, pos, [np.arange(0, 16), np.arange(16, 32),
+                                                     np.arange(32, 48)], bins, 5000)
+    np.savez_compressed(os.path.join(HERE, "binned.npz"), **out)
+
+
+class _NumpyOnly(pickle.Unpickler):
+    _OK = {("numpy.core.multiarray", "scalar"), ("numpy.core.multiarray", "_reconstruct"),
+           ("numpy", "dtype"), ("numpy", "ndarray")}
+
+    def find_class(self, module, name):
+        if (module, name) not in self._OK:
+            raise pickle.UnpicklingError(f"refusing {module}.{name}")
+        if module == "numpy.core.multiarray":
+            import numpy._core.multiarray as mm
+            return getattr(mm, name)
+        return getattr(np, name)
+
+
+def parse_vcf_haplotypes(path):
+    samples, gts, pos = None, [], []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("##"):
+                continue
+            parts = line.rstrip("\n").split("\t")
+            if line.startswith("#CHROM"):
+                samples = parts[9:]
+                continue
+            pos.append(int(parts[1]))
+            row = []
+            for g in parts[9:]:
+                a, b = g.split(":")[0].replace("/", "|").split("|")
+                row.append((-1 if a == "." else int(a), -1 if b == "." else int(b)))
+            gts.append(row)
+    gt = np.array(gts, np.int8)  # (M, n, 2)
+    n = gt.shape[1]
+    hap = np.empty((gt.shape[0], 2 * n), np.int8)
+    hap[:, :n] = gt[:, :, 0]
+    hap[:, n:] = gt[:, :, 1]
+    return hap.T.copy(), np.array(pos, np.int64), samples
+
+
+def gen_moments(M):
+    ref = S.REF_ROOT
+    hap, pos, samples = parse_vcf_haplotypes(os.path.join(ref, "examples/data/im-parsing-example.vcf"))
+    assign = {}
+    with open(os.path.join(ref, "examples/data/im_pop.txt")) as f:
+        next(f)
+        for line in f:
+            s, p = line.split()
+            assign[s] = p
+    n = len(samples)
+    rows = {"deme0": [], "deme1": []}
+    for i, s in enumerate(samples):
+        if assign.get(s) in rows:
+            rows[assign[s]] += [i, i + n]
+    with open(os.path.join(ref, "tests/cache/moments_ld_test_im_4bins_deme0-deme1.pkl"), "rb") as f:
+        res = _NumpyOnly(io.BytesIO(f.read())).load()
+    bins = np.array([res["bins"][0][0]] + [b[1] for b in res["bins"]], np.float64)
+    ld = np.stack([np.asarray(s, np.float64) for s in res["sums"][:-1]])
+    het = np.asarray(res["sums"][-1], np.float64)
+    names = np.array(res["stats"][0])
+    hnames = np.array(res["stats"][1])
+    np.savez_compressed(os.path.join(HERE, "moments_im.npz"), hap=hap, pos=pos,
+                        rows0=np.array(rows["deme0"]), rows1=np.array(rows["deme1"]),
+                        bins=bins, ld_sums=ld, het_sums=het, ld_names=names, het_names=hnames)
+
+
+def gen_geno(M):
+    lp, ls, gk = M["ld_pipeline"], M["ld_statistics"], M["genotype_kernels"]
+    rng = np.random.default_rng(20261206)
+    h = copying_model(rng, 80, 150, 8, 0.03)
+    g = (h[0::2] + h[1::2]).astype(np.int8)  # 40 diploids
+    gm = g.copy()
+    gm[rng.random(g.shape) < 0.04] = -1
+    pos = np.sort(rng.choice(80_000, 150, replace=False)).astype(np.int64)
+    ci, cj = [np.concatenate(x) for x in zip(*[(np.asarray(a), np.asarray(b)) for a, b in
+                                               lp.iter_pairs_within_distance(S.garr(pos), 15_000, 10**6)])]
+    out = dict(geno=g, geno_miss=gm, pos=pos, idx_i=ci, idx_j=cj)
+    c, nv = lp.compute_genotype_counts_for_pairs(S.garr(gm), S.garr(ci), S.garr(cj))
+    out["counts9_miss"], out["nvalid_miss"] = np.asarray(c), np.asarray(nv)
+    c0, nv0 = lp.compute_genotype_counts_for_pairs(S.garr(g), S.garr(ci), S.garr(cj))
+    assert nv0 is None
+    out["counts9"] = np.asarray(c0)
+    rows = np.arange(5, 37, 2)
+    cr, _ = lp.compute_genotype_counts_for_pairs(S.garr(gm), S.garr(ci), S.garr(cj), list(rows))
+    out["rows"], out["counts9_rows"] = rows, np.asarray(cr)
+    for tag, cc in (("", np.asarray(c0)), ("_miss", np.asarray(c))):
+        rev = np.ascontiguousarray(cc[:, ::-1].astype(np.float64))
+        o = np.empty(len(rev))
+        gk._DD_GENO_SINGLE_KERN(((len(rev) + 255) // 256,), (256,), (rev, o, len(rev)))
+        out["dd_geno" + tag] = o
+        o2 = np.empty(len(rev))
+        gk._SIGMA_D2_GENO_KERN(((len(rev) + 255) // 256,), (256,), (rev, o2, len(rev)))
+        out["sigma_d2" + tag] = o2
+    gf = g.astype(np.float64)
+    mu = gf.mean(axis=0)
+    ssd = ((gf - mu) ** 2).sum(axis=0)
+    rfull = np.asarray(ls._tile_rogers_huff_r(S.garr(gf), S.garr(gf), S.garr(mu), S.garr(mu),
+                                              S.garr(ssd), S.garr(ssd), gf.shape[0]))
+    out["rh_r_pairs"] = rfull[ci, cj]
+    iu = np.triu_indices(g.shape[1], k=1)
+    out["rh_r_condensed"] = rfull[iu]
+    np.savez_compressed(os.path.join(HERE, "geno.npz"), **out)
+
+
+def main():
+    M = S.load_reference_modules()
+    gen_hap_counts(M)
+    gen_hap_stats(M)
+    gen_binned(M)
+    gen_moments(M)
+    gen_geno(M)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz") or f.endswith(".txt"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,162 @@
+"""The CPU oracle against fixtures produced by the reference pg_gpu itself.
+
+Fixtures come from tests/golden/make_golden.py (reference code run through a
+numpy stand-in for CuPy) and from the moments result the reference caches in
+its own test suite (tests/test_ld_validation_full.py:38-67).
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import ld_oracle as O
+
+
+def test_pair_enumeration_matches_reference_chunks(golden):
+    z = golden("hap_counts")
+    ii, jj = O.pairs_within_distance(z["pos"], float(z["max_dist"]))
+    assert np.array_equal(ii, z["idx_i"]) and np.array_equal(jj, z["idx_j"])
+    lens = [b[2] for b in O.chunk_bounds(z["pos"], float(z["max_dist"]), int(z["chunk_size"]))]
+    assert np.array_equal(lens, z["chunk_len"])
+    for cs, md in ((1, 2000.0), (10_000, 60_000.0), (50, 0.0)):
+        key = f"chunks_{cs}_{int(md)}"
+        ii, jj = O.pairs_within_distance(z["pos"], md)
+        assert np.array_equal(ii, z[key + "_i"]) and np.array_equal(jj, z[key + "_j"])
+        lens = [b[2] for b in O.chunk_bounds(z["pos"], md, cs)]
+        assert np.array_equal(lens, z[key + "_len"])
+
+
+def test_pair_enumeration_edge_cases():
+    # tests/test_ld_pair_iteration.py:21-115: empty, single SNP, max_dist 0 / inf
+    assert len(O.pairs_within_distance(np.array([], np.int64), 10)[0]) == 0
+    assert len(O.pairs_within_distance(np.array([5]), 10)[0]) == 0
+    ii, jj = O.pairs_within_distance(np.array([1, 2, 2, 3]), 0)
+    assert list(zip(ii, jj)) == [(1, 2)]
+    ii, jj = O.pairs_within_distance(np.arange(6) * 10, np.inf)
+    assert len(ii) == 15
+
+
+def test_counts_match_reference(golden):
+    z = golden("hap_counts")
+    for tag, rows in (("all", None), ("a", z["rows_a"]), ("b", z["rows_b"])):
+        c, nv = O.counts_for_pairs(z["hap"], z["idx_i"], z["idx_j"], rows)
+        assert np.array_equal(c, z[f"counts_{tag}"])
+        assert np.array_equal(nv, z[f"nvalid_{tag}"])
+    c, nv = O.counts_for_pairs(z["hap_nomiss"], z["idx_i"], z["idx_j"])
+    assert nv is None and np.array_equal(c, z["counts_nomiss"])
+
+
+def test_counts_known_answers():
+    # tests/test_haplotype_counting.py:22-52: ind0 = 1|1 , 1|0 ; ind1 = 0|1 , 1|0
+    h = np.empty((4, 2), np.int8)
+    h[0], h[1] = [1, 1], [0, 1]      # hap-0 of ind0, ind1
+    h[2], h[3] = [1, 0], [1, 0]      # hap-1 of ind0, ind1
+    c, nv = O.counts_for_pairs(h, np.array([0]), np.array([1]))
+    assert c.tolist() == [[1, 2, 1, 0]] and nv is None
+
+
+def _close(a, b, rtol=1e-13, atol=1e-300):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = ~np.isnan(a)
+    np.testing.assert_allclose(a[m], b[m], rtol=rtol, atol=atol)
+
+
+def test_public_statistics_match_reference(golden):
+    z = golden("hap_stats")
+    c, nv = z["counts"], z["nvalid"]
+    for pp in itertools.product(range(4), repeat=2):
+        _close(O.dd(c, pp, nv), z["dd_" + "".join(map(str, pp))])
+    for pp in itertools.product(range(4), repeat=3):
+        _close(O.dz(c, pp, nv), z["dz_" + "".join(map(str, pp))])
+    for pp in itertools.product(range(4), repeat=4):
+        _close(O.pi2(c, pp, nv), z["pi2_" + "".join(map(str, pp))])
+    c4 = c[:, :4]
+    _close(O.dd(c4), z["dd_single_nonv"])
+    _close(O.dz(c4), z["dz_single_nonv"])
+    _close(O.pi2(c4), z["pi2_single_nonv"])
+
+
+def test_r_family_matches_reference(golden):
+    z = golden("hap_stats")
+    c4, nv = z["counts"][:, :4], z["nvalid"][:, 0]
+    for f in ("r", "r_squared", "d_prime"):
+        _close(getattr(O, f)(c4, nv), z[f + "_nv"], rtol=1e-12)
+        _close(getattr(O, f)(c4), z[f + "_nonv"], rtol=1e-12)
+
+
+def test_r_known_answers():
+    # tests/test_ld_r_squared.py:15-57, 171-190; tests/test_haplotype_kernels_rsq.py:90-126
+    c = np.array([[5, 0, 0, 5], [25, 25, 25, 25], [0, 5, 5, 0], [5, 5, 0, 0]])
+    r2 = O.r_squared(c)
+    assert r2[0] == 1.0 and r2[1] == 0.0 and r2[2] == 1.0 and np.isnan(r2[3])
+    assert O.r(c)[2] == -1.0
+    dp = O.d_prime(c)
+    assert dp[0] == 1.0 and dp[1] == 0.0 and dp[2] == -1.0 and np.isnan(dp[3])
+
+
+def test_batches_match_reference(golden):
+    z = golden("hap_stats")
+    c, nv = z["counts"], z["nvalid"]
+    for p in range(1, 5):
+        cs = [c[:, 4 * q:4 * q + 4] for q in range(p)]
+        _close(O.multi_pop_stats(cs, [nv[:, q] for q in range(p)]), z[f"multi_{p}"])
+        _close(O.multi_pop_stats(cs, [None] * p), z[f"multi_{p}_nonv"])
+    _close(O.two_pop_stats(c[:, :4], c[:, 4:8], nv[:, 0], nv[:, 1]), z["two_pop"], rtol=1e-14)
+    _close(O.two_pop_stats(c[:, :4], c[:, 4:8], None, None), z["two_pop_nonv"], rtol=1e-14)
+    _close(O.single_pop_stats(c[:, :4], nv[:, 0]), z["single_pop"])
+
+
+def test_names_and_specs_match_reference():
+    import os
+    from tests.conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "ld_names.txt")) as f:
+        lines = f.read().splitlines()
+    for p in range(1, 5):
+        assert lines[2 * (p - 1)].split()[1:] == O.ld_names(p)
+        assert lines[2 * (p - 1) + 1].split()[1:] == O.het_names(p)
+    assert [len(O.stat_specs(p)) for p in (1, 2, 3, 4)] == [3, 15, 45, 105]
+
+
+def test_binned_sums_match_reference(golden):
+    z = golden("binned")
+    rows = [z["rows0"], z["rows1"]]
+    for P, key in ((2, "sums_2pop"), (1, "sums_1pop")):
+        s, _ = O.binned_sums(z["hap"], z["pos"], rows[:P], z["bins"])
+        np.testing.assert_allclose(s, z[key], rtol=1e-13, atol=1e-300)
+    s, _ = O.binned_sums(z["hap"], z["pos"], [np.arange(0, 16), np.arange(16, 32),
+                                              np.arange(32, 48)], z["bins"])
+    np.testing.assert_allclose(s, z["sums_3pop"], rtol=1e-13, atol=1e-300)
+
+
+def test_binned_sums_match_moments_golden(golden):
+    """moments.LD.Parsing on im-parsing-example.vcf, 2 demes, logspace(2,5,4) bins."""
+    z = golden("moments_im")
+    keep = O.biallelic_keep(z["hap"])
+    rows = [z["rows0"], z["rows1"]]
+    s, _ = O.binned_sums(z["hap"][:, keep], z["pos"][keep], rows, z["bins"])
+    assert list(z["ld_names"]) == O.ld_names(2)
+    np.testing.assert_allclose(s, z["ld_sums"], rtol=1e-10)
+    het = O.heterozygosity(z["hap"][:, keep], rows)
+    np.testing.assert_allclose([het[h] for h in z["het_names"]], z["het_sums"], rtol=1e-12)
+
+
+def test_genotype_counts_match_reference(golden):
+    z = golden("geno")
+    c, nv = O.genotype_counts_for_pairs(z["geno_miss"], z["idx_i"], z["idx_j"])
+    assert np.array_equal(c, z["counts9_miss"]) and np.array_equal(nv, z["nvalid_miss"])
+    c, nv = O.genotype_counts_for_pairs(z["geno"], z["idx_i"], z["idx_j"])
+    assert nv is None and np.array_equal(c, z["counts9"])
+    c, _ = O.genotype_counts_for_pairs(z["geno_miss"], z["idx_i"], z["idx_j"], z["rows"])
+    assert np.array_equal(c, z["counts9_rows"])
+
+
+def test_rogers_huff_matches_reference(golden):
+    z = golden("geno")
+    # the reference centres in float64 (rounding noise ~1e-15 where r is 0)
+    _close(O.rogers_huff_r(z["geno"]), z["rh_r_condensed"], rtol=1e-9, atol=1e-12)
+    _close(O.rogers_huff_r_pairs(z["geno"], z["idx_i"], z["idx_j"]), z["rh_r_pairs"],
+           rtol=1e-9, atol=1e-12)
+    with pytest.raises(ValueError):
+        O.rogers_huff_r(z["geno_miss"])
