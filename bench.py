@@ -1,0 +1,439 @@
+"""Benchmark of the two-locus LD hot path on GB300.
+
+Workload (default): two populations of 1,000 haplotypes each x 200,000 SNPs
+over 20 Mb, sharing a 40-founder pool (each population flips 10 % of founder
+alleles; copying model with founder switches at rate 1e-3 per SNP, allele
+flips 1e-3, 2 % entries missing), moments DD/Dz/pi2 (15 statistics) summed
+into 20 log-spaced distance bins from 1 kb to 1 Mb over every pair within
+1 Mb.  One step = pack both populations' bit planes from the resident int8
+panel + one binned-sum launch.  Metric: SNP pairs per second.
+
+  python bench.py [--gpus N --steps K --warmup W] [--form plain|tc]
+  python bench.py --impl reference      # the reference path on host cores
+
+Under torchrun (N > 1) every rank runs an independent replica (weak
+scaling); rank 0 prints the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LD SNP-pairs/s at 2k haps, int8-TC vs plain popcount; % INT8 TC peak; 1×GB300"
+
+WORKLOADS = {
+    # two-population binned moments statistics (the headline)
+    "binned2pop": dict(pops=2, hap_per_pop=1000, n_snp=200_000, length=20_000_000, founders=40,
+                       switch=1e-3, pop_flip=0.10, flip=1e-3, missing=0.02,
+                       bins=np.logspace(3, 6, 21), seed=20261503),
+    # reduced size of the same workload, for profiling captures
+    "binned2pop_small": dict(pops=2, hap_per_pop=1000, n_snp=20_000, length=2_000_000,
+                             founders=40, switch=1e-3, pop_flip=0.10, flip=1e-3, missing=0.02,
+                             bins=np.logspace(3, 6, 21), seed=20261503),
+}
+
+
+def rank_info():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return r, w, lr
+
+
+# --------------------------------------------------------------------------
+# synthetic panel
+# --------------------------------------------------------------------------
+def make_panel(cfg, device):
+    """int8 (2*H, M) panel on the device, sorted int64 positions (host)."""
+    import torch
+    rng = np.random.default_rng(cfg["seed"])
+    M, F, H = cfg["n_snp"], cfg["founders"], cfg["hap_per_pop"]
+    pos = np.sort(rng.choice(cfg["length"], M, replace=False)).astype(np.int64)
+    p = torch.as_tensor(rng.beta(0.3, 0.3, size=M), dtype=torch.float32, device=device)
+    g = torch.Generator(device=device)
+    g.manual_seed(cfg["seed"])
+    founders = (torch.rand((F, M), generator=g, device=device) < p).to(torch.int8)
+    pops = []
+    for _ in range(cfg["pops"]):
+        fp = founders ^ (torch.rand((F, M), generator=g, device=device) < cfg["pop_flip"]).to(torch.int8)
+        sw = torch.rand((H, M), generator=g, device=device) < cfg["switch"]
+        seg = torch.cumsum(sw, dim=1, dtype=torch.int32)
+        del sw
+        choice = torch.randint(0, F, (H, int(seg.max()) + 1), generator=g, device=device,
+                               dtype=torch.int64)
+        idx = torch.gather(choice, 1, seg.to(torch.int64))
+        del seg, choice
+        hap = torch.gather(fp, 0, idx)
+        del idx
+        hap ^= (torch.rand((H, M), generator=g, device=device) < cfg["flip"]).to(torch.int8)
+        hap[torch.rand((H, M), generator=g, device=device) < cfg["missing"]] = -1
+        pops.append(hap)
+    panel = torch.cat(pops, 0).contiguous()
+    torch.cuda.synchronize()
+    return panel, pos
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profile_traffic(form, workload):
+    """dram bytes per launch of the dominant kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = dict(kv.split("=", 1) for kv in line.split() if "=" in kv)
+                if parts.get("form") == form and parts.get("workload") == workload:
+                    return float(parts["traffic_bytes_per_launch"])
+    except (OSError, ValueError, KeyError):
+        pass
+    return None
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle (a restatement of the reference's NumPy path)
+# --------------------------------------------------------------------------
+def _cpu_worker(args):
+    hap, pos, rows, bins, max_dist, a0, a1 = args
+    from oracle import ld_oracle as O
+    t = time.perf_counter()
+    # the pairs of anchors a0..a1 (pair enumeration as ld_pipeline.py:85-121)
+    jmax = np.searchsorted(pos, pos[a0:a1] + max_dist, side="right")
+    per = np.maximum(0, jmax - np.arange(a0, a1) - 1)
+    ii = np.repeat(np.arange(a0, a1), per)
+    jj = ii + 1 + (np.arange(per.sum()) - np.repeat(np.cumsum(per) - per, per))
+    n_sel = len(ii)
+    d = (pos[jj] - pos[ii]).astype(np.float64)
+    b = O.bin_index(d, bins)
+    ok = (b >= 0) & (b < len(bins) - 1)
+    ii, jj, b = ii[ok], jj[ok], b[ok]
+    sums = np.zeros((len(bins) - 1, 15))
+    for s0 in range(0, len(ii), 250_000):
+        cs, nvs = [], []
+        for r in rows:
+            c, nv = O.counts_for_pairs(hap[r], ii[s0:s0 + 250_000], jj[s0:s0 + 250_000])
+            cs.append(c)
+            nvs.append(nv)
+        st = O.multi_pop_stats(cs, nvs)
+        for k in range(st.shape[1]):
+            sums[:, k] += np.bincount(b[s0:s0 + 250_000], weights=st[:, k], minlength=len(bins) - 1)
+    return int(n_sel), time.perf_counter() - t
+
+
+def cpu_sample_inputs(panel, pos, cfg, n_workers, pairs_per_worker):
+    """Contiguous sample: anchors 0..A split over workers, each with its window."""
+    max_dist = float(cfg["bins"][-1])
+    jmax = np.searchsorted(pos, pos + max_dist, side="right")
+    per = np.maximum(0, jmax - np.arange(len(pos)) - 1)
+    tasks = []
+    a = 0
+    H = cfg["hap_per_pop"]
+    rows = [np.arange(q * H, (q + 1) * H) for q in range(cfg["pops"])]
+    for _ in range(n_workers):
+        cum = np.cumsum(per[a:])
+        a1 = a + int(np.searchsorted(cum, pairs_per_worker)) + 1
+        hi = int(jmax[a1 - 1])
+        win = panel[:, a:hi].cpu().numpy()
+        tasks.append((win, pos[a:hi], rows, cfg["bins"], max_dist, 0, a1 - a))
+        a = a1
+    return tasks
+
+
+def run_cpu_baseline(pool, tasks, cores):
+    t = time.perf_counter()
+    res = pool.map(_cpu_worker, tasks)
+    wall = time.perf_counter() - t
+    pairs = sum(r[0] for r in res)
+    return pairs / wall, pairs, wall
+
+
+def make_pool(cores):
+    import multiprocessing as mp
+    return mp.get_context("spawn").Pool(cores)
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_gpu(args, pool, cores):
+    import torch
+    import torch.distributed as dist
+    from pg_gpu_gb300 import _ops
+    from pg_gpu_gb300.haplotype_matrix import HaplotypeMatrix
+
+    rank, world, lrank = rank_info()
+    torch.cuda.set_device(lrank)
+    if world > 1:
+        dist.init_process_group("nccl")
+    cfg = WORKLOADS[args.workload]
+    dev = torch.device("cuda", lrank)
+    panel, pos = make_panel(cfg, dev)
+    H = cfg["hap_per_pop"]
+    rows = [torch.arange(q * H, (q + 1) * H, dtype=torch.int32, device=dev)
+            for q in range(cfg["pops"])]
+    bins = cfg["bins"]
+    pos_d = _ops.positions_f64(pos)
+    _, n_pairs = _ops.band_offsets(pos_d, float(bins[-1]))
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
+
+    def step():
+        packs = [_ops.pack(panel, r) for r in rows]
+        return _ops.binned_sums(packs, pos_d, bins, form=args.form)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # correctness guard on the timed configuration: pair counts per bin
+    _, cnt = step()
+    d = np.diff(bins)
+    assert int(cnt.sum()) <= n_pairs
+
+    # ---- timed region: device-resident inputs ----
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(lrank) as clk:
+        for s in range(args.steps):
+            flush.fill_(s & 0x7F)  # L2 flush between steps (outside the events)
+            ev[s][0].record(stream)
+            packs = [_ops.pack(panel, r) for r in rows]
+            kev[s][0].record(stream)
+            _ops.binned_sums(packs, pos_d, bins, form=args.form)
+            kev[s][1].record(stream)
+            ev[s][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    kern_ms = [a.elapsed_time(b) for a, b in kev]
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * n_pairs * args.steps / total_s
+
+    # ---- end to end through the public API, host buffers ----
+    host = panel.cpu().pin_memory()
+    sets = {f"pop{q}": list(range(q * H, (q + 1) * H)) for q in range(cfg["pops"])}
+    e2e_ms = []
+    for s in range(args.warmup + args.steps):
+        flush.fill_(s & 0x7F)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hm = HaplotypeMatrix(host, pos, sample_sets=sets)
+        out = hm.compute_ld_statistics_gpu_two_pops(bins, "pop0", "pop1", raw=True,
+                                                    ac_filter=False)
+        torch.cuda.synchronize()
+        if s >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        del hm
+    e2e_s = sum(e2e_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n_pairs * args.steps / e2e_s
+    h2d = host.numel() * host.element_size() + pos.nbytes
+    d2h = (len(bins) - 1) * (15 + 1) * 8
+
+    # ---- roofline of the binned-sum kernel ----
+    peaks, peak_src = measured_peaks()
+    k_s = float(np.mean(kern_ms)) / 1e3
+    W = (H + 31) // 32
+    plane_bytes = cfg["n_snp"] * cfg["pops"] * 2 * W * 4
+    traffic = profile_traffic(args.form, args.workload)
+    if args.form == "plain":
+        achieved = plane_bytes / k_s / 1e9
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"{peak_src} hbm_gbs",
+                "algorithmic_bytes_per_launch": plane_bytes,
+                "note": "the plain form is bound by the integer (AND/POPC) pipe, not HBM; "
+                        "int_ops_per_launch / time is reported as int_tops"}
+        roof["int_tops"] = n_pairs * cfg["pops"] * 4 * W * 3 / k_s / 1e12
+    else:
+        ops = n_pairs * 8 * H * cfg["pops"]
+        achieved = ops / k_s / 1e12
+        peak = 2.0 * float(peaks.get("bf16_tflops", 1900.0))
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"2 x {peak_src} bf16_tflops (dense fp8 rate)",
+                "algorithmic_ops_per_launch": ops}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32" if args.form == "plain" else "e4m3",
+        "data": "synthetic (seeded copying model, generated on device)",
+        "config": {"workload": args.workload, "form": args.form, "pops": cfg["pops"],
+                   "haplotypes_per_pop": H, "n_snp": cfg["n_snp"], "max_dist_bp": float(bins[-1]),
+                   "bins": "20 log bins 1e3..1e6", "pairs_per_step": n_pairs,
+                   "l2": "256 MB buffer written between steps; int8 panel 400 MB > L2",
+                   "parallelism": f"replicas x{world}"},
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "api": "HaplotypeMatrix(host int8).compute_ld_statistics_gpu_two_pops(raw=True)"},
+        "gpu_launches": args.steps * (cfg["pops"] + 5),
+        "kernel_ms": float(np.mean(kern_ms)),
+        "roofline": roof,
+    }
+    if pool is not None and rank == 0:
+        tasks = cpu_sample_inputs(panel, pos, cfg, cores, args.cpu_pairs_per_worker)
+        rate, pairs, wall = run_cpu_baseline(pool, tasks, cores)
+        line["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                "sample": f"first {pairs} pairs of the workload (anchors from "
+                                          f"SNP 0), {cores} spawn workers, {wall:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args, pool, cores):
+    """The reference's CPU path (the oracle port) on every host core."""
+    import torch
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    cfg = WORKLOADS[args.workload]
+    dev = torch.device("cuda", 0) if torch.cuda.is_available() else None
+    if dev is None:
+        print(json.dumps({"impl": "reference", "unavailable": "needs the device panel generator"}))
+        return
+    panel, pos = make_panel(cfg, dev)
+    tasks = cpu_sample_inputs(panel, pos, cfg, cores, args.cpu_pairs_per_worker)
+    for _ in range(args.warmup):
+        run_cpu_baseline(pool, tasks[:1], 1)
+    rates, walls, pairs = [], [], 0
+    for _ in range(args.steps):
+        r, p, w = run_cpu_baseline(pool, tasks, cores)
+        rates.append(r)
+        walls.append(w)
+        pairs = p
+    value = float(np.sum([pairs] * len(walls)) / np.sum(walls))
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(walls) * 1e3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "pops": cfg["pops"],
+                       "haplotypes_per_pop": cfg["hap_per_pop"], "n_snp": cfg["n_snp"]},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                             "sample": f"{pairs} pairs per step (contiguous from SNP 0)"},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="plain", choices=["plain", "tc"])
+    ap.add_argument("--workload", default="binned2pop", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-pairs-per-worker", type=int, default=400_000)
+    args = ap.parse_args()
+    rank, world, _ = rank_info()
+    cores = host_cores()
+    # the oracle's process pool starts before the first GPU call (spawn)
+    pool = None
+    if rank == 0 and (args.impl == "reference" or not args.no_cpu):
+        pool = make_pool(cores)
+    try:
+        if args.impl == "reference":
+            run_reference(args, pool, cores)
+        else:
+            run_gpu(args, pool, cores)
+    finally:
+        if pool is not None:
+            pool.close()
+            pool.join()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+/*
+ * pgld.h -- C ABI of libpgld, the GB300 (sm_103a) two-locus LD library.
+ *
+ * Plain pointers and sizes only.  Every entry point returns an int status
+ * (PGLD_OK == 0, negative on error), never throws and never aborts; the
+ * message for the last failure is available from pgld_last_error().
+ * Buffers are owned by the caller: device buffers are passed as raw device
+ * pointers, and work is enqueued on the given stream (a cudaStream_t passed
+ * as void*, NULL = legacy default stream).  Calls are asynchronous unless
+ * noted ("synchronises"), i.e. where a size must come back to the host.
+ * The library owns only the handle and its device workspace; distinct
+ * handles may be used from distinct host threads.
+ *
+ * Reference interfaces cited below are files of kr-colab/pg_gpu.
+ */
+#ifndef PGLD_H
+#define PGLD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGLD_OK 0
+#define PGLD_ERR_INVALID_ARG (-1)
+#define PGLD_ERR_CUDA (-2)
+#define PGLD_ERR_TOO_LARGE (-3)
+#define PGLD_ERR_UNSUPPORTED (-4)
+#define PGLD_ERR_TIMEOUT (-5)
+#define PGLD_ERR_NO_MEMORY (-6)
+
+#define PGLD_MAX_POPS 4
+
+/* Output element types. */
+#define PGLD_F64 0
+#define PGLD_F32 1
+
+/* Count-kernel forms. */
+#define PGLD_FORM_PLAIN 0 /* bit-packed AND + popcount                  */
+#define PGLD_FORM_TC 1    /* tcgen05 tensor-core contraction (sm_103a)  */
+
+typedef struct pgld_context* pgld_handle;
+
+/* ----------------------------------------------------------------------
+ * Per-population bit planes of a haplotype panel.
+ *
+ * For population p with H_p haplotypes, n_words[p] = ceil(H_p / 32) and
+ * planes[p] holds, for every SNP s, 2 * n_words[p] uint32 words:
+ * words [0, n_words) are the carrier plane (bit h set iff hap[h][s] == 1)
+ * and words [n_words, 2 n_words) the reference plane (hap[h][s] == 0).
+ * valid[p] is optional ([n_snp][n_words] bits of hap >= 0); it is needed
+ * only when the panel holds values other than -1/0/1 AND missing data, in
+ * which case the pairwise-valid n is not n11+n10+n01+n00.  When valid[p]
+ * is NULL the per-pair n of population p is n11+n10+n01+n00, which is the
+ * reference's n_valid for 0/1/-1 data (ld_pipeline.py:158-172).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t n_pops;
+  int32_t n_words[PGLD_MAX_POPS];
+  const uint32_t* planes[PGLD_MAX_POPS];
+  const uint32_t* valid[PGLD_MAX_POPS];
+  int64_t n_snp;
+} pgld_hap_panel;
+
+/* Handle management. */
+int pgld_version(void);
+int pgld_create(int device, pgld_handle* out);
+int pgld_destroy(pgld_handle h);
+/* Message of the last failed call on h (h may be NULL: last failure of any
+ * call on this host thread).  Valid until the next call on the thread. */
+const char* pgld_last_error(pgld_handle h);
+/* Reads and clears the device-side error word of h (synchronises). */
+int pgld_device_status(pgld_handle h, int32_t* code_out, void* stream);
+
+/* Pack rows of an int8 (n_rows_total x n_snp) haplotype matrix (row stride
+ * ld bytes, values 1 / 0 / -1) into the bit planes above.  rows: device
+ * int32 row indices (NULL = rows 0..n_rows-1).  valid may be NULL.
+ * flags: device int32[2], OR-ed: flags[0] |= 1 if a -1 was seen,
+ * flags[1] |= 1 if a value outside {-1,0,1} was seen.
+ * Replaces the per-call gathers of ld_pipeline.compute_counts_for_pairs
+ * (ld_pipeline.py:150-158) and HaplotypeMatrix.tally_gpu_haplotypes
+ * (haplotype_matrix.py:1344-1349). */
+int pgld_pack_haplotypes(pgld_handle h, const int8_t* hap, int64_t ld, int64_t n_snp,
+                         const int32_t* rows, int32_t n_rows, uint32_t* planes,
+                         uint32_t* valid, int32_t* flags, void* stream);
+
+/* Joint counts [n11, n10, n01, n00] of listed SNP pairs for one
+ * population; counts row stride counts_ld (int32 elements, >= 4).
+ * n_valid (nullable) receives the pairwise-valid n.
+ * Replaces ld_pipeline.compute_counts_for_pairs (ld_pipeline.py:130-175). */
+int pgld_hap_counts_pairs(pgld_handle h, const uint32_t* planes, const uint32_t* valid,
+                          int32_t n_words, int64_t n_snp, const int32_t* idx_i,
+                          const int32_t* idx_j, int64_t n_pairs, int32_t* counts,
+                          int64_t counts_ld, int32_t* n_valid, void* stream);
+
+/* All-pairs (i<j, row-major upper triangle) counts of one population, the
+ * output of HaplotypeMatrix.tally_gpu_haplotypes (haplotype_matrix.py:
+ * 1320-1434), correct at any sample size.  n_valid may be NULL. */
+int pgld_hap_tally(pgld_handle h, const uint32_t* planes, const uint32_t* valid,
+                   int32_t n_words, int64_t n_snp, int32_t* counts, int32_t* n_valid,
+                   void* stream);
+
+/* ----------------------------------------------------------------------
+ * Statistic terms.  A statistic column is the weighted sum of terms; each
+ * term is one case formula of the reference evaluated on populations
+ * pops[0..3] (roles per kind below).  Numerators and denominators are
+ * formed exactly in 64-bit integers and divided once (float64 for
+ * PGLD_F64 output, float32 for PGLD_F32).
+ * ---------------------------------------------------------------------- */
+enum pgld_kind {
+  PGLD_DD_II = 0,      /* dd(i,i)            ld_statistics.py:1116-1128 */
+  PGLD_DD_IJ = 1,      /* dd(i,j)            ld_statistics.py:1131-1169 */
+  PGLD_DZ_III = 2,     /* dz(i,i,i)          ld_statistics.py:1172-1189 */
+  PGLD_DZ_IIJ = 3,     /* dz(i,i,j) pops=i,j ld_statistics.py:1212-1225 */
+  PGLD_DZ_IJI = 4,     /* dz(i,j,i) pops=i,j ld_statistics.py:1227-1240 */
+  PGLD_DZ_IJJ = 5,     /* dz(i,j,j) pops=i,j ld_statistics.py:1242-1253 */
+  PGLD_DZ_IJK = 6,     /* dz(i,j,k)          ld_statistics.py:1255-1270 */
+  PGLD_PI2_IIII = 7,   /* pi2(i,i,i,i)       ld_statistics.py:1275-1296 */
+  PGLD_PI2_TRIPLE = 8, /* pops = triple, single  ld_statistics.py:1415-1445 */
+  PGLD_PI2_IIKK = 9,   /* kernel form        haplotype_kernels.py:180-190 */
+  PGLD_PI2_IIKK_SYM = 10, /* symmetrised     ld_statistics.py:1327-1339 */
+  PGLD_PI2_IIKL = 11,  /* pops = i,k,l       ld_statistics.py:1448-1481 */
+  PGLD_PI2_IJKK = 12,  /* pops = i,j,k       ld_statistics.py:1484-1516 */
+  PGLD_PI2_IJIJ = 13,  /* pops = i,j         ld_statistics.py:1349-1402 */
+  PGLD_PI2_SHARED = 14,/* pops = shared,a,b  ld_statistics.py:1519-1589 */
+  PGLD_PI2_ALLDIFF = 15,/* pops = i,j,k,l    ld_statistics.py:1592-1617 */
+  PGLD_R = 16,         /* haplotype_kernels.py:20-30, NaN if undefined */
+  PGLD_R2 = 17,        /* haplotype_kernels.py:32-42 */
+  PGLD_DPRIME = 18     /* haplotype_kernels.py:44-62 */
+};
+
+typedef struct {
+  int32_t stat;    /* output column */
+  int32_t kind;    /* enum pgld_kind */
+  int32_t pops[4];
+  double weight;   /* the column is sum over its terms of weight * value */
+} pgld_term;
+
+/* Per-pair counts of up to 4 populations, as device pointers. */
+typedef struct {
+  int32_t n_pops;
+  const int32_t* counts[PGLD_MAX_POPS]; /* [n_pairs][>=4] int32 */
+  int64_t counts_ld[PGLD_MAX_POPS];     /* elements between pairs */
+  const int32_t* n_valid[PGLD_MAX_POPS];/* NULL: n = n11+n10+n01+n00 */
+  int64_t nvalid_ld[PGLD_MAX_POPS];     /* elements between pairs (0 ok) */
+} pgld_pair_counts;
+
+/* The moments statistic table of n_pops populations as terms (host only, no
+ * device needed): the columns follow moments ld_names order and each term is
+ * the case selection of haplotype_kernels.compute_multi_pop_statistics_batch_hap
+ * (haplotype_kernels.py:335-640) applied to generate_stat_specs
+ * (ld_pipeline.py:388-457).  With out == NULL only the sizes are returned. */
+int pgld_stat_terms(int32_t n_pops, pgld_term* out, int32_t capacity, int32_t* n_terms_out,
+                    int32_t* n_stats_out);
+
+/* Statistic columns from per-pair counts.  out is [n_pairs][out_ld] of
+ * out_dtype.  Replaces ld_statistics.dd/dz/pi2/r/r_squared/d_prime
+ * (ld_statistics.py:13-246), compute_two_pop_statistics_batch
+ * (ld_pipeline.py:271-322), compute_single_pop_statistics_batch
+ * (ld_pipeline.py:330-349) and compute_multi_pop_statistics_batch_hap
+ * (haplotype_kernels.py:584-640). */
+int pgld_hap_stats(pgld_handle h, const pgld_pair_counts* counts, int64_t n_pairs,
+                   const pgld_term* terms, int32_t n_terms, int32_t n_stats, void* out,
+                   int32_t out_dtype, int64_t out_ld, void* stream);
+
+/* Number of pairs i<j with pos[j] - pos[i] <= max_dist (synchronises).
+ * pos: device float64, sorted ascending.  offsets (nullable, device int64
+ * [n_snp + 1]) receives the exclusive prefix sum of the per-anchor pair
+ * counts (offsets[n_snp] = total), the quantity the reference's chunker
+ * cumulates (ld_pipeline.py:85-101). */
+int pgld_count_pairs_within(pgld_handle h, const double* pos, int64_t n_snp,
+                            double max_dist, int64_t* n_pairs_out, int64_t* offsets,
+                            void* stream);
+
+/* Pairs of the distance band whose first SNP lies in [i_begin, i_end), in
+ * the reference's order (i-major, j ascending), written to idx_i / idx_j;
+ * n_pairs must equal the number of such pairs (synchronises to check it).
+ * One call per chunk of ld_pipeline.iter_pairs_within_distance
+ * (ld_pipeline.py:57-122). */
+int pgld_pairs_within(pgld_handle h, const double* pos, int64_t n_snp, double max_dist,
+                      int64_t i_begin, int64_t i_end, int32_t* idx_i, int32_t* idx_j,
+                      int64_t n_pairs, void* stream);
+
+/* Per-pair outputs over the distance band of one population, in the
+ * reference's pair order: counts [n_pairs][4] int32, n_valid [n_pairs]
+ * (nullable), and stats [n_pairs][4] float32 = r^2, DD, Dz, pi2 (nullable).
+ * n_pairs must equal pgld_count_pairs_within's result.  Fuses
+ * iter_pairs_within_distance + compute_counts_for_pairs +
+ * compute_single_pop_statistics_batch + r_squared. */
+int pgld_hap_band_pairs(pgld_handle h, const pgld_hap_panel* panel, const double* pos,
+                        double max_dist, int32_t* counts, int32_t* n_valid, float* stats,
+                        int64_t n_pairs, int32_t form, void* stream);
+
+/* Distance-binned sums of the moments LD statistics of n_pops (1..4)
+ * populations over every pair i<j with pos[j]-pos[i] <= max_dist.
+ * The distance used for binning is bin_coord[j]-bin_coord[i] (bin_coord
+ * NULL: pos) in its absolute value; bins are right-open, [bins[k],
+ * bins[k+1]), digitize semantics.  sums: [n_bins][n_stats] float64
+ * (n_stats = 3, 15, 45, 105 in moments ld_names order), overwritten;
+ * pair_counts: [n_bins] int64, nullable.  Per-pair statistics are formed
+ * in float32 from exact integer numerators; bins accumulate in float64.
+ * Replaces moments_ld._compute_ld_sums (moments_ld.py:248-343) and
+ * HaplotypeMatrix.compute_ld_statistics_gpu_{single_pop,two_pops}
+ * (haplotype_matrix.py:1592-1866). */
+int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, const double* pos,
+                         double max_dist, const double* bin_coord, const double* bins,
+                         int32_t n_bins, double* sums, int64_t* pair_counts, int32_t form,
+                         void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PGLD_H */

@@ -1,0 +1,246 @@
+"""Device operations behind the reference-shaped API: packing, counting,
+statistic finalisation and distance-binned sums, all through libpgld.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _torch():
+    import torch
+    return torch
+
+
+# --------------------------------------------------------------------------
+# packed haplotype planes
+# --------------------------------------------------------------------------
+class PackedPop:
+    """Bit planes of one population (carrier / reference, optional validity).
+
+    ``has_missing`` mirrors the reference's ``cp.any(haplotypes == -1)`` over
+    the population's rows (ld_pipeline.py:158); ``has_other`` flags values
+    outside {-1, 0, 1}, for which the validity plane is kept.
+    """
+
+    def __init__(self, planes, valid, n_words, n_rows, n_snp, has_missing, has_other):
+        self.planes = planes
+        self.valid = valid
+        self.n_words = n_words
+        self.n_rows = n_rows
+        self.n_snp = n_snp
+        self.has_missing = has_missing
+        self.has_other = has_other
+
+    @property
+    def valid_for_n(self):
+        """Validity plane when the pairwise n differs from n11+n10+n01+n00."""
+        return self.valid if (self.has_other and self.has_missing) else None
+
+
+def pack(hap, rows=None):
+    """Pack the rows of an int8 (H x M) device matrix into bit planes."""
+    torch = _torch()
+    hap = L.as_device(hap, np.int8)
+    if hap.dim() != 2:
+        raise ValueError("haplotypes must be 2-D (n_haplotypes, n_variants)")
+    n_total, n_snp = hap.shape
+    if rows is not None:
+        rows_t = L.as_device(rows, np.int32)
+        if rows_t.numel() and (int(rows_t.min()) < 0 or int(rows_t.max()) >= n_total):
+            raise IndexError("population row index out of range")
+        n_rows = rows_t.numel()
+    else:
+        rows_t = None
+        n_rows = n_total
+    W = max(1, (n_rows + 31) // 32)
+    planes = torch.empty((n_snp, 2 * W), dtype=torch.int32, device=hap.device)
+    valid = torch.empty((n_snp, W), dtype=torch.int32, device=hap.device)
+    flags = torch.zeros(2, dtype=torch.int32, device=hap.device)
+    if n_rows == 0:
+        planes.zero_()
+        valid.zero_()
+    else:
+        h = L.handle()
+        L.check(L.lib().pgld_pack_haplotypes(h, L.ptr(hap), hap.stride(0), n_snp, L.ptr(rows_t),
+                                             n_rows, L.ptr(planes), L.ptr(valid), L.ptr(flags),
+                                             L.stream_ptr()), h)
+    f = flags.cpu().numpy()
+    return PackedPop(planes, valid, W, n_rows, n_snp, bool(f[0]), bool(f[1]))
+
+
+def panel(pops):
+    pn = L.HapPanel()
+    pn.n_pops = len(pops)
+    for p, pk in enumerate(pops):
+        pn.n_words[p] = pk.n_words
+        pn.planes[p] = pk.planes.data_ptr()
+        v = pk.valid_for_n
+        pn.valid[p] = v.data_ptr() if v is not None else None
+    pn.n_snp = pops[0].n_snp
+    return pn
+
+
+# --------------------------------------------------------------------------
+# counts
+# --------------------------------------------------------------------------
+def counts_pairs(pk, idx_i, idx_j):
+    """(counts int32 (N,4), n_valid int32 (N,) or None) for listed pairs."""
+    torch = _torch()
+    ii = L.as_device(idx_i, np.int32)
+    jj = L.as_device(idx_j, np.int32)
+    if ii.shape != jj.shape:
+        raise ValueError("idx_i and idx_j must have the same shape")
+    n = ii.numel()
+    counts = torch.empty((n, 4), dtype=torch.int32, device=ii.device)
+    nv = torch.empty(n, dtype=torch.int32, device=ii.device) if pk.has_missing else None
+    if n:
+        h = L.handle()
+        v = pk.valid_for_n
+        L.check(L.lib().pgld_hap_counts_pairs(h, L.ptr(pk.planes), L.ptr(v), pk.n_words, pk.n_snp,
+                                              L.ptr(ii), L.ptr(jj), n, L.ptr(counts), 4,
+                                              L.ptr(nv), L.stream_ptr()), h)
+        st = torch.zeros(1, dtype=torch.int32)
+        L.check(L.lib().pgld_device_status(h, ctypes.cast(st.data_ptr(), ctypes.POINTER(
+            ctypes.c_int32)), L.stream_ptr()), h)
+        if int(st[0]):
+            raise IndexError("pair index out of range of the variant axis")
+    return counts, nv
+
+
+def tally(pk):
+    torch = _torch()
+    m = pk.n_snp
+    n = m * (m - 1) // 2
+    counts = torch.empty((n, 4), dtype=torch.int32, device=pk.planes.device)
+    nv = torch.empty(n, dtype=torch.int32, device=pk.planes.device) if pk.has_missing else None
+    if n:
+        h = L.handle()
+        # tally_gpu_haplotypes counts validity as != -1 (haplotype_matrix.py:1398-1418)
+        L.check(L.lib().pgld_hap_tally(h, L.ptr(pk.planes), L.ptr(pk.valid_for_n), pk.n_words, m,
+                                       L.ptr(counts), L.ptr(nv), L.stream_ptr()), h)
+    return counts, nv
+
+
+# --------------------------------------------------------------------------
+# statistics
+# --------------------------------------------------------------------------
+def make_terms(term_list):
+    """[(stat, kind, pops, weight)] -> ctypes array of Term."""
+    arr = (L.Term * len(term_list))()
+    for k, (stat, kind, pops, w) in enumerate(term_list):
+        arr[k].stat = stat
+        arr[k].kind = kind
+        pp = list(pops) + [0] * (4 - len(pops))
+        for q in range(4):
+            arr[k].pops[q] = pp[q]
+        arr[k].weight = w
+    return arr
+
+
+def stats(pop_counts, pop_nvalid, term_list, n_stats, dtype="f64"):
+    """Statistic columns (N, n_stats) from per-pop counts views.
+
+    pop_counts[p]: int32 CUDA tensor view with shape (N, >=4) and unit inner
+    stride; pop_nvalid[p]: int32 CUDA tensor (N,) (any stride) or None.
+    """
+    torch = _torch()
+    n = pop_counts[0].shape[0]
+    out = torch.empty((n, n_stats), dtype=torch.float64 if dtype == "f64" else torch.float32,
+                      device=pop_counts[0].device)
+    if n == 0:
+        return out
+    pc = L.PairCounts()
+    pc.n_pops = len(pop_counts)
+    for p, c in enumerate(pop_counts):
+        if c.dtype != torch.int32 or c.stride(1) != 1:
+            raise ValueError("counts must be int32 with unit column stride")
+        pc.counts[p] = c.data_ptr()
+        pc.counts_ld[p] = c.stride(0)
+        nv = pop_nvalid[p]
+        if nv is not None:
+            if nv.dtype != torch.int32:
+                raise ValueError("n_valid must be int32")
+            pc.n_valid[p] = nv.data_ptr()
+            pc.nvalid_ld[p] = nv.stride(0)
+    terms = make_terms(term_list)
+    h = L.handle()
+    L.check(L.lib().pgld_hap_stats(h, ctypes.byref(pc), n, terms, len(term_list), n_stats,
+                                   L.ptr(out), L.F64 if dtype == "f64" else L.F32, n_stats,
+                                   L.stream_ptr()), h)
+    return out
+
+
+# --------------------------------------------------------------------------
+# distance band
+# --------------------------------------------------------------------------
+def band_offsets(pos_d, max_dist):
+    torch = _torch()
+    m = pos_d.numel()
+    off = torch.empty(m + 1, dtype=torch.int64, device=pos_d.device)
+    tot = ctypes.c_int64()
+    h = L.handle()
+    L.check(L.lib().pgld_count_pairs_within(h, L.ptr(pos_d), m, float(max_dist), ctypes.byref(tot),
+                                            L.ptr(off), L.stream_ptr()), h)
+    return off, int(tot.value)
+
+
+def pairs_range(pos_d, max_dist, i_begin, i_end, n_pairs):
+    torch = _torch()
+    ii = torch.empty(n_pairs, dtype=torch.int32, device=pos_d.device)
+    jj = torch.empty(n_pairs, dtype=torch.int32, device=pos_d.device)
+    h = L.handle()
+    L.check(L.lib().pgld_pairs_within(h, L.ptr(pos_d), pos_d.numel(), float(max_dist), i_begin,
+                                      i_end, L.ptr(ii), L.ptr(jj), n_pairs, L.stream_ptr()), h)
+    return ii, jj
+
+
+def positions_f64(positions):
+    return L.as_device(positions, np.float64)
+
+
+def band_pairs(pk, pos_d, max_dist, with_stats=True):
+    """Fused per-pair outputs of one population over the distance band.
+
+    Returns (counts (N,4) int32, n_valid (N,) int32, stats (N,4) float32 =
+    r^2, DD, Dz, pi2 or None).
+    """
+    torch = _torch()
+    _, n = band_offsets(pos_d, max_dist)
+    dev = pos_d.device
+    counts = torch.empty((n, 4), dtype=torch.int32, device=dev)
+    nv = torch.empty(n, dtype=torch.int32, device=dev)
+    st = torch.empty((n, 4), dtype=torch.float32, device=dev) if with_stats else None
+    h = L.handle()
+    L.check(L.lib().pgld_hap_band_pairs(h, ctypes.byref(panel([pk])), L.ptr(pos_d),
+                                        float(max_dist), L.ptr(counts), L.ptr(nv), L.ptr(st), n,
+                                        L.FORM_PLAIN, L.stream_ptr()), h)
+    return counts, nv, st
+
+
+def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="plain"):
+    """(sums (n_bins, n_stats) float64 tensor, pair counts (n_bins,) int64)."""
+    torch = _torch()
+    bins_np = np.asarray(bins, dtype=np.float64)
+    if bins_np.ndim != 1 or len(bins_np) < 2:
+        raise ValueError("bins must hold at least two edges")
+    if np.any(np.diff(bins_np) <= 0):
+        raise ValueError("bins must be strictly increasing")
+    n_bins = len(bins_np) - 1
+    P = len(pops)
+    n_stats = {1: 3, 2: 15, 3: 45, 4: 105}[P]
+    dev = pos_d.device
+    bins_d = torch.as_tensor(bins_np, device=dev)
+    sums = torch.empty((n_bins, n_stats), dtype=torch.float64, device=dev)
+    cnt = torch.empty(n_bins, dtype=torch.int64, device=dev)
+    md = float(bins_np[-1]) if max_dist is None else float(max_dist)
+    bc = None if bin_coord is None else L.as_device(bin_coord, np.float64)
+    h = L.handle()
+    L.check(L.lib().pgld_hap_binned_sums(h, ctypes.byref(panel(pops)), L.ptr(pos_d), md, L.ptr(bc),
+                                         L.ptr(bins_d), n_bins, L.ptr(sums), L.ptr(cnt),
+                                         L.FORM_TC if form == "tc" else L.FORM_PLAIN,
+                                         L.stream_ptr()), h)
+    return sums, cnt

@@ -1,0 +1,48 @@
+// Shared declarations of the distance-band kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pgld_internal.cuh"
+
+int pgld_band_offsets(pgld_context* h, const double* pos, long long n_snp, double max_dist,
+                      long long* off, void* scratch, size_t scratch_bytes, cudaStream_t st);
+
+namespace pgld {
+
+constexpr int kTile = 32;      // SNPs per tile side of the plain band kernel
+constexpr int kMaxBins = 64;   // distance bins per call
+constexpr int kModeBinned = 0;
+constexpr int kModePairs = 1;
+
+struct BandArgs {
+  int n_pops;
+  int W[PGLD_MAX_POPS];
+  const uint32_t* planes[PGLD_MAX_POPS];
+  const uint32_t* valid[PGLD_MAX_POPS];
+  long long n_snp;
+  const double* pos;
+  double max_dist;
+  const double* bcoord;  // binning coordinate (NULL: pos)
+  const double* bins;
+  int n_bins;
+  const long long* item_off;  // [n_blocks + 1] tile work list offsets
+  long long n_blocks;
+  // binned mode
+  double* sums;
+  int64_t* pair_counts;
+  const pgld_term* terms;
+  int n_terms;
+  int n_stats;
+  // pairs mode
+  const long long* pair_off;
+  int32_t* counts;
+  int32_t* nvalid;
+  float* stats;
+};
+
+int band_schedule(pgld_context* h, const double* pos, long long n_snp, double max_dist,
+                  long long* items, void* scratch, size_t scratch_bytes, cudaStream_t st);
+int launch_band_plain(pgld_context* h, const BandArgs& a, int mode, cudaStream_t st);
+
+}  // namespace pgld

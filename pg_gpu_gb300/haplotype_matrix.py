@@ -1,0 +1,354 @@
+"""HaplotypeMatrix: the reference container and its LD methods on libpgld.
+
+Mirrors pg_gpu.haplotype_matrix.HaplotypeMatrix (haplotype_matrix.py:34-170)
+for the data it holds (an int8 (n_haplotypes, n_variants) matrix with 1 / 0 /
+-1, sorted positions, named sample sets) and re-implements its two-locus LD
+methods (haplotype_matrix.py:1092-1866).  'GPU' storage is a CUDA torch
+tensor; packed bit planes of each population are cached after first use.
+"""
+from __future__ import annotations
+
+import gzip
+from collections import OrderedDict
+
+import numpy as np
+
+from . import _lib as L
+from . import _ops
+
+
+def _is_torch(x):
+    try:
+        import torch
+        return isinstance(x, torch.Tensor)
+    except ImportError:
+        return False
+
+
+class HaplotypeMatrix:
+    def __init__(self, genotypes, positions, chrom_start=None, chrom_end=None,
+                 sample_sets=None, n_total_sites=None, samples=None, accessible_mask=None):
+        g_dev = _is_torch(genotypes) or hasattr(genotypes, "__cuda_array_interface__")
+        if not g_dev and not isinstance(genotypes, np.ndarray):
+            raise ValueError("genotypes must be a numpy array or a CUDA array")
+        size = genotypes.numel() if _is_torch(genotypes) else np.asarray(genotypes).size \
+            if not g_dev else int(np.prod(genotypes.shape))
+        if size == 0:
+            raise ValueError("genotypes cannot be empty")
+        if len(positions) == 0:
+            raise ValueError("positions cannot be empty")
+        if g_dev:
+            self._device = "GPU"
+            self._haplotypes = L.as_device(genotypes, np.int8)
+            self._positions = L.as_device(positions)
+        else:
+            self._device = "CPU"
+            self._haplotypes = np.asarray(genotypes)
+            self._positions = np.asarray(positions.cpu().numpy() if _is_torch(positions)
+                                         else positions)
+        self.chrom_start = chrom_start
+        self.chrom_end = chrom_end
+        self._sample_sets = None
+        if sample_sets is not None:
+            self.sample_sets = sample_sets
+        self.n_total_sites = n_total_sites
+        self.samples = samples
+        self.accessible_mask = accessible_mask
+        self._packed = {}
+
+    # ------------------------------------------------------------------ data
+    @property
+    def haplotypes(self):
+        return self._haplotypes
+
+    @haplotypes.setter
+    def haplotypes(self, value):
+        self._haplotypes = value
+        self._packed = {}
+
+    @property
+    def positions(self):
+        return self._positions
+
+    @positions.setter
+    def positions(self, value):
+        self._positions = value
+
+    @property
+    def device(self):
+        return self._device
+
+    @property
+    def num_haplotypes(self):
+        return int(self._haplotypes.shape[0])
+
+    @property
+    def num_variants(self):
+        return int(self._haplotypes.shape[1])
+
+    @property
+    def shape(self):
+        return tuple(self._haplotypes.shape)
+
+    @property
+    def sample_sets(self):
+        if self._sample_sets is None:
+            return {"all": list(range(self.num_haplotypes))}
+        return self._sample_sets
+
+    @sample_sets.setter
+    def sample_sets(self, sample_sets):
+        if not isinstance(sample_sets, dict):
+            raise ValueError("sample_sets must be a dictionary")
+        for v in sample_sets.values():
+            if not isinstance(v, list):
+                raise ValueError("values in sample_sets must be lists")
+        self._sample_sets = sample_sets
+        self._packed = {}
+
+    def transfer_to_gpu(self):
+        if self._device == "CPU":
+            self._haplotypes = L.as_device(self._haplotypes, np.int8)
+            self._positions = L.as_device(self._positions)
+            self._device = "GPU"
+
+    def transfer_to_cpu(self):
+        if self._device == "GPU":
+            self._haplotypes = self._haplotypes.cpu().numpy()
+            self._positions = self._positions.cpu().numpy()
+            self._device = "CPU"
+            self._packed = {}
+
+    def _pos_np(self):
+        p = self._positions
+        return p.cpu().numpy() if _is_torch(p) else np.asarray(p)
+
+    def get_subset(self, positions_idx):
+        idx = np.asarray(positions_idx.cpu().numpy() if _is_torch(positions_idx)
+                         else positions_idx)
+        if self._device == "GPU":
+            import torch
+            ti = torch.as_tensor(idx, device=self._haplotypes.device, dtype=torch.int64)
+            hap = self._haplotypes.index_select(1, ti)
+            pos = self._positions.index_select(0, ti)
+        else:
+            hap = self._haplotypes[:, idx]
+            pos = self._positions[idx]
+        return HaplotypeMatrix(hap, pos, self.chrom_start, self.chrom_end, self._sample_sets,
+                               self.n_total_sites, self.samples)
+
+    def apply_biallelic_filter(self):
+        """Keep sites with both 0 and 1 and no value >= 2 (haplotype_matrix.py:724-789)."""
+        if self._device == "GPU":
+            h = self._haplotypes
+            keep = ((h >= 2).sum(0) == 0) & ((h == 0).sum(0) > 0) & ((h == 1).sum(0) > 0)
+            idx = keep.nonzero().flatten()
+        else:
+            h = self._haplotypes
+            keep = (np.sum(h >= 2, 0) == 0) & (np.sum(h == 0, 0) > 0) & (np.sum(h == 1, 0) > 0)
+            idx = np.where(keep)[0]
+        out = self.get_subset(idx)
+        if len(idx):
+            pos = out._pos_np()
+            out.chrom_start, out.chrom_end = int(pos[0]), int(pos[-1])
+        return out
+
+    @classmethod
+    def from_vcf(cls, path, region=None, samples=None, include_invariant=False,
+                 accessible_bed=None):
+        """Phased GT of a plain or gzipped VCF; rows = all hap-0 then all hap-1
+        (haplotype_matrix.py:324-328)."""
+        if region is not None:
+            raise NotImplementedError("region queries need a tabix reader")
+        opener = gzip.open if str(path).endswith(".gz") else open
+        names, gts, pos = None, [], []
+        with opener(path, "rt") as f:
+            for line in f:
+                if line.startswith("##"):
+                    continue
+                parts = line.rstrip("\n").split("\t")
+                if line.startswith("#CHROM"):
+                    names = parts[9:]
+                    continue
+                pos.append(int(parts[1]))
+                row = []
+                for g in parts[9:]:
+                    gt = g.split(":")[0].replace("/", "|").split("|")
+                    a = -1 if gt[0] in (".", "") else int(gt[0])
+                    b = -1 if len(gt) < 2 or gt[1] in (".", "") else int(gt[1])
+                    row.append((a, b))
+                gts.append(row)
+        if not gts:
+            raise ValueError(f"No variants found in {path}")
+        gt = np.asarray(gts, dtype=np.int8)
+        keep_s = np.arange(gt.shape[1])
+        if samples is not None:
+            keep_s = np.array([names.index(s) for s in samples])
+            names = list(samples)
+        gt = gt[:, keep_s, :]
+        n = gt.shape[1]
+        hap = np.empty((gt.shape[0], 2 * n), np.int8)
+        hap[:, :n] = gt[:, :, 0]
+        hap[:, n:] = gt[:, :, 1]
+        pos = np.asarray(pos, np.int64)
+        return cls(np.ascontiguousarray(hap.T), pos, int(pos[0]), int(pos[-1]),
+                   samples=list(names),
+                   n_total_sites=gt.shape[0] if include_invariant else None)
+
+    # ------------------------------------------------------------- packing
+    def _pop_rows(self, pop):
+        if pop is None:
+            return None
+        if self._sample_sets is None:
+            raise ValueError("sample_sets must be defined to use pop parameter")
+        if pop not in self._sample_sets:
+            raise KeyError(f"Population key {pop} must exist in sample_sets")
+        return self._sample_sets[pop]
+
+    def packed(self, pop=None):
+        """Cached bit planes of a population (None: every haplotype)."""
+        self.transfer_to_gpu()
+        key = pop
+        if key not in self._packed:
+            rows = self._pop_rows(pop)
+            self._packed[key] = _ops.pack(self._haplotypes, rows)
+        return self._packed[key]
+
+    # ------------------------------------------------------------ LD methods
+    def tally_gpu_haplotypes(self, pop=None):
+        """All-pairs [n11,n10,n01,n00] and n_valid or None (haplotype_matrix.py:1320-1434).
+
+        Exact at any sample size (the reference's no-missing int8 X.T@X wraps
+        at 128 haplotypes)."""
+        return _ops.tally(self.packed(pop))
+
+    def tally_gpu_haplotypes_two_pops(self, pop1, pop2):
+        """(counts (N,8), n_valid1, n_valid2) (haplotype_matrix.py:1518-1589)."""
+        import torch
+        if self._sample_sets is None:
+            raise ValueError("sample_sets must be defined to use this function")
+        if pop1 not in self._sample_sets or pop2 not in self._sample_sets:
+            raise KeyError(f"Population keys {pop1} and {pop2} must exist in sample_sets")
+        c1, nv1 = _ops.tally(self.packed(pop1))
+        c2, nv2 = _ops.tally(self.packed(pop2))
+        any_missing = bool((self._haplotypes == -1).any())
+        if any_missing:
+            nv1 = nv1 if nv1 is not None else c1.sum(1, dtype=torch.int32)
+            nv2 = nv2 if nv2 is not None else c2.sum(1, dtype=torch.int32)
+            return torch.cat([c1, c2], 1), nv1, nv2
+        return torch.cat([c1, c2], 1), None, None
+
+    def _binned(self, bp_bins, pops):
+        bins = np.asarray(bp_bins, dtype=np.float64)
+        packs = [self.packed(p) for p in pops]
+        sums, cnt = _ops.binned_sums(packs, _ops.positions_f64(self._positions), bins)
+        return bins, sums.cpu().numpy(), cnt.cpu().numpy()
+
+    def compute_ld_statistics_gpu_single_pop(self, bp_bins, raw=False, ac_filter=True,
+                                             chunk_size="auto"):
+        """{(lo, hi): (DD, Dz, pi2)} sums or means per bin (haplotype_matrix.py:1592-1716)."""
+        if ac_filter:
+            return self.apply_biallelic_filter().compute_ld_statistics_gpu_single_pop(
+                bp_bins, raw=raw, ac_filter=False, chunk_size=chunk_size)
+        bins, sums, cnt = self._binned(bp_bins, [None])
+        out = {}
+        for i in range(len(bins) - 1):
+            key = (float(bins[i]), float(bins[i + 1]))
+            if raw:
+                out[key] = tuple(float(v) for v in sums[i])
+            elif cnt[i] > 0:
+                out[key] = tuple(float(v) for v in sums[i] / cnt[i])
+            else:
+                out[key] = (0.0, 0.0, 0.0)
+        return out
+
+    def compute_ld_statistics_gpu_two_pops(self, bp_bins, pop1, pop2, raw=False,
+                                           ac_filter=True, chunk_size="auto"):
+        """{(lo, hi): OrderedDict of the 15 statistics} (haplotype_matrix.py:1719-1866)."""
+        if ac_filter:
+            return self.apply_biallelic_filter().compute_ld_statistics_gpu_two_pops(
+                bp_bins, pop1, pop2, raw=raw, ac_filter=False, chunk_size=chunk_size)
+        from .ld_pipeline import ld_names
+        names = ld_names(2)
+        bins, sums, cnt = self._binned(bp_bins, [pop1, pop2])
+        out = {}
+        for i in range(len(bins) - 1):
+            key = (float(bins[i]), float(bins[i + 1]))
+            if raw:
+                out[key] = OrderedDict((n, float(v)) for n, v in zip(names, sums[i]))
+            elif cnt[i] > 0:
+                out[key] = OrderedDict((n, float(v) / cnt[i]) for n, v in zip(names, sums[i]))
+            else:
+                out[key] = OrderedDict((n, 0.0) for n in names)
+        return out
+
+    def windowed_r_squared(self, bp_bins, percentile=50, pop=None, estimator="r2"):
+        """Percentiles of r^2 per distance bin and pair counts (haplotype_matrix.py:1235-1317)."""
+        import torch
+        if estimator == "rogers_huff":
+            raise NotImplementedError("estimator='rogers_huff' goes through GenotypeMatrix")
+        if estimator != "r2":
+            raise ValueError(f"Unknown estimator: {estimator!r} (expected 'r2' or 'rogers_huff')")
+        from .ld_statistics import r_squared
+        counts, nv = self.tally_gpu_haplotypes(pop=pop)
+        r2 = r_squared(counts, nv)
+        m = self.num_variants
+        ii, jj = torch.triu_indices(m, m, 1, device=r2.device)
+        pos = _ops.positions_f64(self._positions)
+        d = (pos[jj] - pos[ii]).cpu().numpy()
+        bins = np.asarray(bp_bins, dtype=np.float64)
+        nb = len(bins) - 1
+        b = np.digitize(d, bins) - 1
+        r2c = r2.cpu().numpy()
+        ok = (b >= 0) & (b < nb) & ~np.isnan(r2c)
+        percentile = np.atleast_1d(percentile)
+        res = np.full((nb, len(percentile)), np.nan)
+        pc = np.zeros(nb, dtype=int)
+        for i in range(nb):
+            sel = r2c[ok & (b == i)]
+            pc[i] = sel.size
+            if sel.size:
+                res[i] = np.percentile(sel, percentile)
+        return (res[:, 0] if res.shape[1] == 1 else res), pc
+
+    def pairwise_r2(self, estimator="r2"):
+        """(m, m) r^2 from joint frequencies, zero diagonal (haplotype_matrix.py:1138-1170)."""
+        import torch
+        if estimator != "r2":
+            raise ValueError(f"Unknown estimator: {estimator!r} (expected 'r2' or 'rogers_huff')")
+        D, p = self._pairwise_ld_core()
+        pq = p * (1 - p)
+        den = torch.outer(pq, pq)
+        r2 = torch.where(den > 0, D * D / torch.where(den > 0, den, 1.0), 0.0)
+        r2.fill_diagonal_(0)
+        return r2
+
+    def pairwise_LD_v(self):
+        D, _ = self._pairwise_ld_core()
+        D.fill_diagonal_(0)
+        return D
+
+    def _pairwise_ld_core(self):
+        """D = pAB - pA pB and per-site p from all-pairs counts (haplotype_matrix.py:1092-1130)."""
+        import torch
+        m = self.num_variants
+        counts, nv = self.tally_gpu_haplotypes()
+        pk = self.packed(None)
+        h = self._haplotypes
+        valid = (h >= 0).sum(0).to(torch.float64)
+        p = torch.where(valid > 0, h.clamp(min=0).sum(0).to(torch.float64) /
+                        torch.where(valid > 0, valid, 1.0), 0.0)
+        c = counts.to(torch.float64)
+        n = c.sum(1) if nv is None else nv.to(torch.float64)
+        # joint_n counts hap >= 0 at both sites; with only 0/1/-1 data that is n
+        if pk.has_other:
+            raise NotImplementedError("pairwise LD of non-biallelic codes")
+        pab = torch.where(n > 0, c[:, 0] / torch.where(n > 0, n, 1.0), 0.0)
+        ii, jj = torch.triu_indices(m, m, 1, device=c.device)
+        P = torch.zeros((m, m), dtype=torch.float64, device=c.device)
+        P[ii, jj] = pab
+        P[jj, ii] = pab
+        diag = torch.where(valid > 0, h.clamp(min=0).sum(0).to(torch.float64) /
+                           torch.where(valid > 0, valid, 1.0), 0.0)
+        P[torch.arange(m), torch.arange(m)] = diag
+        return P - torch.outer(p, p), p

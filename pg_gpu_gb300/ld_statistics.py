@@ -1,0 +1,172 @@
+"""Drop-in for the LD-statistic functions of pg_gpu.ld_statistics.
+
+dd / dz / pi2 / r / r_squared / d_prime / compute_ld_statistics keep the
+reference signatures (ld_statistics.py:13-246, 1030-1079) and population /
+n_valid conventions (ld_statistics.py:1082-1113); the arithmetic runs in
+libpgld with exact 64-bit integer numerators and a single float64 division,
+so results equal the reference's float64 values wherever its own evaluation
+is exact, and stay exact where its int32 fast path would wrap.
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Optional, Tuple, Union
+
+import numpy as np
+
+from . import _lib as L
+from . import _ops
+from .ld_pipeline import case_of
+
+__all__ = ["dd", "dz", "pi2", "dd_within", "dd_between", "r", "r_squared", "d_prime",
+           "compute_ld_statistics", "rogers_huff_r", "rogers_huff_r_squared"]
+
+
+def _counts(counts):
+    c = L.as_device(counts, np.int32)
+    if c.dim() != 2 or c.shape[1] % 4 != 0 or c.shape[1] == 0:
+        raise ValueError("counts must have shape (N, 4*P)")
+    return c
+
+
+def _nv_tensor(x):
+    return None if x is None else L.as_device(x, np.int32)
+
+
+def _pop_views(c, n_valid, pops_needed):
+    """Per-population (counts view, n_valid view or None), as _get_pop_data."""
+    P = c.shape[1] // 4
+    views, nvs = [], []
+    nv2d = None
+    if n_valid is not None and not isinstance(n_valid, tuple):
+        nv2d = _nv_tensor(n_valid)
+    tup = None
+    if isinstance(n_valid, tuple):
+        tup = [(_nv_tensor(x) if x is not None else None) for x in n_valid]
+    for p in range(P):
+        views.append(c[:, 4 * p:4 * p + 4])
+        if n_valid is None:
+            nvs.append(None)
+        elif tup is not None:
+            nvs.append(tup[p] if p < len(tup) else None)
+        elif nv2d.dim() == 2:
+            nvs.append(nv2d[:, p])
+        else:
+            nvs.append(nv2d)
+    return views, nvs
+
+
+def _one(counts, n_valid, kind, roles, views=None, nvs=None):
+    c = _counts(counts)
+    if views is None:
+        views, nvs = _pop_views(c, n_valid, None)
+    out = _ops.stats(views, nvs, [(0, kind, roles, 1.0)], 1)
+    return out[:, 0]
+
+
+def dd(counts, populations: Optional[Union[Tuple[int, int], int]] = None,
+       n_valid=None):
+    """D^2 for one population or between two (ld_statistics.py:13-65)."""
+    c = _counts(counts)
+    if populations is None:
+        if c.shape[1] == 4:
+            return _one(c, n_valid, L.DD_II, (0,))
+        nv = n_valid
+        if nv is not None and not isinstance(nv, tuple):
+            t = _nv_tensor(nv)
+            nv = t[:, 0] if t.dim() == 2 else t
+        return _one(c[:, :4], nv, L.DD_II, (0,))
+    a, b = populations
+    if a == b:
+        return _one(c, n_valid, L.DD_II, (a,))
+    views, nvs = _pop_views(c, n_valid, None)
+    if isinstance(n_valid, tuple):
+        # _dd_between reads the tuple by position (ld_statistics.py:1145-1147)
+        nvs = list(nvs)
+        t0 = _nv_tensor(n_valid[0]) if len(n_valid) > 0 else None
+        t1 = _nv_tensor(n_valid[1]) if len(n_valid) > 1 else None
+        nvs[a], nvs[b] = t0, t1
+    return _one(c, n_valid, L.DD_IJ, (a, b), views, nvs)
+
+
+def dz(counts, populations: Optional[Tuple[int, int, int]] = None, n_valid=None):
+    """Dz for any population triple (ld_statistics.py:68-97)."""
+    c = _counts(counts)
+    if populations is None:
+        if c.shape[1] == 4:
+            return _one(c, n_valid, L.DZ_III, (0,))
+        populations = (0, 0, 0)
+    kind, roles = case_of("dz", tuple(populations))
+    return _one(c, n_valid, kind, roles)
+
+
+def pi2(counts, populations: Optional[Tuple[int, int, int, int]] = None, n_valid=None):
+    """pi2 for any population quadruple (ld_statistics.py:100-129, 1299-1412)."""
+    c = _counts(counts)
+    if populations is None:
+        if c.shape[1] == 4:
+            return _one(c, n_valid, L.PI2_IIII, (0,))
+        populations = (0, 0, 0, 0)
+    kind, roles = case_of("pi2", tuple(populations), symmetric_iikk=True)
+    return _one(c, n_valid, kind, roles)
+
+
+def dd_within(counts, n_valid=None):
+    return dd(counts, None, n_valid)
+
+
+def dd_between(counts, pop1_idx: int, pop2_idx: int, n_valid=None):
+    return dd(counts, (pop1_idx, pop2_idx), n_valid)
+
+
+def _r_family(counts, n_valid, kind):
+    c = _counts(counts)[:, :4]
+    nv = _nv_tensor(n_valid)
+    out = _ops.stats([c], [nv], [(0, kind, (0,), 1.0)], 1)
+    return out[:, 0]
+
+
+def r(counts, n_valid=None):
+    """Signed r from counts, NaN where undefined (ld_statistics.py:167-191)."""
+    return _r_family(counts, n_valid, L.R)
+
+
+def r_squared(counts, n_valid=None):
+    """r^2 from counts, NaN where undefined (ld_statistics.py:194-217)."""
+    return _r_family(counts, n_valid, L.R2)
+
+
+def d_prime(counts, n_valid=None):
+    """Lewontin's D', NaN where undefined (ld_statistics.py:220-246)."""
+    return _r_family(counts, n_valid, L.DPRIME)
+
+
+def compute_ld_statistics(counts, statistics: List[str] = ("dd", "dz", "pi2"),
+                          populations: Optional[Dict[str, Union[Tuple, None]]] = None,
+                          n_valid=None) -> Dict:
+    """Several statistics in one call (ld_statistics.py:1030-1079)."""
+    populations = populations or {}
+    out = {}
+    for stat in statistics:
+        if stat == "dd":
+            out["dd"] = dd(counts, populations.get("dd"), n_valid)
+        elif stat == "dz":
+            out["dz"] = dz(counts, populations.get("dz"), n_valid)
+        elif stat == "pi2":
+            out["pi2"] = pi2(counts, populations.get("pi2"), n_valid)
+        elif stat == "r":
+            out["r"] = r(counts, n_valid)
+        elif stat == "r_squared":
+            out["r_squared"] = r_squared(counts, n_valid)
+        else:
+            raise ValueError(f"Unknown statistic: {stat}")
+    return out
+
+
+def rogers_huff_r(matrix, tile_size=None):
+    """Condensed Rogers-Huff r of all variant pairs (ld_statistics.py:492-521)."""
+    from . import _geno
+    return _geno.rogers_huff_r(matrix)
+
+
+def rogers_huff_r_squared(matrix, tile_size=None):
+    return rogers_huff_r(matrix) ** 2

@@ -1,0 +1,251 @@
+"""GPU parity of the haplotype LD path against the reference fixtures and the oracle.
+
+Counts are compared bit-for-bit.  float64 statistics come from exact integer
+numerators divided once, so they match the reference to 1e-13 relative.
+float32 per-pair statistics are held to 1e-6 relative of the float64 oracle.
+Binned sums are held to |gpu - oracle| <= 2e-6 * sum|x| per bin and
+statistic (float32 per-pair values, float64 accumulation).
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import ld_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+from pg_gpu_gb300 import _ops, haplotype_kernels, ld_pipeline, ld_statistics  # noqa: E402
+from pg_gpu_gb300._lib import PgldError  # noqa: E402
+
+SUM_TOL = 2e-6
+
+
+def np_(t):
+    return None if t is None else t.cpu().numpy()
+
+
+def _close(a, b, rtol=1e-13, atol=0.0):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = ~np.isnan(a)
+    np.testing.assert_allclose(a[m], b[m], rtol=rtol, atol=atol)
+
+
+def copying_model(rng, H, M, F, switch, missing=0.0, flip=1e-3):
+    p = rng.beta(0.3, 0.3, size=M)
+    f = (rng.random((F, M)) < p).astype(np.int8)
+    sw = rng.random((H, M)) < switch
+    seg = np.cumsum(sw, axis=1)
+    choice = rng.integers(0, F, size=(H, seg.max() + 1))
+    hap = f[np.take_along_axis(choice, seg, axis=1), np.arange(M)[None, :]]
+    hap ^= (rng.random(hap.shape) < flip).astype(np.int8)
+    if missing:
+        hap[rng.random(hap.shape) < missing] = -1
+    return hap.astype(np.int8)
+
+
+# --------------------------------------------------------------------------
+# reference fixtures
+# --------------------------------------------------------------------------
+def test_counts_match_reference(golden):
+    z = golden("hap_counts")
+    for tag, rows in (("all", None), ("a", z["rows_a"]), ("b", z["rows_b"])):
+        c, nv = ld_pipeline.compute_counts_for_pairs(z["hap"], z["idx_i"], z["idx_j"], rows)
+        assert np.array_equal(np_(c), z[f"counts_{tag}"])
+        assert np.array_equal(np_(nv), z[f"nvalid_{tag}"])
+    c, nv = ld_pipeline.compute_counts_for_pairs(z["hap_nomiss"], z["idx_i"], z["idx_j"])
+    assert nv is None and np.array_equal(np_(c), z["counts_nomiss"])
+
+
+def test_pair_chunks_match_reference(golden):
+    z = golden("hap_counts")
+    chunks = list(ld_pipeline.iter_pairs_within_distance(z["pos"], float(z["max_dist"]),
+                                                         int(z["chunk_size"])))
+    assert [len(c[0]) for c in chunks] == list(z["chunk_len"])
+    assert np.array_equal(np.concatenate([np_(c[0]) for c in chunks]), z["idx_i"])
+    assert np.array_equal(np.concatenate([np_(c[1]) for c in chunks]), z["idx_j"])
+    for cs, md in ((1, 2000.0), (10_000, 60_000.0), (50, 0.0)):
+        key = f"chunks_{cs}_{int(md)}"
+        ch = list(ld_pipeline.iter_pairs_within_distance(z["pos"], md, cs))
+        assert [len(c[0]) for c in ch] == list(z[key + "_len"])
+        if ch:
+            assert np.array_equal(np.concatenate([np_(c[0]) for c in ch]), z[key + "_i"])
+            assert np.array_equal(np.concatenate([np_(c[1]) for c in ch]), z[key + "_j"])
+    assert list(ld_pipeline.iter_pairs_within_distance(np.array([5.0]), 10, 10)) == []
+
+
+def test_public_statistics_match_reference(golden):
+    z = golden("hap_stats")
+    c, nv = z["counts"], z["nvalid"]
+    for pp in itertools.product(range(4), repeat=2):
+        _close(np_(ld_statistics.dd(c, pp, nv)), z["dd_" + "".join(map(str, pp))])
+    for pp in itertools.product(range(4), repeat=3):
+        _close(np_(ld_statistics.dz(c, pp, nv)), z["dz_" + "".join(map(str, pp))])
+    for pp in itertools.product(range(4), repeat=4):
+        _close(np_(ld_statistics.pi2(c, pp, nv)), z["pi2_" + "".join(map(str, pp))])
+    c4 = c[:, :4]
+    _close(np_(ld_statistics.dd(c4)), z["dd_single_nonv"])
+    _close(np_(ld_statistics.dz(c4)), z["dz_single_nonv"])
+    _close(np_(ld_statistics.pi2(c4)), z["pi2_single_nonv"])
+    for f in ("r", "r_squared", "d_prime"):
+        _close(np_(getattr(ld_statistics, f)(c4, nv[:, 0])), z[f + "_nv"], rtol=1e-12)
+        _close(np_(getattr(ld_statistics, f)(c4)), z[f + "_nonv"], rtol=1e-12)
+
+
+def test_batches_match_reference(golden):
+    z = golden("hap_stats")
+    c, nv = z["counts"], z["nvalid"]
+    for p in range(1, 5):
+        cs = [c[:, 4 * q:4 * q + 4] for q in range(p)]
+        got = haplotype_kernels.compute_multi_pop_statistics_batch_hap(
+            cs, [nv[:, q] for q in range(p)], None, ld_pipeline.generate_stat_specs(p))
+        _close(np_(got), z[f"multi_{p}"])
+        got = haplotype_kernels.compute_multi_pop_statistics_batch_hap(
+            cs, [None] * p, None, ld_pipeline.generate_stat_specs(p))
+        _close(np_(got), z[f"multi_{p}_nonv"])
+    _close(np_(ld_pipeline.compute_two_pop_statistics_batch(c[:, :4], c[:, 4:8], nv[:, 0],
+                                                            nv[:, 1])), z["two_pop"], rtol=1e-14)
+    _close(np_(ld_pipeline.compute_two_pop_statistics_batch(c[:, :4], c[:, 4:8], None, None)),
+           z["two_pop_nonv"], rtol=1e-14)
+    _close(np_(ld_pipeline.compute_single_pop_statistics_batch(c[:, :4], nv[:, 0])),
+           z["single_pop"])
+
+
+def _binned_check(hap, pos, rows, bins, form="plain"):
+    hap_d = torch.as_tensor(hap, device="cuda")
+    pops = [_ops.pack(hap_d, r) for r in rows]
+    sums, cnt = _ops.binned_sums(pops, _ops.positions_f64(pos), bins, form=form)
+    ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True)
+    assert np.array_equal(np_(cnt), ref_cnt)
+    err = np.abs(np_(sums) - ref)
+    assert np.all(err <= SUM_TOL * ref_abs + 1e-300), float((err / np.maximum(ref_abs, 1e-300)).max())
+    return np_(sums), ref_abs
+
+
+def _near(got, want, scale):
+    assert np.all(np.abs(got - want) <= SUM_TOL * scale + 1e-12 * np.abs(want))
+
+
+def test_binned_sums_match_reference(golden):
+    z = golden("binned")
+    rows = [z["rows0"], z["rows1"]]
+    s2, a2 = _binned_check(z["hap"], z["pos"], rows, z["bins"])
+    _near(s2, z["sums_2pop"], a2)
+    s1, a1 = _binned_check(z["hap"], z["pos"], rows[:1], z["bins"])
+    _near(s1, z["sums_1pop"], a1)
+    s3, a3 = _binned_check(z["hap"], z["pos"],
+                           [np.arange(0, 16), np.arange(16, 32), np.arange(32, 48)], z["bins"])
+    _near(s3, z["sums_3pop"], a3)
+
+
+def test_binned_sums_match_moments_golden(golden):
+    z = golden("moments_im")
+    keep = O.biallelic_keep(z["hap"])
+    s, a = _binned_check(z["hap"][:, keep], z["pos"][keep], [z["rows0"], z["rows1"]], z["bins"])
+    _near(s, z["ld_sums"], a)
+
+
+# --------------------------------------------------------------------------
+# oracle comparisons: sizes, ragged word counts, large samples
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("H", [1, 31, 32, 33, 63, 64, 65, 127, 128, 129, 700])
+def test_counts_ragged_sizes(H):
+    rng = np.random.default_rng(H)
+    M = 70
+    hap = copying_model(rng, H, M, 5, 0.05, missing=0.03)
+    pos = np.sort(rng.choice(10_000, M, replace=False))
+    ii, jj = O.pairs_within_distance(pos, 3000)
+    c, nv = ld_pipeline.compute_counts_for_pairs(hap, ii, jj)
+    rc, rnv = O.counts_for_pairs(hap, ii, jj)
+    assert np.array_equal(np_(c), rc)
+    assert (nv is None) == (rnv is None)
+    if rnv is not None:
+        assert np.array_equal(np_(nv), rnv)
+    # tally: every pair, correct where the reference's int8 X.T@X wraps (H >= 128)
+    pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
+    tc, tnv = _ops.tally(pk)
+    oc, onv = O.tally(hap)
+    assert np.array_equal(np_(tc), oc)
+    if onv is not None:
+        assert np.array_equal(np_(tnv), onv)
+
+
+def test_large_sample_statistics_are_exact():
+    # 1000 haplotypes per population: the reference's int32 fast path wraps here
+    rng = np.random.default_rng(3)
+    hap = copying_model(rng, 2000, 120, 40, 1e-3, missing=0.02)
+    pos = np.sort(rng.choice(50_000, 120, replace=False))
+    ii, jj = O.pairs_within_distance(pos, 20_000)
+    rows = [np.arange(1000), np.arange(1000, 2000)]
+    c1, nv1 = ld_pipeline.compute_counts_for_pairs(hap, ii, jj, rows[0])
+    c2, nv2 = ld_pipeline.compute_counts_for_pairs(hap, ii, jj, rows[1])
+    got = np_(ld_pipeline.compute_two_pop_statistics_batch(c1, c2, nv1, nv2))
+    ref = O.two_pop_stats(np_(c1), np_(c2), np_(nv1), np_(nv2))
+    _close(got, ref, rtol=1e-15)
+
+
+def test_band_pairs_fp32_outputs():
+    rng = np.random.default_rng(11)
+    H, M = 2000, 600
+    hap = copying_model(rng, H, M, 50, 5e-4, missing=0.02)
+    pos = np.sort(rng.choice(200_000, M, replace=False)).astype(np.int64)
+    pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
+    counts, nv, st = _ops.band_pairs(pk, _ops.positions_f64(pos), 20_000)
+    ii, jj = O.pairs_within_distance(pos, 20_000)
+    rc, rnv = O.counts_for_pairs(hap, ii, jj)
+    assert np.array_equal(np_(counts), rc) and np.array_equal(np_(nv), rnv)
+    st = np_(st).astype(np.float64)
+    ref = np.stack([O.r_squared(rc, rnv), O.dd(rc, None, rnv), O.dz(rc, None, rnv),
+                    O.pi2(rc, None, rnv)], axis=1)
+    assert np.array_equal(np.isnan(st), np.isnan(ref))
+    m = ~np.isnan(ref) & (np.abs(ref) > 1e-30)
+    rel = np.abs(st[m] - ref[m]) / np.abs(ref[m])
+    assert rel.max() <= 1e-6, rel.max()
+
+
+def test_binned_sums_two_pops_large_h():
+    rng = np.random.default_rng(5)
+    hap = copying_model(rng, 2000, 400, 40, 1e-3, missing=0.02)
+    pos = np.sort(rng.choice(400_000, 400, replace=False)).astype(np.int64)
+    bins = np.logspace(3, 5, 11)
+    _binned_check(hap, pos, [np.arange(1000), np.arange(1000, 2000)], bins)
+
+
+def test_binned_sums_genetic_distance():
+    rng = np.random.default_rng(9)
+    hap = copying_model(rng, 64, 300, 8, 5e-3, missing=0.01)
+    pos = np.sort(rng.choice(100_000, 300, replace=False)).astype(np.int64)
+    gmap = np.cumsum(rng.random(300)) * 1e-5
+    bins = np.array([0.0, 1e-4, 3e-4, 1e-3])
+    rows = [np.arange(32), np.arange(32, 64)]
+    hap_d = torch.as_tensor(hap, device="cuda")
+    pops = [_ops.pack(hap_d, r) for r in rows]
+    sums, cnt = _ops.binned_sums(pops, _ops.positions_f64(pos), bins, max_dist=40_000,
+                                 bin_coord=gmap)
+    ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, coords=gmap, max_dist=40_000,
+                                          abs_sums=True)
+    assert np.array_equal(np_(cnt), ref_cnt)
+    assert np.all(np.abs(np_(sums) - ref) <= SUM_TOL * ref_abs + 1e-300)
+
+
+def test_edge_cases_and_errors():
+    hap = np.zeros((4, 1), np.int8)
+    c, nv = ld_pipeline.compute_counts_for_pairs(hap, np.zeros(0, np.int32), np.zeros(0, np.int32))
+    assert c.shape == (0, 4) and nv is None
+    with pytest.raises(IndexError):
+        ld_pipeline.compute_counts_for_pairs(np.zeros((4, 3), np.int8), [0], [5])
+    with pytest.raises(ValueError):
+        _ops.binned_sums([_ops.pack(np.zeros((4, 3), np.int8))], _ops.positions_f64([1.0, 2, 3]),
+                         [10.0, 5.0])
+    # one SNP: no pairs, zero sums
+    pk = _ops.pack(np.ones((8, 1), np.int8))
+    s, n = _ops.binned_sums([pk], _ops.positions_f64([1.0]), [0.0, 10.0])
+    assert float(s.abs().sum()) == 0.0 and int(n.sum()) == 0
+    with pytest.raises(PgldError):
+        _ops.binned_sums([pk], _ops.positions_f64([1.0]), np.linspace(0, 1, 200))
