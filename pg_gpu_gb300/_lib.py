@@ -88,7 +88,7 @@ _SIGS = {
 }
 
 _lib = None
-_lock = threading.Lock()
+_lock = threading.RLock()
 _handles = {}
 
 
@@ -130,6 +130,7 @@ def handle(device=None):
     dev = torch.cuda.current_device() if device is None else int(device)
     h = _handles.get(dev)
     if h is None:
+        lib()
         with _lock:
             h = _handles.get(dev)
             if h is None:

@@ -108,7 +108,12 @@ __global__ void __launch_bounds__(kThreads) band_plain_kernel(BandArgs a) {
     for (int x = threadIdx.x; x <= a.n_bins; x += kThreads) sm.bins[x] = a.bins[x];
   }
   __syncthreads();
-  const i64 n_items = a.item_off[a.n_blocks];
+  i64 n_items = a.item_off[a.n_blocks];
+  // a tile list longer than the upper triangle of tile blocks is corrupt
+  if (n_items < 0 || n_items > a.n_blocks * (a.n_blocks + 1) / 2) {
+    if (threadIdx.x == 0 && a.status) atomicCAS(a.status, 0, 2001);
+    n_items = 0;
+  }
 
   for (i64 item = blockIdx.x; item < n_items; item += gridDim.x) {
     const i64 bi = item_block(a.item_off, a.n_blocks, item);
@@ -348,6 +353,7 @@ extern "C" int pgld_hap_band_pairs(pgld_handle h, const pgld_hap_panel* panel, c
   rc = pgld::band_schedule(h, pos, n, max_dist, items, scratch, std::max(sb1, sb2), st);
   if (rc) return rc;
   pgld::BandArgs a{};
+  a.status = h->dev_status;
   fill_panel(a, panel);
   a.pos = pos;
   a.max_dist = max_dist;
@@ -391,6 +397,7 @@ extern "C" int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, 
   rc = pgld::band_schedule(h, pos, n, max_dist, items, scratch, sb, st);
   if (rc) return rc;
   pgld::BandArgs a{};
+  a.status = h->dev_status;
   fill_panel(a, panel);
   a.pos = pos;
   a.max_dist = max_dist;

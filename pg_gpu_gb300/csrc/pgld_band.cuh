@@ -39,6 +39,7 @@ struct BandArgs {
   int32_t* counts;
   int32_t* nvalid;
   float* stats;
+  int32_t* status;  // device error word of the handle
 };
 
 int band_schedule(pgld_context* h, const double* pos, long long n_snp, double max_dist,

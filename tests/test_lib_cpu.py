@@ -88,3 +88,25 @@ def test_host_api_refuses_without_device():
     from pg_gpu_gb300._lib import PgldError
     with pytest.raises((PgldError, RuntimeError, AssertionError)):
         ld_pipeline.compute_counts_for_pairs(np.zeros((4, 3), np.int8), [0], [1])
+
+
+def test_loader_lock_is_reentrant():
+    """handle() loads the library while holding the loader lock."""
+    import threading
+    from pg_gpu_gb300 import _lib
+    _lib.lib()
+    saved = _lib._lib
+    _lib._lib = None
+    done = []
+
+    def run():
+        with _lib._lock:
+            _lib.lib()
+        done.append(True)
+
+    t = threading.Thread(target=run, daemon=True)
+    t.start()
+    t.join(20)
+    if not done:
+        _lib._lib = saved
+    assert done, "library loader deadlocked under its own lock"
