@@ -208,6 +208,28 @@ int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, const doubl
                          int32_t n_bins, double* sums, int64_t* pair_counts, int32_t form,
                          void* stream);
 
+/* pgld_hap_binned_sums for callers that cannot allocate device memory.
+ * No counterpart in the reference.  Some callers of this library cannot call
+ * cudaMalloc: a host application that hands every byte of the device to its
+ * own pool allocator (a cudaMalloc outside the pool fails once the pool has
+ * reserved the device, or is forbidden by the host), or a latency-bound loop
+ * that cannot afford cudaMalloc's implicit device-wide synchronisation.  This
+ * entry point needs no handle and allocates nothing: the tile work list and
+ * its prefix-sum partials live in a 4 MiB file-scope static device array that
+ * every GPU loading the library holds until the process exits, which limits a
+ * call to 16,771,040 SNPs (larger panels are rejected with
+ * PGLD_ERR_TOO_LARGE before any work is queued).  The caller still passes
+ * every input and output buffer; sums and pair_counts are zeroed by the call.
+ * The first call on a device resolves the static array's device address and
+ * fills constant term tables, so make it before any stream capture.  All
+ * calls on a device share the one array: calls that overlap on the GPU (other
+ * streams or host threads) race and must be serialised by the caller.
+ * Plain form only; arguments and results as pgld_hap_binned_sums. */
+int pgld_hap_binned_sums_noalloc(int device, const pgld_hap_panel* panel, const double* pos,
+                                 double max_dist, const double* bin_coord, const double* bins,
+                                 int32_t n_bins, double* sums, int64_t* pair_counts,
+                                 void* stream);
+
 #ifdef __cplusplus
 }
 #endif
