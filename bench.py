@@ -356,7 +356,9 @@ def run_gpu(args, pool, cores):
         "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "api": "HaplotypeMatrix(host int8).compute_ld_statistics_gpu_two_pops(raw=True)"},
-        "gpu_launches": args.steps * (cfg["pops"] + 5),
+        # per step: one pack per population, then the binned call: (tc: one operand
+        # expansion per population) + tile counts + 3 scan launches + the band kernel
+        "gpu_launches": args.steps * (cfg["pops"] * (2 if args.form == "tc" else 1) + 5),
         "kernel_ms": float(np.mean(kern_ms)),
         "roofline": roof,
     }

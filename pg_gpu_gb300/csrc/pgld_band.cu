@@ -20,10 +20,10 @@ using pgld::i64;
 namespace pgld {
 
 __global__ void band_items_kernel(const double* __restrict__ pos, i64 n_snp, double max_dist,
-                                  i64 n_blocks, i64* __restrict__ items) {
+                                  i64 n_blocks, int tile, i64* __restrict__ items) {
   for (i64 b = (i64)blockIdx.x * blockDim.x + threadIdx.x; b < n_blocks;
        b += (i64)gridDim.x * blockDim.x) {
-    i64 last = min(n_snp - 1, b * kTile + kTile - 1);
+    i64 last = min(n_snp - 1, b * tile + tile - 1);
     double lim = pos[last] + max_dist;
     i64 lo = last, hi = n_snp;
     while (lo < hi) {
@@ -31,16 +31,16 @@ __global__ void band_items_kernel(const double* __restrict__ pos, i64 n_snp, dou
       if (pos[mid] <= lim) lo = mid + 1; else hi = mid;
     }
     i64 jhi = lo - 1;  // last j paired with `last` (>= last)
-    i64 bj_hi = max(b, jhi / kTile);
+    i64 bj_hi = max(b, jhi / tile);
     items[b] = bj_hi - b + 1;
   }
 }
 
 int band_schedule(pgld_context* h, const double* pos, i64 n_snp, double max_dist, i64* items,
-                  void* scratch, size_t scratch_bytes, cudaStream_t st) {
-  i64 nb = (n_snp + kTile - 1) / kTile;
+                  void* scratch, size_t scratch_bytes, cudaStream_t st, int tile) {
+  i64 nb = (n_snp + tile - 1) / tile;
   unsigned blocks = (unsigned)std::max<i64>(1, std::min<i64>((nb + 255) / 256, h->n_sm * 4));
-  band_items_kernel<<<blocks, 256, 0, st>>>(pos, n_snp, max_dist, nb, items);
+  band_items_kernel<<<blocks, 256, 0, st>>>(pos, n_snp, max_dist, nb, tile, items);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_items_kernel");
   return exclusive_scan_i64(h, items, nb, scratch, scratch_bytes, st);
@@ -271,6 +271,7 @@ static int launch_p(pgld_context* h, const BandArgs& a, cudaStream_t st) {
 }
 
 int launch_band_plain(pgld_context* h, const BandArgs& a, int mode, cudaStream_t st) {
+  if (band_fast_applies(a, mode)) return launch_band_fast(h, a, mode, st);
   if (mode == kModePairs) return launch_p<1, kModePairs>(h, a, st);
   switch (a.n_pops) {
     case 1: return launch_p<1, kModeBinned>(h, a, st);

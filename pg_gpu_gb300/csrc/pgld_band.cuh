@@ -42,8 +42,14 @@ struct BandArgs {
   int32_t* status;  // device error word of the handle
 };
 
+// tile work list of `tile`-SNP blocks: items[b] = tiles of row block b, then
+// exclusively scanned in place (items[n_blocks] = total)
 int band_schedule(pgld_context* h, const double* pos, long long n_snp, double max_dist,
-                  long long* items, void* scratch, size_t scratch_bytes, cudaStream_t st);
+                  long long* items, void* scratch, size_t scratch_bytes, cudaStream_t st,
+                  int tile = kTile);
 int launch_band_plain(pgld_context* h, const BandArgs& a, int mode, cudaStream_t st);
+// the one/two-population kernel with the float32 epilogue (pgld_band_fast.cu)
+bool band_fast_applies(const BandArgs& a, int mode);
+int launch_band_fast(pgld_context* h, const BandArgs& a, int mode, cudaStream_t st);
 
 }  // namespace pgld

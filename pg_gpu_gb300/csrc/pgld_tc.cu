@@ -1,12 +1,721 @@
 // tcgen05 tensor-core form of the binned band kernel (sm_103a).
+//
+// The joint counts of a SNP pair are dot products of 0/1 vectors over the
+// haplotypes: with A = the carrier / reference rows of 64 SNPs i (rows 2i,
+// 2i+1) and B the same for 64 SNPs j, D = A B^T holds n11, n10, n01, n00 of
+// all 4096 pairs of the tile.  Operands are E4M3 bytes (0x38 = 1.0, 0x00 = 0)
+// in K-major rows padded to 128 bytes; products are exact and the float32
+// accumulators hold integers below 2^24, so the counts are exact.
+//
+// One CTA per SM (it owns all 512 TMEM columns):
+//   warp 0      TMA producer: 128-row x 128-byte A and B boxes (SWIZZLE_128B)
+//               into a ring of smem stages, one K chunk of one population each
+//   warp 1      allocates TMEM; one lane issues tcgen05.mma M=128 N=128 K=32
+//               (kind::f8f6f4) into accumulator stage t%2 (population p at
+//               columns 256*(t%2) + 128*p), commits stages and tiles
+//   warps 4-11  epilogue: tcgen05.ld the counts, exchange C/Z rows with a lane
+//               shuffle, float32 statistics (pgld_epilogue.cuh), bin sums
+// Every mbarrier wait is bounded; on expiry the kernel records an error code
+// in the status word, drains its own copies and MMAs, frees TMEM and returns.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <mutex>
 
 #include "pgld_band.cuh"
+#include "pgld_epilogue.cuh"
 #include "pgld_internal.cuh"
+#include "pgld_scan.cuh"
 
-int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel) { return 0; }
+namespace pgld {
+namespace tc {
+
+constexpr int kTileSnp = 64;
+constexpr int kRows = 128;          // 2 planes x 64 SNPs
+constexpr int kKChunk = 128;        // bytes (= E4M3 elements) of K per stage
+constexpr int kBoxBytes = kRows * kKChunk;  // 16 KB
+constexpr int kStageBytes = 2 * kBoxBytes;  // A + B
+constexpr int kEpiWarps = 8;
+constexpr int kEpiThreads = kEpiWarps * 32;
+constexpr int kThreads = (4 + kEpiWarps) * 32;
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kOne = 0x38;     // E4M3 1.0
+constexpr long long kSpinLimit = 1ll << 26;
+
+// instruction descriptor: D f32, A/B E4M3, both K-major, N = 128, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((128u >> 3) << 17) |
+                            ((128u >> 4) << 24);
+
+struct Params {
+  int n_pops;
+  int kchunks[2];
+  long long n_snp;
+  const double* pos;
+  double max_dist;
+  const double* bcoord;
+  const double* bins;
+  int n_bins;
+  const long long* item_off;
+  long long n_blocks;
+  double* sums;
+  int64_t* pair_counts;
+  int32_t* status;
+  int stages;
+};
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false once ~2 s of SM clock passed or another role aborted
+constexpr long long kWaitCycles = 4000000000ll;
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
+  const long long t0 = clock64();
+  for (long long k = 0; k < kSpinLimit; ++k) {
+    if (mbar_try(b, parity)) return true;
+    if ((k & 63) == 63 && (*abort_flag || clock64() - t0 > kWaitCycles)) return false;
+  }
+  return false;
+}
+// drain wait: bounded by time only
+__device__ __forceinline__ void mbar_wait_drain(uint64_t* b, uint32_t parity) {
+  const long long t0 = clock64();
+  for (long long k = 0; k < kSpinLimit; ++k) {
+    if (mbar_try(b, parity)) return;
+    if ((k & 63) == 63 && clock64() - t0 > kWaitCycles) return;
+  }
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x,
+                                            int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  // K-major, 128-byte swizzle: SBO = 1024 B (8 rows x 128 B), LBO unused (1),
+  // descriptor version 1 (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63)
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+__device__ __forceinline__ void mma_f8(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void epi_bar() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+}
+
+__device__ __forceinline__ int f2i_exact(uint32_t bits) {
+  // the counts are exact integers below 2^22 stored as float32
+  return __float_as_int(__uint_as_float(bits) + 12582912.0f) - 0x4B400000;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int bin_of_int(const int* thr, int n_bins, int d) {
+  if (d < thr[0] || d >= thr[n_bins]) return -1;
+  int lo = 0, hi = n_bins;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (thr[mid] <= d) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ int bin_of_f64(const double* sb, int n_bins, double d) {
+  if (!(d >= sb[0]) || !(d < sb[n_bins])) return -1;
+  int lo = 0, hi = n_bins;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (sb[mid] <= d) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+struct Meta {
+  int reli[kTileSnp], relj[kTileSnp];
+  int isint[2 * kTileSnp];
+  int tile_int, tile_bin;
+};
+
+struct Ctrl {
+  uint64_t full[8], empty[8], tfull[2], tempty[2], drain;
+  uint32_t tmem_base;
+  int abort_flag;
+  int produced, consumed;
+};
+
+__device__ __forceinline__ void set_abort(Ctrl* c, int32_t* status, int code) {
+  if (status) atomicCAS(status, 0, code);
+  *(volatile int*)&c->abort_flag = 1;
+}
+
+template <int P>
+__global__ void __launch_bounds__(kThreads, 1)
+    band_tc_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
+                   Params a) {
+  constexpr int S = (P == 1) ? 3 : 15;
+  extern __shared__ unsigned char smem_dyn[];
+  // 1024-byte aligned base for the swizzled stages
+  unsigned char* base =
+      smem_dyn + ((1024 - (smem_u32(smem_dyn) & 1023)) & 1023);
+  const int stages = a.stages;
+  unsigned char* ring = base;
+  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kStageBytes);
+  Meta* meta = reinterpret_cast<Meta*>(ctrl + 1);  // [2]
+  double* sbins = reinterpret_cast<double*>(meta + 2);
+  int* thr = reinterpret_cast<int*>(sbins + (kMaxBins + 1));
+  double* accw = reinterpret_cast<double*>(thr + (kMaxBins + 2));  // [kEpiWarps][n_bins][S]
+  unsigned long long* cntw = reinterpret_cast<unsigned long long*>(accw + kEpiWarps * a.n_bins * S);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n_bins = a.n_bins;
+  volatile int* abort_flag = &ctrl->abort_flag;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&ctrl->full[s], 1);
+      mbar_init(&ctrl->empty[s], 1);
+    }
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&ctrl->tfull[s], 1);
+      mbar_init(&ctrl->tempty[s], kEpiWarps);
+    }
+    mbar_init(&ctrl->drain, 1);
+    ctrl->abort_flag = 0;
+    ctrl->produced = 0;
+    ctrl->consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ctrl->tmem_base)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (warp >= 4) {
+    const int t = threadIdx.x - 128;
+    for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) accw[x] = 0.0;
+    for (int x = t; x < kEpiWarps * n_bins; x += kEpiThreads) cntw[x] = 0ull;
+    for (int x = t; x <= n_bins; x += kEpiThreads) {
+      const double b = a.bins[x];
+      sbins[x] = b;
+      const double cb = ceil(b);
+      thr[x] = cb > 2147483647.0 ? 2147483647 : (cb < -2147483647.0 ? -2147483647 : (int)cb);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = ctrl->tmem_base;
+
+  long long n_items = a.item_off[a.n_blocks];
+  if (n_items < 0 || n_items > a.n_blocks * (a.n_blocks + 1) / 2) {
+    if (threadIdx.x == 0) set_abort(ctrl, a.status, 3001);
+    n_items = 0;
+  }
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued = 0;
+      for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x) {
+        long long lo = 0, hi = a.n_blocks;
+        while (hi - lo > 1) {
+          const long long mid = (lo + hi) >> 1;
+          if (a.item_off[mid] <= item) lo = mid; else hi = mid;
+        }
+        const int yi = (int)(lo * kRows), yj = (int)((lo + (item - a.item_off[lo])) * kRows);
+        for (int p = 0; p < P && !*abort_flag; ++p) {
+          const CUtensorMap* map = p == 0 ? &map0 : &map1;
+          for (int kc = 0; kc < a.kchunks[p]; ++kc) {
+            if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+              set_abort(ctrl, a.status, 3002);
+              break;
+            }
+            mbar_expect_tx(&ctrl->full[stage], kStageBytes);
+            unsigned char* sa = ring + (size_t)stage * kStageBytes;
+            tma_load_2d(sa, map, &ctrl->full[stage], kc * kKChunk, yi);
+            tma_load_2d(sa + kBoxBytes, map, &ctrl->full[stage], kc * kKChunk, yj);
+            ++issued;
+            if (++stage == stages) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+      }
+      if (*abort_flag) {
+        // drain: every issued copy lands before the CTA may exit
+        const int consumed = *(volatile int*)&ctrl->consumed;
+        int st2 = consumed % stages;
+        uint32_t ph2 = (uint32_t)((consumed / stages) & 1);
+        for (int k = consumed; k < issued; ++k) {
+          mbar_wait_drain(&ctrl->full[st2], ph2);
+          if (++st2 == stages) {
+            st2 = 0;
+            ph2 ^= 1;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int t = 0;
+      int consumed = 0;
+      bool any = false;
+      for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
+        const int acc = t & 1;
+        const uint32_t aph = (uint32_t)((t >> 1) & 1);
+        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
+          set_abort(ctrl, a.status, 3003);
+          break;
+        }
+        tc_fence_after();
+        bool ok = true;
+        for (int p = 0; p < P && ok; ++p) {
+          const uint32_t d = tmem_base + (uint32_t)(acc * 256 + p * 128);
+          for (int kc = 0; kc < a.kchunks[p]; ++kc) {
+            if (!mbar_wait(&ctrl->full[stage], phase, abort_flag)) {
+              set_abort(ctrl, a.status, 3004);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(ring + (size_t)stage * kStageBytes);
+            const uint64_t da = smem_desc(sa), db = smem_desc(sa + kBoxBytes);
+#pragma unroll
+            for (int k = 0; k < kKChunk / 32; ++k)
+              mma_f8(d, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), (kc | k) != 0);
+            mma_commit(&ctrl->empty[stage]);
+            any = true;
+            *(volatile int*)&ctrl->consumed = ++consumed;
+            if (++stage == stages) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+        if (!ok) break;
+        mma_commit(&ctrl->tfull[acc]);
+      }
+      if (*abort_flag && any) {
+        // drain: every issued MMA completes before TMEM is freed
+        mma_commit(&ctrl->drain);
+        mbar_wait_drain(&ctrl->drain, 0);
+      }
+    }
+  } else if (warp >= 4) {
+    // ---------------- epilogue ----------------
+    const int e = warp - 4;
+    const int quarter = warp & 3;       // TMEM lanes 32*quarter .. +31
+    const int half = e >> 2;            // j columns 32*half .. +31 of the tile
+    const int row = quarter * 32 + lane;  // D row: SNP i = row/2, plane = row&1
+    const int il = row >> 1, plane = row & 1;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    const double maxd = a.max_dist;
+    const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
+    int t = 0;
+    for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
+      const int acc = t & 1;
+      const uint32_t aph = (uint32_t)((t >> 1) & 1);
+      long long lo = 0, hi = a.n_blocks;
+      while (hi - lo > 1) {
+        const long long mid = (lo + hi) >> 1;
+        if (a.item_off[mid] <= item) lo = mid; else hi = mid;
+      }
+      const long long bi = lo, bj = bi + (item - a.item_off[bi]);
+      const long long i0 = bi * kTileSnp, j0 = bj * kTileSnp;
+      Meta& m = meta[acc];
+      // tile coordinates (threads 0..127 of the epilogue): integer offsets from pos[i0]
+      epi_bar();  // every epilogue warp is done with the previous tile's metadata
+      const int et = threadIdx.x - 128;
+      if (et < 2 * kTileSnp) {
+        const int tt = et & (kTileSnp - 1);
+        const long long s = (et < kTileSnp ? i0 : j0) + tt;
+        int r = 0, isint = 1;
+        if (s < a.n_snp) {
+          const double rel = a.pos[s] - a.pos[i0];
+          isint = (rel == rint(rel)) && fabs(rel) < 1073741824.0;
+          r = isint ? (int)rel : 0;
+        }
+        if (et < kTileSnp) m.reli[tt] = r; else m.relj[tt] = r;
+        m.isint[et] = isint;
+      }
+      epi_bar();
+      if (et == 0) {
+        int all = (a.bcoord == nullptr);
+        for (int k = 0; k < 2 * kTileSnp; ++k) all &= m.isint[k];
+        m.tile_int = all;
+        int tb = -1;
+        if (all && bj > bi && j0 + kTileSnp <= a.n_snp) {
+          const int dmin = m.relj[0] - m.reli[kTileSnp - 1];
+          const int dmax = m.relj[kTileSnp - 1] - m.reli[0];
+          if (dmax <= maxd_int) {
+            const int b0 = bin_of_int(thr, n_bins, dmin);
+            if (b0 >= 0 && b0 == bin_of_int(thr, n_bins, dmax)) tb = b0;
+          }
+        }
+        m.tile_bin = tb;
+      }
+      epi_bar();
+      const int tile_bin = m.tile_bin;
+      const bool tint = m.tile_int;
+
+      bool ready = true;
+      if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
+      ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
+      if (!ready) {
+        if (lane == 0) set_abort(ctrl, a.status, 3005);
+        break;
+      }
+      tc_fence_after();
+
+      float accs[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) accs[s] = 0.f;
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
+        uint32_t r[P][16];
+        const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
+#pragma unroll
+        for (int p = 0; p < P; ++p) tmem_ld16(tmem_base + lane_base + col + p * 128, r[p]);
+        tmem_wait_ld();
+        if (c == 3) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
+        }
+        float chunk[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) chunk[s] = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          int cnt[P][4];
+#pragma unroll
+          for (int p = 0; p < P; ++p) {
+            // plane 0 rows hold (n11, n10) of every j, plane 1 rows (n01, n00):
+            // swap halves with the partner lane so each lane owns whole pairs
+            const uint32_t s0 = plane ? r[p][4 * q] : r[p][4 * q + 2];
+            const uint32_t s1 = plane ? r[p][4 * q + 1] : r[p][4 * q + 3];
+            const uint32_t g0 = __shfl_xor_sync(0xffffffffu, s0, 1);
+            const uint32_t g1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+            if (plane == 0) {
+              cnt[p][0] = f2i_exact(r[p][4 * q]);
+              cnt[p][1] = f2i_exact(r[p][4 * q + 1]);
+              cnt[p][2] = f2i_exact(g0);
+              cnt[p][3] = f2i_exact(g1);
+            } else {
+              cnt[p][0] = f2i_exact(g0);
+              cnt[p][1] = f2i_exact(g1);
+              cnt[p][2] = f2i_exact(r[p][4 * q + 2]);
+              cnt[p][3] = f2i_exact(r[p][4 * q + 3]);
+            }
+          }
+          const int jl = half * 32 + c * 8 + 2 * q + plane;
+          const long long i = i0 + il, j = j0 + jl;
+          float st[S];
+          {
+            fast::Pop p0 = fast::make(cnt[0][0], cnt[0][1], cnt[0][2], cnt[0][3],
+                                      cnt[0][0] + cnt[0][1] + cnt[0][2] + cnt[0][3]);
+            if (P == 1) {
+              fast::stats1(p0, st);
+            } else {
+              fast::Pop p1 = fast::make(cnt[P - 1][0], cnt[P - 1][1], cnt[P - 1][2], cnt[P - 1][3],
+                                        cnt[P - 1][0] + cnt[P - 1][1] + cnt[P - 1][2] + cnt[P - 1][3]);
+              fast::stats2(p0, p1, st);
+            }
+          }
+          if (tile_bin >= 0) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) chunk[s] += st[s];
+          } else {
+            bool ok = (i < j) && (j < a.n_snp);
+            int b = -1;
+            if (tint) {
+              const int d = m.relj[jl] - m.reli[il];
+              if (ok && d <= maxd_int) b = bin_of_int(thr, n_bins, d);
+            } else if (ok) {
+              const double dp = a.pos[j] - a.pos[i];
+              if (dp <= maxd) {
+                const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
+                b = bin_of_f64(sbins, n_bins, d);
+              }
+            }
+            unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
+            while (pending) {
+              const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
+              const bool mine = (b == bb);
+              const unsigned grp = __ballot_sync(0xffffffffu, mine);
+#pragma unroll
+              for (int s = 0; s < S; ++s) {
+                const float v = warp_sum(mine ? st[s] : 0.f);
+                if (lane == 0) accw[(e * n_bins + bb) * S + s] += (double)v;
+              }
+              if (lane == 0) cntw[e * n_bins + bb] += (unsigned long long)__popc(grp);
+              pending &= ~grp;
+            }
+          }
+        }
+        if (tile_bin >= 0) {
+#pragma unroll
+          for (int s = 0; s < S; ++s) accs[s] += chunk[s];
+        }
+      }
+      if (tile_bin >= 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const float v = warp_sum(accs[s]);
+          if (lane == 0) accw[(e * n_bins + tile_bin) * S + s] += (double)v;
+        }
+        if (lane == 0) cntw[e * n_bins + tile_bin] += 32ull * 16ull;
+      }
+    }
+  }
+
+  // ---------------- teardown ----------------
+  tc_fence_before();
+  __syncthreads();
+  if (warp >= 4 && !ctrl->abort_flag) {
+    const int t = threadIdx.x - 128;
+    for (int x = t; x < n_bins * S; x += kEpiThreads) {
+      double v = 0.0;
+#pragma unroll
+      for (int w = 0; w < kEpiWarps; ++w) v += accw[w * n_bins * S + x];
+      if (v != 0.0) atomicAdd(a.sums + x, v);
+    }
+    if (a.pair_counts)
+      for (int x = t; x < n_bins; x += kEpiThreads) {
+        unsigned long long v = 0;
+#pragma unroll
+        for (int w = 0; w < kEpiWarps; ++w) v += cntw[w * n_bins + x];
+        if (v) atomicAdd(reinterpret_cast<unsigned long long*>(a.pair_counts) + x, v);
+      }
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// operand packing: bit planes -> E4M3 rows (2 per SNP), K padded to 128
+// ---------------------------------------------------------------------------
+__global__ void pack_tc_kernel(const uint32_t* __restrict__ planes, int W, long long n_snp,
+                               int k_pad, uint32_t* __restrict__ out) {
+  // one thread writes 4 bytes (4 haplotypes) of one operand row
+  const int words_per_row = k_pad / 4;
+  const long long total = 2 * n_snp * (long long)words_per_row;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const long long rowi = x / words_per_row;
+    const int wq = (int)(x - rowi * words_per_row);  // 4-haplotype group
+    const long long s = rowi >> 1;
+    const int plane = (int)(rowi & 1);
+    const int h0 = wq * 4;
+    const int w = h0 >> 5;
+    uint32_t bits = 0;
+    if (w < W) bits = (__ldg(planes + s * 2 * W + plane * W + w) >> (h0 & 31)) & 0xF;
+    uint32_t v = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) v |= ((bits >> b) & 1u) * (kOne << (8 * b));
+    out[x] = v;
+  }
+}
+
+}  // namespace tc
+}  // namespace pgld
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+int get_encode(pgld_context* h) {
+  std::call_once(g_encode_once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  });
+  if (!g_encode)
+    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+  return PGLD_OK;
+}
+
+int make_map(pgld_context* h, CUtensorMap* map, const void* base, long long rows, int k_pad) {
+  cuuint64_t dims[2] = {(cuuint64_t)k_pad, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)k_pad};
+  cuuint32_t box[2] = {(cuuint32_t)pgld::tc::kKChunk, (cuuint32_t)pgld::tc::kRows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return pgld_fail(h, PGLD_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return PGLD_OK;
+}
+
+}  // namespace
+
+int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel) {
+  if (panel->n_pops < 1 || panel->n_pops > 2) return 0;
+  for (int p = 0; p < panel->n_pops; ++p) {
+    if (panel->valid[p] != nullptr) return 0;
+    if (panel->n_words[p] > 64) return 0;  // <= 2048 haplotypes per population
+  }
+  return 1;
+}
 
 int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
                    cudaStream_t st) {
-  return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "tensor-core form not built");
+  using namespace pgld::tc;
+  int rc = get_encode(h);
+  if (rc) return rc;
+  const long long n = panel->n_snp;
+  const int P = panel->n_pops;
+  const int S = P == 1 ? 3 : 15;
+  const long long nb = (n + kTileSnp - 1) / kTileSnp;
+  if (2 * (nb * kTileSnp) > 2147483647LL)
+    return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: too many SNPs");
+  int k_pad[2] = {0, 0};
+  size_t op_bytes[2] = {0, 0};
+  for (int p = 0; p < P; ++p) {
+    k_pad[p] = ((panel->n_words[p] * 32 + kKChunk - 1) / kKChunk) * kKChunk;
+    op_bytes[p] = (size_t)2 * n * k_pad[p];
+  }
+  const size_t sb = pgld::scan_scratch_bytes(nb);
+  auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+  const size_t off_items = 0, off_scan = al((nb + 1) * 8), off_op0 = off_scan + al(sb),
+               off_op1 = off_op0 + al(op_bytes[0]);
+  void* ws = nullptr;
+  rc = pgld_workspace(h, off_op1 + al(op_bytes[1]) + 1024, &ws);
+  if (rc) return rc;
+  char* w = (char*)ws;
+  long long* items = (long long*)(w + off_items);
+  unsigned char* ops[2] = {(unsigned char*)(w + off_op0), (unsigned char*)(w + off_op1)};
+
+  // operands
+  for (int p = 0; p < P; ++p) {
+    const long long words = 2 * n * (long long)(k_pad[p] / 4);
+    unsigned blocks = (unsigned)std::min<long long>((words + 255) / 256, (long long)h->n_sm * 16);
+    pack_tc_kernel<<<std::max(1u, blocks), 256, 0, st>>>(panel->planes[p], panel->n_words[p], n,
+                                                          k_pad[p], (uint32_t*)ops[p]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_tc_kernel");
+  }
+  // 64-SNP tile work list
+  rc = pgld::band_schedule(h, a.pos, n, a.max_dist, items, w + off_scan, sb, st, kTileSnp);
+  if (rc) return rc;
+  CUtensorMap maps[2];
+  for (int p = 0; p < P; ++p) {
+    rc = make_map(h, &maps[p], ops[p], 2 * n, k_pad[p]);
+    if (rc) return rc;
+  }
+  if (P == 1) maps[1] = maps[0];
+
+  Params prm{};
+  prm.n_pops = P;
+  for (int p = 0; p < P; ++p) prm.kchunks[p] = k_pad[p] / kKChunk;
+  prm.n_snp = n;
+  prm.pos = a.pos;
+  prm.max_dist = a.max_dist;
+  prm.bcoord = a.bcoord;
+  prm.bins = a.bins;
+  prm.n_bins = a.n_bins;
+  prm.item_off = items;
+  prm.n_blocks = nb;
+  prm.sums = a.sums;
+  prm.pair_counts = a.pair_counts;
+  prm.status = h->dev_status;
+
+  const size_t fixed = sizeof(Ctrl) + 2 * sizeof(Meta) + (pgld::kMaxBins + 1) * 8 +
+                       (pgld::kMaxBins + 2) * 4 + (size_t)kEpiWarps * a.n_bins * (S + 1) * 8 + 1024;
+  int max_smem = 0;
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStageBytes);
+  if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: shared memory");
+  prm.stages = stages;
+  const size_t smem = (size_t)stages * kStageBytes + fixed;
+  auto kern = P == 1 ? band_tc_kernel<1> : band_tc_kernel<2>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc smem attribute");
+  kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(maps[0], maps[1], prm);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc_kernel");
+  return PGLD_OK;
 }

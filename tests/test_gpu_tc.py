@@ -1,0 +1,92 @@
+"""GPU parity of the tcgen05 tensor-core binned-sum form.
+
+Same bar as the plain form: pair counts per bin equal the oracle's exactly,
+and every bin sum is within 2e-6 * sum|x| of the float64 oracle.  Cases cover
+one and two populations, SNP counts that leave partial 64-SNP tiles, sample
+sizes that are not multiples of 128 (K padding), 1,000 haplotypes per
+population, genetic-map distances and non-integer positions.
+"""
+import numpy as np
+import pytest
+
+from oracle import ld_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+from pg_gpu_gb300 import _ops  # noqa: E402
+
+SUM_TOL = 2e-6
+
+
+def copying_model(rng, H, M, F, switch, missing=0.0, flip=1e-3):
+    p = rng.beta(0.3, 0.3, size=M)
+    f = (rng.random((F, M)) < p).astype(np.int8)
+    sw = rng.random((H, M)) < switch
+    seg = np.cumsum(sw, axis=1)
+    choice = rng.integers(0, F, size=(H, seg.max() + 1))
+    hap = f[np.take_along_axis(choice, seg, axis=1), np.arange(M)[None, :]]
+    hap ^= (rng.random(hap.shape) < flip).astype(np.int8)
+    if missing:
+        hap[rng.random(hap.shape) < missing] = -1
+    return hap.astype(np.int8)
+
+
+def check(hap, pos, rows, bins, **kw):
+    hap_d = torch.as_tensor(hap, device="cuda")
+    pops = [_ops.pack(hap_d, r) for r in rows]
+    sums, cnt = _ops.binned_sums(pops, _ops.positions_f64(pos), bins, form="tc", **kw)
+    okw = {}
+    if "bin_coord" in kw:
+        okw["coords"] = kw["bin_coord"]
+    if "max_dist" in kw:
+        okw["max_dist"] = kw["max_dist"]
+    ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True, **okw)
+    assert np.array_equal(cnt.cpu().numpy(), ref_cnt)
+    err = np.abs(sums.cpu().numpy() - ref)
+    worst = float((err / np.maximum(ref_abs, 1e-300)).max())
+    assert np.all(err <= SUM_TOL * ref_abs + 1e-300), worst
+    return worst
+
+
+@pytest.mark.parametrize("P", [1, 2])
+def test_tc_matches_reference_fixture(golden, P):
+    z = golden("binned")
+    check(z["hap"], z["pos"], [z["rows0"], z["rows1"]][:P], z["bins"])
+
+
+def test_tc_matches_moments_golden(golden):
+    z = golden("moments_im")
+    keep = O.biallelic_keep(z["hap"])
+    check(z["hap"][:, keep], z["pos"][keep], [z["rows0"], z["rows1"]], z["bins"])
+
+
+@pytest.mark.parametrize("H,M", [(40, 65), (130, 129), (300, 191), (257, 640)])
+def test_tc_ragged_sizes(H, M):
+    rng = np.random.default_rng(H * 1000 + M)
+    hap = copying_model(rng, H, M, 6, 0.02, missing=0.03)
+    pos = np.sort(rng.choice(M * 300, M, replace=False)).astype(np.int64)
+    bins = np.logspace(2, np.log10(M * 150), 8)
+    h2 = H // 2
+    check(hap, pos, [np.arange(h2)], bins)
+    check(hap, pos, [np.arange(h2), np.arange(h2, H)], bins)
+
+
+def test_tc_large_populations():
+    rng = np.random.default_rng(12)
+    hap = copying_model(rng, 2000, 700, 40, 1e-3, missing=0.02)
+    pos = np.sort(rng.choice(700_000, 700, replace=False)).astype(np.int64)
+    check(hap, pos, [np.arange(1000), np.arange(1000, 2000)], np.logspace(3, 5.3, 13))
+
+
+def test_tc_genetic_distance_and_fractional_positions():
+    rng = np.random.default_rng(21)
+    hap = copying_model(rng, 96, 400, 8, 5e-3, missing=0.01)
+    pos = np.sort(rng.choice(200_000, 400, replace=False)).astype(np.float64) + 0.25
+    gmap = np.cumsum(rng.random(400)) * 1e-5
+    rows = [np.arange(48), np.arange(48, 96)]
+    check(hap, pos, rows, np.array([0.0, 1e-4, 3e-4, 1e-3]), max_dist=60_000, bin_coord=gmap)
+    check(hap, pos, rows, np.logspace(2, 4.7, 9))
