@@ -266,31 +266,44 @@ def run_gpu(args, pool, cores):
     assert int(cnt.sum()) <= n_pairs
 
     # ---- timed region: device-resident inputs ----
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(lrank) as clk:
-        for s in range(args.steps):
-            flush.fill_(s & 0x7F)  # L2 flush between steps (outside the events)
-            ev[s][0].record(stream)
+    def timed(form):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        for _ in range(args.warmup):
             packs = [_ops.pack(panel, r) for r in rows]
-            kev[s][0].record(stream)
-            _ops.binned_sums(packs, pos_d, bins, form=args.form)
-            kev[s][1].record(stream)
-            ev[s][1].record(stream)
+            _ops.binned_sums(packs, pos_d, bins, form=form)
+        if world > 1:
+            dist.barrier()
         torch.cuda.synchronize()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    kern_ms = [a.elapsed_time(b) for a, b in kev]
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * n_pairs * args.steps / total_s
+        with ClockSampler(lrank) as clk:
+            for s in range(args.steps):
+                flush.fill_(s & 0x7F)  # L2 flush between steps (outside the events)
+                ev[s][0].record(stream)
+                packs = [_ops.pack(panel, r) for r in rows]
+                kev[s][0].record(stream)
+                _ops.binned_sums(packs, pos_d, bins, form=form)
+                kev[s][1].record(stream)
+                ev[s][1].record(stream)
+            torch.cuda.synchronize()
+        step_ms = [a.elapsed_time(b) for a, b in ev]
+        kern_ms = [a.elapsed_time(b) for a, b in kev]
+        total = sum(step_ms) / 1e3
+        if world > 1:
+            t = torch.tensor([total], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total = float(t.item())
+        return world * n_pairs * args.steps / total, step_ms, kern_ms, clk
+
+    value, step_ms, kern_ms, clk = timed(args.form)
+    compare = None
+    if not args.no_compare:
+        other = "plain" if args.form == "tc" else "tc"
+        v2, s2, k2, c2 = timed(other)
+        compare = {"form": other, "value": v2, "unit": "pairs/s",
+                   "ms_per_step": float(np.mean(s2)), "kernel_ms": float(np.mean(k2)),
+                   "clocks": c2.summary(), "ratio_this_over_other": value / v2}
 
     # ---- end to end through the public API, host buffers ----
     host = panel.cpu().pin_memory()
@@ -361,6 +374,7 @@ def run_gpu(args, pool, cores):
         "gpu_launches": args.steps * (cfg["pops"] * (2 if args.form == "tc" else 1) + 5),
         "kernel_ms": float(np.mean(kern_ms)),
         "roofline": roof,
+        "compare": compare,
     }
     if pool is not None and rank == 0:
         tasks = cpu_sample_inputs(panel, pos, cfg, cores, args.cpu_pairs_per_worker)
@@ -415,7 +429,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain", "tc"])
+    ap.add_argument("--form", default="tc", choices=["plain", "tc"])
+    ap.add_argument("--no-compare", action="store_true", help="skip timing the other form")
     ap.add_argument("--workload", default="binned2pop", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-pairs-per-worker", type=int, default=400_000)

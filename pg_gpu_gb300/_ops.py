@@ -221,8 +221,18 @@ def band_pairs(pk, pos_d, max_dist, with_stats=True):
     return counts, nv, st
 
 
-def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="plain"):
-    """(sums (n_bins, n_stats) float64 tensor, pair counts (n_bins,) int64)."""
+def tc_applies(pops):
+    """The tensor-core form takes 1-2 populations of <= 2048 haplotypes (0/1/-1 codes)."""
+    return len(pops) <= 2 and all(pk.n_words <= 64 and pk.valid_for_n is None for pk in pops)
+
+
+def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto"):
+    """(sums (n_bins, n_stats) float64 tensor, pair counts (n_bins,) int64).
+
+    form: "tc" (tcgen05 tensor cores), "plain" (AND + popcount) or "auto"
+    (tensor cores whenever they apply)."""
+    if form == "auto":
+        form = "tc" if tc_applies(pops) else "plain"
     torch = _torch()
     bins_np = np.asarray(bins, dtype=np.float64)
     if bins_np.ndim != 1 or len(bins_np) < 2:

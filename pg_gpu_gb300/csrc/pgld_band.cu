@@ -306,6 +306,8 @@ static void fill_panel(pgld::BandArgs& a, const pgld_hap_panel* panel) {
     a.valid[p] = p < panel->n_pops ? panel->valid[p] : nullptr;
   }
   a.n_snp = panel->n_snp;
+  a.nmax = 0;
+  for (int p = 0; p < panel->n_pops; ++p) a.nmax = std::max(a.nmax, 32 * panel->n_words[p]);
 }
 
 int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel);

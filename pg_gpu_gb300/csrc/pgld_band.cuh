@@ -40,6 +40,7 @@ struct BandArgs {
   int32_t* nvalid;
   float* stats;
   int32_t* status;  // device error word of the handle
+  int nmax;         // largest per-population sample size (32 * max words)
 };
 
 // tile work list of `tile`-SNP blocks: items[b] = tiles of row block b, then

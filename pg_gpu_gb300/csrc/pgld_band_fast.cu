@@ -76,17 +76,36 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// count (< 2^22) to float32 without the conversion pipe
+__device__ __forceinline__ float cnt_f(int v) { return __int_as_float(0x4B400000 + v) - 12582912.0f; }
+
+__device__ __forceinline__ fast::Pop pop_of(const int (&c)[4]) {
+  return fast::make(cnt_f(c[0]), cnt_f(c[1]), cnt_f(c[2]), cnt_f(c[3]));
+}
+
 template <int P>
-__device__ __forceinline__ void pair_stats(const int (&c)[P][4], float* s) {
-  fast::Pop p0 = fast::make(c[0][0], c[0][1], c[0][2], c[0][3],
-                            c[0][0] + c[0][1] + c[0][2] + c[0][3]);
+__device__ __forceinline__ void pair_stats(const int (&c)[P][4], const fast::Recip& T, float* s) {
+  const fast::Pop p0 = pop_of(c[0]);
   if (P == 1) {
-    fast::stats1(p0, s);
+    fast::stats1(p0, T, s);
   } else {
-    fast::Pop p1 = fast::make(c[P - 1][0], c[P - 1][1], c[P - 1][2], c[P - 1][3],
-                              c[P - 1][0] + c[P - 1][1] + c[P - 1][2] + c[P - 1][3]);
-    fast::stats2(p0, p1, s);
+    fast::stats2(p0, pop_of(c[P - 1]), T, s);
   }
+}
+
+// per-CTA reciprocal tables for n = 0..nmax, after the bin accumulators
+__device__ __forceinline__ fast::Recip build_recip(float* base, int nmax, int tid, int nthreads) {
+  fast::Recip T;
+  float* inv = base;
+  float* r2 = base + (nmax + 1);
+  float* r3 = base + 2 * (nmax + 1);
+  float* r4 = base + 3 * (nmax + 1);
+  for (int n = tid; n <= nmax; n += nthreads) fast::recip_entry(n, inv + n, r2 + n, r3 + n, r4 + n);
+  T.inv = inv;
+  T.r2 = r2;
+  T.r3 = r3;
+  T.r4 = r4;
+  return T;
 }
 
 template <int P, int MODE>
@@ -97,8 +116,10 @@ __global__ void __launch_bounds__(kThreads) band_fast_kernel(BandArgs a) {
   double* accw = reinterpret_cast<double*>(smem_raw + sizeof(FastSmem));  // [warp][bin][S]
   unsigned long long* cntw =
       reinterpret_cast<unsigned long long*>(accw + (MODE == kModeBinned ? kWarps * a.n_bins * S : 0));
+  float* tables = reinterpret_cast<float*>(cntw + (MODE == kModeBinned ? kWarps * a.n_bins : 0));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int n_bins = a.n_bins;
+  const fast::Recip T = build_recip(tables, a.nmax, threadIdx.x, kThreads);
 
   if (MODE == kModeBinned) {
     for (int x = threadIdx.x; x < kWarps * n_bins * S; x += kThreads) accw[x] = 0.0;
@@ -207,7 +228,7 @@ __global__ void __launch_bounds__(kThreads) band_fast_kernel(BandArgs a) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) cq[p][k] = c[p][q][k];
         float st[S];
-        pair_stats<P>(cq, st);
+        pair_stats<P>(cq, T, st);
 #pragma unroll
         for (int s = 0; s < S; ++s) acc[s] += st[s];
       }
@@ -250,18 +271,16 @@ __global__ void __launch_bounds__(kThreads) band_fast_kernel(BandArgs a) {
           const int n = cq[0][0] + cq[0][1] + cq[0][2] + cq[0][3];
           if (a.nvalid) a.nvalid[k] = n;
           if (a.stats) {
-            const fast::Pop p0 = fast::make(cq[0][0], cq[0][1], cq[0][2], cq[0][3], n);
+            const fast::Pop p0 = pop_of(cq[0]);
             float st[3];
-            fast::stats1(p0, st);
-            const long long rd = (long long)(p0.pA * (n - p0.pA)) * (long long)(p0.pB * (n - p0.pB));
-            const float r2 = rd > 0 ? fast::i64_to_f32((long long)p0.x * p0.x) / fast::i64_to_f32(rd)
-                                    : __int_as_float(0x7fc00000);
+            fast::stats1(p0, T, st);
+            const float r2 = fast::r2_of(p0);
             reinterpret_cast<float4*>(a.stats)[k] = make_float4(r2, st[0], st[1], st[2]);
           }
         }
       } else {
         float st[S];
-        pair_stats<P>(cq, st);
+        pair_stats<P>(cq, T, st);
         unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
         while (pending) {
           const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
@@ -302,6 +321,7 @@ int launch_fast_p(pgld_context* h, const BandArgs& a, cudaStream_t st) {
   constexpr int S = (P == 1) ? 3 : 15;
   size_t smem = sizeof(FastSmem);
   if (MODE == kModeBinned) smem += (size_t)kWarps * a.n_bins * (S + 1) * 8;
+  smem += (size_t)4 * (a.nmax + 1) * sizeof(float);
   auto kern = band_fast_kernel<P, MODE>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_fast smem attribute");
@@ -319,10 +339,11 @@ int launch_fast_p(pgld_context* h, const BandArgs& a, cudaStream_t st) {
 
 // one or two populations without validity planes take the fast kernel
 bool band_fast_applies(const BandArgs& a, int mode) {
-  if (mode == kModePairs) return a.n_pops == 1 && a.valid[0] == nullptr && a.W[0] <= 128;
+  // the float32 epilogue is exact for at most 2048 haplotypes per population
+  if (mode == kModePairs) return a.n_pops == 1 && a.valid[0] == nullptr && a.W[0] <= 64;
   if (a.n_pops > 2) return false;
   for (int p = 0; p < a.n_pops; ++p)
-    if (a.valid[p] != nullptr || a.W[p] > 128) return false;  // n <= 4096 per population
+    if (a.valid[p] != nullptr || a.W[p] > 64) return false;
   return true;
 }
 

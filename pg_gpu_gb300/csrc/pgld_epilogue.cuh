@@ -1,14 +1,24 @@
 // Fast float32 finalisation of the moments statistics for 1 and 2
 // populations, shared by the plain and tensor-core band kernels.
 //
-// Every numerator is an exact integer (int32 where it fits, int64 where a
-// sum can cancel) and is converted to float32 once; products of exact
+// Counts arrive as exact float32 integers.  With at most 2048 haplotypes per
+// population every feature below (marginals, c1*c4, x = c1c4 - c2c3,
+// dA*dB + e, the quadratic cofactors of pi2(i,j,i,j), ...) is an integer of
+// magnitude < 2^24, so it is formed exactly in float32 -- on the float32
+// pipes, with no integer-to-float conversions.
+//
+// Numerators whose terms can cancel are evaluated exactly as an unevaluated
+// sum s + e of two float32 (error-free products via fma and error-free sums,
+// "TwoProduct" / "TwoSum"): every term is an integer, so the low parts are
+// small integers that add exactly and s + e rounds once.  64-bit integer
+// multiplies would run at the float64 rate on GB300.  Products of exact
 // integers that cannot cancel are formed directly in float32.  Denominators
-// are exact integers rounded once to float32 and inverted with an IEEE
-// division, so each statistic carries at most four roundings (< 2.5e-7
-// relative).  The formulas are the case formulas of ld_statistics.py
-// (1116-1617) evaluated for the population patterns of the moments tables
-// for one and two populations (ld_pipeline.py:357-457).
+// come from per-CTA tables of reciprocals indexed by the valid sample size n
+// (1/n, 1/(n(n-1)), 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3)), each the IEEE
+// reciprocal of the exact integer rounded once to float32), so each statistic
+// carries at most six roundings (< 4e-7 relative).  The formulas are the case
+// formulas of ld_statistics.py (1116-1617) for the population patterns of the
+// moments tables of one and two populations (ld_pipeline.py:357-457).
 #pragma once
 #include <stdint.h>
 
@@ -25,125 +35,180 @@ namespace fast {
 
 typedef long long i64;
 
-// int32 in [-2^22, 2^22) or int64 in [-2^44, 2^44) to float32, correctly
-// rounded, without the conversion pipe: the exponent-bias trick places the
-// integer in the mantissa of a known float and subtracts the bias.
-PGLD_HD float small_i2f(int v) {
+constexpr int kMaxN = 2048;
+
+// rounded-to-nearest float32 operations that the compiler may not fuse into
+// fma (the error-free transformations depend on each rounding)
+PGLD_HD float fadd(float a, float b) {
 #ifdef __CUDA_ARCH__
-  return __int_as_float(0x4B400000 + v) - 12582912.0f;
+  return __fadd_rn(a, b);
 #else
-  return (float)v;
+  return a + b;
+#endif
+}
+PGLD_HD float fsub(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+PGLD_HD float fmul(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;
 #endif
 }
 
-PGLD_HD float i64_to_f32(i64 v) {
+// exact float32 integer in [0, 2^22) to int without the conversion pipe
+PGLD_HD int f2i_small(float f) {
 #ifdef __CUDA_ARCH__
-  const int hi = (int)(v >> 22);
-  if (hi >= -(1 << 22) && hi < (1 << 22)) {
-    const int lo = (int)(v & 0x3FFFFF);
-    const float fhi = __int_as_float(0x4B400000 + hi) - 12582912.0f;
-    const float flo = __int_as_float(0x4B000000 | lo) - 8388608.0f;
-    return fmaf(fhi, 4194304.0f, flo);  // one rounding
-  }
-  return __ll2float_rn(v);
+  return __float_as_int(f + 12582912.0f) - 0x4B400000;
 #else
-  return (float)v;
+  return (int)f;
 #endif
 }
 
-PGLD_HD float recip_or_zero(float d) { return d > 0.0f ? 1.0f / d : 0.0f; }
-
-// exact per-population integer features
-struct Pop {
-  int c1, c2, c3, c4, n;
-  int pA, qA, pB, qB;
-  int a, b, x;  // c1c4, c2c3, c1c4 - c2c3
-  int dA, dB, e;  // qA - pA, qB - pB, (c2+c3) - (c1+c4)
-  float xf;
-  float nn1f;     // n(n-1)
-  float d4f;      // n(n-1)(n-2)(n-3) rounded once
-  float t3f;      // n(n-1)(n-2) rounded once
+// an integer held exactly as s + e
+struct X2 {
+  float s, e;
 };
 
-PGLD_HD Pop make(int c1, int c2, int c3, int c4, int n) {
+PGLD_HD X2 x2_prod(float a, float b) {
+  const float p = fmul(a, b);
+  return {p, fmaf(a, b, -p)};
+}
+
+// acc += a * b, exactly (a, b integers of magnitude < 2^24)
+PGLD_HD void x2_add_prod(X2& acc, float a, float b) {
+  const float p = fmul(a, b);
+  const float pe = fmaf(a, b, -p);
+  const float s = fadd(acc.s, p);
+  const float bb = fsub(s, acc.s);
+  const float t = fadd(fsub(acc.s, fsub(s, bb)), fsub(p, bb));
+  acc.s = s;
+  acc.e = fadd(acc.e, fadd(pe, t));
+}
+
+PGLD_HD float x2_value(const X2& v) { return fadd(v.s, v.e); }
+
+// reciprocal tables, entries 0..nmax (0 where the integer is 0)
+struct Recip {
+  const float* inv;  // 1/n
+  const float* r2;   // 1/(n(n-1))
+  const float* r3;   // 1/(n(n-1)(n-2))
+  const float* r4;   // 1/(n(n-1)(n-2)(n-3))
+};
+
+PGLD_HD void recip_entry(int n, float* inv, float* r2, float* r3, float* r4) {
+  const i64 m1 = n, m2 = m1 * (n - 1), m3 = m2 * (n - 2), m4 = m3 * (n - 3);
+  *inv = m1 > 0 ? 1.0f / (float)m1 : 0.0f;
+  *r2 = m2 > 0 ? 1.0f / (float)m2 : 0.0f;
+  *r3 = m3 > 0 ? 1.0f / (float)m3 : 0.0f;
+  *r4 = m4 > 0 ? 1.0f / (float)m4 : 0.0f;
+}
+
+// exact per-population features as float32 integers
+struct Pop {
+  float c1, c2, c3, c4;
+  float pA, qA, pB, qB;
+  float a, b, x;    // c1c4, c2c3, c1c4 - c2c3
+  float dA, dB, e;  // qA - pA, qB - pB, (c2+c3) - (c1+c4)
+  int n;            // c1 + c2 + c3 + c4 (the pairwise valid n of 0/1/-1 data)
+};
+
+PGLD_HD Pop make(float c1, float c2, float c3, float c4) {
   Pop p;
-  p.c1 = c1; p.c2 = c2; p.c3 = c3; p.c4 = c4; p.n = n;
+  p.c1 = c1; p.c2 = c2; p.c3 = c3; p.c4 = c4;
   p.pA = c1 + c2; p.qA = c3 + c4; p.pB = c1 + c3; p.qB = c2 + c4;
   p.a = c1 * c4; p.b = c2 * c3; p.x = p.a - p.b;
   p.dA = p.qA - p.pA; p.dB = p.qB - p.pB; p.e = (c2 + c3) - (c1 + c4);
-  p.xf = (float)p.x;
-  const int nn1 = n * (n - 1);
-  p.nn1f = (float)nn1;
-  p.d4f = (n >= 4) ? p.nn1f * (float)((n - 2) * (n - 3)) : 0.0f;
-  p.t3f = (n >= 3) ? p.nn1f * (float)(n - 2) : 0.0f;
+  p.n = f2i_small(p.pA + p.qA);
   return p;
 }
 
-// numerators of the single-population cases (exact)
-PGLD_HD i64 dd_num(const Pop& p) {
-  return (i64)p.x * p.x - ((i64)p.a * (p.c1 + p.c4 - 1) + (i64)p.b * (p.c2 + p.c3 - 1));
+// c1(c1-1)c4(c4-1) + c2(c2-1)c3(c3-1) - 2c1c2c3c4 = x^2 - a(c1+c4-1) - b(c2+c3-1)
+PGLD_HD float dd_num(const Pop& p) {
+  X2 v = x2_prod(p.x, p.x);
+  x2_add_prod(v, p.a, 1.0f - p.c1 - p.c4);
+  x2_add_prod(v, p.b, 1.0f - p.c2 - p.c3);
+  return x2_value(v);
 }
-PGLD_HD float dz_num_f(const Pop& p) {
-  // x*(dA*dB + e) + 2(a+b): the fma rounds once, and whenever the two terms
-  // can cancel the product is below 2^24 and exact
-  return fmaf(p.xf, (float)(p.dA * p.dB + p.e), (float)(2 * (p.a + p.b)));
-}
-PGLD_HD i64 pi2_num(const Pop& p) {
-  return (i64)(p.pA * p.pB) * (p.qB * p.qA) - (i64)p.a * (-1 + p.c1 + 3 * p.c2 + 3 * p.c3 + p.c4) -
-         (i64)p.b * (-1 + 3 * p.c1 + p.c2 + p.c3 + 3 * p.c4);
+// x*(dA*dB + e) + 2(a+b): the fma rounds once, and whenever the two terms can
+// cancel the product is below 2^24 and exact
+PGLD_HD float dz_num(const Pop& p) { return fmaf(p.x, p.dA * p.dB + p.e, 2.0f * (p.a + p.b)); }
+PGLD_HD float pi2_num(const Pop& p) {
+  X2 v = x2_prod(p.pA * p.pB, p.qB * p.qA);
+  x2_add_prod(v, p.a, 1.0f - p.c1 - 3.0f * p.c2 - 3.0f * p.c3 - p.c4);
+  x2_add_prod(v, p.b, 1.0f - 3.0f * p.c1 - p.c2 - p.c3 - 3.0f * p.c4);
+  return x2_value(v);
 }
 // pi2 with population t three times and s once, times 2
-PGLD_HD i64 triple_num2(const Pop& t, const Pop& s) {
-  return (i64)(t.pA * t.qA) * (t.qB * s.pB + t.pB * s.qB - 2 * s.qB) +
-         (i64)(t.pA * t.c4 + t.c2 * t.qA) * (s.qB - s.pB);
+PGLD_HD float triple_num2(const Pop& t, const Pop& s) {
+  X2 v = x2_prod(t.pA * t.qA, t.qB * s.pB + t.pB * s.qB - 2.0f * s.qB);
+  x2_add_prod(v, t.pA * t.c4 + t.c2 * t.qA, s.qB - s.pB);
+  return x2_value(v);
 }
 // pi2(i,j,i,j) times 4 (symmetric in the two populations)
-PGLD_HD i64 ijij_num4(const Pop& A, const Pop& B) {
-  const int a1 = A.c1, a2 = A.c2, a3 = A.c3, a4 = A.c4;
-  const int b1 = B.c1, b2 = B.c2, b3 = B.c3, b4 = B.c4;
-  i64 q = (i64)(A.qB * A.qA) * (B.pA * B.pB) + (i64)(A.pB * A.qA) * (B.pA * B.qB) +
-          (i64)(A.pA * A.qB) * (B.pB * B.qA) + (i64)(A.pA * A.pB) * (B.qB * B.qA);
-  const int g1 = a4 - a2 * a3 - a2 * a4 - a3 * a4 - a4 * a4 - a4 * b1;
-  const int g2 = a3 - a1 * a3 - a3 * a3 - a1 * a4 - a3 * a4 - a3 * b1 - a4 * b1 - a3 * b2;
-  const int g3 = a2 - a1 * a2 - a2 * a2 - a1 * a4 - a2 * a4 - a2 * b1 - a4 * b1 - a1 * b2 - a4 * b2 -
-                 a2 * b3;
-  const int g4 = a1 - a1 * a1 - a1 * a2 - a1 * a3 - a2 * a3 - a2 * b1 - a3 * b1 - a1 * b2 - a3 * b2 -
-                 a1 * b3 - a2 * b3 - a1 * b4;
-  return q + (i64)b1 * g1 + (i64)b2 * g2 + (i64)b3 * g3 + (i64)b4 * g4;
+PGLD_HD float ijij_num4(const Pop& A, const Pop& B) {
+  const float a1 = A.c1, a2 = A.c2, a3 = A.c3, a4 = A.c4;
+  const float b1 = B.c1, b2 = B.c2, b3 = B.c3, b4 = B.c4;
+  const float g1 = a4 - a2 * a3 - a2 * a4 - a3 * a4 - a4 * a4 - a4 * b1;
+  const float g2 = a3 - a1 * a3 - a3 * a3 - a1 * a4 - a3 * a4 - a3 * b1 - a4 * b1 - a3 * b2;
+  const float g3 = a2 - a1 * a2 - a2 * a2 - a1 * a4 - a2 * a4 - a2 * b1 - a4 * b1 - a1 * b2 -
+                   a4 * b2 - a2 * b3;
+  const float g4 = a1 - a1 * a1 - a1 * a2 - a1 * a3 - a2 * a3 - a2 * b1 - a3 * b1 - a1 * b2 -
+                   a3 * b2 - a1 * b3 - a2 * b3 - a1 * b4;
+  X2 v = x2_prod(A.qB * A.qA, B.pA * B.pB);
+  x2_add_prod(v, A.pB * A.qA, B.pA * B.qB);
+  x2_add_prod(v, A.pA * A.qB, B.pB * B.qA);
+  x2_add_prod(v, A.pA * A.pB, B.qB * B.qA);
+  x2_add_prod(v, b1, g1);
+  x2_add_prod(v, b2, g2);
+  x2_add_prod(v, b3, g3);
+  x2_add_prod(v, b4, g4);
+  return x2_value(v);
 }
 
 // DD, Dz, pi2 of one population (moments order for one population)
-PGLD_HD void stats1(const Pop& p, float out[3]) {
-  const float r4 = recip_or_zero(p.d4f);
-  out[0] = i64_to_f32(dd_num(p)) * r4;
-  out[1] = dz_num_f(p) * r4;
-  out[2] = i64_to_f32(pi2_num(p)) * r4;
+PGLD_HD void stats1(const Pop& p, const Recip& T, float out[3]) {
+  const float r4 = T.r4[p.n];
+  out[0] = dd_num(p) * r4;
+  out[1] = dz_num(p) * r4;
+  out[2] = pi2_num(p) * r4;
+}
+
+// r^2 = x^2 / (pA (n-pA) pB (n-pB)), NaN where undefined
+PGLD_HD float r2_of(const Pop& p) {
+  const float num = x2_value(x2_prod(p.x, p.x));
+  const float den = x2_value(x2_prod(p.pA * p.qA, p.pB * p.qB));
+  return den > 0.0f ? num / den : NAN;
 }
 
 // the 15 two-population statistics in moments ld_names(2) order:
 // DD_0_0 DD_0_1 DD_1_1 Dz_0_0_0 Dz_0_0_1 Dz_0_1_1 Dz_1_0_0 Dz_1_0_1 Dz_1_1_1
 // pi2_0_0_0_0 pi2_0_0_0_1 pi2_0_0_1_1 pi2_0_1_0_1 pi2_0_1_1_1 pi2_1_1_1_1
-PGLD_HD void stats2(const Pop& p, const Pop& q, float o[15]) {
-  const float r4p = recip_or_zero(p.d4f), r4q = recip_or_zero(q.d4f);
-  const float r22 = recip_or_zero(p.nn1f * q.nn1f);
-  const float r31p = recip_or_zero((float)q.n * p.t3f);  // n_q * n_p(n_p-1)(n_p-2)
-  const float r31q = recip_or_zero((float)p.n * q.t3f);
-  o[0] = i64_to_f32(dd_num(p)) * r4p;
-  o[1] = (p.xf * q.xf) * r22;
-  o[2] = i64_to_f32(dd_num(q)) * r4q;
-  o[3] = dz_num_f(p) * r4p;
-  o[4] = (p.xf * (float)(p.dA * q.dB + p.dB * q.dA)) * (0.5f * r31p);
-  o[5] = (p.xf * (float)(q.e + q.dB * q.dA)) * r22;
-  o[6] = (q.xf * (float)(p.e + p.dB * p.dA)) * r22;
-  o[7] = (q.xf * (float)(q.dA * p.dB + q.dB * p.dA)) * (0.5f * r31q);
-  o[8] = dz_num_f(q) * r4q;
-  o[9] = i64_to_f32(pi2_num(p)) * r4p;
-  o[10] = i64_to_f32(triple_num2(p, q)) * (0.5f * r31p);
-  o[11] = fmaf((float)(p.pA * p.qA), (float)(q.pB * q.qB), (float)(q.pA * q.qA) * (float)(p.pB * p.qB)) *
-          (0.5f * r22);
-  o[12] = i64_to_f32(ijij_num4(p, q)) * (0.25f * r22);
-  o[13] = i64_to_f32(triple_num2(q, p)) * (0.5f * r31q);
-  o[14] = i64_to_f32(pi2_num(q)) * r4q;
+PGLD_HD void stats2(const Pop& p, const Pop& q, const Recip& T, float o[15]) {
+  const float r4p = T.r4[p.n], r4q = T.r4[q.n];
+  const float r22 = T.r2[p.n] * T.r2[q.n];
+  const float r31p = T.r3[p.n] * T.inv[q.n];  // 1 / (n_q * n_p(n_p-1)(n_p-2))
+  const float r31q = T.r3[q.n] * T.inv[p.n];
+  o[0] = dd_num(p) * r4p;
+  o[1] = (p.x * q.x) * r22;
+  o[2] = dd_num(q) * r4q;
+  o[3] = dz_num(p) * r4p;
+  o[4] = (p.x * (p.dA * q.dB + p.dB * q.dA)) * (0.5f * r31p);
+  o[5] = (p.x * (q.e + q.dB * q.dA)) * r22;
+  o[6] = (q.x * (p.e + p.dB * p.dA)) * r22;
+  o[7] = (q.x * (q.dA * p.dB + q.dB * p.dA)) * (0.5f * r31q);
+  o[8] = dz_num(q) * r4q;
+  o[9] = pi2_num(p) * r4p;
+  o[10] = triple_num2(p, q) * (0.5f * r31p);
+  o[11] = fmaf(p.pA * p.qA, q.pB * q.qB, (q.pA * q.qA) * (p.pB * p.qB)) * (0.5f * r22);
+  o[12] = ijij_num4(p, q) * (0.25f * r22);
+  o[13] = triple_num2(q, p) * (0.5f * r31q);
+  o[14] = pi2_num(q) * r4q;
 }
 
 }  // namespace fast

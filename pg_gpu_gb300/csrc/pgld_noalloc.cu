@@ -7,6 +7,7 @@
 // until the process exits.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -172,6 +173,8 @@ extern "C" int pgld_hap_binned_sums_noalloc(int device, const pgld_hap_panel* pa
           a.valid[p] = p < P ? panel->valid[p] : nullptr;
         }
         a.n_snp = n;
+        a.nmax = 0;
+        for (int p = 0; p < P; ++p) a.nmax = std::max(a.nmax, 32 * panel->n_words[p]);
         a.pos = pos;
         a.max_dist = max_dist;
         a.bcoord = bin_coord;

@@ -63,6 +63,9 @@ struct Params {
   int64_t* pair_counts;
   int32_t* status;
   int stages;
+  int nmax;  // largest per-population sample size (reciprocal table length - 1)
+  const int* ipos;     // integer positions (valid when *ipos_bad == 0)
+  const int* ipos_bad;
 };
 
 // ---------------------------------------------------------------------------
@@ -159,14 +162,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
-__device__ __forceinline__ void epi_bar() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
-}
-
-__device__ __forceinline__ int f2i_exact(uint32_t bits) {
-  // the counts are exact integers below 2^22 stored as float32
-  return __float_as_int(__uint_as_float(bits) + 12582912.0f) - 0x4B400000;
-}
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -193,12 +188,6 @@ __device__ __forceinline__ int bin_of_f64(const double* sb, int n_bins, double d
   return lo;
 }
 
-struct Meta {
-  int reli[kTileSnp], relj[kTileSnp];
-  int isint[2 * kTileSnp];
-  int tile_int, tile_bin;
-};
-
 struct Ctrl {
   uint64_t full[8], empty[8], tfull[2], tempty[2], drain;
   uint32_t tmem_base;
@@ -209,6 +198,28 @@ struct Ctrl {
 __device__ __forceinline__ void set_abort(Ctrl* c, int32_t* status, int code) {
   if (status) atomicCAS(status, 0, code);
   *(volatile int*)&c->abort_flag = 1;
+}
+
+// compensated (Neumaier) float32 accumulation: slot.x = sum, slot.y = correction
+__device__ __forceinline__ void kahan_add(float2* slot, float v) {
+  const float s = slot->x;
+  const float t = __fadd_rn(s, v);
+  const float bp = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(v, bp));
+  slot->x = t;
+  slot->y = __fadd_rn(slot->y, err);
+}
+
+// every lane receives the warp total of each statistic; lane s keeps stat s
+template <int S>
+__device__ __forceinline__ float warp_totals_pick(const float (&v)[S], int lane) {
+  float mine = 0.f;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const float t = warp_sum(v[s]);
+    if (lane == s) mine = t;
+  }
+  return mine;
 }
 
 template <int P>
@@ -223,11 +234,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int stages = a.stages;
   unsigned char* ring = base;
   Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kStageBytes);
-  Meta* meta = reinterpret_cast<Meta*>(ctrl + 1);  // [2]
-  double* sbins = reinterpret_cast<double*>(meta + 2);
+  double* sbins = reinterpret_cast<double*>(ctrl + 1);
   int* thr = reinterpret_cast<int*>(sbins + (kMaxBins + 1));
-  double* accw = reinterpret_cast<double*>(thr + (kMaxBins + 2));  // [kEpiWarps][n_bins][S]
-  unsigned long long* cntw = reinterpret_cast<unsigned long long*>(accw + kEpiWarps * a.n_bins * S);
+  float2* kacc = reinterpret_cast<float2*>(thr + (kMaxBins + 2));  // [kEpiWarps][n_bins][S]
+  unsigned long long* kcnt =
+      reinterpret_cast<unsigned long long*>(kacc + kEpiWarps * a.n_bins * S);  // [kEpiWarps][n_bins]
+  float* tables = reinterpret_cast<float*>(kcnt + kEpiWarps * a.n_bins);     // 4 x (nmax + 1)
+  fast::Recip T;
+  T.inv = tables;
+  T.r2 = tables + (a.nmax + 1);
+  T.r3 = tables + 2 * (a.nmax + 1);
+  T.r4 = tables + 3 * (a.nmax + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_bins = a.n_bins;
@@ -257,8 +274,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (warp >= 4) {
     const int t = threadIdx.x - 128;
-    for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) accw[x] = 0.0;
-    for (int x = t; x < kEpiWarps * n_bins; x += kEpiThreads) cntw[x] = 0ull;
+    for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) kacc[x] = make_float2(0.f, 0.f);
+    for (int x = t; x < kEpiWarps * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
+    for (int x = t; x <= a.nmax; x += kEpiThreads)
+      fast::recip_entry(x, tables + x, tables + (a.nmax + 1) + x, tables + 2 * (a.nmax + 1) + x,
+                        tables + 3 * (a.nmax + 1) + x);
     for (int x = t; x <= n_bins; x += kEpiThreads) {
       const double b = a.bins[x];
       sbins[x] = b;
@@ -374,14 +394,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp >= 4) {
     // ---------------- epilogue ----------------
+    // Warp e reads TMEM lane quarter (warp & 3) and column half (e >> 2): the
+    // 16 x 32 sub-tile i in i0 + 16*quarter + [0,16), j in j0 + 32*half + [0,32).
     const int e = warp - 4;
-    const int quarter = warp & 3;       // TMEM lanes 32*quarter .. +31
-    const int half = e >> 2;            // j columns 32*half .. +31 of the tile
+    const int quarter = warp & 3;
+    const int half = e >> 2;
     const int row = quarter * 32 + lane;  // D row: SNP i = row/2, plane = row&1
     const int il = row >> 1, plane = row & 1;
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
+    const bool use_int = (a.bcoord == nullptr) && (*a.ipos_bad == 0);
+    float2* my_acc = kacc + (size_t)e * n_bins * S;
+    unsigned long long* my_cnt = kcnt + (size_t)e * n_bins;
     int t = 0;
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
       const int acc = t & 1;
@@ -393,41 +418,28 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       const long long bi = lo, bj = bi + (item - a.item_off[bi]);
       const long long i0 = bi * kTileSnp, j0 = bj * kTileSnp;
-      Meta& m = meta[acc];
-      // tile coordinates (threads 0..127 of the epilogue): integer offsets from pos[i0]
-      epi_bar();  // every epilogue warp is done with the previous tile's metadata
-      const int et = threadIdx.x - 128;
-      if (et < 2 * kTileSnp) {
-        const int tt = et & (kTileSnp - 1);
-        const long long s = (et < kTileSnp ? i0 : j0) + tt;
-        int r = 0, isint = 1;
-        if (s < a.n_snp) {
-          const double rel = a.pos[s] - a.pos[i0];
-          isint = (rel == rint(rel)) && fabs(rel) < 1073741824.0;
-          r = isint ? (int)rel : 0;
-        }
-        if (et < kTileSnp) m.reli[tt] = r; else m.relj[tt] = r;
-        m.isint[et] = isint;
-      }
-      epi_bar();
-      if (et == 0) {
-        int all = (a.bcoord == nullptr);
-        for (int k = 0; k < 2 * kTileSnp; ++k) all &= m.isint[k];
-        m.tile_int = all;
-        int tb = -1;
-        if (all && bj > bi && j0 + kTileSnp <= a.n_snp) {
-          const int dmin = m.relj[0] - m.reli[kTileSnp - 1];
-          const int dmax = m.relj[kTileSnp - 1] - m.reli[0];
-          if (dmax <= maxd_int) {
-            const int b0 = bin_of_int(thr, n_bins, dmin);
-            if (b0 >= 0 && b0 == bin_of_int(thr, n_bins, dmax)) tb = b0;
+      const long long si0 = i0 + 16 * quarter, sj0 = j0 + 32 * half;
+      const long long i = i0 + il;
+
+      // classify the warp's sub-tile: 0 one bin, 1 two adjacent bins, 2 general
+      int mode = 2, b0 = -1, thr_mid = 0;
+      if (use_int && bj > bi && sj0 + 31 < a.n_snp) {
+        const int dmin = a.ipos[sj0] - a.ipos[si0 + 15];
+        const int dmax = a.ipos[sj0 + 31] - a.ipos[si0];
+        if (dmax <= maxd_int) {
+          const int blo = bin_of_int(thr, n_bins, dmin);
+          const int bhi = bin_of_int(thr, n_bins, dmax);
+          if (blo >= 0 && bhi == blo) {
+            mode = 0;
+            b0 = blo;
+          } else if (blo >= 0 && bhi == blo + 1) {
+            mode = 1;
+            b0 = blo;
+            thr_mid = thr[bhi];
           }
         }
-        m.tile_bin = tb;
       }
-      epi_bar();
-      const int tile_bin = m.tile_bin;
-      const bool tint = m.tile_int;
+      const int ipos_i = (use_int && i < a.n_snp) ? a.ipos[i] : 0;
 
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
@@ -438,9 +450,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       tc_fence_after();
 
-      float accs[S];
+      float acc_lo[S], acc_hi[S];
 #pragma unroll
-      for (int s = 0; s < S; ++s) accs[s] = 0.f;
+      for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
+      int n_hi = 0;
 #pragma unroll 1
       for (int c = 0; c < 4; ++c) {
         uint32_t r[P][16];
@@ -453,54 +466,65 @@ __global__ void __launch_bounds__(kThreads, 1)
           __syncwarp();
           if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
         }
-        float chunk[S];
+        // counts of this lane's four pairs of the chunk, as exact float32:
+        // plane 0 rows hold (n11, n10) of every j, plane 1 rows (n01, n00), so
+        // partner lanes swap halves and each lane owns whole pairs
+        float cf[4][P][4];
 #pragma unroll
-        for (int s = 0; s < S; ++s) chunk[s] = 0.f;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          int cnt[P][4];
+        for (int q = 0; q < 4; ++q)
 #pragma unroll
           for (int p = 0; p < P; ++p) {
-            // plane 0 rows hold (n11, n10) of every j, plane 1 rows (n01, n00):
-            // swap halves with the partner lane so each lane owns whole pairs
             const uint32_t s0 = plane ? r[p][4 * q] : r[p][4 * q + 2];
             const uint32_t s1 = plane ? r[p][4 * q + 1] : r[p][4 * q + 3];
-            const uint32_t g0 = __shfl_xor_sync(0xffffffffu, s0, 1);
-            const uint32_t g1 = __shfl_xor_sync(0xffffffffu, s1, 1);
-            if (plane == 0) {
-              cnt[p][0] = f2i_exact(r[p][4 * q]);
-              cnt[p][1] = f2i_exact(r[p][4 * q + 1]);
-              cnt[p][2] = f2i_exact(g0);
-              cnt[p][3] = f2i_exact(g1);
-            } else {
-              cnt[p][0] = f2i_exact(g0);
-              cnt[p][1] = f2i_exact(g1);
-              cnt[p][2] = f2i_exact(r[p][4 * q + 2]);
-              cnt[p][3] = f2i_exact(r[p][4 * q + 3]);
-            }
+            const float g0 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
+            const float g1 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
+            const float m0 = __uint_as_float(plane ? r[p][4 * q + 2] : r[p][4 * q]);
+            const float m1 = __uint_as_float(plane ? r[p][4 * q + 3] : r[p][4 * q + 1]);
+            cf[q][p][0] = plane ? g0 : m0;
+            cf[q][p][1] = plane ? g1 : m1;
+            cf[q][p][2] = plane ? m0 : g0;
+            cf[q][p][3] = plane ? m1 : g1;
           }
+        // one pair per iteration over rotating arrays: the statistics code is
+        // emitted once (instruction-cache footprint)
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
           const int jl = half * 32 + c * 8 + 2 * q + plane;
-          const long long i = i0 + il, j = j0 + jl;
+          const long long j = j0 + jl;
           float st[S];
           {
-            fast::Pop p0 = fast::make(cnt[0][0], cnt[0][1], cnt[0][2], cnt[0][3],
-                                      cnt[0][0] + cnt[0][1] + cnt[0][2] + cnt[0][3]);
+            const fast::Pop p0 = fast::make(cf[0][0][0], cf[0][0][1], cf[0][0][2], cf[0][0][3]);
             if (P == 1) {
-              fast::stats1(p0, st);
+              fast::stats1(p0, T, st);
             } else {
-              fast::Pop p1 = fast::make(cnt[P - 1][0], cnt[P - 1][1], cnt[P - 1][2], cnt[P - 1][3],
-                                        cnt[P - 1][0] + cnt[P - 1][1] + cnt[P - 1][2] + cnt[P - 1][3]);
-              fast::stats2(p0, p1, st);
+              const fast::Pop p1 =
+                  fast::make(cf[0][P - 1][0], cf[0][P - 1][1], cf[0][P - 1][2], cf[0][P - 1][3]);
+              fast::stats2(p0, p1, T, st);
             }
           }
-          if (tile_bin >= 0) {
 #pragma unroll
-            for (int s = 0; s < S; ++s) chunk[s] += st[s];
+          for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int p = 0; p < P; ++p)
+#pragma unroll
+              for (int m = 0; m < 4; ++m) cf[k][p][m] = cf[k + 1][p][m];
+          if (mode == 0) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) acc_lo[s] += st[s];
+          } else if (mode == 1) {
+            const bool up = (a.ipos[j] - ipos_i) >= thr_mid;
+            const float fu = up ? 1.f : 0.f, fl = up ? 0.f : 1.f;
+            n_hi += up ? 1 : 0;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              acc_hi[s] = fmaf(fu, st[s], acc_hi[s]);
+              acc_lo[s] = fmaf(fl, st[s], acc_lo[s]);
+            }
           } else {
             bool ok = (i < j) && (j < a.n_snp);
             int b = -1;
-            if (tint) {
-              const int d = m.relj[jl] - m.reli[il];
+            if (use_int) {
+              const int d = ok ? a.ipos[j] - ipos_i : 0;
               if (ok && d <= maxd_int) b = bin_of_int(thr, n_bins, d);
             } else if (ok) {
               const double dp = a.pos[j] - a.pos[i];
@@ -514,28 +538,29 @@ __global__ void __launch_bounds__(kThreads, 1)
               const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
               const bool mine = (b == bb);
               const unsigned grp = __ballot_sync(0xffffffffu, mine);
+              float v[S];
 #pragma unroll
-              for (int s = 0; s < S; ++s) {
-                const float v = warp_sum(mine ? st[s] : 0.f);
-                if (lane == 0) accw[(e * n_bins + bb) * S + s] += (double)v;
-              }
-              if (lane == 0) cntw[e * n_bins + bb] += (unsigned long long)__popc(grp);
+              for (int s = 0; s < S; ++s) v[s] = mine ? st[s] : 0.f;
+              const float tot = warp_totals_pick<S>(v, lane);
+              if (lane < S) kahan_add(my_acc + bb * S + lane, tot);
+              if (lane == 31) my_cnt[bb] += (unsigned long long)__popc(grp);
               pending &= ~grp;
             }
           }
         }
-        if (tile_bin >= 0) {
-#pragma unroll
-          for (int s = 0; s < S; ++s) accs[s] += chunk[s];
-        }
       }
-      if (tile_bin >= 0) {
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const float v = warp_sum(accs[s]);
-          if (lane == 0) accw[(e * n_bins + tile_bin) * S + s] += (double)v;
+      if (mode <= 1) {
+        const float tot = warp_totals_pick<S>(acc_lo, lane);
+        if (lane < S) kahan_add(my_acc + b0 * S + lane, tot);
+        const int hi_total = __reduce_add_sync(0xffffffffu, n_hi);
+        if (mode == 1) {
+          const float tot_hi = warp_totals_pick<S>(acc_hi, lane);
+          if (lane < S) kahan_add(my_acc + (b0 + 1) * S + lane, tot_hi);
         }
-        if (lane == 0) cntw[e * n_bins + tile_bin] += 32ull * 16ull;
+        if (lane == 31) {
+          my_cnt[b0] += (unsigned long long)(512 - hi_total);
+          if (mode == 1) my_cnt[b0 + 1] += (unsigned long long)hi_total;
+        }
       }
     }
   }
@@ -548,14 +573,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x < n_bins * S; x += kEpiThreads) {
       double v = 0.0;
 #pragma unroll
-      for (int w = 0; w < kEpiWarps; ++w) v += accw[w * n_bins * S + x];
+      for (int w = 0; w < kEpiWarps; ++w) {
+        const float2 k = kacc[w * n_bins * S + x];
+        v += (double)k.x + (double)k.y;
+      }
       if (v != 0.0) atomicAdd(a.sums + x, v);
     }
     if (a.pair_counts)
       for (int x = t; x < n_bins; x += kEpiThreads) {
         unsigned long long v = 0;
 #pragma unroll
-        for (int w = 0; w < kEpiWarps; ++w) v += cntw[w * n_bins + x];
+        for (int w = 0; w < kEpiWarps; ++w) v += kcnt[w * n_bins + x];
         if (v) atomicAdd(reinterpret_cast<unsigned long long*>(a.pair_counts) + x, v);
       }
   }
@@ -564,6 +592,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(kTmemCols)
                  : "memory");
+  }
+}
+
+// integer copy of the positions for exact integer distances; *bad = 1 when a
+// position is not an integer or lies outside (-2^30, 2^30)
+__global__ void pos_to_int_kernel(const double* __restrict__ pos, long long n, int* __restrict__ ipos,
+                                  int* __restrict__ bad) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    const double v = pos[k];
+    const bool ok = (v == rint(v)) && fabs(v) < 1073741824.0;
+    ipos[k] = ok ? (int)v : 0;
+    if (!ok) atomicOr(bad, 1);
   }
 }
 
@@ -661,9 +702,10 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
   const size_t sb = pgld::scan_scratch_bytes(nb);
   auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
   const size_t off_items = 0, off_scan = al((nb + 1) * 8), off_op0 = off_scan + al(sb),
-               off_op1 = off_op0 + al(op_bytes[0]);
+               off_op1 = off_op0 + al(op_bytes[0]), off_ipos = off_op1 + al(op_bytes[1]),
+               off_bad = off_ipos + al((size_t)n * 4);
   void* ws = nullptr;
-  rc = pgld_workspace(h, off_op1 + al(op_bytes[1]) + 1024, &ws);
+  rc = pgld_workspace(h, off_bad + 1024, &ws);
   if (rc) return rc;
   char* w = (char*)ws;
   long long* items = (long long*)(w + off_items);
@@ -681,6 +723,16 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
   // 64-SNP tile work list
   rc = pgld::band_schedule(h, a.pos, n, a.max_dist, items, w + off_scan, sb, st, kTileSnp);
   if (rc) return rc;
+  int* ipos = (int*)(w + off_ipos);
+  int* ipos_bad = (int*)(w + off_bad);
+  {
+    cudaError_t e = cudaMemsetAsync(ipos_bad, 0, 4, st);
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "memset");
+    unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, h->n_sm * 8));
+    pos_to_int_kernel<<<blocks, 256, 0, st>>>(a.pos, n, ipos, ipos_bad);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pos_to_int_kernel");
+  }
   CUtensorMap maps[2];
   for (int p = 0; p < P; ++p) {
     rc = make_map(h, &maps[p], ops[p], 2 * n, k_pad[p]);
@@ -702,9 +754,14 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
   prm.sums = a.sums;
   prm.pair_counts = a.pair_counts;
   prm.status = h->dev_status;
+  prm.ipos = ipos;
+  prm.ipos_bad = ipos_bad;
+  prm.nmax = 0;
+  for (int p = 0; p < P; ++p) prm.nmax = std::max(prm.nmax, 32 * panel->n_words[p]);
 
-  const size_t fixed = sizeof(Ctrl) + 2 * sizeof(Meta) + (pgld::kMaxBins + 1) * 8 +
-                       (pgld::kMaxBins + 2) * 4 + (size_t)kEpiWarps * a.n_bins * (S + 1) * 8 + 1024;
+  const size_t fixed = sizeof(Ctrl) + (pgld::kMaxBins + 1) * 8 + (pgld::kMaxBins + 2) * 4 +
+                       (size_t)kEpiWarps * a.n_bins * (S + 1) * 8 +
+                       (size_t)4 * (prm.nmax + 1) * sizeof(float) + 1024;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
   int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStageBytes);

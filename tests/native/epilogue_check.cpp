@@ -1,18 +1,27 @@
 // Host build of the float32 statistic epilogue (pg_gpu_gb300/csrc/pgld_epilogue.cuh)
-// for tests/test_epilogue_cpu.py: the same formulas as the device kernels, with
-// the host's correctly rounded conversions in place of the device bit tricks.
+// for tests/test_epilogue_cpu.py: the same formulas and reciprocal tables as the
+// device kernels, with the host's correctly rounded conversions in place of the
+// device bit tricks.
+#include <vector>
+
 #include "../../pg_gpu_gb300/csrc/pgld_epilogue.cuh"
 
 extern "C" void pgld_check_stats(const int* counts, const int* n, int N, int P, float* out) {
   using namespace pgld::fast;
+  int nmax = 0;
+  for (int k = 0; k < N * 2; ++k) nmax = n[k] > nmax ? n[k] : nmax;
+  std::vector<float> tab(4 * (nmax + 1));
+  for (int v = 0; v <= nmax; ++v)
+    recip_entry(v, &tab[v], &tab[(nmax + 1) + v], &tab[2 * (nmax + 1) + v], &tab[3 * (nmax + 1) + v]);
+  Recip T{&tab[0], &tab[nmax + 1], &tab[2 * (nmax + 1)], &tab[3 * (nmax + 1)]};
   for (int k = 0; k < N; ++k) {
     const int* c = counts + 8 * k;
-    Pop p = make(c[0], c[1], c[2], c[3], n[2 * k]);
+    Pop p = make((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
     if (P == 1) {
-      stats1(p, out + 3 * k);
+      stats1(p, T, out + 3 * k);
     } else {
-      Pop q = make(c[4], c[5], c[6], c[7], n[2 * k + 1]);
-      stats2(p, q, out + 15 * k);
+      Pop q = make((float)c[4], (float)c[5], (float)c[6], (float)c[7]);
+      stats2(p, q, T, out + 15 * k);
     }
   }
 }
