@@ -150,24 +150,20 @@ PGLD_HD float triple_num2(const Pop& t, const Pop& s) {
   x2_add_prod(v, t.pA * t.c4 + t.c2 * t.qA, s.qB - s.pB);
   return x2_value(v);
 }
-// pi2(i,j,i,j) times 4 (symmetric in the two populations)
+// pi2(i,j,i,j) times 4 (symmetric in the two populations).  The quartic and
+// cubic polynomial of the reference (ld_statistics.py:1349-1402) equals
+//   H_A H_B + (1 - n_A - n_B) K - x_A e_B - x_B e_A
+// with H_A = qA_A pA_B + pA_A qA_B, H_B = qB_A pB_B + pB_A qB_B and
+// K = c1_A c4_B + c2_A c3_B + c3_A c2_B + c4_A c1_B (an algebraic identity,
+// checked term by term against the oracle in tests/test_epilogue_cpu.py).
 PGLD_HD float ijij_num4(const Pop& A, const Pop& B) {
-  const float a1 = A.c1, a2 = A.c2, a3 = A.c3, a4 = A.c4;
-  const float b1 = B.c1, b2 = B.c2, b3 = B.c3, b4 = B.c4;
-  const float g1 = a4 - a2 * a3 - a2 * a4 - a3 * a4 - a4 * a4 - a4 * b1;
-  const float g2 = a3 - a1 * a3 - a3 * a3 - a1 * a4 - a3 * a4 - a3 * b1 - a4 * b1 - a3 * b2;
-  const float g3 = a2 - a1 * a2 - a2 * a2 - a1 * a4 - a2 * a4 - a2 * b1 - a4 * b1 - a1 * b2 -
-                   a4 * b2 - a2 * b3;
-  const float g4 = a1 - a1 * a1 - a1 * a2 - a1 * a3 - a2 * a3 - a2 * b1 - a3 * b1 - a1 * b2 -
-                   a3 * b2 - a1 * b3 - a2 * b3 - a1 * b4;
-  X2 v = x2_prod(A.qB * A.qA, B.pA * B.pB);
-  x2_add_prod(v, A.pB * A.qA, B.pA * B.qB);
-  x2_add_prod(v, A.pA * A.qB, B.pB * B.qA);
-  x2_add_prod(v, A.pA * A.pB, B.qB * B.qA);
-  x2_add_prod(v, b1, g1);
-  x2_add_prod(v, b2, g2);
-  x2_add_prod(v, b3, g3);
-  x2_add_prod(v, b4, g4);
+  const float HA = A.qA * B.pA + A.pA * B.qA;
+  const float HB = A.qB * B.pB + A.pB * B.qB;
+  const float K = A.c1 * B.c4 + A.c2 * B.c3 + A.c3 * B.c2 + A.c4 * B.c1;
+  X2 v = x2_prod(HA, HB);
+  x2_add_prod(v, 1.0f - (A.pA + A.qA) - (B.pA + B.qA), K);
+  x2_add_prod(v, -A.x, B.e);
+  x2_add_prod(v, -B.x, A.e);
   return x2_value(v);
 }
 
