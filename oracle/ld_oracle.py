@@ -686,3 +686,258 @@ def rogers_huff_r_pairs(geno, idx_i, idx_j):
     ok = den > 0
     out[ok] = cov[ok].astype(np.float64) / np.sqrt(den[ok].astype(np.float64))
     return out
+
+
+# ---------------------------------------------------------------------------
+# genotype path: 9-way counts -> moments genotype statistics
+# (genotype_kernels.py:27-936, ld_statistics_genotype.py:1518-1598)
+# ---------------------------------------------------------------------------
+def _geno_poly(table, g):
+    """sum of coef * g[a] * g[b] * g[c] over a monomial table (g[9] = 1)."""
+    acc = np.zeros(g.shape[1], I64)
+    for coef, (a, b, c) in table:
+        acc = acc + coef * g[a] * g[b] * g[c]
+    return acc
+
+
+class GenoPop:
+    """Integer per-pair features of one population from 9-way counts.
+
+    ``counts`` columns are the reference's n00, n01, ..., n22 (dosage at the
+    first SNP times 3 plus dosage at the second, ld_pipeline.py:183-217); the
+    features use moments order g1 = n22, ..., g9 = n00 (genotype_kernels.py:
+    423-435).  Every half- or quarter-integer quantity of _PopDataGeno
+    (genotype_kernels.py:437-521) is carried scaled to an integer:
+    P2 = 2 pA, R2 = 2 qA, Q2 = 2 pB, S2 = 2 qB, X.. = 4 x.., D16 = 16 D_geno.
+    """
+
+    def __init__(self, counts, n_valid=None):
+        c = np.asarray(counts).astype(I64)
+        g = [c[:, 8 - k] for k in range(9)] + [np.ones(len(c), I64)]
+        self.g = np.stack(g)
+        g1, g2, g3, g4, g5, g6, g7, g8, g9 = g[:9]
+        self.ns = c.sum(axis=1)
+        self.n = self.ns if n_valid is None else np.asarray(n_valid).astype(I64)
+        self.P2 = 2 * (g1 + g2 + g3) + g4 + g5 + g6
+        self.R2 = g4 + g5 + g6 + 2 * (g7 + g8 + g9)
+        self.Q2 = 2 * (g1 + g4 + g7) + g2 + g5 + g8
+        self.S2 = g2 + g5 + g8 + 2 * (g3 + g6 + g9)
+        self.X00 = 4 * g1 + 2 * g2 + 2 * g4 + g5
+        self.X01 = 2 * g2 + 4 * g3 + g5 + 2 * g6
+        self.X10 = 2 * g4 + g5 + 4 * g7 + 2 * g8
+        self.X11 = g5 + 2 * g6 + 2 * g8 + 4 * g9
+        self.D16 = self.X00 * self.X11 - self.X01 * self.X10
+        self.a = -g1 + g3 - g4 + g6 - g7 + g9
+        self.b = -g1 - g2 - g3 + g7 + g8 + g9
+        cc = -g1 + g3 + g7 - g9
+        # half of MA / MB of the Dz precompute (genotype_kernels.py:175-196)
+        mah = g7 * (g2 + 2 * g3 + g5 + 2 * g6) + g8 * (g3 + g6 - g1 - g4) \
+            - g9 * (2 * g1 + g2 + 2 * g4 + g5)
+        mbh = g3 * (g4 + g5) - g6 * (g1 + g2) + (g7 + g8) * (2 * g3 + g6) \
+            - g9 * (2 * g1 + 2 * g2 + g4 + g5)
+        self.W = cc + self.a * self.b                   # Wjj
+        self.U16 = self.D16 * (1 + self.b) + 8 * mah    # 16 Ucoef
+        self.V16 = self.D16 * (1 + self.a) + 8 * mbh    # 16 Vcoef
+        n = self.n
+        self.m = np.maximum(4 * n * (n - 1), 1)         # B_L / C.. denominators
+        self.BL = self.P2 * self.R2 - (g4 + g5 + g6)    # 4 n(n-1) B_L
+        self.BR = self.Q2 * self.S2 - (g2 + g5 + g8)    # 4 n(n-1) B_R
+        self.C00 = self.P2 * self.Q2 - self.X00         # 16 n(n-1) C00
+        self.C01 = self.P2 * self.S2 - self.X01
+        self.C10 = self.R2 * self.Q2 - self.X10
+        self.C11 = self.R2 * self.S2 - self.X11
+        self.Bs = self.X00 - self.X01 - self.X10 + self.X11  # 4 Bsgn
+        # triple coefficients, times 16 (genotype_kernels.py:500-521)
+        L0 = g5 + 2 * g6 + 2 * g8 + 4 * g9
+        L1 = g5 + 2 * g6
+        M1 = g5 + 2 * g8
+        nR3 = 3 * (g4 + g5 + g6) + 4 * (g7 + g8 + g9)
+        nR5 = 5 * (g4 + g5 + g6) + 8 * (g7 + g8 + g9)
+        b5A = -2 * g2 - 4 * g3 + 4 * g4 + g5 - 2 * g6 + 8 * g7 + 4 * g8 + 4
+        b6A = -g5 - 2 * g6 - 4 * g7 - 4 * g8 - 4 * g9
+        nL3 = 3 * (g2 + g5 + g8) + 4 * (g3 + g6 + g9)
+        nL5 = 5 * (g2 + g5 + g8) + 8 * (g3 + g6 + g9)
+        b5B = 4 * g2 + 8 * g3 - 2 * g4 + g5 + 4 * g6 - 4 * g7 - 2 * g8 + 4
+        b6B = -4 * g3 - g5 - 4 * g6 - 2 * g8 - 4 * g9
+        P2, Q2, R2, S2 = self.P2, self.Q2, self.R2, self.S2
+        self.AQ3 = -S2 * nR3 + P2 * S2 * R2 + R2 * L0 + 2 * L1 - P2 * L0
+        self.AS3 = -Q2 * nR5 + P2 * Q2 * R2 + R2 * b5A + 2 * b6A + P2 * L0
+        self.BP3 = -R2 * nL3 + Q2 * S2 * R2 + S2 * L0 + 2 * M1 - Q2 * L0
+        self.BR3 = -P2 * nL5 + P2 * Q2 * S2 + S2 * b5B + 2 * b6B + Q2 * L0
+
+
+def _fdiv(num, den):
+    """num / den in float64 with IEEE results for den == 0 (no guard)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.asarray(num).astype(np.float64) / np.asarray(den).astype(np.float64)
+
+
+def _gate(ok, num, den):
+    out = np.zeros(np.broadcast(num, den).shape, np.float64)
+    ok = np.asarray(ok) & (np.asarray(den) != 0)
+    out[ok] = np.asarray(num)[ok].astype(np.float64) / np.asarray(den)[ok].astype(np.float64)
+    return out
+
+
+def geno_dd(pp, pops):
+    """DD of _DD_GENO_SINGLE_KERN / _DD_GENO_BETWEEN_KERN (genotype_kernels.py:27-83)."""
+    from oracle.geno_tables import DD_POLY
+    a, b = pp
+    if a == b:
+        p = pops[a]
+        num = 16 * _geno_poly(DD_POLY, p.g) + p.D16 * p.D16
+        return _gate(p.ns >= 4, num, 64 * _d4(p.ns))
+    A, B = pops[a], pops[b]
+    den = A.n * (A.n - 1) * B.n * (B.n - 1)
+    return _gate(den > 0, A.D16 * B.D16, 64 * den)
+
+
+def geno_dz(pp, pops):
+    """Dz cases of compute_all_dz_geno (genotype_kernels.py:614-713)."""
+    from oracle.geno_tables import DZ_QUARTIC
+    i, j, k = pp
+    if i == j == k:
+        p = pops[i]
+        num = 4 * _geno_poly(DZ_QUARTIC, p.g) + p.a * p.b * p.D16
+        return _gate(p.ns >= 4, num, 8 * _d4(p.ns))
+    if i == j:    # Dz(i,i,k): repeated i, singleton k
+        I, K = pops[i], pops[k]
+        return _fdiv(I.U16 * K.a, 8 * K.n * I.n * (I.n - 1) * (I.n - 2))
+    if i == k:    # Dz(i,j,i): repeated i, singleton j
+        I, J = pops[i], pops[j]
+        return _fdiv(I.V16 * J.b, 8 * J.n * I.n * (I.n - 1) * (I.n - 2))
+    if j == k:    # Dz(i,j,j)
+        I, J = pops[i], pops[j]
+        return _fdiv(I.D16 * J.W, 8 * J.n * (J.n - 1) * I.n * (I.n - 1))
+    I, J, K = pops[i], pops[j], pops[k]
+    return _fdiv(I.D16 * J.b * K.a, 8 * I.n * (I.n - 1) * J.n * K.n)
+
+
+def _geno_shared_roles(i, j, k, l):
+    if i == k:
+        return i, j, l
+    if i == l:
+        return i, j, k
+    if j == k:
+        return j, i, l
+    if j == l:
+        return j, i, k
+    return 0, 0, 0
+
+
+def geno_pi2(pp, pops):
+    """pi2 cases of compute_all_pi2_geno (genotype_kernels.py:722-886)."""
+    from oracle.geno_tables import PI2_CORR
+    i, j, k, l = pp
+    cnt = {}
+    for q in pp:
+        cnt[q] = cnt.get(q, 0) + 1
+    nu, mc = len(cnt), max(cnt.values())
+    if nu == 1:
+        p = pops[i]
+        num = p.P2 * p.Q2 * p.S2 * p.R2 + _geno_poly(PI2_CORR, p.g)
+        return _gate(p.ns >= 4, num, 16 * _d4(p.ns))
+    if mc == 3:
+        t = [q for q, v in cnt.items() if v == 3][0]
+        s = [q for q, v in cnt.items() if v == 1][0]
+        T, Sg = pops[t], pops[s]
+        d = T.n * (T.n - 1) * (T.n - 2) * Sg.n
+        if i == t and j == t:
+            num = T.AQ3 * Sg.Q2 + T.AS3 * Sg.S2
+        else:
+            num = T.BP3 * Sg.P2 + T.BR3 * Sg.R2
+        return _gate(d > 0, num, 32 * d)
+    if i == j and k == l:
+        I, K = pops[i], pops[k]
+        return _fdiv(I.BL * K.BR, I.m * K.m)
+    if i == j:
+        I, K, L = pops[i], pops[k], pops[l]
+        return _fdiv(I.BL * (K.Q2 * L.S2 + K.S2 * L.Q2), I.m * 8 * K.n * L.n)
+    if k == l:
+        I, J, K = pops[i], pops[j], pops[k]
+        return _fdiv((I.P2 * J.R2 + I.R2 * J.P2) * K.BR, 8 * I.n * J.n * K.m)
+    if (i == k and j == l) or (i == l and j == k):
+        A, B = pops[i], pops[j]
+        PQa, RSa, PSa, QRa, PRa = (A.P2 * A.Q2, A.R2 * A.S2, A.P2 * A.S2, A.Q2 * A.R2,
+                                   A.P2 * A.R2)
+        PQb, RSb, PSb, QRb = B.P2 * B.Q2, B.R2 * B.S2, B.P2 * B.S2, B.Q2 * B.R2
+        Ta = A.R2 * (4 + A.X01 - A.X10)
+        Ua = A.S2 * (2 + A.R2)
+        num = (-2 * RSa * B.Q2 - A.X11 * PQb + RSa * PQb - 2 * A.R2 * PSb
+               - PQa * B.X11 - RSa * B.X11 + PSa * B.X11 + QRa * B.X11
+               - 2 * PRa * B.S2 + Ta * B.S2 + A.X11 * PSb + QRa * PSb
+               + 2 * Ua * B.R2 - A.X01 * QRb + PSa * QRb
+               - 2 * PSa * B.R2 - 2 * A.P2 * RSb + A.X01 * RSb + PQa * RSb
+               + A.X11 * B.Bs + A.Bs * B.X11 - 4 * A.X11 * B.X11)
+        d = A.n * (A.n - 1) * B.n * (B.n - 1)
+        return _gate(d > 0, num, 64 * d)
+    if nu == 3:
+        s, a, b = _geno_shared_roles(i, j, k, l)
+        Sg, A, B = pops[s], pops[a], pops[b]
+        num = A.R2 * (Sg.C00 * B.S2 + Sg.C01 * B.Q2) + A.P2 * (Sg.C10 * B.S2 + Sg.C11 * B.Q2)
+        return _fdiv(num, 16 * Sg.m * A.n * B.n)
+    I, J, K, L = pops[i], pops[j], pops[k], pops[l]
+    return _fdiv((I.P2 * J.R2 + I.R2 * J.P2) * (K.Q2 * L.S2 + K.S2 * L.Q2),
+                 64 * I.n * J.n * K.n * L.n)
+
+
+def geno_case_value(kind, pp, pops):
+    if kind == "dd":
+        return geno_dd(pp, pops)
+    if kind == "dz":
+        return geno_dz(pp, pops)
+    return geno_pi2(pp, pops)
+
+
+def geno_multi_pop_stats(counts_per_pop, n_valid_per_pop, specs=None):
+    """(N, n_stats) float64 as compute_multi_pop_statistics_batch_geno
+    (genotype_kernels.py:889-936)."""
+    P = len(counts_per_pop)
+    specs = stat_specs(P) if specs is None else specs
+    pops = [GenoPop(c, nv) for c, nv in zip(counts_per_pop, n_valid_per_pop)]
+    cache = {}
+    out = np.zeros((len(np.asarray(counts_per_pop[0])), len(specs)), np.float64)
+    for s, (_, calls) in enumerate(specs):
+        acc = 0.0
+        for w, kind, pp in calls:
+            key = (kind, pp)
+            if key not in cache:
+                cache[key] = geno_case_value(kind, pp, pops)
+            acc = acc + (cache[key] if (w == 1.0 and len(calls) == 1) else w * cache[key])
+        out[:, s] = acc
+    return out
+
+
+def dd_geno_single(counts):
+    """_DD_GENO_SINGLE_KERN on reference-order 9-way counts."""
+    return geno_dd((0, 0), [GenoPop(counts)])
+
+
+def sigma_d2_geno(counts):
+    """DD / pi2 ratio of _SIGMA_D2_GENO_KERN (genotype_kernels.py:91-169):
+    NaN where fewer than 4 individuals or the pi2 numerator is not positive."""
+    from oracle.geno_tables import DD_POLY, PI2_CORR
+    p = GenoPop(counts)
+    dd = 16 * _geno_poly(DD_POLY, p.g) + p.D16 * p.D16
+    pi = p.P2 * p.Q2 * p.S2 * p.R2 + _geno_poly(PI2_CORR, p.g)
+    out = np.full(len(dd), np.nan)
+    ok = (p.ns >= 4) & (pi > 0)
+    out[ok] = dd[ok].astype(np.float64) / (4.0 * pi[ok].astype(np.float64))
+    return out
+
+
+def rogers_huff_r_counts(counts):
+    """Rogers-Huff r from reference-order 9-way counts: exact integer moments
+    of the individuals valid at both SNPs, one float64 division."""
+    c = np.asarray(counts).astype(I64)
+    ga = np.array([0, 0, 0, 1, 1, 1, 2, 2, 2], I64)
+    gb = np.array([0, 1, 2, 0, 1, 2, 0, 1, 2], I64)
+    n = c.sum(axis=1)
+    si, sj = c @ ga, c @ gb
+    sii, sjj, sij = c @ (ga * ga), c @ (gb * gb), c @ (ga * gb)
+    cov = n * sij - si * sj
+    den = (n * sii - si * si) * (n * sjj - sj * sj)
+    out = np.full(len(c), np.nan)
+    ok = den > 0
+    out[ok] = cov[ok].astype(np.float64) / np.sqrt(den[ok].astype(np.float64))
+    return out

@@ -283,6 +283,33 @@ def gen_geno(M):
     np.savez_compressed(os.path.join(HERE, "geno.npz"), **out)
 
 
+def gen_geno_stats(M):
+    """Genotype moments statistics of 1-4 populations from the reference's
+    compute_multi_pop_statistics_batch_geno (genotype_kernels.py:889-936)."""
+    lp, gk = M["ld_pipeline"], M["genotype_kernels"]
+    rng = np.random.default_rng(20261207)
+    sizes = (14, 9, 22, 6)
+    N = 240
+    out = {}
+    cs, nvs = [], []
+    for q, n_ind in enumerate(sizes):
+        # random 9-way tables with a few edge rows (tiny and monomorphic samples)
+        n = rng.integers(4, n_ind + 1, size=N)
+        c = np.stack([rng.multinomial(k, rng.dirichlet([0.4] * 9)) for k in n]).astype(np.int32)
+        c[:4] = [[0] * 9, [1, 0, 0, 0, 1, 0, 0, 0, 1], [0, 0, 0, 0, 5, 0, 0, 0, 0],
+                 [2, 0, 0, 0, 0, 0, 0, 0, 2]]
+        cs.append(c)
+        nvs.append(c.sum(1).astype(np.int32))
+        out[f"counts_{q}"] = c
+    for p in range(1, 5):
+        specs = lp.generate_stat_specs(p)
+        out[f"multi_{p}"] = np.asarray(gk.compute_multi_pop_statistics_batch_geno(
+            [S.garr(cs[q]) for q in range(p)], [S.garr(nvs[q]) for q in range(p)], None, specs))
+        out[f"multi_{p}_nonv"] = np.asarray(gk.compute_multi_pop_statistics_batch_geno(
+            [S.garr(cs[q]) for q in range(p)], [None] * p, None, specs))
+    np.savez_compressed(os.path.join(HERE, "geno_stats.npz"), **out)
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -290,6 +317,7 @@ def main():
     gen_binned(M)
     gen_moments(M)
     gen_geno(M)
+    gen_geno_stats(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -160,3 +160,44 @@ def test_rogers_huff_matches_reference(golden):
            rtol=1e-9, atol=1e-12)
     with pytest.raises(ValueError):
         O.rogers_huff_r(z["geno_miss"])
+
+
+def _same_ieee(got, ref, rtol):
+    """Equal NaN / inf pattern, finite values within rtol."""
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    inf = np.isinf(ref)
+    assert np.array_equal(np.isinf(got), inf) and np.array_equal(got[inf], ref[inf])
+    f = np.isfinite(ref)
+    np.testing.assert_allclose(got[f], ref[f], rtol=rtol, atol=0)
+
+
+def test_genotype_dd_and_sigma_d2_match_reference_kernels(golden):
+    z = golden("geno")
+    for tag in ("", "_miss"):
+        c = z["counts9" + tag]
+        # _DD_GENO_SINGLE_KERN and _SIGMA_D2_GENO_KERN run as host C++
+        _same_ieee(O.dd_geno_single(c), z["dd_geno" + tag], 1e-12)
+        _same_ieee(O.sigma_d2_geno(c), z["sigma_d2" + tag], 1e-12)
+
+
+def test_rogers_huff_from_counts_matches_reference(golden):
+    z = golden("geno")
+    _close(O.rogers_huff_r_counts(z["counts9"]), z["rh_r_pairs"], rtol=1e-9, atol=1e-12)
+    # with missing data the reference raises; the pairwise-complete definition
+    # equals the dosage-level restatement
+    c, _ = O.genotype_counts_for_pairs(z["geno_miss"], z["idx_i"], z["idx_j"])
+    _close(O.rogers_huff_r_counts(c),
+           O.rogers_huff_r_pairs(z["geno_miss"], z["idx_i"], z["idx_j"]), rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("P", [1, 2, 3, 4])
+def test_genotype_multi_pop_stats_match_reference(golden, P):
+    # compute_multi_pop_statistics_batch_geno (genotype_kernels.py:889-936),
+    # every dd / dz / pi2 case of 1-4 populations, with and without n_valid
+    z = golden("geno_stats")
+    cs = [z[f"counts_{q}"] for q in range(P)]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        got = O.geno_multi_pop_stats(cs, [c.sum(1) for c in cs])
+        got0 = O.geno_multi_pop_stats(cs, [None] * P)
+    _same_ieee(got, z[f"multi_{P}"], 1e-13)
+    _same_ieee(got0, z[f"multi_{P}_nonv"], 1e-13)
