@@ -127,7 +127,28 @@ enum pgld_kind {
   PGLD_PI2_ALLDIFF = 15,/* pops = i,j,k,l    ld_statistics.py:1592-1617 */
   PGLD_R = 16,         /* haplotype_kernels.py:20-30, NaN if undefined */
   PGLD_R2 = 17,        /* haplotype_kernels.py:32-42 */
-  PGLD_DPRIME = 18     /* haplotype_kernels.py:44-62 */
+  PGLD_DPRIME = 18,    /* haplotype_kernels.py:44-62 */
+  /* Genotype (unphased diploid) kinds on 9-way counts, the cases of
+   * compute_all_{dd,dz,pi2}_geno (genotype_kernels.py:560-886). */
+  PGLD_G_DD_II = 32,   /* _DD_GENO_SINGLE_KERN   genotype_kernels.py:27-71   */
+  PGLD_G_DD_IJ = 33,   /* _DD_GENO_BETWEEN_KERN  genotype_kernels.py:73-83   */
+  PGLD_G_DZ_III = 34,  /* _DZ_III_KERN           genotype_kernels.py:235-279 */
+  PGLD_G_DZ_IIJ = 35,  /* _DZ_IIJ_KERN pops=i,j  genotype_kernels.py:208-215 */
+  PGLD_G_DZ_IJI = 36,  /* _DZ_IJI_KERN pops=i,j  genotype_kernels.py:217-224 */
+  PGLD_G_DZ_IJJ = 37,  /* _DZ_IJJ_KERN pops=i,j  genotype_kernels.py:226-233 */
+  PGLD_G_DZ_IJK = 38,  /* _DZ_DISTINCT_KERN      genotype_kernels.py:199-206 */
+  PGLD_G_PI2_IIII = 39,/* _PI2_IIII_KERN         genotype_kernels.py:364-398 */
+  PGLD_G_PI2_IIIJ = 40,/* pops=triple,single, calls (t,t,..) genotype_kernels.py:319-329 */
+  PGLD_G_PI2_IJII = 41,/* pops=triple,single, other calls    genotype_kernels.py:330-339 */
+  PGLD_G_PI2_IIKK = 42,/* genotype_kernels.py:286-291 */
+  PGLD_G_PI2_IIKL = 43,/* pops=i,k,l genotype_kernels.py:293-299 */
+  PGLD_G_PI2_IJKK = 44,/* pops=i,j,k genotype_kernels.py:301-307 */
+  PGLD_G_PI2_IJIJ = 45,/* pops=i,j   genotype_kernels.py:341-361 */
+  PGLD_G_PI2_SHARED = 46,/* pops=shared,a,b genotype_kernels.py:309-317 */
+  PGLD_G_PI2_ALLDIFF = 47,/* genotype_kernels.py:279-285 */
+  PGLD_G_SIGMA_D2 = 48,/* DD/pi2 ratio, NaN if undefined  genotype_kernels.py:91-169 */
+  PGLD_G_RH_R = 49,    /* Rogers-Huff r (pairwise-complete), ld_statistics.py:410-443 */
+  PGLD_G_RH_R2 = 50    /* Rogers-Huff r^2 */
 };
 
 typedef struct {
@@ -207,6 +228,82 @@ int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, const doubl
                          double max_dist, const double* bin_coord, const double* bins,
                          int32_t n_bins, double* sums, int64_t* pair_counts, int32_t form,
                          void* stream);
+
+/* ----------------------------------------------------------------------
+ * Genotype (unphased diploid dosage) path.
+ *
+ * A population of N individuals is packed into W = ceil(N / 32) words per
+ * plane and three planes per SNP: planes[s][0:W] = (g == 0),
+ * [W:2W] = (g == 1), [2W:3W] = (g == 2).  Missing (-1) is in no plane.
+ * valid (optional, [n_snp][W] bits of g >= 0) and ext (optional,
+ * [n_snp][6W]: planes of the values 3..8) are needed only when the matrix
+ * holds values above 2: the reference's counting kernel counts such an
+ * individual as valid and, through its class index 3 g_i + g_j, folds the
+ * values 3..8 at the second SNP into the classes 3..8 (ld_pipeline.py:
+ * 193-210); ext reproduces that.  Populations hold at most 8,192
+ * individuals (the exact 64-bit statistic numerators).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t n_pops;
+  int32_t n_words[PGLD_MAX_POPS];
+  const uint32_t* planes[PGLD_MAX_POPS];
+  const uint32_t* valid[PGLD_MAX_POPS];
+  const uint32_t* ext[PGLD_MAX_POPS];
+  int64_t n_snp;
+} pgld_geno_panel;
+
+/* Pack rows of an int8 (n_rows_total x n_snp) dosage matrix (row stride ld
+ * bytes, values 0/1/2, negative = missing) into the planes above (valid and
+ * ext nullable).  flags:
+ * device int32[2], flags[0] |= 1 if a negative value was seen (the
+ * reference's has_missing, ld_pipeline.py:253), flags[1] |= 1 if a value
+ * above 2 was seen.  Replaces the gathers of
+ * ld_pipeline.compute_genotype_counts_for_pairs (ld_pipeline.py:242-250). */
+int pgld_pack_genotypes(pgld_handle h, const int8_t* geno, int64_t ld, int64_t n_snp,
+                        const int32_t* rows, int32_t n_rows, uint32_t* planes, uint32_t* valid,
+                        uint32_t* ext, int32_t* flags, void* stream);
+
+/* 9-way counts [n00, n01, n02, n10, ..., n22] (row stride counts_ld >= 9)
+ * of listed SNP pairs and the pairwise-valid n (nullable).  Replaces
+ * ld_pipeline.compute_genotype_counts_for_pairs + _GENO_COUNTS_KERN
+ * (ld_pipeline.py:183-263). */
+int pgld_geno_counts_pairs(pgld_handle h, const uint32_t* planes, const uint32_t* valid,
+                           const uint32_t* ext, int32_t n_words, int64_t n_snp, const int32_t* idx_i,
+                           const int32_t* idx_j, int64_t n_pairs, int32_t* counts,
+                           int64_t counts_ld, int32_t* n_valid, void* stream);
+
+/* The moments statistic table of n_pops populations as genotype terms (host
+ * only): the case selection of compute_multi_pop_statistics_batch_geno
+ * (genotype_kernels.py:889-936) applied to generate_stat_specs
+ * (ld_pipeline.py:388-457). */
+int pgld_geno_stat_terms(int32_t n_pops, pgld_term* out, int32_t capacity, int32_t* n_terms_out,
+                         int32_t* n_stats_out);
+
+/* Statistic columns from per-pair 9-way counts (counts_ld >= 9), genotype
+ * kinds only.  Replaces compute_multi_pop_statistics_batch_geno
+ * (genotype_kernels.py:889-936), ld_statistics_genotype.sigma_d2_geno
+ * (ld_statistics_genotype.py:1518-1598) and the per-pair Rogers-Huff r. */
+int pgld_geno_stats(pgld_handle h, const pgld_pair_counts* counts, int64_t n_pairs,
+                    const pgld_term* terms, int32_t n_terms, int32_t n_stats, void* out,
+                    int32_t out_dtype, int64_t out_ld, void* stream);
+
+/* Per-pair outputs over the distance band of one population, in the
+ * reference's pair order: counts [n_pairs][9] int32 (nullable), n_valid
+ * (nullable) and stats [n_pairs][4] float32 = Rogers-Huff r^2 (pairwise-
+ * complete), DD, Dz, pi2 (nullable; 16-byte aligned).  n_pairs must equal
+ * pgld_count_pairs_within's result.  Fuses iter_pairs_within_distance +
+ * compute_genotype_counts_for_pairs + the single-population genotype
+ * statistics + rogers_huff_r_squared. */
+int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel, const double* pos,
+                         double max_dist, int32_t* counts, int32_t* n_valid, float* stats,
+                         int64_t n_pairs, void* stream);
+
+/* Distance-binned sums of the moments genotype statistics of n_pops (1..4)
+ * populations, arguments and bins as pgld_hap_binned_sums.  Replaces
+ * moments_ld._compute_ld_sums with use_genotypes=True (moments_ld.py:248-343). */
+int pgld_geno_binned_sums(pgld_handle h, const pgld_geno_panel* panel, const double* pos,
+                          double max_dist, const double* bin_coord, const double* bins,
+                          int32_t n_bins, double* sums, int64_t* pair_counts, void* stream);
 
 /* pgld_hap_binned_sums for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers of this library cannot call

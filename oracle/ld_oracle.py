@@ -941,3 +941,80 @@ def rogers_huff_r_counts(counts):
     ok = den > 0
     out[ok] = cov[ok].astype(np.float64) / np.sqrt(den[ok].astype(np.float64))
     return out
+
+
+def geno_binned_sums(geno, positions, pop_rows, bins, coords=None, max_dist=None,
+                     pair_block=1_000_000, abs_sums=False):
+    """Genotype-mode binned sums (moments_ld.py:248-343 with use_genotypes=True),
+    on an already union-filtered dosage matrix; returns (sums, pair counts[, abs])."""
+    pos = np.asarray(positions)
+    coord = pos.astype(np.float64) if coords is None else np.asarray(coords, np.float64)
+    bins = np.asarray(bins, np.float64)
+    n_bins = len(bins) - 1
+    P = len(pop_rows)
+    if max_dist is None:
+        max_dist = float(bins[-1])
+    ii, jj = pairs_within_distance(pos, max_dist)
+    specs = stat_specs(P)
+    sums = np.zeros((n_bins, len(specs)))
+    asums = np.zeros((n_bins, len(specs)))
+    npairs = np.zeros(n_bins, np.int64)
+    g = np.asarray(geno)
+    subs = [g[np.asarray(r), :] for r in pop_rows]
+    for s0 in range(0, len(ii), pair_block):
+        ci, cj = ii[s0:s0 + pair_block], jj[s0:s0 + pair_block]
+        d = np.abs(coord[cj] - coord[ci]) if coords is not None else (coord[cj] - coord[ci])
+        b = bin_index(d, bins)
+        keep = (b >= 0) & (b < n_bins)
+        if not np.any(keep):
+            continue
+        ci, cj, b = ci[keep], cj[keep], b[keep]
+        cs, nvs = [], []
+        for sub in subs:
+            c, nv = genotype_counts_for_pairs(sub, ci, cj)
+            cs.append(c)
+            nvs.append(nv)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            st = geno_multi_pop_stats(cs, nvs, specs)
+        for k in range(len(specs)):
+            sums[:, k] += np.bincount(b, weights=st[:, k], minlength=n_bins)
+            if abs_sums:
+                asums[:, k] += np.bincount(b, weights=np.abs(st[:, k]), minlength=n_bins)
+        npairs += np.bincount(b, minlength=n_bins)
+    if abs_sums:
+        return sums, npairs, asums
+    return sums, npairs
+
+
+def union_polymorphic(geno, pop_rows):
+    """Variants kept by the genotype path's union filter (moments_ld.py:256-280)."""
+    rows = sorted(set(int(i) for r in pop_rows for i in r))
+    sub = np.asarray(geno)[rows]
+    v = sub >= 0
+    alt = np.where(v, sub, 0).astype(np.int64).sum(0)
+    nv = v.sum(0)
+    return (alt > 0) & (alt < 2 * nv) & (nv >= 2)
+
+
+def geno_heterozygosity(geno, pop_rows):
+    """H_i_j statistics (moments_ld.py:346-388), genotype mode."""
+    g = np.asarray(geno)
+    alt, ref, size = [], [], []
+    for rws in pop_rows:
+        sub = g[np.asarray(rws), :]
+        v = sub >= 0
+        a = np.where(v, sub, 0).astype(np.int64).sum(0).astype(np.float64)
+        nh = 2.0 * v.sum(0).astype(np.float64)
+        alt.append(a)
+        ref.append(nh - a)
+        size.append(nh)
+    out = {}
+    P = len(pop_rows)
+    for i in range(P):
+        for j in range(i, P):
+            if i == j:
+                out[f"H_{i}_{j}"] = float(np.sum(2.0 * ref[i] * alt[i] / (size[i] * (size[i] - 1))))
+            else:
+                out[f"H_{i}_{j}"] = float(np.sum((ref[i] * alt[j] + alt[i] * ref[j])
+                                                 / (size[i] * size[j])))
+    return out

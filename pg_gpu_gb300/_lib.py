@@ -24,6 +24,10 @@ DD_II, DD_IJ, DZ_III, DZ_IIJ, DZ_IJI, DZ_IJJ, DZ_IJK = range(7)
 (PI2_IIII, PI2_TRIPLE, PI2_IIKK, PI2_IIKK_SYM, PI2_IIKL, PI2_IJKK, PI2_IJIJ, PI2_SHARED,
  PI2_ALLDIFF) = range(7, 16)
 R, R2, DPRIME = 16, 17, 18
+# genotype kinds
+(G_DD_II, G_DD_IJ, G_DZ_III, G_DZ_IIJ, G_DZ_IJI, G_DZ_IJJ, G_DZ_IJK, G_PI2_IIII, G_PI2_IIIJ,
+ G_PI2_IJII, G_PI2_IIKK, G_PI2_IIKL, G_PI2_IJKK, G_PI2_IJIJ, G_PI2_SHARED, G_PI2_ALLDIFF,
+ G_SIGMA_D2, G_RH_R, G_RH_R2) = range(32, 51)
 
 
 class PgldError(RuntimeError):
@@ -59,6 +63,8 @@ class GenoPanel(ctypes.Structure):
     _fields_ = [("n_pops", ctypes.c_int32),
                 ("n_words", ctypes.c_int32 * MAX_POPS),
                 ("planes", ctypes.c_void_p * MAX_POPS),
+                ("valid", ctypes.c_void_p * MAX_POPS),
+                ("ext", ctypes.c_void_p * MAX_POPS),
                 ("n_snp", ctypes.c_int64)]
 
 
@@ -85,6 +91,17 @@ _SIGS = {
                             ctypes.c_int),
     "pgld_hap_binned_sums": ([_P, ctypes.POINTER(HapPanel), _P, _D, _P, _P, _I32, _P, _P, _I32,
                               _P], ctypes.c_int),
+    "pgld_pack_genotypes": ([_P, _P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
+    "pgld_geno_counts_pairs": ([_P, _P, _P, _P, _I32, _I64, _P, _P, _I64, _P, _I64, _P, _P],
+                               ctypes.c_int),
+    "pgld_geno_stat_terms": ([_I32, _P, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)],
+                             ctypes.c_int),
+    "pgld_geno_stats": ([_P, ctypes.POINTER(PairCounts), _I64, ctypes.POINTER(Term), _I32, _I32,
+                         _P, _I32, _I64, _P], ctypes.c_int),
+    "pgld_geno_band_pairs": ([_P, ctypes.POINTER(GenoPanel), _P, _D, _P, _P, _P, _I64, _P],
+                             ctypes.c_int),
+    "pgld_geno_binned_sums": ([_P, ctypes.POINTER(GenoPanel), _P, _D, _P, _P, _I32, _P, _P, _P],
+                              ctypes.c_int),
     "pgld_hap_binned_sums_noalloc": ([ctypes.c_int, ctypes.POINTER(HapPanel), _P, _D, _P, _P, _I32,
                                       _P, _P, _P], ctypes.c_int),
 }

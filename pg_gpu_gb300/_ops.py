@@ -141,11 +141,12 @@ def make_terms(term_list):
     return arr
 
 
-def stats(pop_counts, pop_nvalid, term_list, n_stats, dtype="f64"):
+def stats(pop_counts, pop_nvalid, term_list, n_stats, dtype="f64", geno=False):
     """Statistic columns (N, n_stats) from per-pop counts views.
 
-    pop_counts[p]: int32 CUDA tensor view with shape (N, >=4) and unit inner
-    stride; pop_nvalid[p]: int32 CUDA tensor (N,) (any stride) or None.
+    pop_counts[p]: int32 CUDA tensor view with shape (N, >=4) (haplotype
+    counts) or (N, >=9) (genotype counts, geno=True) and unit inner stride;
+    pop_nvalid[p]: int32 CUDA tensor (N,) (any stride) or None.
     """
     torch = _torch()
     n = pop_counts[0].shape[0]
@@ -168,9 +169,9 @@ def stats(pop_counts, pop_nvalid, term_list, n_stats, dtype="f64"):
             pc.nvalid_ld[p] = nv.stride(0)
     terms = make_terms(term_list)
     h = L.handle()
-    L.check(L.lib().pgld_hap_stats(h, ctypes.byref(pc), n, terms, len(term_list), n_stats,
-                                   L.ptr(out), L.F64 if dtype == "f64" else L.F32, n_stats,
-                                   L.stream_ptr()), h)
+    fn = L.lib().pgld_geno_stats if geno else L.lib().pgld_hap_stats
+    L.check(fn(h, ctypes.byref(pc), n, terms, len(term_list), n_stats, L.ptr(out),
+               L.F64 if dtype == "f64" else L.F32, n_stats, L.stream_ptr()), h)
     return out
 
 
@@ -253,4 +254,169 @@ def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto"):
                                          L.ptr(bins_d), n_bins, L.ptr(sums), L.ptr(cnt),
                                          L.FORM_TC if form == "tc" else L.FORM_PLAIN,
                                          L.stream_ptr()), h)
+    return sums, cnt
+
+
+# --------------------------------------------------------------------------
+# genotype (unphased diploid dosage) path
+# --------------------------------------------------------------------------
+MAX_GENO_N = 8192
+
+
+class PackedGeno:
+    """Dosage bit planes (g == 0, 1, 2) of one population.
+
+    ``has_missing`` mirrors the reference's ``cp.any(g < 0)`` over the
+    population's rows (ld_pipeline.py:253); ``has_other`` flags dosages above
+    2, for which the validity plane and the planes of the values 3..8 (``ext``,
+    folded into classes like the reference's counting kernel) are kept.
+    """
+
+    def __init__(self, planes, valid, n_words, n_rows, n_snp, has_missing, has_other, ext=None):
+        self.planes = planes
+        self.valid = valid
+        self.ext = ext
+        self.n_words = n_words
+        self.n_rows = n_rows
+        self.n_snp = n_snp
+        self.has_missing = has_missing
+        self.has_other = has_other
+
+    @property
+    def valid_for_n(self):
+        """Validity plane when the pairwise n differs from the sum of the 9
+        counts: dosages above 2 and missing data (with no missing data the
+        reference's n is the sum of the counts, ld_pipeline.py:253-263)."""
+        return self.valid if (self.has_other and self.has_missing) else None
+
+    @property
+    def ext_planes(self):
+        return self.ext if self.has_other else None
+
+
+def pack_geno(geno, rows=None):
+    """Pack the rows of an int8 (n_individuals x M) device dosage matrix."""
+    torch = _torch()
+    g = L.as_device(geno, np.int8)
+    if g.dim() != 2:
+        raise ValueError("genotypes must be 2-D (n_individuals, n_variants)")
+    n_total, n_snp = g.shape
+    if rows is not None:
+        rows_t = L.as_device(rows, np.int32)
+        if rows_t.numel() and (int(rows_t.min()) < 0 or int(rows_t.max()) >= n_total):
+            raise IndexError("population row index out of range")
+        n_rows = rows_t.numel()
+    else:
+        rows_t = None
+        n_rows = n_total
+    if n_rows > MAX_GENO_N:
+        raise ValueError(f"{n_rows} individuals exceed {MAX_GENO_N} per population")
+    W = max(1, (n_rows + 31) // 32)
+    planes = torch.empty((n_snp, 3 * W), dtype=torch.int32, device=g.device)
+    valid = torch.empty((n_snp, W), dtype=torch.int32, device=g.device)
+    flags = torch.zeros(2, dtype=torch.int32, device=g.device)
+    ext = None
+    if n_rows == 0:
+        planes.zero_()
+        valid.zero_()
+    else:
+        h = L.handle()
+        L.check(L.lib().pgld_pack_genotypes(h, L.ptr(g), g.stride(0), n_snp, L.ptr(rows_t), n_rows,
+                                            L.ptr(planes), L.ptr(valid), None, L.ptr(flags),
+                                            L.stream_ptr()), h)
+        if int(flags[1]):
+            # dosages above 2: the planes of the values 3..8 as well
+            ext = torch.empty((n_snp, 6 * W), dtype=torch.int32, device=g.device)
+            L.check(L.lib().pgld_pack_genotypes(h, L.ptr(g), g.stride(0), n_snp, L.ptr(rows_t),
+                                                n_rows, L.ptr(planes), L.ptr(valid), L.ptr(ext),
+                                                L.ptr(flags), L.stream_ptr()), h)
+    f = flags.cpu().numpy()
+    return PackedGeno(planes, valid, W, n_rows, n_snp, bool(f[0]), bool(f[1]), ext)
+
+
+def geno_panel(pops):
+    pn = L.GenoPanel()
+    pn.n_pops = len(pops)
+    for p, pk in enumerate(pops):
+        pn.n_words[p] = pk.n_words
+        pn.planes[p] = pk.planes.data_ptr()
+        v = pk.valid_for_n
+        pn.valid[p] = v.data_ptr() if v is not None else None
+        x = pk.ext_planes
+        pn.ext[p] = x.data_ptr() if x is not None else None
+    pn.n_snp = pops[0].n_snp
+    return pn
+
+
+def geno_counts_pairs(pk, idx_i, idx_j):
+    """(counts int32 (N,9) n00..n22, n_valid int32 (N,) or None) for listed pairs."""
+    torch = _torch()
+    ii = L.as_device(idx_i, np.int32)
+    jj = L.as_device(idx_j, np.int32)
+    if ii.shape != jj.shape:
+        raise ValueError("idx_i and idx_j must have the same shape")
+    n = ii.numel()
+    counts = torch.empty((n, 9), dtype=torch.int32, device=ii.device)
+    nv = torch.empty(n, dtype=torch.int32, device=ii.device) if pk.has_missing else None
+    if n:
+        h = L.handle()
+        L.check(L.lib().pgld_geno_counts_pairs(h, L.ptr(pk.planes), L.ptr(pk.valid_for_n),
+                                               L.ptr(pk.ext_planes), pk.n_words, pk.n_snp, L.ptr(ii), L.ptr(jj), n,
+                                               L.ptr(counts), 9, L.ptr(nv), L.stream_ptr()), h)
+        st = torch.zeros(1, dtype=torch.int32)
+        L.check(L.lib().pgld_device_status(h, ctypes.cast(st.data_ptr(), ctypes.POINTER(
+            ctypes.c_int32)), L.stream_ptr()), h)
+        if int(st[0]):
+            raise IndexError("pair index out of range of the variant axis")
+    return counts, nv
+
+
+def geno_spec_terms(P):
+    """[(stat, kind, pops, weight)] of the moments genotype table of P populations."""
+    n_terms, n_stats = ctypes.c_int32(), ctypes.c_int32()
+    L.check(L.lib().pgld_geno_stat_terms(P, None, 0, ctypes.byref(n_terms), ctypes.byref(n_stats)))
+    arr = (L.Term * n_terms.value)()
+    L.check(L.lib().pgld_geno_stat_terms(P, arr, n_terms.value, ctypes.byref(n_terms),
+                                         ctypes.byref(n_stats)))
+    return [(t.stat, t.kind, tuple(t.pops), t.weight) for t in arr], n_stats.value
+
+
+def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True):
+    """Fused per-pair genotype outputs over the distance band.
+
+    Returns (counts (N,9) int32 or None, n_valid (N,) int32, stats (N,4)
+    float32 = Rogers-Huff r^2, DD, Dz, pi2 or None)."""
+    torch = _torch()
+    _, n = band_offsets(pos_d, max_dist)
+    dev = pos_d.device
+    counts = torch.empty((n, 9), dtype=torch.int32, device=dev) if with_counts else None
+    nv = torch.empty(n, dtype=torch.int32, device=dev)
+    st = torch.empty((n, 4), dtype=torch.float32, device=dev) if with_stats else None
+    h = L.handle()
+    L.check(L.lib().pgld_geno_band_pairs(h, ctypes.byref(geno_panel([pk])), L.ptr(pos_d),
+                                         float(max_dist), L.ptr(counts), L.ptr(nv), L.ptr(st), n,
+                                         L.stream_ptr()), h)
+    return counts, nv, st
+
+
+def geno_binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None):
+    """(sums (n_bins, n_stats) float64, pair counts (n_bins,) int64), genotype statistics."""
+    torch = _torch()
+    bins_np = np.asarray(bins, dtype=np.float64)
+    if bins_np.ndim != 1 or len(bins_np) < 2:
+        raise ValueError("bins must hold at least two edges")
+    if np.any(np.diff(bins_np) <= 0):
+        raise ValueError("bins must be strictly increasing")
+    n_bins = len(bins_np) - 1
+    n_stats = {1: 3, 2: 15, 3: 45, 4: 105}[len(pops)]
+    dev = pos_d.device
+    bins_d = torch.as_tensor(bins_np, device=dev)
+    sums = torch.empty((n_bins, n_stats), dtype=torch.float64, device=dev)
+    cnt = torch.empty(n_bins, dtype=torch.int64, device=dev)
+    md = float(bins_np[-1]) if max_dist is None else float(max_dist)
+    bc = None if bin_coord is None else L.as_device(bin_coord, np.float64)
+    h = L.handle()
+    L.check(L.lib().pgld_geno_binned_sums(h, ctypes.byref(geno_panel(pops)), L.ptr(pos_d), md,
+                                          L.ptr(bc), L.ptr(bins_d), n_bins, L.ptr(sums),
+                                          L.ptr(cnt), L.stream_ptr()), h)
     return sums, cnt

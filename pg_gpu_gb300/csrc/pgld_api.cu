@@ -62,6 +62,10 @@ int pgld_n_stats(int P) {
   return (P >= 1 && P <= 4) ? n[P] : 0;
 }
 
+// genotype kinds are the haplotype kinds shifted by this offset, except the
+// two triple forms of pi2 (genotype_kernels.py:744-746)
+constexpr int kGenoShift = PGLD_G_DD_II - PGLD_DD_II;
+
 static void add_dd(std::vector<pgld_term>& t, int stat, double w, int a, int b) {
   pgld_term x{};
   x.stat = stat;
@@ -106,7 +110,8 @@ static void add_dz(std::vector<pgld_term>& t, int stat, double w, int i, int j, 
 }
 
 // case selection of haplotype_kernels.compute_all_pi2_hap (haplotype_kernels.py:463-486)
-static void add_pi2(std::vector<pgld_term>& t, int stat, double w, int i, int j, int k, int l) {
+static void add_pi2(std::vector<pgld_term>& t, int stat, double w, int i, int j, int k, int l,
+                    bool geno) {
   pgld_term x{};
   x.stat = stat;
   x.weight = w;
@@ -123,6 +128,11 @@ static void add_pi2(std::vector<pgld_term>& t, int stat, double w, int i, int j,
     for (auto& kv : cnt) {
       if (kv.second == 3) x.pops[0] = kv.first;
       if (kv.second == 1) x.pops[1] = kv.first;
+    }
+    if (geno) {
+      x.kind = (i == x.pops[0] && j == x.pops[0]) ? PGLD_G_PI2_IIIJ : PGLD_G_PI2_IJII;
+      t.push_back(x);
+      return;
     }
   } else if (i == j && k == l) {
     x.kind = PGLD_PI2_IIKK;
@@ -156,10 +166,16 @@ static void add_pi2(std::vector<pgld_term>& t, int stat, double w, int i, int j,
     x.kind = PGLD_PI2_ALLDIFF;
     for (int q = 0; q < 4; ++q) x.pops[q] = pp[q];
   }
+  if (geno) {
+    static const int map[] = {0, 0, 0, 0, 0, 0, 0, PGLD_G_PI2_IIII, 0, PGLD_G_PI2_IIKK, 0,
+                              PGLD_G_PI2_IIKL, PGLD_G_PI2_IJKK, PGLD_G_PI2_IJIJ,
+                              PGLD_G_PI2_SHARED, PGLD_G_PI2_ALLDIFF};
+    x.kind = map[x.kind];
+  }
   t.push_back(x);
 }
 
-void pgld_build_spec_terms(int P, std::vector<pgld_term>& t) {
+void pgld_build_spec_terms(int P, std::vector<pgld_term>& t, bool geno) {
   t.clear();
   int s = 0;
   for (int i = 0; i < P; ++i)
@@ -184,29 +200,32 @@ void pgld_build_spec_terms(int P, std::vector<pgld_term>& t) {
           if (i == j) {
             if (k == l) {
               if (i == k) {
-                add_pi2(t, s, 1.0, i, j, k, l);
+                add_pi2(t, s, 1.0, i, j, k, l, geno);
               } else {
-                add_pi2(t, s, 0.5, i, j, k, l);
-                add_pi2(t, s, 0.5, k, l, i, j);
+                add_pi2(t, s, 0.5, i, j, k, l, geno);
+                add_pi2(t, s, 0.5, k, l, i, j, geno);
               }
             } else {
-              add_pi2(t, s, 0.25, i, j, k, l);
-              add_pi2(t, s, 0.25, i, j, l, k);
-              add_pi2(t, s, 0.25, k, l, i, j);
-              add_pi2(t, s, 0.25, l, k, i, j);
+              add_pi2(t, s, 0.25, i, j, k, l, geno);
+              add_pi2(t, s, 0.25, i, j, l, k, geno);
+              add_pi2(t, s, 0.25, k, l, i, j, geno);
+              add_pi2(t, s, 0.25, l, k, i, j, geno);
             }
           } else if (k == l) {
-            add_pi2(t, s, 0.25, i, j, k, l);
-            add_pi2(t, s, 0.25, j, i, k, l);
-            add_pi2(t, s, 0.25, k, l, i, j);
-            add_pi2(t, s, 0.25, k, l, j, i);
+            add_pi2(t, s, 0.25, i, j, k, l, geno);
+            add_pi2(t, s, 0.25, j, i, k, l, geno);
+            add_pi2(t, s, 0.25, k, l, i, j, geno);
+            add_pi2(t, s, 0.25, k, l, j, i, geno);
           } else {
             const int o[8][4] = {{i, j, k, l}, {i, j, l, k}, {j, i, k, l}, {j, i, l, k},
                                  {k, l, i, j}, {l, k, i, j}, {k, l, j, i}, {l, k, j, i}};
-            for (auto& q : o) add_pi2(t, s, 0.125, q[0], q[1], q[2], q[3]);
+            for (auto& q : o) add_pi2(t, s, 0.125, q[0], q[1], q[2], q[3], geno);
           }
           ++s;
         }
+  if (geno)
+    for (auto& x : t)
+      if (x.kind <= PGLD_DZ_IJK) x.kind += kGenoShift;
 }
 
 extern "C" int pgld_stat_terms(int32_t n_pops, pgld_term* out, int32_t capacity,
@@ -277,6 +296,16 @@ extern "C" int pgld_create(int device, pgld_handle* out) {
     }
     h->spec_n_terms[P] = (int)t.size();
     h->spec_n_stats[P] = pgld_n_stats(P);
+    pgld_build_spec_terms(P, t, true);
+    if (cudaMalloc(&h->gspec_terms[P], t.size() * sizeof(pgld_term)) != cudaSuccess ||
+        cudaMemcpy(h->gspec_terms[P], t.data(), t.size() * sizeof(pgld_term),
+                   cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      pgld_destroy(h);
+      cudaSetDevice(prev);
+      return pgld_fail(nullptr, PGLD_ERR_NO_MEMORY, "pgld_create: genotype term tables");
+    }
+    h->gspec_n_terms[P] = (int)t.size();
   }
   cudaSetDevice(prev);
   *out = h;
@@ -293,6 +322,8 @@ extern "C" int pgld_destroy(pgld_handle h) {
   if (h->dev_status) cudaFree(h->dev_status);
   for (int P = 0; P <= PGLD_MAX_POPS; ++P)
     if (h->spec_terms[P]) cudaFree(h->spec_terms[P]);
+  for (int P = 0; P <= PGLD_MAX_POPS; ++P)
+    if (h->gspec_terms[P]) cudaFree(h->gspec_terms[P]);
   cudaSetDevice(prev);
   delete h;
   return PGLD_OK;

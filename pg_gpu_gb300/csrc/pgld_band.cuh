@@ -20,6 +20,7 @@ struct BandArgs {
   int W[PGLD_MAX_POPS];
   const uint32_t* planes[PGLD_MAX_POPS];
   const uint32_t* valid[PGLD_MAX_POPS];
+  const uint32_t* gext[PGLD_MAX_POPS];  // genotype planes of the values 3..8 (or NULL)
   long long n_snp;
   const double* pos;
   double max_dist;

@@ -23,6 +23,9 @@ struct pgld_context {
   pgld_term* spec_terms[PGLD_MAX_POPS + 1] = {nullptr};
   int spec_n_terms[PGLD_MAX_POPS + 1] = {0};
   int spec_n_stats[PGLD_MAX_POPS + 1] = {0};
+  // the same tables with the genotype case kinds
+  pgld_term* gspec_terms[PGLD_MAX_POPS + 1] = {nullptr};
+  int gspec_n_terms[PGLD_MAX_POPS + 1] = {0};
 };
 
 // --------------------------------------------------------------------------
@@ -45,7 +48,8 @@ int pgld_workspace(pgld_context* h, size_t bytes, void** out);
 
 // moments statistic names / term tables (ld_pipeline.py:357-457)
 int pgld_n_stats(int n_pops);
-void pgld_build_spec_terms(int n_pops, std::vector<pgld_term>& out);
+// geno: the genotype case kinds of compute_multi_pop_statistics_batch_geno
+void pgld_build_spec_terms(int n_pops, std::vector<pgld_term>& out, bool geno = false);
 
 // --------------------------------------------------------------------------
 // exact integer per-population features and case formulas

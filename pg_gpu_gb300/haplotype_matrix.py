@@ -195,6 +195,28 @@ class HaplotypeMatrix:
                    samples=list(names),
                    n_total_sites=gt.shape[0] if include_invariant else None)
 
+    def load_pop_file(self, pop_file, pops=None):
+        """Sample sets from a sample / pop file; sample i owns haplotype rows i and
+        i + n_samples (haplotype_matrix.py:475-512)."""
+        if self.samples is None:
+            raise ValueError("No sample names stored. Use from_vcf() to load data.")
+        n = len(self.samples)
+        pop_map = {}
+        with open(pop_file) as f:
+            for line in f:
+                parts = line.strip().split()
+                if len(parts) >= 2 and parts[0] != "sample":
+                    pop_map[parts[0]] = parts[1]
+        if pops is None:
+            pops = sorted(set(pop_map.values()))
+        sets = {p: [] for p in pops}
+        for i, name in enumerate(self.samples):
+            p = pop_map.get(name)
+            if p in sets:
+                sets[p].append(i)
+                sets[p].append(i + n)
+        self.sample_sets = sets
+
     # ------------------------------------------------------------- packing
     def _pop_rows(self, pop):
         if pop is None:

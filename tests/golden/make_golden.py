@@ -261,6 +261,12 @@ def gen_geno(M):
     c0, nv0 = lp.compute_genotype_counts_for_pairs(S.garr(g), S.garr(ci), S.garr(cj))
     assert nv0 is None
     out["counts9"] = np.asarray(c0)
+    # dosages above 2 (multi-allelic codes summed): the kernel folds 3 g_i + g_j
+    godd = gm.copy()
+    mask = rng.random(g.shape) < 0.05
+    godd[mask] = rng.integers(3, 10, size=int(mask.sum()))
+    co, nvo = lp.compute_genotype_counts_for_pairs(S.garr(godd), S.garr(ci), S.garr(cj))
+    out["geno_odd"], out["counts9_odd"], out["nvalid_odd"] = godd, np.asarray(co), np.asarray(nvo)
     rows = np.arange(5, 37, 2)
     cr, _ = lp.compute_genotype_counts_for_pairs(S.garr(gm), S.garr(ci), S.garr(cj), list(rows))
     out["rows"], out["counts9_rows"] = rows, np.asarray(cr)
@@ -310,6 +316,48 @@ def gen_geno_stats(M):
     np.savez_compressed(os.path.join(HERE, "geno_stats.npz"), **out)
 
 
+def gen_geno_binned(M):
+    """Genotype-mode binned sums: the loop of moments_ld._compute_ld_sums
+    (moments_ld.py:248-343, use_genotypes=True) driven through the reference's
+    own iter_pairs_within_distance, compute_genotype_counts_for_pairs and
+    compute_multi_pop_statistics_batch_geno, with 2 and 3 populations."""
+    lp, gk = M["ld_pipeline"], M["genotype_kernels"]
+    rng = np.random.default_rng(20261208)
+    h = copying_model(rng, 96, 360, 10, 0.02, missing=0.0)
+    g = (h[0::2] + h[1::2]).astype(np.int8)  # 48 diploids
+    g[rng.random(g.shape) < 0.03] = -1
+    pos = np.sort(rng.choice(400_000, 360, replace=False)).astype(np.int64)
+    bins = np.array([0.0, 2e3, 5e3, 1e4, 2.5e4, 5e4, 1e5], np.float64)
+    rows = [np.arange(0, 16), np.arange(16, 34), np.arange(34, 48)]
+    out = dict(geno=g, pos=pos, bins=bins, rows0=rows[0], rows1=rows[1], rows2=rows[2])
+    for P in (2, 3):
+        sel = sorted(set(int(i) for r in rows[:P] for i in r))
+        sub = g[sel].astype(np.int64)
+        v = sub >= 0
+        alt = np.where(v, sub, 0).sum(0)
+        nv = v.sum(0)
+        keep = np.where((alt > 0) & (alt < 2 * nv) & (nv >= 2))[0]
+        gk_ = g[:, keep]
+        pk = pos[keep].astype(np.float64)
+        specs = lp.generate_stat_specs(P)
+        sums = np.zeros((len(bins) - 1, len(specs)))
+        for ci, cj in lp.iter_pairs_within_distance(S.garr(pk), float(bins[-1]), 10_000):
+            ci, cj = np.asarray(ci), np.asarray(cj)
+            cb = np.digitize(pk[cj] - pk[ci], bins) - 1
+            cs, nvs = [], []
+            for r in rows[:P]:
+                c, nvv = lp.compute_genotype_counts_for_pairs(S.garr(gk_), S.garr(ci), S.garr(cj),
+                                                              list(r))
+                cs.append(c)
+                nvs.append(nvv)
+            st = np.asarray(gk.compute_multi_pop_statistics_batch_geno(cs, nvs, None, specs))
+            ok = (cb >= 0) & (cb < len(bins) - 1)
+            np.add.at(sums, (cb[ok][:, None], np.arange(len(specs))[None, :]), st[ok])
+        out[f"keep_{P}"] = keep
+        out[f"sums_{P}"] = sums
+    np.savez_compressed(os.path.join(HERE, "geno_binned.npz"), **out)
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -318,6 +366,7 @@ def main():
     gen_moments(M)
     gen_geno(M)
     gen_geno_stats(M)
+    gen_geno_binned(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -64,6 +64,21 @@ def test_stat_tables_agree(lib):
     assert lib.pgld_stat_terms(5, None, 0, None, None) < 0
 
 
+def test_genotype_stat_tables_agree(lib):
+    from pg_gpu_gb300 import _geno, _lib as L, ld_pipeline
+    for P in (1, 2, 3, 4):
+        nt, ns = ctypes.c_int32(), ctypes.c_int32()
+        assert lib.pgld_geno_stat_terms(P, None, 0, ctypes.byref(nt), ctypes.byref(ns)) == 0
+        arr = (L.Term * nt.value)()
+        assert lib.pgld_geno_stat_terms(P, arr, nt.value, ctypes.byref(nt), ctypes.byref(ns)) == 0
+        ct = [(t.stat, t.kind, tuple(t.pops), t.weight) for t in arr]
+        py = _geno.specs_to_terms(ld_pipeline.generate_stat_specs(P))
+        assert ns.value == len(ld_pipeline.ld_names(P)) and len(py) == len(ct)
+        for (s, k, roles, w), (cs, ck, cp, cw) in zip(py, ct):
+            assert (s, k, w) == (cs, ck, cw) and tuple(roles) == cp[:len(roles)]
+            assert L.G_DD_II <= ck <= L.G_PI2_ALLDIFF
+
+
 def test_errors_are_status_codes(lib):
     import torch
     if torch.cuda.is_available():

@@ -201,3 +201,22 @@ def test_genotype_multi_pop_stats_match_reference(golden, P):
         got0 = O.geno_multi_pop_stats(cs, [None] * P)
     _same_ieee(got, z[f"multi_{P}"], 1e-13)
     _same_ieee(got0, z[f"multi_{P}_nonv"], 1e-13)
+
+
+@pytest.mark.parametrize("P", [2, 3])
+def test_genotype_binned_sums_match_reference(golden, P):
+    # the genotype loop of moments_ld._compute_ld_sums run through the
+    # reference's own pair iterator, counter and statistics
+    z = golden("geno_binned")
+    rows = [z[f"rows{q}"] for q in range(P)]
+    keep = np.where(O.union_polymorphic(z["geno"], rows))[0]
+    assert np.array_equal(keep, z[f"keep_{P}"])
+    s, _ = O.geno_binned_sums(z["geno"][:, keep], z["pos"][keep], rows, z["bins"])
+    np.testing.assert_allclose(s, z[f"sums_{P}"], rtol=1e-12, atol=1e-12 * np.abs(s).max())
+
+
+def test_genotype_counts_fold_dosages_above_two(golden):
+    # the reference kernel's class index 3 g_i + g_j folds the values 3..8
+    z = golden("geno")
+    c, nv = O.genotype_counts_for_pairs(z["geno_odd"], z["idx_i"], z["idx_j"])
+    assert np.array_equal(c, z["counts9_odd"]) and np.array_equal(nv, z["nvalid_odd"])
