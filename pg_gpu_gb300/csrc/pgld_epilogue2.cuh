@@ -1,0 +1,160 @@
+// Two pairs at a time: the float32 moments epilogue of pgld_epilogue.cuh on
+// float2 operands, so that every addition, multiplication and fused
+// multiply-add is one packed sm_100+ instruction (FADD2 / FMUL2 / FFMA2) for
+// two SNP pairs.  The arithmetic of each lane is exactly that of the scalar
+// code: the same exact integer features, the same error-free TwoProduct /
+// TwoSum numerators and the same reciprocal-table divisions, so each lane's
+// statistics equal the scalar epilogue's bit for bit.
+#pragma once
+#include "pgld_epilogue.cuh"
+
+#ifndef __CUDACC__
+struct float2 {
+  float x, y;
+};
+inline float2 make_float2(float x, float y) { return {x, y}; }
+#endif
+
+namespace pgld {
+namespace fast2 {
+
+typedef float2 V;
+
+#if defined(__CUDA_ARCH__)
+PGLD_HD V vadd(V a, V b) { return __fadd2_rn(a, b); }
+PGLD_HD V vmul(V a, V b) { return __fmul2_rn(a, b); }
+PGLD_HD V vfma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
+#else
+// host build (numerical tests): one rounded float operation per lane
+PGLD_HD V vadd(V a, V b) { return make_float2(a.x + b.x, a.y + b.y); }
+PGLD_HD V vmul(V a, V b) { return make_float2(a.x * b.x, a.y * b.y); }
+PGLD_HD V vfma(V a, V b, V c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)); }
+#endif
+PGLD_HD V vneg(V a) { return make_float2(-a.x, -a.y); }
+PGLD_HD V vsub(V a, V b) { return vadd(a, vneg(b)); }
+PGLD_HD V vs(float a) { return make_float2(a, a); }
+
+struct X2 {
+  V s, e;
+};
+
+PGLD_HD X2 x2_prod(V a, V b) {
+  const V p = vmul(a, b);
+  return {p, vfma(a, b, vneg(p))};
+}
+PGLD_HD void x2_add_prod(X2& acc, V a, V b) {
+  const V p = vmul(a, b);
+  const V pe = vfma(a, b, vneg(p));
+  const V s = vadd(acc.s, p);
+  const V bb = vsub(s, acc.s);
+  const V t = vadd(vsub(acc.s, vsub(s, bb)), vsub(p, bb));
+  acc.s = s;
+  acc.e = vadd(acc.e, vadd(pe, t));
+}
+PGLD_HD V x2_value(const X2& v) { return vadd(v.s, v.e); }
+
+struct Pop {
+  V c1, c2, c3, c4;
+  V pA, qA, pB, qB;
+  V a, b, x;
+  V dA, dB, e;
+  int n0, n1;  // valid n of each lane
+};
+
+PGLD_HD int f2i(float f) { return fast::f2i_small(f); }
+
+PGLD_HD Pop make(V c1, V c2, V c3, V c4) {
+  Pop p;
+  p.c1 = c1; p.c2 = c2; p.c3 = c3; p.c4 = c4;
+  p.pA = vadd(c1, c2); p.qA = vadd(c3, c4); p.pB = vadd(c1, c3); p.qB = vadd(c2, c4);
+  p.a = vmul(c1, c4); p.b = vmul(c2, c3); p.x = vsub(p.a, p.b);
+  p.dA = vsub(p.qA, p.pA); p.dB = vsub(p.qB, p.pB);
+  p.e = vsub(vadd(c2, c3), vadd(c1, c4));
+  const V n = vadd(p.pA, p.qA);
+  p.n0 = f2i(n.x);
+  p.n1 = f2i(n.y);
+  return p;
+}
+
+PGLD_HD V dd_num(const Pop& p) {
+  X2 v = x2_prod(p.x, p.x);
+  x2_add_prod(v, p.a, vsub(vsub(vs(1.0f), p.c1), p.c4));
+  x2_add_prod(v, p.b, vsub(vsub(vs(1.0f), p.c2), p.c3));
+  return x2_value(v);
+}
+PGLD_HD V dz_num(const Pop& p) {
+  return vfma(p.x, vfma(p.dA, p.dB, p.e), vmul(vs(2.0f), vadd(p.a, p.b)));
+}
+PGLD_HD V pi2_num(const Pop& p) {
+  X2 v = x2_prod(vmul(p.pA, p.pB), vmul(p.qB, p.qA));
+  // 1 - c1 - 3 c2 - 3 c3 - c4 and 1 - 3 c1 - c2 - c3 - 3 c4
+  const V s23 = vadd(p.c2, p.c3), s14 = vadd(p.c1, p.c4);
+  x2_add_prod(v, p.a, vsub(vfma(vs(-3.0f), s23, vs(1.0f)), s14));
+  x2_add_prod(v, p.b, vsub(vfma(vs(-3.0f), s14, vs(1.0f)), s23));
+  return x2_value(v);
+}
+PGLD_HD V triple_num2(const Pop& t, const Pop& s) {
+  X2 v = x2_prod(vmul(t.pA, t.qA),
+                 vfma(vs(-2.0f), s.qB, vfma(t.qB, s.pB, vmul(t.pB, s.qB))));
+  x2_add_prod(v, vfma(t.pA, t.c4, vmul(t.c2, t.qA)), vsub(s.qB, s.pB));
+  return x2_value(v);
+}
+PGLD_HD V ijij_num4(const Pop& A, const Pop& B) {
+  const V HA = vfma(A.qA, B.pA, vmul(A.pA, B.qA));
+  const V HB = vfma(A.qB, B.pB, vmul(A.pB, B.qB));
+  const V K = vfma(A.c1, B.c4, vfma(A.c2, B.c3, vfma(A.c3, B.c2, vmul(A.c4, B.c1))));
+  X2 v = x2_prod(HA, HB);
+  x2_add_prod(v, vsub(vsub(vs(1.0f), vadd(A.pA, A.qA)), vadd(B.pA, B.qA)), K);
+  x2_add_prod(v, vneg(A.x), B.e);
+  x2_add_prod(v, vneg(B.x), A.e);
+  return x2_value(v);
+}
+
+PGLD_HD V tab(const float* t, int n0, int n1) { return make_float2(t[n0], t[n1]); }
+
+
+// the 15 two-population statistics in moments ld_names(2) order, two pairs;
+// each value goes to sink(k, value) as soon as it is formed, so a caller that
+// only accumulates never holds all fifteen
+template <class Sink>
+PGLD_HD void stats2_to(const Pop& p, const Pop& q, const fast::Recip& T, Sink&& sink) {
+  const V r4p = tab(T.r4, p.n0, p.n1), r4q = tab(T.r4, q.n0, q.n1);
+  const V r22 = vmul(tab(T.r2, p.n0, p.n1), tab(T.r2, q.n0, q.n1));
+  sink(0, vmul(dd_num(p), r4p));
+  sink(1, vmul(vmul(p.x, q.x), r22));
+  sink(2, vmul(dd_num(q), r4q));
+  sink(3, vmul(dz_num(p), r4p));
+  sink(8, vmul(dz_num(q), r4q));
+  sink(9, vmul(pi2_num(p), r4p));
+  sink(14, vmul(pi2_num(q), r4q));
+  sink(5, vmul(vmul(p.x, vfma(q.dB, q.dA, q.e)), r22));
+  sink(6, vmul(vmul(q.x, vfma(p.dB, p.dA, p.e)), r22));
+  sink(11, vmul(vfma(vmul(p.pA, p.qA), vmul(q.pB, q.qB), vmul(vmul(q.pA, q.qA), vmul(p.pB, p.qB))),
+                vmul(vs(0.5f), r22)));
+  sink(12, vmul(ijij_num4(p, q), vmul(vs(0.25f), r22)));
+  const V h31p = vmul(vs(0.5f), vmul(tab(T.r3, p.n0, p.n1), tab(T.inv, q.n0, q.n1)));
+  sink(4, vmul(vmul(p.x, vfma(p.dA, q.dB, vmul(p.dB, q.dA))), h31p));
+  sink(10, vmul(triple_num2(p, q), h31p));
+  const V h31q = vmul(vs(0.5f), vmul(tab(T.r3, q.n0, q.n1), tab(T.inv, p.n0, p.n1)));
+  sink(7, vmul(vmul(q.x, vfma(q.dA, p.dB, vmul(q.dB, p.dA))), h31q));
+  sink(13, vmul(triple_num2(q, p), h31q));
+}
+
+PGLD_HD void stats2(const Pop& p, const Pop& q, const fast::Recip& T, V o[15]) {
+  stats2_to(p, q, T, [&](int k, V v) { o[k] = v; });
+}
+
+template <class Sink>
+PGLD_HD void stats1_to(const Pop& p, const fast::Recip& T, Sink&& sink) {
+  const V r4 = tab(T.r4, p.n0, p.n1);
+  sink(0, vmul(dd_num(p), r4));
+  sink(1, vmul(dz_num(p), r4));
+  sink(2, vmul(pi2_num(p), r4));
+}
+
+PGLD_HD void stats1(const Pop& p, const fast::Recip& T, V o[3]) {
+  stats1_to(p, T, [&](int k, V v) { o[k] = v; });
+}
+
+}  // namespace fast2
+}  // namespace pgld

@@ -26,6 +26,7 @@
 
 #include "pgld_band.cuh"
 #include "pgld_epilogue.cuh"
+#include "pgld_epilogue2.cuh"
 #include "pgld_internal.cuh"
 #include "pgld_scan.cuh"
 
@@ -450,6 +451,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       tc_fence_after();
 
+      // bin accumulators of the warp's sub-tile, two lanes per statistic
+      // (the float2 halves hold the even / odd pairs of each thread)
       float acc_lo[S], acc_hi[S];
 #pragma unroll
       for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
@@ -485,66 +488,71 @@ __global__ void __launch_bounds__(kThreads, 1)
             cf[q][p][2] = plane ? m0 : g0;
             cf[q][p][3] = plane ? m1 : g1;
           }
-        // one pair per iteration over rotating arrays: the statistics code is
-        // emitted once (instruction-cache footprint)
+        // two pairs per iteration (packed float2 arithmetic) over rotating
+        // arrays: the statistics code is emitted once (instruction cache)
 #pragma unroll 1
-        for (int q = 0; q < 4; ++q) {
-          const int jl = half * 32 + c * 8 + 2 * q + plane;
-          const long long j = j0 + jl;
-          float st[S];
-          {
-            const fast::Pop p0 = fast::make(cf[0][0][0], cf[0][0][1], cf[0][0][2], cf[0][0][3]);
-            if (P == 1) {
-              fast::stats1(p0, T, st);
-            } else {
-              const fast::Pop p1 =
-                  fast::make(cf[0][P - 1][0], cf[0][P - 1][1], cf[0][P - 1][2], cf[0][P - 1][3]);
-              fast::stats2(p0, p1, T, st);
-            }
-          }
+        for (int qq = 0; qq < 2; ++qq) {
+          const fast2::Pop p0 = fast2::make(
+              make_float2(cf[0][0][0], cf[1][0][0]), make_float2(cf[0][0][1], cf[1][0][1]),
+              make_float2(cf[0][0][2], cf[1][0][2]), make_float2(cf[0][0][3], cf[1][0][3]));
+          const fast2::Pop p1 = fast2::make(make_float2(cf[0][P - 1][0], cf[1][P - 1][0]),
+                                            make_float2(cf[0][P - 1][1], cf[1][P - 1][1]),
+                                            make_float2(cf[0][P - 1][2], cf[1][P - 1][2]),
+                                            make_float2(cf[0][P - 1][3], cf[1][P - 1][3]));
 #pragma unroll
-          for (int k = 0; k < 3; ++k)
+          for (int k = 0; k < 2; ++k)
 #pragma unroll
             for (int p = 0; p < P; ++p)
 #pragma unroll
-              for (int m = 0; m < 4; ++m) cf[k][p][m] = cf[k + 1][p][m];
+              for (int m = 0; m < 4; ++m) cf[k][p][m] = cf[k + 2][p][m];
+          float2 st[S];
+          if constexpr (P == 1) fast2::stats1(p0, T, st);
+          else fast2::stats2(p0, p1, T, st);
           if (mode == 0) {
 #pragma unroll
-            for (int s = 0; s < S; ++s) acc_lo[s] += st[s];
+            for (int s = 0; s < S; ++s) acc_lo[s] += st[s].x + st[s].y;
           } else if (mode == 1) {
-            const bool up = (a.ipos[j] - ipos_i) >= thr_mid;
-            const float fu = up ? 1.f : 0.f, fl = up ? 0.f : 1.f;
-            n_hi += up ? 1 : 0;
+            const long long ja = j0 + half * 32 + c * 8 + 4 * qq + plane;
+            const bool up0 = (a.ipos[ja] - ipos_i) >= thr_mid;
+            const bool up1 = (a.ipos[ja + 2] - ipos_i) >= thr_mid;
+            const float2 fu = make_float2(up0 ? 1.f : 0.f, up1 ? 1.f : 0.f);
+            const float2 fl = make_float2(up0 ? 0.f : 1.f, up1 ? 0.f : 1.f);
+            n_hi += (up0 ? 1 : 0) + (up1 ? 1 : 0);
 #pragma unroll
             for (int s = 0; s < S; ++s) {
-              acc_hi[s] = fmaf(fu, st[s], acc_hi[s]);
-              acc_lo[s] = fmaf(fl, st[s], acc_lo[s]);
+              acc_hi[s] = fmaf(fu.x, st[s].x, fmaf(fu.y, st[s].y, acc_hi[s]));
+              acc_lo[s] = fmaf(fl.x, st[s].x, fmaf(fl.y, st[s].y, acc_lo[s]));
             }
           } else {
-            bool ok = (i < j) && (j < a.n_snp);
-            int b = -1;
-            if (use_int) {
-              const int d = ok ? a.ipos[j] - ipos_i : 0;
-              if (ok && d <= maxd_int) b = bin_of_int(thr, n_bins, d);
-            } else if (ok) {
-              const double dp = a.pos[j] - a.pos[i];
-              if (dp <= maxd) {
-                const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
-                b = bin_of_f64(sbins, n_bins, d);
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+              const int jl = half * 32 + c * 8 + 2 * (2 * qq + h) + plane;
+              const long long j = j0 + jl;
+              bool ok = (i < j) && (j < a.n_snp);
+              int b = -1;
+              if (use_int) {
+                const int d = ok ? a.ipos[j] - ipos_i : 0;
+                if (ok && d <= maxd_int) b = bin_of_int(thr, n_bins, d);
+              } else if (ok) {
+                const double dp = a.pos[j] - a.pos[i];
+                if (dp <= maxd) {
+                  const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
+                  b = bin_of_f64(sbins, n_bins, d);
+                }
               }
-            }
-            unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
-            while (pending) {
-              const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
-              const bool mine = (b == bb);
-              const unsigned grp = __ballot_sync(0xffffffffu, mine);
-              float v[S];
+              unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
+              while (pending) {
+                const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
+                const bool mine = (b == bb);
+                const unsigned grp = __ballot_sync(0xffffffffu, mine);
+                float v[S];
 #pragma unroll
-              for (int s = 0; s < S; ++s) v[s] = mine ? st[s] : 0.f;
-              const float tot = warp_totals_pick<S>(v, lane);
-              if (lane < S) kahan_add(my_acc + bb * S + lane, tot);
-              if (lane == 31) my_cnt[bb] += (unsigned long long)__popc(grp);
-              pending &= ~grp;
+                for (int s = 0; s < S; ++s) v[s] = mine ? (h ? st[s].y : st[s].x) : 0.f;
+                const float tot = warp_totals_pick<S>(v, lane);
+                if (lane < S) kahan_add(my_acc + bb * S + lane, tot);
+                if (lane == 31) my_cnt[bb] += (unsigned long long)__popc(grp);
+                pending &= ~grp;
+              }
             }
           }
         }

@@ -4,7 +4,7 @@
 // device bit tricks.
 #include <vector>
 
-#include "../../pg_gpu_gb300/csrc/pgld_epilogue.cuh"
+#include "../../pg_gpu_gb300/csrc/pgld_epilogue2.cuh"
 
 extern "C" void pgld_check_stats(const int* counts, const int* n, int N, int P, float* out) {
   using namespace pgld::fast;
@@ -23,5 +23,32 @@ extern "C" void pgld_check_stats(const int* counts, const int* n, int N, int P, 
       Pop q = make((float)c[4], (float)c[5], (float)c[6], (float)c[7]);
       stats2(p, q, T, out + 15 * k);
     }
+  }
+}
+
+// the packed two-pair form: rows k and N-1-k share one float2 evaluation
+extern "C" void pgld_check_stats2(const int* counts, const int* n, int N, int P, float* out) {
+  using namespace pgld::fast;
+  namespace f2 = pgld::fast2;
+  int nmax = 0;
+  for (int k = 0; k < N * 2; ++k) nmax = n[k] > nmax ? n[k] : nmax;
+  std::vector<float> tab(4 * (nmax + 1));
+  for (int v = 0; v <= nmax; ++v)
+    recip_entry(v, &tab[v], &tab[(nmax + 1) + v], &tab[2 * (nmax + 1) + v], &tab[3 * (nmax + 1) + v]);
+  Recip T{&tab[0], &tab[nmax + 1], &tab[2 * (nmax + 1)], &tab[3 * (nmax + 1)]};
+  const int S = P == 1 ? 3 : 15;
+  for (int k = 0; k < N; ++k) {
+    const int* a = counts + 8 * k;
+    const int* b = counts + 8 * (N - 1 - k);
+    auto v = [&](int m) { return make_float2((float)a[m], (float)b[m]); };
+    f2::Pop p = f2::make(v(0), v(1), v(2), v(3));
+    float2 o[15];
+    if (P == 1) {
+      f2::stats1(p, T, o);
+    } else {
+      f2::Pop q = f2::make(v(4), v(5), v(6), v(7));
+      f2::stats2(p, q, T, o);
+    }
+    for (int s = 0; s < S; ++s) out[S * k + s] = o[s].x;
   }
 }

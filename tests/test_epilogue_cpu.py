@@ -26,6 +26,7 @@ def check_lib(tmp_path_factory):
     subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-o", so, SRC])
     L = ctypes.CDLL(so)
     L.pgld_check_stats.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_int] * 2 + [ctypes.c_void_p]
+    L.pgld_check_stats2.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_int] * 2 + [ctypes.c_void_p]
     return L
 
 
@@ -68,3 +69,19 @@ def test_fast_epilogue_within_1e6_of_oracle(check_lib, nmax):
         m = np.abs(ref) > 1e-30
         rel = np.abs(got[m] - ref[m]) / np.abs(ref[m])
         assert rel.max() <= 1e-6, (P, nmax, rel.max())
+
+
+@pytest.mark.parametrize("nmax", [6, 1000, 2048])
+def test_packed_epilogue_equals_scalar(check_lib, nmax):
+    """The float2 (two pairs per instruction) epilogue is bit-identical per lane."""
+    rng = np.random.default_rng(100 + nmax)
+    N = 5000
+    c = _tables(rng, N, nmax)
+    nvalid = np.ascontiguousarray(np.stack([c[:, :4].sum(1), c[:, 4:].sum(1)], 1).astype(np.int32))
+    for P in (1, 2):
+        S = 3 if P == 1 else 15
+        a = np.zeros((N, S), np.float32)
+        b = np.zeros((N, S), np.float32)
+        check_lib.pgld_check_stats(c.ctypes.data, nvalid.ctypes.data, N, P, a.ctypes.data)
+        check_lib.pgld_check_stats2(c.ctypes.data, nvalid.ctypes.data, N, P, b.ctypes.data)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
