@@ -305,6 +305,22 @@ int pgld_geno_binned_sums(pgld_handle h, const pgld_geno_panel* panel, const dou
                           double max_dist, const double* bin_coord, const double* bins,
                           int32_t n_bins, double* sums, int64_t* pair_counts, void* stream);
 
+/* Per-window sums over batched, uneven windows in one launch, one
+ * population.  Window w holds the SNPs snp_idx[win_begin[w] .. win_end[w])
+ * (device int64 bounds; device int32 indices into the panel, n_idx entries;
+ * snp_idx NULL = the identity with n_idx = n_snp); windows may overlap and
+ * every pair a < b inside a window contributes.  sums:
+ * [n_win][6] float64 = r^2 (pairs where it is defined), sigma_D^2 = DD / pi2
+ * numerators (pairs with n >= 4; 0 where the pi2 numerator is 0), DD, Dz,
+ * pi2 (single-population moments statistics; 0 below n = 4), naive r^2 of
+ * per-site allele frequencies.  counts: [n_win][3] int64 = pairs, pairs with
+ * r^2 defined, pairs with n >= 4.  Replaces the per-window loops of
+ * _zns_from_precomputed / _zns_tiled over _tile_counts / _tile_sigma_d2 /
+ * _tile_r2_naive (ld_statistics.py:281-341, 534-676).  Synchronises. */
+int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel, const int32_t* snp_idx,
+                         int64_t n_idx, const int64_t* win_begin, const int64_t* win_end,
+                         int32_t n_win, double* sums, int64_t* counts, void* stream);
+
 /* pgld_hap_binned_sums for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers of this library cannot call
  * cudaMalloc: a host application that hands every byte of the device to its

@@ -1018,3 +1018,72 @@ def geno_heterozygosity(geno, pop_rows):
                 out[f"H_{i}_{j}"] = float(np.sum((ref[i] * alt[j] + alt[i] * ref[j])
                                                  / (size[i] * size[j])))
     return out
+
+
+# ---------------------------------------------------------------------------
+# per-window sums and ZnS  (ld_statistics.py:250-341, 534-676)
+# ---------------------------------------------------------------------------
+def segregating(hap):
+    """Sites with 0 < derived count < valid count (ld_statistics.py:266-271)."""
+    h = np.asarray(hap)
+    dac = np.maximum(h, 0).astype(np.int64).sum(0)
+    nv = (h >= 0).sum(0)
+    return (dac > 0) & (dac < nv)
+
+
+def window_sums(hap, idx, win_begin, win_end):
+    """(sums [n_win][6], counts [n_win][3]) as pgld_hap_window_sums: r^2,
+    sigma_D^2 (projection), DD, Dz, pi2, naive r^2; pairs, r^2-defined, n >= 4.
+    Window w covers idx[win_begin[w]:win_end[w]]."""
+    h = np.asarray(hap)
+    idx = np.asarray(idx, np.int64)
+    dac_all = (h == 1).sum(0).astype(np.int64)
+    nv_all = (h >= 0).sum(0).astype(np.int64)
+    n_win = len(win_begin)
+    sums = np.zeros((n_win, 6))
+    cnts = np.zeros((n_win, 3), np.int64)
+    for w in range(n_win):
+        sel = idx[win_begin[w]:win_end[w]]
+        m = len(sel)
+        if m < 2:
+            continue
+        a, b = np.triu_indices(m, 1)
+        ii, jj = sel[a], sel[b]
+        c, nv = counts_for_pairs(h, ii, jj)
+        n = c.astype(I64).sum(1)
+        cnts[w, 0] = len(ii)
+        r2 = r_squared(c, nv)
+        ok = ~np.isnan(r2)
+        sums[w, 0] = r2[ok].sum()
+        cnts[w, 1] = ok.sum()
+        p = Pop(c, n)
+        dd_n, _ = dd_ii(p)
+        pi_n, _ = pi2_iiii(p)
+        four = n >= 4
+        cnts[w, 2] = four.sum()
+        with np.errstate(divide="ignore", invalid="ignore"):
+            sig = np.where(four & (pi_n != 0), dd_n / np.where(pi_n != 0, pi_n, 1), 0.0)
+        sums[w, 1] = sig.sum()
+        sums[w, 2] = dd(c, None, n).sum()
+        sums[w, 3] = dz(c, None, n).sum()
+        sums[w, 4] = pi2(c, None, n).sum()
+        pi_ = dac_all[ii] / np.maximum(nv_all[ii], 1)
+        pj_ = dac_all[jj] / np.maximum(nv_all[jj], 1)
+        pab = np.where(n > 0, c[:, 0] / np.maximum(n, 1), 0.0)
+        D = pab - pi_ * pj_
+        den = pi_ * (1 - pi_) * pj_ * (1 - pj_)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            sums[w, 5] = np.where(den > 0, D * D / np.where(den > 0, den, 1), 0.0).sum()
+    return sums, cnts
+
+
+def zns_window(hap, s, e, projection=True):
+    """ZnS of the SNPs [s, e) as _zns_from_precomputed (ld_statistics.py:595-676)."""
+    h = np.asarray(hap)[:, s:e]
+    seg = np.where(segregating(h))[0]
+    if len(seg) < 2:
+        return 0.0
+    sums, cnts = window_sums(h, seg, [0], [len(seg)])
+    if projection:
+        return sums[0, 1] / cnts[0, 2] if cnts[0, 2] > 0 else 0.0
+    return sums[0, 5] / cnts[0, 0]

@@ -222,6 +222,41 @@ def band_pairs(pk, pos_d, max_dist, with_stats=True):
     return counts, nv, st
 
 
+WINDOW_COLUMNS = ("r2", "sigma_d2", "dd", "dz", "pi2", "r2_naive")
+
+
+def window_sums(pk, idx, win_begin, win_end):
+    """Per-window sums (n_win, 6) float64 and counts (n_win, 3) int64 over
+    every pair inside each window (one launch for all windows).
+
+    idx: int32 SNP indices (None: identity); window w covers
+    idx[win_begin[w]:win_end[w]].  Columns: WINDOW_COLUMNS; counts: pairs,
+    pairs with r^2 defined, pairs with n >= 4."""
+    torch = _torch()
+    dev = pk.planes.device
+    wb = L.as_device(win_begin, np.int64)
+    we = L.as_device(win_end, np.int64)
+    if wb.shape != we.shape:
+        raise ValueError("win_begin and win_end must have the same shape")
+    n_win = wb.numel()
+    sums = torch.empty((max(n_win, 0), 6), dtype=torch.float64, device=dev)
+    cnt = torch.empty((max(n_win, 0), 3), dtype=torch.int64, device=dev)
+    if n_win <= 0:
+        return sums, cnt
+    ii = None if idx is None else L.as_device(idx, np.int32)
+    n_idx = pk.n_snp if ii is None else ii.numel()
+    h = L.handle()
+    L.check(L.lib().pgld_hap_window_sums(h, ctypes.byref(panel([pk])), L.ptr(ii), n_idx, L.ptr(wb),
+                                         L.ptr(we), n_win, L.ptr(sums), L.ptr(cnt),
+                                         L.stream_ptr()), h)
+    st = torch.zeros(1, dtype=torch.int32)
+    L.check(L.lib().pgld_device_status(h, ctypes.cast(st.data_ptr(), ctypes.POINTER(
+        ctypes.c_int32)), L.stream_ptr()), h)
+    if int(st[0]):
+        raise IndexError(f"window or SNP index out of range (device status {int(st[0])})")
+    return sums, cnt
+
+
 def tc_applies(pops):
     """The tensor-core form takes 1-2 populations of <= 2048 haplotypes (0/1/-1 codes)."""
     return len(pops) <= 2 and all(pk.n_words <= 64 and pk.valid_for_n is None for pk in pops)

@@ -170,3 +170,86 @@ def rogers_huff_r(matrix, tile_size=None):
 
 def rogers_huff_r_squared(matrix, tile_size=None):
     return rogers_huff_r(matrix) ** 2
+
+
+# --------------------------------------------------------------------------
+# ZnS over windows (ld_statistics.py:534-735, windowed_analysis.py:2013-2062)
+# --------------------------------------------------------------------------
+def _segregating_index(hap):
+    """Indices of the sites with 0 < derived count < valid count (ld_statistics.py:250-277)."""
+    import torch
+    h = L.as_device(hap, np.int8)
+    dac = h.clamp(min=0).to(torch.int32).sum(0)
+    nv = (h >= 0).to(torch.int32).sum(0)
+    return ((dac > 0) & (dac < nv)).nonzero().flatten().to(torch.int32)
+
+
+def _zns_windows(matrix, win_start, win_stop, estimator):
+    """ZnS of each SNP window [win_start[w], win_stop[w]) over its segregating
+    sites (_zns_from_precomputed, ld_statistics.py:595-676), all windows in
+    one launch; 0.0 where a window has fewer than 2 segregating sites."""
+    if estimator not in ("sigma_d2", "r2"):
+        raise ValueError(f"unknown estimator {estimator!r}")
+    matrix.transfer_to_gpu()
+    ws = np.asarray(win_start, np.int64)
+    we = np.asarray(win_stop, np.int64)
+    if ws.shape != we.shape:
+        raise ValueError("win_start and win_stop must have the same shape")
+    seg = _segregating_index(matrix.haplotypes)
+    seg_np = seg.cpu().numpy()
+    b = np.searchsorted(seg_np, ws, side="left").astype(np.int64)
+    e = np.searchsorted(seg_np, we, side="left").astype(np.int64)
+    sums, cnt = _ops.window_sums(matrix.packed(None), seg, b, e)
+    s, c = sums.cpu().numpy(), cnt.cpu().numpy()
+    out = np.zeros(len(ws))
+    for w in range(len(ws)):
+        if e[w] - b[w] < 2:
+            continue
+        if estimator == "sigma_d2":
+            out[w] = s[w, 1] / c[w, 2] if c[w, 2] > 0 else 0.0
+        else:
+            out[w] = s[w, 5] / c[w, 0]
+    return out
+
+
+def windowed_zns(matrix, win_start, win_stop, estimator="sigma_d2"):
+    """Per-window ZnS for SNP windows [win_start[w], win_stop[w]) in one launch:
+    the zns loop of windowed_analysis (windowed_analysis.py:2013-2062), where
+    windows of fewer than 4 SNPs are NaN and the estimator defaults to the
+    unbiased sigma_D^2 (estimator "r2": mean naive r^2)."""
+    out = _zns_windows(matrix, win_start, win_stop, estimator)
+    short = (np.asarray(win_stop, np.int64) - np.asarray(win_start, np.int64)) < 4
+    out[short] = np.nan
+    return out
+
+
+def zns(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
+    """Kelly's ZnS (ld_statistics.py:679-731).
+
+    A HaplotypeMatrix takes the unbiased sigma_D^2 estimator by default
+    ("auto"), or naive r^2 ("r2"), over its segregating sites (missing_data
+    "exclude" first drops sites with missing calls), in one device pass; a
+    precomputed square r^2 matrix gives its mean off-diagonal value.
+    """
+    from .haplotype_matrix import HaplotypeMatrix
+    is_hm = isinstance(r2_matrix_or_matrix, HaplotypeMatrix)
+    if estimator == "auto":
+        estimator = "sigma_d2" if is_hm else "r2"
+    if estimator not in ("r2", "sigma_d2"):
+        raise ValueError(f"unknown estimator {estimator!r}")
+    if is_hm:
+        hm = r2_matrix_or_matrix
+        hm.transfer_to_gpu()
+        if missing_data == "exclude":
+            keep = ((hm.haplotypes < 0).sum(0) == 0).nonzero().flatten()
+            hm = hm.get_subset(keep)
+        return float(_zns_windows(hm, [0], [hm.num_variants], estimator)[0])
+    if estimator == "sigma_d2":
+        raise ValueError("estimator='sigma_d2' requires a HaplotypeMatrix, "
+                         "not a pre-computed r² array")
+    import torch
+    r2 = L.as_device(r2_matrix_or_matrix, np.float64)
+    m = r2.shape[0]
+    if m < 2:
+        return 0.0
+    return float((r2.sum() - torch.trace(r2)) / (m * (m - 1)))

@@ -358,6 +358,25 @@ def gen_geno_binned(M):
     np.savez_compressed(os.path.join(HERE, "geno_binned.npz"), **out)
 
 
+def gen_windows(M):
+    """Per-window ZnS from the reference's _zns_from_precomputed
+    (ld_statistics.py:595-676), projection (sigma_D^2) and naive r^2."""
+    ls = M["ld_statistics"]
+    rng = np.random.default_rng(20261209)
+    hap = copying_model(rng, 60, 700, 8, 0.01, missing=0.03)
+    bounds = np.array([0, 3, 40, 41, 130, 300, 301, 520, 700])
+    hc = np.where(hap >= 0, hap, 0).astype(np.float64)
+    vm = (hap >= 0).astype(np.float64)
+    zp, zn = [], []
+    for s, e in zip(bounds[:-1], bounds[1:]):
+        zp.append(ls._zns_from_precomputed(S.garr(hc), S.garr(vm), int(s), int(e), tile_size=64,
+                                            use_projection=True))
+        zn.append(ls._zns_from_precomputed(S.garr(hc), S.garr(vm), int(s), int(e), tile_size=64,
+                                            use_projection=False))
+    np.savez_compressed(os.path.join(HERE, "windows.npz"), hap=hap, bounds=bounds,
+                        zns_proj=np.array(zp, np.float64), zns_naive=np.array(zn, np.float64))
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -367,6 +386,7 @@ def main():
     gen_geno(M)
     gen_geno_stats(M)
     gen_geno_binned(M)
+    gen_windows(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -1,0 +1,97 @@
+"""GPU parity of the batched-window path (one launch over all windows).
+
+Per-window sums of float32 per-pair statistics accumulate in float64; they are
+held to |gpu - oracle| <= 2e-6 * sum|x| per window and statistic, pair counts
+exactly, and ZnS to the reference's _zns_from_precomputed fixtures at 1e-5.
+"""
+import numpy as np
+import pytest
+
+from oracle import ld_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+from pg_gpu_gb300 import _ops, ld_statistics  # noqa: E402
+from pg_gpu_gb300.haplotype_matrix import HaplotypeMatrix  # noqa: E402
+
+
+def copying_model(rng, H, M, F, switch, missing=0.0, flip=1e-3):
+    p = rng.beta(0.3, 0.3, size=M)
+    f = (rng.random((F, M)) < p).astype(np.int8)
+    sw = rng.random((H, M)) < switch
+    seg = np.cumsum(sw, axis=1)
+    choice = rng.integers(0, F, size=(H, seg.max() + 1))
+    hap = f[np.take_along_axis(choice, seg, axis=1), np.arange(M)[None, :]]
+    hap ^= (rng.random(hap.shape) < flip).astype(np.int8)
+    if missing:
+        hap[rng.random(hap.shape) < missing] = -1
+    return hap.astype(np.int8)
+
+
+@pytest.mark.parametrize("H", [33, 400])
+def test_window_sums_match_oracle(H):
+    rng = np.random.default_rng(H)
+    M = 900
+    hap = copying_model(rng, H, M, 12, 2e-3, missing=0.02)
+    seg = np.where(O.segregating(hap))[0].astype(np.int32)
+    # uneven and overlapping windows, including empty and one-SNP ones
+    ns = len(seg)
+    b = np.minimum(np.array([0, 0, 5, 5, 100, 131, 400, 700, 60], np.int64), ns)
+    e = np.minimum(np.array([0, 1, 5, 37, 300, 131 + 64, 700, ns, 200], np.int64), ns)
+    assert ns > 300
+    pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
+    sums, cnt = _ops.window_sums(pk, torch.as_tensor(seg, device="cuda"), b, e)
+    ref, rcnt = O.window_sums(hap, seg, b, e)
+    assert np.array_equal(cnt.cpu().numpy(), rcnt)
+    got = sums.cpu().numpy()
+    # scale: per-pair magnitudes (the float32 per-pair values sum to these)
+    for w in range(len(b)):
+        sel = seg[b[w]:e[w]]
+        if len(sel) < 2:
+            assert np.all(got[w] == 0)
+            continue
+        a_, b_ = np.triu_indices(len(sel), 1)
+        c, nv = O.counts_for_pairs(hap, sel[a_], sel[b_])
+        n = c.astype(np.int64).sum(1)
+        scale = np.array([np.nansum(np.abs(O.r_squared(c, nv))),
+                          np.abs(ref[w, 1]) + 1e-12 * rcnt[w, 2],
+                          np.abs(O.dd(c, None, n)).sum(), np.abs(O.dz(c, None, n)).sum(),
+                          np.abs(O.pi2(c, None, n)).sum(), abs(ref[w, 5])])
+        # sigma_D^2 terms can cancel: bound by the sum of |dd / pi2| per pair
+        p = O.Pop(c, n)
+        ddn, _ = O.dd_ii(p)
+        pin, _ = O.pi2_iiii(p)
+        ok = (n >= 4) & (pin != 0)
+        scale[1] = np.abs(ddn[ok] / pin[ok]).sum()
+        assert np.all(np.abs(got[w] - ref[w]) <= 2e-6 * scale + 1e-12), (w, got[w], ref[w])
+
+
+def test_zns_matches_reference(golden):
+    z = golden("windows")
+    hm = HaplotypeMatrix(z["hap"], np.arange(z["hap"].shape[1]))
+    bnd = z["bounds"]
+    got = ld_statistics.windowed_zns(hm, bnd[:-1], bnd[1:])
+    want = np.where(np.diff(bnd) < 4, np.nan, z["zns_proj"])
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    m = ~np.isnan(want)
+    np.testing.assert_allclose(got[m], want[m], rtol=1e-5, atol=1e-9)
+    got_r2 = ld_statistics.windowed_zns(hm, bnd[:-1], bnd[1:], estimator="r2")
+    want_r2 = np.where(np.diff(bnd) < 4, np.nan, z["zns_naive"])
+    np.testing.assert_allclose(got_r2[m], want_r2[m], rtol=1e-5, atol=1e-9)
+    # whole-matrix ZnS: one window over every site
+    full = O.zns_window(z["hap"], 0, z["hap"].shape[1], True)
+    assert ld_statistics.zns(hm) == pytest.approx(full, rel=1e-5)
+    assert ld_statistics.zns(hm, estimator="r2") == pytest.approx(
+        O.zns_window(z["hap"], 0, z["hap"].shape[1], False), rel=1e-5)
+
+
+def test_window_errors():
+    pk = _ops.pack(np.zeros((8, 10), np.int8))
+    with pytest.raises(IndexError):
+        _ops.window_sums(pk, torch.arange(10, dtype=torch.int32, device="cuda"), [0], [11])
+    with pytest.raises(IndexError):
+        _ops.window_sums(pk, torch.tensor([0, 3, 99], dtype=torch.int32, device="cuda"), [0], [3])

@@ -220,3 +220,12 @@ def test_genotype_counts_fold_dosages_above_two(golden):
     z = golden("geno")
     c, nv = O.genotype_counts_for_pairs(z["geno_odd"], z["idx_i"], z["idx_j"])
     assert np.array_equal(c, z["counts9_odd"]) and np.array_equal(nv, z["nvalid_odd"])
+
+
+def test_window_zns_matches_reference(golden):
+    # _zns_from_precomputed (ld_statistics.py:595-676) per window, both estimators
+    z = golden("windows")
+    b = z["bounds"]
+    for k, (s, e) in enumerate(zip(b[:-1], b[1:])):
+        assert O.zns_window(z["hap"], s, e, True) == pytest.approx(z["zns_proj"][k], rel=1e-12)
+        assert O.zns_window(z["hap"], s, e, False) == pytest.approx(z["zns_naive"][k], rel=1e-12)
