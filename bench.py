@@ -423,6 +423,136 @@ def run_reference(args, pool, cores):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------------------
+# secondary workloads (measurement of the other paths; not the headline line)
+# --------------------------------------------------------------------------
+def _copying_panel(gen, H, M, F, switch, flip, missing, device):
+    import torch
+    p = torch.distributions.Beta(0.3, 0.3).sample((M,)).to(device)
+    founders = (torch.rand((F, M), generator=gen, device=device) < p).to(torch.int8)
+    sw = torch.rand((H, M), generator=gen, device=device) < switch
+    seg = torch.cumsum(sw, dim=1, dtype=torch.int32)
+    choice = torch.randint(0, F, (H, int(seg.max()) + 1), generator=gen, device=device)
+    hap = torch.gather(founders, 0, torch.gather(choice, 1, seg.to(torch.int64)))
+    hap ^= (torch.rand((H, M), generator=gen, device=device) < flip).to(torch.int8)
+    if missing:
+        hap[torch.rand((H, M), generator=gen, device=device) < missing] = -1
+    return hap
+
+
+def run_windows(args):
+    """Batched uneven windows: 400 haplotypes, 512 windows of log-uniform
+    500..20,000 SNPs (own seed each), every within-window pair; one launch over
+    all windows against one launch per window."""
+    import torch
+    from pg_gpu_gb300 import _ops
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(20261504)
+    sizes = np.exp(rng.uniform(np.log(500), np.log(20_000), 512)).astype(np.int64)
+    torch.manual_seed(20261504)
+    parts = []
+    for w, m in enumerate(sizes):
+        g = torch.Generator(device=dev)
+        g.manual_seed(20261504 + w)
+        parts.append(_copying_panel(g, 400, int(m), 20, 1e-3, 1e-3, 0.0, dev))
+    panel = torch.cat(parts, 1).contiguous()
+    del parts
+    ends = np.cumsum(sizes)
+    begins = ends - sizes
+    n_pairs = int((sizes * (sizes - 1) // 2).sum())
+    pk = _ops.pack(panel)
+    wb = torch.as_tensor(begins, device=dev)
+    we = torch.as_tensor(ends, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
+
+    def one():
+        return _ops.window_sums(pk, None, wb, we)
+
+    def per_window():
+        for w in range(len(sizes)):
+            _ops.window_sums(pk, None, wb[w:w + 1], we[w:w + 1])
+
+    def timeit(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for s in range(steps):
+            flush.fill_(s & 0x7F)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ms.append((time.perf_counter() - t) * 1e3)
+        return float(np.mean(ms))
+
+    t_one = timeit(one, args.steps)
+    t_per = timeit(per_window, max(1, args.steps // 2))
+    sums, cnt = one()
+    assert int(cnt[:, 0].sum()) == n_pairs
+    print(json.dumps({
+        "metric": "within-window SNP-pairs/s, 512 uneven windows, 400 haplotypes",
+        "value": n_pairs / (t_one / 1e3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_one, "higher_is_better": True,
+        "dtype": "u32", "data": "synthetic (copying model, seed per window)",
+        "config": {"workload": "windows512", "haplotypes": 400, "windows": 512,
+                   "n_snp": int(sizes.sum()), "pairs": n_pairs, "form": "plain"},
+        "per_window_launches": {"ms_per_step": t_per, "value": n_pairs / (t_per / 1e3),
+                                "ratio_one_launch_over_per_window": t_per / t_one}}), flush=True)
+
+
+def run_geno_band(args):
+    """Unphased genotype LD: 1,000 diploids x 500,000 SNPs over 50 Mb (dosage =
+    sum of two copying-model haplotypes, 60 founders, switch 5e-4, 3 % missing);
+    per-pair 9-way counts, Rogers-Huff r^2 and DD / Dz / pi2 for every pair
+    within 200 kb."""
+    import torch
+    from pg_gpu_gb300 import _ops
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(20261505)
+    M = args.geno_snps
+    hap = _copying_panel(g, 2000, M, 60, 5e-4, 1e-3, 0.0, dev)
+    geno = (hap[0::2] + hap[1::2]).to(torch.int8)
+    del hap
+    geno[torch.rand(geno.shape, generator=g, device=dev) < 0.03] = -1
+    rng = np.random.default_rng(20261505)
+    pos = np.sort(rng.choice(int(50_000_000 * M / 500_000), M, replace=False)).astype(np.int64)
+    pos_d = _ops.positions_f64(pos)
+    _, n_pairs = _ops.band_offsets(pos_d, 200_000)
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
+
+    def step():
+        pk = _ops.pack_geno(geno)
+        return _ops.geno_band_pairs(pk, pos_d, 200_000, with_counts=args.geno_counts)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = []
+    for s in range(args.steps):
+        flush.fill_(s & 0x7F)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        out = step()
+        b.record()
+        ev.append((a, b))
+        del out
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    print(json.dumps({
+        "metric": "genotype LD SNP-pairs/s (counts9 + RH r^2 + DD/Dz/pi2 per pair)",
+        "value": n_pairs / (ms / 1e3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "u32",
+        "data": "synthetic (copying-model dosages, 3 % missing)",
+        "config": {"workload": "geno_band", "individuals": 1000, "n_snp": M,
+                   "max_dist_bp": 200_000, "pairs": n_pairs,
+                   "per_pair_bytes_written": (36 if args.geno_counts else 0) + 4 + 16}}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -431,7 +561,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="tc", choices=["plain", "tc"])
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other form")
-    ap.add_argument("--workload", default="binned2pop", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="binned2pop",
+                    choices=sorted(WORKLOADS) + ["windows512", "geno_band"])
+    ap.add_argument("--geno-snps", type=int, default=500_000)
+    ap.add_argument("--geno-counts", action="store_true", help="also write the 9-way counts")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-pairs-per-worker", type=int, default=400_000)
     args = ap.parse_args()
@@ -439,11 +572,17 @@ def main():
     cores = host_cores()
     # the oracle's process pool starts before the first GPU call (spawn)
     pool = None
+    if args.workload in ("windows512", "geno_band"):
+        args.no_cpu = True
     if rank == 0 and (args.impl == "reference" or not args.no_cpu):
         pool = make_pool(cores)
     try:
         if args.impl == "reference":
             run_reference(args, pool, cores)
+        elif args.workload == "windows512":
+            run_windows(args)
+        elif args.workload == "geno_band":
+            run_geno_band(args)
         else:
             run_gpu(args, pool, cores)
     finally:
