@@ -553,6 +553,56 @@ def run_geno_band(args):
           flush=True)
 
 
+def run_hap_band(args):
+    """Haplotype LD with missing data, per-pair outputs: 2,000 haplotypes x
+    100,000 SNPs over 10 Mb (50 founders, switch 5e-4, 2 % missing), every pair
+    within 100 kb: int32 counts, n and float32 r^2 / DD / Dz / pi2 per pair;
+    the tensor-core form against the plain popcount form."""
+    import torch
+    from pg_gpu_gb300 import _ops
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(20261502)
+    M = 100_000
+    hap = _copying_panel(g, 2000, M, 50, 5e-4, 1e-3, 0.02, dev)
+    rng = np.random.default_rng(20261502)
+    pos = np.sort(rng.choice(10_000_000, M, replace=False)).astype(np.int64)
+    pos_d = _ops.positions_f64(pos)
+    _, n_pairs = _ops.band_offsets(pos_d, 100_000)
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
+    res = {}
+    for form in ("tc", "plain"):
+        def step():
+            pk = _ops.pack(hap)
+            return _ops.band_pairs(pk, pos_d, 100_000, form=form)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        ev = []
+        for s_ in range(args.steps):
+            flush.fill_(s_ & 0x7F)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            out = step()
+            b.record()
+            ev.append((a, b))
+            del out
+        torch.cuda.synchronize()
+        res[form] = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    print(json.dumps({
+        "metric": "haplotype LD SNP-pairs/s with per-pair outputs (counts, n, r^2, DD, Dz, pi2)",
+        "value": n_pairs / (res["tc"] / 1e3), "unit": "pairs/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["tc"],
+        "higher_is_better": True, "dtype": "e4m3",
+        "data": "synthetic (copying model, 2 % missing)",
+        "config": {"workload": "hap_band", "haplotypes": 2000, "n_snp": M,
+                   "max_dist_bp": 100_000, "pairs": n_pairs, "per_pair_bytes_written": 36},
+        "compare": {"form": "plain", "ms_per_step": res["plain"],
+                    "value": n_pairs / (res["plain"] / 1e3),
+                    "ratio_tc_over_plain": res["plain"] / res["tc"]}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -562,7 +612,7 @@ def main():
     ap.add_argument("--form", default="tc", choices=["plain", "tc"])
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other form")
     ap.add_argument("--workload", default="binned2pop",
-                    choices=sorted(WORKLOADS) + ["windows512", "geno_band"])
+                    choices=sorted(WORKLOADS) + ["windows512", "geno_band", "hap_band"])
     ap.add_argument("--geno-snps", type=int, default=500_000)
     ap.add_argument("--geno-counts", action="store_true", help="also write the 9-way counts")
     ap.add_argument("--no-cpu", action="store_true")
@@ -572,7 +622,7 @@ def main():
     cores = host_cores()
     # the oracle's process pool starts before the first GPU call (spawn)
     pool = None
-    if args.workload in ("windows512", "geno_band"):
+    if args.workload in ("windows512", "geno_band", "hap_band"):
         args.no_cpu = True
     if rank == 0 and (args.impl == "reference" or not args.no_cpu):
         pool = make_pool(cores)
@@ -583,6 +633,8 @@ def main():
             run_windows(args)
         elif args.workload == "geno_band":
             run_geno_band(args)
+        elif args.workload == "hap_band":
+            run_hap_band(args)
         else:
             run_gpu(args, pool, cores)
     finally:

@@ -203,12 +203,15 @@ def positions_f64(positions):
     return L.as_device(positions, np.float64)
 
 
-def band_pairs(pk, pos_d, max_dist, with_stats=True):
+def band_pairs(pk, pos_d, max_dist, with_stats=True, form="auto"):
     """Fused per-pair outputs of one population over the distance band.
 
     Returns (counts (N,4) int32, n_valid (N,) int32, stats (N,4) float32 =
-    r^2, DD, Dz, pi2 or None).
+    r^2, DD, Dz, pi2 or None).  form: "tc" (tcgen05 tensor cores), "plain"
+    (AND + popcount) or "auto" (tensor cores whenever they apply).
     """
+    if form == "auto":
+        form = "tc" if tc_applies([pk]) else "plain"
     torch = _torch()
     _, n = band_offsets(pos_d, max_dist)
     dev = pos_d.device
@@ -218,7 +221,8 @@ def band_pairs(pk, pos_d, max_dist, with_stats=True):
     h = L.handle()
     L.check(L.lib().pgld_hap_band_pairs(h, ctypes.byref(panel([pk])), L.ptr(pos_d),
                                         float(max_dist), L.ptr(counts), L.ptr(nv), L.ptr(st), n,
-                                        L.FORM_PLAIN, L.stream_ptr()), h)
+                                        L.FORM_TC if form == "tc" else L.FORM_PLAIN,
+                                        L.stream_ptr()), h)
     return counts, nv, st
 
 

@@ -187,6 +187,8 @@ __global__ void __launch_bounds__(kThreads) band_plain_kernel(BandArgs a) {
         pc[p] = make_pop(c[p][q][0], c[p][q][1], c[p][q][2], c[p][q][3], n);
       }
       if (MODE == kModePairs) {
+        // rows come from the band offsets: write exactly the pairs they list
+        if (i < j && j < a.n_snp) ok = (j - i - 1) < (a.pair_off[i + 1] - a.pair_off[i]);
         if (ok) {
           const i64 k = a.pair_off[i] + (j - i - 1);
           int4 cc = make_int4(c[0][q][0], c[0][q][1], c[0][q][2], c[0][q][3]);
@@ -313,6 +315,8 @@ static void fill_panel(pgld::BandArgs& a, const pgld_hap_panel* panel) {
 int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel);
 int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
                    cudaStream_t st);
+int pgld_tc_pairs(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
+                  cudaStream_t st);
 
 extern "C" int pgld_hap_band_pairs(pgld_handle h, const pgld_hap_panel* panel, const double* pos,
                                    double max_dist, int32_t* counts, int32_t* n_valid,
@@ -321,7 +325,10 @@ extern "C" int pgld_hap_band_pairs(pgld_handle h, const pgld_hap_panel* panel, c
   int rc = check_panel(h, panel, "pgld_hap_band_pairs");
   if (rc) return rc;
   PGLD_REQUIRE(h, panel->n_pops == 1, "pgld_hap_band_pairs: one population per call");
-  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN, "pgld_hap_band_pairs: only the plain form");
+  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC, "pgld_hap_band_pairs: form");
+  if (form == PGLD_FORM_TC && !pgld_tc_supported(h, panel))
+    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "pgld_hap_band_pairs: tensor-core form needs "
+                     "<= 2048 haplotypes and no separate validity plane");
   PGLD_REQUIRE(h, max_dist >= 0, "pgld_hap_band_pairs: negative max_dist");
   PGLD_REQUIRE(h, n_pairs >= 0, "pgld_hap_band_pairs: n_pairs < 0");
   const i64 n = panel->n_snp;
@@ -366,6 +373,7 @@ extern "C" int pgld_hap_band_pairs(pgld_handle h, const pgld_hap_panel* panel, c
   a.counts = counts;
   a.nvalid = n_valid;
   a.stats = stats;
+  if (form == PGLD_FORM_TC) return pgld_tc_pairs(h, panel, a, st);
   return pgld::launch_band_plain(h, a, pgld::kModePairs, st);
 }
 

@@ -265,6 +265,8 @@ __global__ void __launch_bounds__(kThreads) band_fast_kernel(BandArgs a) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) cq[p][k] = c[p][q][k];
       if (MODE == kModePairs) {
+        // rows come from the band offsets: write exactly the pairs they list
+        if (i < j && j < a.n_snp) ok = (j - i - 1) < (a.pair_off[i + 1] - a.pair_off[i]);
         if (ok) {
           const long long k = a.pair_off[i] + (j - i - 1);
           reinterpret_cast<int4*>(a.counts)[k] = make_int4(cq[0][0], cq[0][1], cq[0][2], cq[0][3]);

@@ -441,6 +441,8 @@ __global__ void __launch_bounds__(kThreads) geno_band_kernel(BandArgs a) {
         cp[p] = cc[p];
       }
       if (MODE == kModePairs) {
+        // rows come from the band offsets: write exactly the pairs they list
+        if (i < j && j < a.n_snp) ok = (j - i - 1) < (a.pair_off[i + 1] - a.pair_off[i]);
         if (ok) {
           const i64 k = a.pair_off[i] + (j - i - 1);
           if (a.counts) {

@@ -67,6 +67,11 @@ struct Params {
   int nmax;  // largest per-population sample size (reciprocal table length - 1)
   const int* ipos;     // integer positions (valid when *ipos_bad == 0)
   const int* ipos_bad;
+  // per-pair outputs (pairs mode, one population)
+  const long long* pair_off;  // [n_snp + 1] first output row of each anchor SNP
+  int32_t* counts;            // [n_pairs][4]
+  int32_t* nvalid;            // [n_pairs] or NULL
+  float* stats;               // [n_pairs][4] r^2, DD, Dz, pi2, or NULL
 };
 
 // ---------------------------------------------------------------------------
@@ -223,7 +228,9 @@ __device__ __forceinline__ float warp_totals_pick(const float (&v)[S], int lane)
   return mine;
 }
 
-template <int P>
+// MODE kModeBinned: distance-binned moments sums of P populations;
+// kModePairs: per-pair counts / n / (r^2, DD, Dz, pi2) of one population
+template <int P, int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     band_tc_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                    Params a) {
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x <= a.nmax; x += kEpiThreads)
       fast::recip_entry(x, tables + x, tables + (a.nmax + 1) + x, tables + 2 * (a.nmax + 1) + x,
                         tables + 3 * (a.nmax + 1) + x);
-    for (int x = t; x <= n_bins; x += kEpiThreads) {
+    for (int x = t; MODE == kModeBinned && x <= n_bins; x += kEpiThreads) {
       const double b = a.bins[x];
       sbins[x] = b;
       const double cb = ceil(b);
@@ -424,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
       // classify the warp's sub-tile: 0 one bin, 1 two adjacent bins, 2 general
       int mode = 2, b0 = -1, thr_mid = 0;
-      if (use_int && bj > bi && sj0 + 31 < a.n_snp) {
+      if (MODE == kModeBinned && use_int && bj > bi && sj0 + 31 < a.n_snp) {
         const int dmin = a.ipos[sj0] - a.ipos[si0 + 15];
         const int dmax = a.ipos[sj0 + 31] - a.ipos[si0];
         if (dmax <= maxd_int) {
@@ -451,8 +458,55 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       tc_fence_after();
 
-      // bin accumulators of the warp's sub-tile, two lanes per statistic
-      // (the float2 halves hold the even / odd pairs of each thread)
+      if constexpr (MODE == kModePairs) {
+        // per-pair outputs: each lane owns whole pairs (i, j) after the C / Z
+        // exchange; rows k = pair_off[i] + (j - i - 1) in the reference's order
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+          uint32_t r[16];
+          const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
+          tmem_ld16(tmem_base + lane_base + col, r);
+          tmem_wait_ld();
+          if (c == 3) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const uint32_t s0 = plane ? r[4 * q] : r[4 * q + 2];
+            const uint32_t s1 = plane ? r[4 * q + 1] : r[4 * q + 3];
+            const float g0 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
+            const float g1 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
+            const float m0 = __uint_as_float(plane ? r[4 * q + 2] : r[4 * q]);
+            const float m1 = __uint_as_float(plane ? r[4 * q + 3] : r[4 * q + 1]);
+            const float c1 = plane ? g0 : m0, c2 = plane ? g1 : m1;
+            const float c3 = plane ? m0 : g0, c4 = plane ? m1 : g1;
+            const long long j = j0 + half * 32 + c * 8 + 2 * q + plane;
+            // the pair's row comes from the band offsets themselves, so a pair
+            // is written exactly when the offsets list it
+            bool ok = (i < j) && (j < a.n_snp);
+            if (ok) ok = (j - i - 1) < (a.pair_off[i + 1] - a.pair_off[i]);
+            if (ok) {
+              const long long k = a.pair_off[i] + (j - i - 1);
+              const fast::Pop p = fast::make(c1, c2, c3, c4);
+              reinterpret_cast<int4*>(a.counts)[k] =
+                  make_int4(fast::f2i_small(c1), fast::f2i_small(c2), fast::f2i_small(c3),
+                            fast::f2i_small(c4));
+              if (a.nvalid) a.nvalid[k] = p.n;
+              if (a.stats) {
+                const float r4 = T.r4[p.n];
+                reinterpret_cast<float4*>(a.stats)[k] =
+                    make_float4(fast::r2_of(p), fast::dd_num(p) * r4, fast::dz_num(p) * r4,
+                                fast::pi2_num(p) * r4);
+              }
+            }
+          }
+        }
+        continue;
+      }
+
+      // bin accumulators of the warp's sub-tile
       float acc_lo[S], acc_hi[S];
 #pragma unroll
       for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
@@ -690,14 +744,18 @@ int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel) {
   return 1;
 }
 
-int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
-                   cudaStream_t st) {
+// the tensor-core band kernel in binned (mode kModeBinned) or per-pair
+// (kModePairs, one population) mode; a carries the band, bins or outputs
+static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a, int mode,
+                     cudaStream_t st) {
   using namespace pgld::tc;
   int rc = get_encode(h);
   if (rc) return rc;
   const long long n = panel->n_snp;
   const int P = panel->n_pops;
   const int S = P == 1 ? 3 : 15;
+  if (mode == pgld::kModePairs && P != 1)
+    return pgld_fail(h, PGLD_ERR_INVALID_ARG, "tensor-core pairs form: one population");
   const long long nb = (n + kTileSnp - 1) / kTileSnp;
   if (2 * (nb * kTileSnp) > 2147483647LL)
     return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: too many SNPs");
@@ -707,15 +765,24 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
     k_pad[p] = ((panel->n_words[p] * 32 + kKChunk - 1) / kKChunk) * kKChunk;
     op_bytes[p] = (size_t)2 * n * k_pad[p];
   }
-  const size_t sb = pgld::scan_scratch_bytes(nb);
+  // the scan scratch serves both the tile list and (pairs mode) the per-SNP
+  // pair offsets; the offsets live in this call's own workspace layout, since
+  // pgld_workspace may move the workspace (a caller's copy would be stale)
+  const size_t sb = pgld::scan_scratch_bytes(std::max<long long>(nb, n));
   auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
   const size_t off_items = 0, off_scan = al((nb + 1) * 8), off_op0 = off_scan + al(sb),
                off_op1 = off_op0 + al(op_bytes[0]), off_ipos = off_op1 + al(op_bytes[1]),
-               off_bad = off_ipos + al((size_t)n * 4);
+               off_bad = off_ipos + al((size_t)n * 4), off_poff = off_bad + 1024,
+               total = off_poff + (mode == pgld::kModePairs ? al((size_t)(n + 1) * 8) : 0);
   void* ws = nullptr;
-  rc = pgld_workspace(h, off_bad + 1024, &ws);
+  rc = pgld_workspace(h, total, &ws);
   if (rc) return rc;
   char* w = (char*)ws;
+  long long* poff = mode == pgld::kModePairs ? (long long*)(w + off_poff) : nullptr;
+  if (poff) {
+    rc = pgld_band_offsets(h, a.pos, n, a.max_dist, poff, w + off_scan, sb, st);
+    if (rc) return rc;
+  }
   long long* items = (long long*)(w + off_items);
   unsigned char* ops[2] = {(unsigned char*)(w + off_op0), (unsigned char*)(w + off_op1)};
 
@@ -764,6 +831,10 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
   prm.status = h->dev_status;
   prm.ipos = ipos;
   prm.ipos_bad = ipos_bad;
+  prm.pair_off = poff;
+  prm.counts = a.counts;
+  prm.nvalid = a.nvalid;
+  prm.stats = a.stats;
   prm.nmax = 0;
   for (int p = 0; p < P; ++p) prm.nmax = std::max(prm.nmax, 32 * panel->n_words[p]);
 
@@ -776,11 +847,23 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
   if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: shared memory");
   prm.stages = stages;
   const size_t smem = (size_t)stages * kStageBytes + fixed;
-  auto kern = P == 1 ? band_tc_kernel<1> : band_tc_kernel<2>;
+  auto kern = mode == pgld::kModePairs
+                  ? band_tc_kernel<1, pgld::kModePairs>
+                  : (P == 1 ? band_tc_kernel<1, pgld::kModeBinned> : band_tc_kernel<2, pgld::kModeBinned>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc smem attribute");
   kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(maps[0], maps[1], prm);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc_kernel");
   return PGLD_OK;
+}
+
+int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
+                   cudaStream_t st) {
+  return tc_launch(h, panel, a, pgld::kModeBinned, st);
+}
+
+int pgld_tc_pairs(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
+                  cudaStream_t st) {
+  return tc_launch(h, panel, a, pgld::kModePairs, st);
 }

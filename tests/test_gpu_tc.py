@@ -90,3 +90,30 @@ def test_tc_genetic_distance_and_fractional_positions():
     rows = [np.arange(48), np.arange(48, 96)]
     check(hap, pos, rows, np.array([0.0, 1e-4, 3e-4, 1e-3]), max_dist=60_000, bin_coord=gmap)
     check(hap, pos, rows, np.logspace(2, 4.7, 9))
+
+
+@pytest.mark.parametrize("H,M", [(2000, 600), (130, 700), (33, 257)])
+def test_tc_band_pairs_match_oracle(H, M):
+    # per-pair counts, n and float32 r^2 / DD / Dz / pi2 of the tensor-core
+    # form: counts bit-exact, statistics within 1e-6 of the float64 oracle,
+    # and equal to the plain form's output
+    rng = np.random.default_rng(H + M)
+    hap = (rng.random((H, M)) < rng.beta(0.3, 0.3, M)).astype(np.int8)
+    hap[rng.random(hap.shape) < 0.02] = -1
+    pos = np.sort(rng.choice(200_000, M, replace=False)).astype(np.int64)
+    pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
+    pos_d = _ops.positions_f64(pos)
+    c_tc, nv_tc, st_tc = _ops.band_pairs(pk, pos_d, 20_000, form="tc")
+    c_pl, nv_pl, st_pl = _ops.band_pairs(pk, pos_d, 20_000, form="plain")
+    ii, jj = O.pairs_within_distance(pos, 20_000)
+    rc, rnv = O.counts_for_pairs(hap, ii, jj)
+    assert np.array_equal(c_tc.cpu().numpy(), rc) and np.array_equal(nv_tc.cpu().numpy(), rnv)
+    assert np.array_equal(c_pl.cpu().numpy(), rc)
+    st = st_tc.cpu().numpy().astype(np.float64)
+    ref = np.stack([O.r_squared(rc, rnv), O.dd(rc, None, rnv), O.dz(rc, None, rnv),
+                    O.pi2(rc, None, rnv)], axis=1)
+    assert np.array_equal(np.isnan(st), np.isnan(ref))
+    m = ~np.isnan(ref) & (np.abs(ref) > 1e-30)
+    assert (np.abs(st[m] - ref[m]) / np.abs(ref[m])).max() <= 1e-6
+    z = ref == 0
+    assert np.all(st[z] == 0)
