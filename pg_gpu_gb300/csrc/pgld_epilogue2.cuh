@@ -31,8 +31,10 @@ PGLD_HD V vmul(V a, V b) { return make_float2(a.x * b.x, a.y * b.y); }
 PGLD_HD V vfma(V a, V b, V c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)); }
 #endif
 PGLD_HD V vneg(V a) { return make_float2(-a.x, -a.y); }
-PGLD_HD V vsub(V a, V b) { return vadd(a, vneg(b)); }
 PGLD_HD V vs(float a) { return make_float2(a, a); }
+// a - b as one fused operation: b * (-1) is exact, so the sum rounds once,
+// exactly like a correctly rounded subtraction
+PGLD_HD V vsub(V a, V b) { return vfma(b, vs(-1.0f), a); }
 
 struct X2 {
   V s, e;
