@@ -526,7 +526,9 @@ def run_geno_band(args):
 
     def step():
         pk = _ops.pack_geno(geno)
-        return _ops.geno_band_pairs(pk, pos_d, 200_000, with_counts=args.geno_counts)
+        # the workload's outputs: genotype DD and Rogers-Huff r^2 per pair
+        return _ops.geno_band_pairs(pk, pos_d, 200_000, with_counts=args.geno_counts,
+                                    columns=("r2", "dd"))
 
     for _ in range(args.warmup):
         step()
@@ -543,7 +545,7 @@ def run_geno_band(args):
     torch.cuda.synchronize()
     ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
     print(json.dumps({
-        "metric": "genotype LD SNP-pairs/s (counts9 + RH r^2 + DD/Dz/pi2 per pair)",
+        "metric": "genotype LD SNP-pairs/s (n, Rogers-Huff r^2 and genotype DD per pair)",
         "value": n_pairs / (ms / 1e3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "u32",
         "data": "synthetic (copying-model dosages, 3 % missing)",

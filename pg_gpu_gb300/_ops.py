@@ -420,11 +420,21 @@ def geno_spec_terms(P):
     return [(t.stat, t.kind, tuple(t.pops), t.weight) for t in arr], n_stats.value
 
 
-def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True):
+GENO_BAND_COLUMNS = ("r2", "dd", "dz", "pi2")
+
+
+def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True,
+                    columns=GENO_BAND_COLUMNS):
     """Fused per-pair genotype outputs over the distance band.
 
     Returns (counts (N,9) int32 or None, n_valid (N,) int32, stats (N,4)
-    float32 = Rogers-Huff r^2, DD, Dz, pi2 or None)."""
+    float32 = Rogers-Huff r^2, DD, Dz, pi2 or None); only the named columns
+    are evaluated, the others hold 0."""
+    mask = 0
+    for c in columns:
+        if c not in GENO_BAND_COLUMNS:
+            raise ValueError(f"unknown column {c!r}")
+        mask |= 1 << GENO_BAND_COLUMNS.index(c)
     torch = _torch()
     _, n = band_offsets(pos_d, max_dist)
     dev = pos_d.device
@@ -433,8 +443,8 @@ def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True):
     st = torch.empty((n, 4), dtype=torch.float32, device=dev) if with_stats else None
     h = L.handle()
     L.check(L.lib().pgld_geno_band_pairs(h, ctypes.byref(geno_panel([pk])), L.ptr(pos_d),
-                                         float(max_dist), L.ptr(counts), L.ptr(nv), L.ptr(st), n,
-                                         L.stream_ptr()), h)
+                                         float(max_dist), L.ptr(counts), L.ptr(nv), L.ptr(st),
+                                         mask, n, L.stream_ptr()), h)
     return counts, nv, st
 
 

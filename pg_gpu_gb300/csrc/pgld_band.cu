@@ -198,13 +198,13 @@ __global__ void __launch_bounds__(kThreads) band_plain_kernel(BandArgs a) {
             const PopC& p0 = pc[0];
             float r2;
             i64 rd = r_den(p0);
-            r2 = rd > 0 ? __ll2float_rn(p0.x * p0.x) / __ll2float_rn(rd) : __int_as_float(0x7fc00000);
+            r2 = rd > 0 ? ll2f(p0.x * p0.x) / ll2f(rd) : __int_as_float(0x7fc00000);
             ND v1 = dd_ii(p0), v2 = dz_iii(p0), v3 = pi2_iiii(p0);
             float4 o;
             o.x = r2;
-            o.y = v1.den > 0 ? __ll2float_rn(v1.num) / __ll2float_rn(v1.den) : 0.f;
-            o.z = v2.den > 0 ? __ll2float_rn(v2.num) / __ll2float_rn(v2.den) : 0.f;
-            o.w = v3.den > 0 ? __ll2float_rn(v3.num) / __ll2float_rn(v3.den) : 0.f;
+            o.y = v1.den > 0 ? ll2f(v1.num) / ll2f(v1.den) : 0.f;
+            o.z = v2.den > 0 ? ll2f(v2.num) / ll2f(v2.den) : 0.f;
+            o.w = v3.den > 0 ? ll2f(v3.num) / ll2f(v3.den) : 0.f;
             reinterpret_cast<float4*>(a.stats)[k] = o;
           }
         }

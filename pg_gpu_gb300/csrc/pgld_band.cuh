@@ -42,6 +42,7 @@ struct BandArgs {
   float* stats;
   int32_t* status;  // device error word of the handle
   int nmax;         // largest per-population sample size (32 * max words)
+  int stat_mask;    // genotype pairs mode: columns to compute (bit k = column k)
 };
 
 // tile work list of `tile`-SNP blocks: items[b] = tiles of row block b, then

@@ -171,7 +171,7 @@ __device__ __forceinline__ double gv_f64(const GV& v) {
 }
 __device__ __forceinline__ float gv_f32(const GV& v) {
   if (v.gated && !v.ok) return 0.f;
-  return __ll2float_rn(v.num) / __ll2float_rn(v.den);
+  return ll2f(v.num) / ll2f(v.den);
 }
 
 // r or r^2 of Rogers-Huff, NaN where a SNP has no variance among the valid
@@ -186,7 +186,7 @@ __device__ __forceinline__ float rh2_f32(const int* c) {
   const RH m = rh_moments(c);
   const i64 den = m.vi * m.vj;
   if (den <= 0) return __int_as_float(0x7fc00000);
-  return __ll2float_rn(m.cov * m.cov) / __ll2float_rn(den);
+  return ll2f(m.cov * m.cov) / ll2f(den);
 }
 
 template <typename T>
@@ -195,7 +195,7 @@ __device__ __forceinline__ T term_value(const pgld_term& tm, const GPop* P, cons
     const GV v = sigma_d2(P[tm.pops[0]]);
     if (!v.ok) return (T)__longlong_as_double(0x7ff8000000000000ll);
     return sizeof(T) == 8 ? (T)(__ll2double_rn(v.num) / __ll2double_rn(v.den))
-                          : (T)(__ll2float_rn(v.num) / __ll2float_rn(v.den));
+                          : (T)(ll2f(v.num) / ll2f(v.den));
   }
   if (tm.kind == PGLD_G_RH_R || tm.kind == PGLD_G_RH_R2) {
     if (sizeof(T) == 4 && tm.kind == PGLD_G_RH_R2) return (T)rh2_f32(cc[tm.pops[0]]);
@@ -452,11 +452,13 @@ __global__ void __launch_bounds__(kThreads) geno_band_kernel(BandArgs a) {
           }
           if (a.nvalid) a.nvalid[k] = (int32_t)P[0].n;
           if (a.stats) {
-            float4 o;
-            o.x = rh2_f32(cc[0]);
-            o.y = gv_f32(dd_single(P[0]));
-            o.z = gv_f32(dz_single(P[0]));
-            o.w = gv_f32(pi2_single(P[0]));
+            // only the requested columns are evaluated (the polynomials are
+            // the bulk of the per-pair work); the others are written as 0
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (a.stat_mask & 1) o.x = rh2_f32(cc[0]);
+            if (a.stat_mask & 2) o.y = gv_f32(dd_single(P[0]));
+            if (a.stat_mask & 4) o.z = gv_f32(dz_single(P[0]));
+            if (a.stat_mask & 8) o.w = gv_f32(pi2_single(P[0]));
             reinterpret_cast<float4*>(a.stats)[k] = o;
           }
         }
@@ -684,7 +686,8 @@ static void fill_geno_panel(pgld::BandArgs& a, const pgld_geno_panel* panel) {
 
 extern "C" int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel, const double* pos,
                                     double max_dist, int32_t* counts, int32_t* n_valid,
-                                    float* stats, int64_t n_pairs, void* stream) {
+                                    float* stats, int32_t stat_mask, int64_t n_pairs,
+                                    void* stream) {
   PGLD_REQUIRE(h, h != nullptr, "pgld_geno_band_pairs: NULL handle");
   int rc = check_geno_panel(h, panel, "pgld_geno_band_pairs");
   if (rc) return rc;
@@ -700,6 +703,7 @@ extern "C" int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel,
   PGLD_REQUIRE(h, pos != nullptr, "pgld_geno_band_pairs: NULL pos");
   PGLD_REQUIRE(h, !stats || ((uintptr_t)stats & 15) == 0,
                "pgld_geno_band_pairs: stats must be 16-byte aligned");
+  PGLD_REQUIRE(h, (stat_mask & ~15) == 0, "pgld_geno_band_pairs: stat_mask %d", stat_mask);
   PGLD_CHECK_CUDA(h, cudaSetDevice(h->device));
   cudaStream_t st = (cudaStream_t)stream;
   const i64 nb = (n + pgld::geno::kT - 1) / pgld::geno::kT;
@@ -735,6 +739,7 @@ extern "C" int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel,
   a.counts = counts;
   a.nvalid = n_valid;
   a.stats = stats;
+  a.stat_mask = stat_mask;
   return pgld::geno::launch_geno_band<pgld::kModePairs, 1>(h, a, st);
 }
 

@@ -138,6 +138,12 @@ def test_band_pairs_fp32_outputs():
     m = ~np.isnan(ref) & (np.abs(ref) > 1e-30)
     rel = np.abs(st[m] - ref[m]) / np.abs(ref[m])
     assert rel.max() <= 1e-6, rel.max()
+    # a column subset evaluates only those columns, bit-identical
+    _, _, st2 = _ops.geno_band_pairs(pk, _ops.positions_f64(pos), 200_000, with_counts=False,
+                                     columns=("r2", "dd"))
+    st2 = np_(st2).astype(np.float64)
+    assert np.array_equal(st2[:, :2], st[:, :2], equal_nan=True)
+    assert np.all(st2[:, 2:] == 0)
 
 
 @pytest.mark.parametrize("P", [2, 3])
