@@ -523,36 +523,40 @@ def run_geno_band(args):
     pos_d = _ops.positions_f64(pos)
     _, n_pairs = _ops.band_offsets(pos_d, 200_000)
     flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
+    res = {}
+    for form in ("tc", "plain"):
+        def step():
+            pk = _ops.pack_geno(geno)
+            # the workload's outputs: genotype DD and Rogers-Huff r^2 per pair
+            return _ops.geno_band_pairs(pk, pos_d, 200_000, with_counts=args.geno_counts,
+                                        columns=("r2", "dd"), form=form)
 
-    def step():
-        pk = _ops.pack_geno(geno)
-        # the workload's outputs: genotype DD and Rogers-Huff r^2 per pair
-        return _ops.geno_band_pairs(pk, pos_d, 200_000, with_counts=args.geno_counts,
-                                    columns=("r2", "dd"))
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    ev = []
-    for s in range(args.steps):
-        flush.fill_(s & 0x7F)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        out = step()
-        b.record()
-        ev.append((a, b))
-        del out
-    torch.cuda.synchronize()
-    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        ev = []
+        for s_ in range(args.steps):
+            flush.fill_(s_ & 0x7F)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            out = step()
+            b.record()
+            ev.append((a, b))
+            del out
+        torch.cuda.synchronize()
+        res[form] = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    ms = res["tc"]
     print(json.dumps({
         "metric": "genotype LD SNP-pairs/s (n, Rogers-Huff r^2 and genotype DD per pair)",
         "value": n_pairs / (ms / 1e3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "u32",
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "e4m3",
         "data": "synthetic (copying-model dosages, 3 % missing)",
         "config": {"workload": "geno_band", "individuals": 1000, "n_snp": M,
-                   "max_dist_bp": 200_000, "pairs": n_pairs,
-                   "per_pair_bytes_written": (36 if args.geno_counts else 0) + 4 + 16}}),
-          flush=True)
+                   "max_dist_bp": 200_000, "pairs": n_pairs, "form": "tc",
+                   "per_pair_bytes_written": (36 if args.geno_counts else 0) + 4 + 16},
+        "compare": {"form": "plain", "ms_per_step": res["plain"],
+                    "value": n_pairs / (res["plain"] / 1e3),
+                    "ratio_tc_over_plain": res["plain"] / ms}}), flush=True)
 
 
 def run_hap_band(args):

@@ -292,12 +292,14 @@ int pgld_geno_stats(pgld_handle h, const pgld_pair_counts* counts, int64_t n_pai
  * (nullable) and stats [n_pairs][4] float32 = Rogers-Huff r^2 (pairwise-
  * complete), DD, Dz, pi2 (nullable; 16-byte aligned), of which only the
  * columns in stat_mask (bit k = column k) are evaluated, the others written
- * as 0.  n_pairs must equal pgld_count_pairs_within's result.  Fuses
+ * as 0.  n_pairs must equal pgld_count_pairs_within's result.  form
+ * PGLD_FORM_TC counts on the tensor cores (dosages 0/1/2 and missing only:
+ * no valid / ext planes), PGLD_FORM_PLAIN with AND + popcount.  Fuses
  * iter_pairs_within_distance + compute_genotype_counts_for_pairs + the
  * single-population genotype statistics + rogers_huff_r_squared. */
 int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel, const double* pos,
                          double max_dist, int32_t* counts, int32_t* n_valid, float* stats,
-                         int32_t stat_mask, int64_t n_pairs, void* stream);
+                         int32_t stat_mask, int64_t n_pairs, int32_t form, void* stream);
 
 /* Distance-binned sums of the moments genotype statistics of n_pops (1..4)
  * populations, arguments and bins as pgld_hap_binned_sums.  Replaces

@@ -98,7 +98,8 @@ _SIGS = {
                              ctypes.c_int),
     "pgld_geno_stats": ([_P, ctypes.POINTER(PairCounts), _I64, ctypes.POINTER(Term), _I32, _I32,
                          _P, _I32, _I64, _P], ctypes.c_int),
-    "pgld_geno_band_pairs": ([_P, ctypes.POINTER(GenoPanel), _P, _D, _P, _P, _P, _I32, _I64, _P],
+    "pgld_geno_band_pairs": ([_P, ctypes.POINTER(GenoPanel), _P, _D, _P, _P, _P, _I32, _I64, _I32,
+                              _P],
                              ctypes.c_int),
     "pgld_geno_binned_sums": ([_P, ctypes.POINTER(GenoPanel), _P, _D, _P, _P, _I32, _P, _P, _P],
                               ctypes.c_int),

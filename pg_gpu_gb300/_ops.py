@@ -424,12 +424,16 @@ GENO_BAND_COLUMNS = ("r2", "dd", "dz", "pi2")
 
 
 def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True,
-                    columns=GENO_BAND_COLUMNS):
+                    columns=GENO_BAND_COLUMNS, form="auto"):
     """Fused per-pair genotype outputs over the distance band.
 
     Returns (counts (N,9) int32 or None, n_valid (N,) int32, stats (N,4)
     float32 = Rogers-Huff r^2, DD, Dz, pi2 or None); only the named columns
-    are evaluated, the others hold 0."""
+    are evaluated, the others hold 0.  form: "tc" (tensor-core counts),
+    "plain" (AND + popcount) or "auto" (tensor cores unless a dosage above 2
+    needs the extra planes)."""
+    if form == "auto":
+        form = "plain" if pk.has_other else "tc"
     mask = 0
     for c in columns:
         if c not in GENO_BAND_COLUMNS:
@@ -444,7 +448,8 @@ def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True,
     h = L.handle()
     L.check(L.lib().pgld_geno_band_pairs(h, ctypes.byref(geno_panel([pk])), L.ptr(pos_d),
                                          float(max_dist), L.ptr(counts), L.ptr(nv), L.ptr(st),
-                                         mask, n, L.stream_ptr()), h)
+                                         mask, n, L.FORM_TC if form == "tc" else L.FORM_PLAIN,
+                                         L.stream_ptr()), h)
     return counts, nv, st
 
 

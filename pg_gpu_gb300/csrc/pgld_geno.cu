@@ -169,10 +169,6 @@ __device__ __forceinline__ double gv_f64(const GV& v) {
   if (v.gated && !v.ok) return 0.0;
   return __ll2double_rn(v.num) / __ll2double_rn(v.den);
 }
-__device__ __forceinline__ float gv_f32(const GV& v) {
-  if (v.gated && !v.ok) return 0.f;
-  return ll2f(v.num) / ll2f(v.den);
-}
 
 // r or r^2 of Rogers-Huff, NaN where a SNP has no variance among the valid
 __device__ __forceinline__ double rh_f64(const int* c, bool square) {
@@ -181,12 +177,6 @@ __device__ __forceinline__ double rh_f64(const int* c, bool square) {
   if (den <= 0) return __longlong_as_double(0x7ff8000000000000ll);
   if (square) return __ll2double_rn(m.cov * m.cov) / __ll2double_rn(den);
   return __ll2double_rn(m.cov) / sqrt(__ll2double_rn(den));
-}
-__device__ __forceinline__ float rh2_f32(const int* c) {
-  const RH m = rh_moments(c);
-  const i64 den = m.vi * m.vj;
-  if (den <= 0) return __int_as_float(0x7fc00000);
-  return ll2f(m.cov * m.cov) / ll2f(den);
 }
 
 template <typename T>
@@ -684,10 +674,14 @@ static void fill_geno_panel(pgld::BandArgs& a, const pgld_geno_panel* panel) {
   a.n_snp = panel->n_snp;
 }
 
+int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const double* pos,
+                       double max_dist, int32_t* counts, int32_t* n_valid, float* stats,
+                       int32_t stat_mask, cudaStream_t st);
+
 extern "C" int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel, const double* pos,
                                     double max_dist, int32_t* counts, int32_t* n_valid,
                                     float* stats, int32_t stat_mask, int64_t n_pairs,
-                                    void* stream) {
+                                    int32_t form, void* stream) {
   PGLD_REQUIRE(h, h != nullptr, "pgld_geno_band_pairs: NULL handle");
   int rc = check_geno_panel(h, panel, "pgld_geno_band_pairs");
   if (rc) return rc;
@@ -704,6 +698,10 @@ extern "C" int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel,
   PGLD_REQUIRE(h, !stats || ((uintptr_t)stats & 15) == 0,
                "pgld_geno_band_pairs: stats must be 16-byte aligned");
   PGLD_REQUIRE(h, (stat_mask & ~15) == 0, "pgld_geno_band_pairs: stat_mask %d", stat_mask);
+  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC, "pgld_geno_band_pairs: form");
+  if (form == PGLD_FORM_TC && (panel->ext[0] != nullptr || panel->valid[0] != nullptr))
+    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "pgld_geno_band_pairs: the tensor-core form "
+                     "takes dosages 0/1/2 only (missing allowed)");
   PGLD_CHECK_CUDA(h, cudaSetDevice(h->device));
   cudaStream_t st = (cudaStream_t)stream;
   const i64 nb = (n + pgld::geno::kT - 1) / pgld::geno::kT;
@@ -725,6 +723,8 @@ extern "C" int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel,
     return pgld_fail(h, PGLD_ERR_INVALID_ARG, "pgld_geno_band_pairs: n_pairs %lld != %lld in band",
                      (long long)n_pairs, (long long)tot);
   if (tot == 0) return PGLD_OK;
+  if (form == PGLD_FORM_TC)
+    return pgld_geno_tc_pairs(h, panel, pos, max_dist, counts, n_valid, stats, stat_mask, st);
   rc = pgld::band_schedule(h, pos, n, max_dist, items, scratch, std::max(sb1, sb2), st,
                            pgld::geno::kT);
   if (rc) return rc;

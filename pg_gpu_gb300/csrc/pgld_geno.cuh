@@ -226,5 +226,20 @@ __host__ __device__ __forceinline__ RH rh_moments(const int* c) {
   return {n * sij - si * sj, n * sii - si * si, n * sjj - sj * sj};
 }
 
+#ifdef __CUDACC__
+// float32 value of a statistic (at most five roundings: two per conversion)
+__device__ __forceinline__ float gv_f32(const GV& v) {
+  if (v.gated && !v.ok) return 0.f;
+  return ll2f(v.num) / ll2f(v.den);
+}
+// Rogers-Huff r^2 in float32, NaN where a SNP has no variance among the valid
+__device__ __forceinline__ float rh2_f32(const int* c) {
+  const RH m = rh_moments(c);
+  const i64 den = m.vi * m.vj;
+  if (den <= 0) return __int_as_float(0x7fc00000);
+  return ll2f(m.cov * m.cov) / ll2f(den);
+}
+#endif
+
 }  // namespace geno
 }  // namespace pgld

@@ -29,25 +29,17 @@
 #include "pgld_epilogue2.cuh"
 #include "pgld_internal.cuh"
 #include "pgld_scan.cuh"
+#include "pgld_tcgen05.cuh"
 
 namespace pgld {
 namespace tc {
 
 constexpr int kTileSnp = 64;
-constexpr int kRows = 128;          // 2 planes x 64 SNPs
-constexpr int kKChunk = 128;        // bytes (= E4M3 elements) of K per stage
-constexpr int kBoxBytes = kRows * kKChunk;  // 16 KB
-constexpr int kStageBytes = 2 * kBoxBytes;  // A + B
 constexpr int kEpiWarps = 8;
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kThreads = (4 + kEpiWarps) * 32;
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kOne = 0x38;     // E4M3 1.0
-constexpr long long kSpinLimit = 1ll << 26;
 
-// instruction descriptor: D f32, A/B E4M3, both K-major, N = 128, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((128u >> 3) << 17) |
-                            ((128u >> 4) << 24);
 
 struct Params {
   int n_pops;
@@ -74,101 +66,6 @@ struct Params {
   float* stats;               // [n_pairs][4] r^2, DD, Dz, pi2, or NULL
 };
 
-// ---------------------------------------------------------------------------
-// PTX wrappers
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: false once ~2 s of SM clock passed or another role aborted
-constexpr long long kWaitCycles = 4000000000ll;
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
-  const long long t0 = clock64();
-  for (long long k = 0; k < kSpinLimit; ++k) {
-    if (mbar_try(b, parity)) return true;
-    if ((k & 63) == 63 && (*abort_flag || clock64() - t0 > kWaitCycles)) return false;
-  }
-  return false;
-}
-// drain wait: bounded by time only
-__device__ __forceinline__ void mbar_wait_drain(uint64_t* b, uint32_t parity) {
-  const long long t0 = clock64();
-  for (long long k = 0; k < kSpinLimit; ++k) {
-    if (mbar_try(b, parity)) return;
-    if ((k & 63) == 63 && clock64() - t0 > kWaitCycles) return;
-  }
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x,
-                                            int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
-      : "memory");
-}
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  // K-major, 128-byte swizzle: SBO = 1024 B (8 rows x 128 B), LBO unused (1),
-  // descriptor version 1 (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63)
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFF);
-  d |= (uint64_t)1 << 16;
-  d |= (uint64_t)(1024 >> 4) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-__device__ __forceinline__ void mma_f8(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t accum) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accum)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-      "[%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -192,18 +89,6 @@ __device__ __forceinline__ int bin_of_f64(const double* sb, int n_bins, double d
     if (sb[mid] <= d) lo = mid; else hi = mid;
   }
   return lo;
-}
-
-struct Ctrl {
-  uint64_t full[8], empty[8], tfull[2], tempty[2], drain;
-  uint32_t tmem_base;
-  int abort_flag;
-  int produced, consumed;
-};
-
-__device__ __forceinline__ void set_abort(Ctrl* c, int32_t* status, int code) {
-  if (status) atomicCAS(status, 0, code);
-  *(volatile int*)&c->abort_flag = 1;
 }
 
 // compensated (Neumaier) float32 accumulation: slot.x = sum, slot.y = correction
@@ -701,39 +586,8 @@ __global__ void pack_tc_kernel(const uint32_t* __restrict__ planes, int W, long 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-namespace {
-
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-std::once_flag g_encode_once;
-
-int get_encode(pgld_context* h) {
-  std::call_once(g_encode_once, [] {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-  });
-  if (!g_encode)
-    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
-  return PGLD_OK;
-}
-
-int make_map(pgld_context* h, CUtensorMap* map, const void* base, long long rows, int k_pad) {
-  cuuint64_t dims[2] = {(cuuint64_t)k_pad, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)k_pad};
-  cuuint32_t box[2] = {(cuuint32_t)pgld::tc::kKChunk, (cuuint32_t)pgld::tc::kRows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims,
-                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return pgld_fail(h, PGLD_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-  return PGLD_OK;
-}
-
-}  // namespace
+using pgld::tchost::get_encode;
+using pgld::tchost::make_map;
 
 int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel) {
   if (panel->n_pops < 1 || panel->n_pops > 2) return 0;

@@ -146,6 +146,24 @@ def test_band_pairs_fp32_outputs():
     assert np.all(st2[:, 2:] == 0)
 
 
+@pytest.mark.parametrize("n_ind,M", [(1, 90), (31, 200), (33, 333), (130, 257), (1000, 300)])
+def test_tc_band_pairs_match_plain_and_oracle(n_ind, M):
+    # the tensor-core genotype form: counts bit-exact, statistics bit-identical
+    # to the plain form (the same float32 epilogue on the same counts)
+    rng = np.random.default_rng(n_ind * 7 + M)
+    g = dosages(rng, n_ind, M, 12, 2e-3, missing=0.03)
+    pos = np.sort(rng.choice(100_000, M, replace=False)).astype(np.int64)
+    pk = _ops.pack_geno(torch.as_tensor(g, device="cuda"))
+    pos_d = _ops.positions_f64(pos)
+    c_tc, nv_tc, st_tc = _ops.geno_band_pairs(pk, pos_d, 30_000, form="tc")
+    c_pl, nv_pl, st_pl = _ops.geno_band_pairs(pk, pos_d, 30_000, form="plain")
+    ii, jj = O.pairs_within_distance(pos, 30_000)
+    rc, rnv = O.genotype_counts_for_pairs(g, ii, jj)
+    assert np.array_equal(np_(c_tc), rc) and np.array_equal(np_(c_pl), rc)
+    assert np.array_equal(np_(nv_tc), np_(nv_pl))
+    assert np.array_equal(np_(st_tc), np_(st_pl), equal_nan=True)
+
+
 @pytest.mark.parametrize("P", [2, 3])
 def test_binned_sums_match_reference(golden, P):
     z = golden("geno_binned")
