@@ -467,11 +467,14 @@ def run_windows(args):
     flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
 
     def one():
-        return _ops.window_sums(pk, None, wb, we)
+        return _ops.window_sums(pk, None, wb, we, form="tc")
+
+    def one_plain():
+        return _ops.window_sums(pk, None, wb, we, form="plain")
 
     def per_window():
         for w in range(len(sizes)):
-            _ops.window_sums(pk, None, wb[w:w + 1], we[w:w + 1])
+            _ops.window_sums(pk, None, wb[w:w + 1], we[w:w + 1], form="plain")
 
     def timeit(fn, steps):
         for _ in range(args.warmup):
@@ -488,18 +491,23 @@ def run_windows(args):
         return float(np.mean(ms))
 
     t_one = timeit(one, args.steps)
+    t_plain = timeit(one_plain, args.steps)
     t_per = timeit(per_window, max(1, args.steps // 2))
     sums, cnt = one()
     assert int(cnt[:, 0].sum()) == n_pairs
+    s_pl, c_pl = one_plain()
+    assert torch.equal(cnt, c_pl)
     print(json.dumps({
         "metric": "within-window SNP-pairs/s, 512 uneven windows, 400 haplotypes",
         "value": n_pairs / (t_one / 1e3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_one, "higher_is_better": True,
-        "dtype": "u32", "data": "synthetic (copying model, seed per window)",
+        "dtype": "e4m3", "data": "synthetic (copying model, seed per window)",
         "config": {"workload": "windows512", "haplotypes": 400, "windows": 512,
-                   "n_snp": int(sizes.sum()), "pairs": n_pairs, "form": "plain"},
-        "per_window_launches": {"ms_per_step": t_per, "value": n_pairs / (t_per / 1e3),
-                                "ratio_one_launch_over_per_window": t_per / t_one}}), flush=True)
+                   "n_snp": int(sizes.sum()), "pairs": n_pairs, "form": "tc"},
+        "plain_one_launch": {"ms_per_step": t_plain, "value": n_pairs / (t_plain / 1e3)},
+        "plain_per_window_launches": {"ms_per_step": t_per, "value": n_pairs / (t_per / 1e3),
+                                      "ratio_tc_one_launch_over_this": t_per / t_one}}),
+          flush=True)
 
 
 def run_geno_band(args):

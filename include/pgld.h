@@ -317,12 +317,15 @@ int pgld_geno_binned_sums(pgld_handle h, const pgld_geno_panel* panel, const dou
  * numerators (pairs with n >= 4; 0 where the pi2 numerator is 0), DD, Dz,
  * pi2 (single-population moments statistics; 0 below n = 4), naive r^2 of
  * per-site allele frequencies.  counts: [n_win][3] int64 = pairs, pairs with
- * r^2 defined, pairs with n >= 4.  Replaces the per-window loops of
+ * r^2 defined, pairs with n >= 4.  form PGLD_FORM_TC counts on the tensor
+ * cores (<= 2048 haplotypes, no validity plane), PGLD_FORM_PLAIN with AND +
+ * popcount.  Replaces the per-window loops of
  * _zns_from_precomputed / _zns_tiled over _tile_counts / _tile_sigma_d2 /
  * _tile_r2_naive (ld_statistics.py:281-341, 534-676).  Synchronises. */
 int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel, const int32_t* snp_idx,
                          int64_t n_idx, const int64_t* win_begin, const int64_t* win_end,
-                         int32_t n_win, double* sums, int64_t* counts, void* stream);
+                         int32_t n_win, double* sums, int64_t* counts, int32_t form,
+                         void* stream);
 
 /* pgld_hap_binned_sums for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers of this library cannot call

@@ -229,13 +229,16 @@ def band_pairs(pk, pos_d, max_dist, with_stats=True, form="auto"):
 WINDOW_COLUMNS = ("r2", "sigma_d2", "dd", "dz", "pi2", "r2_naive")
 
 
-def window_sums(pk, idx, win_begin, win_end):
+def window_sums(pk, idx, win_begin, win_end, form="auto"):
     """Per-window sums (n_win, 6) float64 and counts (n_win, 3) int64 over
     every pair inside each window (one launch for all windows).
 
     idx: int32 SNP indices (None: identity); window w covers
     idx[win_begin[w]:win_end[w]].  Columns: WINDOW_COLUMNS; counts: pairs,
-    pairs with r^2 defined, pairs with n >= 4."""
+    pairs with r^2 defined, pairs with n >= 4.  form: "tc", "plain" or
+    "auto" (tensor cores whenever they apply)."""
+    if form == "auto":
+        form = "tc" if tc_applies([pk]) else "plain"
     torch = _torch()
     dev = pk.planes.device
     wb = L.as_device(win_begin, np.int64)
@@ -252,6 +255,7 @@ def window_sums(pk, idx, win_begin, win_end):
     h = L.handle()
     L.check(L.lib().pgld_hap_window_sums(h, ctypes.byref(panel([pk])), L.ptr(ii), n_idx, L.ptr(wb),
                                          L.ptr(we), n_win, L.ptr(sums), L.ptr(cnt),
+                                         L.FORM_TC if form == "tc" else L.FORM_PLAIN,
                                          L.stream_ptr()), h)
     st = torch.zeros(1, dtype=torch.int32)
     L.check(L.lib().pgld_device_status(h, ctypes.cast(st.data_ptr(), ctypes.POINTER(

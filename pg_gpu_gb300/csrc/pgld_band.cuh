@@ -14,6 +14,7 @@ constexpr int kTile = 32;      // SNPs per tile side of the plain band kernel
 constexpr int kMaxBins = 64;   // distance bins per call
 constexpr int kModeBinned = 0;
 constexpr int kModePairs = 1;
+constexpr int kModeWindows = 2;
 
 struct BandArgs {
   int n_pops;

@@ -30,6 +30,7 @@
 #include "pgld_internal.cuh"
 #include "pgld_scan.cuh"
 #include "pgld_tcgen05.cuh"
+#include "pgld_window.cuh"
 
 namespace pgld {
 namespace tc {
@@ -64,7 +65,63 @@ struct Params {
   int32_t* counts;            // [n_pairs][4]
   int32_t* nvalid;            // [n_pairs] or NULL
   float* stats;               // [n_pairs][4] r^2, DD, Dz, pi2, or NULL
+  // windows mode (one population): operand rows are list positions
+  const long long* win_begin;  // [n_win] list ranges
+  const long long* win_end;
+  int n_win;
+  const long long* tile_off;   // [n_win + 1] prefix of 64-SNP tiles per window
+  const int32_t* idx;          // list position -> SNP (NULL: identity)
+  const float4* site;          // per-SNP (dac, nv, 1 / nv, 1 / pq) of the naive r^2
+  long long n_panel;           // SNPs of the panel (bound of idx values)
+  double* wsums;               // [n_win][6]
+  unsigned long long* wcnt;    // [n_win][3]
 };
+
+// the tile of a work item: first list positions of its rows i0 and columns
+// j0, the end of its range, and (windows mode) its window
+struct TileRef {
+  long long i0, j0, end, bi, bj;
+  int w;
+};
+
+template <int MODE>
+__device__ __forceinline__ TileRef decode_item(const Params& a, long long item) {
+  TileRef r;
+  if constexpr (MODE == kModeWindows) {
+    int lo = 0, hi = a.n_win;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (a.tile_off[mid] <= item) lo = mid; else hi = mid;
+    }
+    const long long base = a.win_begin[lo], m = a.win_end[lo] - base;
+    const long long T = (m + kTileSnp - 1) / kTileSnp;
+    const long long t = item - a.tile_off[lo];
+    long long rlo = 0, rhi = T;  // row bi starts at bi*T - bi(bi-1)/2
+    while (rhi - rlo > 1) {
+      const long long mid = (rlo + rhi) >> 1;
+      if (mid * T - mid * (mid - 1) / 2 <= t) rlo = mid; else rhi = mid;
+    }
+    r.bi = rlo;
+    r.bj = rlo + (t - (rlo * T - rlo * (rlo - 1) / 2));
+    r.i0 = base + r.bi * kTileSnp;
+    r.j0 = base + r.bj * kTileSnp;
+    r.end = base + m;
+    r.w = lo;
+  } else {
+    long long lo = 0, hi = a.n_blocks;
+    while (hi - lo > 1) {
+      const long long mid = (lo + hi) >> 1;
+      if (a.item_off[mid] <= item) lo = mid; else hi = mid;
+    }
+    r.bi = lo;
+    r.bj = lo + (item - a.item_off[lo]);
+    r.i0 = r.bi * kTileSnp;
+    r.j0 = r.bj * kTileSnp;
+    r.end = a.n_snp;
+    r.w = 0;
+  }
+  return r;
+}
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -184,8 +241,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tmem_base = ctrl->tmem_base;
 
-  long long n_items = a.item_off[a.n_blocks];
-  if (n_items < 0 || n_items > a.n_blocks * (a.n_blocks + 1) / 2) {
+  long long n_items = MODE == kModeWindows ? a.tile_off[a.n_win] : a.item_off[a.n_blocks];
+  if (n_items < 0 || (MODE != kModeWindows && n_items > a.n_blocks * (a.n_blocks + 1) / 2)) {
     if (threadIdx.x == 0) set_abort(ctrl, a.status, 3001);
     n_items = 0;
   }
@@ -197,12 +254,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t phase = 0;
       int issued = 0;
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x) {
-        long long lo = 0, hi = a.n_blocks;
-        while (hi - lo > 1) {
-          const long long mid = (lo + hi) >> 1;
-          if (a.item_off[mid] <= item) lo = mid; else hi = mid;
-        }
-        const int yi = (int)(lo * kRows), yj = (int)((lo + (item - a.item_off[lo])) * kRows);
+        const TileRef tr = decode_item<MODE>(a, item);
+        const int yi = (int)(2 * tr.i0), yj = (int)(2 * tr.j0);
         for (int p = 0; p < P && !*abort_flag; ++p) {
           const CUtensorMap* map = p == 0 ? &map0 : &map1;
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
@@ -297,20 +350,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
-    const bool use_int = (a.bcoord == nullptr) && (*a.ipos_bad == 0);
+    const bool use_int = MODE != kModeWindows && (a.bcoord == nullptr) && (*a.ipos_bad == 0);
     float2* my_acc = kacc + (size_t)e * n_bins * S;
     unsigned long long* my_cnt = kcnt + (size_t)e * n_bins;
     int t = 0;
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
       const int acc = t & 1;
       const uint32_t aph = (uint32_t)((t >> 1) & 1);
-      long long lo = 0, hi = a.n_blocks;
-      while (hi - lo > 1) {
-        const long long mid = (lo + hi) >> 1;
-        if (a.item_off[mid] <= item) lo = mid; else hi = mid;
-      }
-      const long long bi = lo, bj = bi + (item - a.item_off[bi]);
-      const long long i0 = bi * kTileSnp, j0 = bj * kTileSnp;
+      const TileRef tr = decode_item<MODE>(a, item);
+      const long long bi = tr.bi, bj = tr.bj;
+      const long long i0 = tr.i0, j0 = tr.j0;
       const long long si0 = i0 + 16 * quarter, sj0 = j0 + 32 * half;
       const long long i = i0 + il;
 
@@ -332,7 +381,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       }
-      const int ipos_i = (use_int && i < a.n_snp) ? a.ipos[i] : 0;
+      const int ipos_i = (MODE != kModeWindows && use_int && i < a.n_snp) ? a.ipos[i] : 0;
 
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
@@ -342,6 +391,60 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       tc_fence_after();
+
+      if constexpr (MODE == kModeWindows) {
+        // per-window sums: every pair of list positions a < b < end of the
+        // item's window (the statistics of pgld_hap_window_sums)
+        float ws[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        int np = 0, nr2 = 0, nfour = 0;
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+          uint32_t r[16];
+          const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
+          tmem_ld16(tmem_base + lane_base + col, r);
+          tmem_wait_ld();
+          if (c == 3) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
+          }
+#pragma unroll 1
+          for (int q = 0; q < 4; ++q) {
+            const uint32_t s0 = plane ? r[4 * q] : r[4 * q + 2];
+            const uint32_t s1 = plane ? r[4 * q + 1] : r[4 * q + 3];
+            const float g0 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
+            const float g1 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
+            const float m0 = __uint_as_float(plane ? r[4 * q + 2] : r[4 * q]);
+            const float m1 = __uint_as_float(plane ? r[4 * q + 3] : r[4 * q + 1]);
+            const float c1 = plane ? g0 : m0, c2 = plane ? g1 : m1;
+            const float c3 = plane ? m0 : g0, c4 = plane ? m1 : g1;
+            const long long j = j0 + half * 32 + c * 8 + 2 * q + plane;
+            if (!(i < j && j < tr.end)) continue;
+            const fast::Pop p = fast::make(c1, c2, c3, c4);
+            ++np;
+            const long long si = a.idx ? (long long)a.idx[i] : i;
+            const long long sj = a.idx ? (long long)a.idx[j] : j;
+            const bool sok = si >= 0 && si < a.n_panel && sj >= 0 && sj < a.n_panel;
+            const float4 fi = sok ? a.site[si] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 fj = sok ? a.site[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
+            win::window_pair(p, p.n, c1, T.inv[p.n], T.r4[p.n], fi, fj, ws, nr2, nfour);
+          }
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2) {
+          const float v = warp_sum(ws[s2]);
+          if (lane == 0 && v != 0.f) atomicAdd(a.wsums + (long long)tr.w * 6 + s2, (double)v);
+        }
+        const int tp = __reduce_add_sync(0xffffffffu, np);
+        const int tr2 = __reduce_add_sync(0xffffffffu, nr2);
+        const int tf = __reduce_add_sync(0xffffffffu, nfour);
+        if (lane == 0) {
+          if (tp) atomicAdd(a.wcnt + (long long)tr.w * 3 + 0, (unsigned long long)tp);
+          if (tr2) atomicAdd(a.wcnt + (long long)tr.w * 3 + 1, (unsigned long long)tr2);
+          if (tf) atomicAdd(a.wcnt + (long long)tr.w * 3 + 2, (unsigned long long)tf);
+        }
+        continue;
+      }
 
       if constexpr (MODE == kModePairs) {
         // per-pair outputs: each lane owns whole pairs (i, j) after the C / Z
@@ -559,15 +662,23 @@ __global__ void pos_to_int_kernel(const double* __restrict__ pos, long long n, i
 // operand packing: bit planes -> E4M3 rows (2 per SNP), K padded to 128
 // ---------------------------------------------------------------------------
 __global__ void pack_tc_kernel(const uint32_t* __restrict__ planes, int W, long long n_snp,
-                               int k_pad, uint32_t* __restrict__ out) {
-  // one thread writes 4 bytes (4 haplotypes) of one operand row
+                               long long n_rows, const int32_t* __restrict__ idx, int k_pad,
+                               uint32_t* __restrict__ out, int32_t* __restrict__ status) {
+  // one thread writes 4 bytes (4 haplotypes) of one operand row; operand row
+  // pair r holds SNP idx[r] (idx NULL: SNP r); an index outside the panel
+  // gives a zero row and sets the status word
   const int words_per_row = k_pad / 4;
-  const long long total = 2 * n_snp * (long long)words_per_row;
+  const long long total = 2 * n_rows * (long long)words_per_row;
   for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
     const long long rowi = x / words_per_row;
     const int wq = (int)(x - rowi * words_per_row);  // 4-haplotype group
-    const long long s = rowi >> 1;
+    long long s = idx ? (long long)idx[rowi >> 1] : (rowi >> 1);
+    if (s < 0 || s >= n_snp) {
+      if (status) atomicCAS(status, 0, 3102);
+      out[x] = 0u;
+      continue;
+    }
     const int plane = (int)(rowi & 1);
     const int h0 = wq * 4;
     const int w = h0 >> 5;
@@ -645,7 +756,8 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
     const long long words = 2 * n * (long long)(k_pad[p] / 4);
     unsigned blocks = (unsigned)std::min<long long>((words + 255) / 256, (long long)h->n_sm * 16);
     pack_tc_kernel<<<std::max(1u, blocks), 256, 0, st>>>(panel->planes[p], panel->n_words[p], n,
-                                                          k_pad[p], (uint32_t*)ops[p]);
+                                                          n, nullptr, k_pad[p], (uint32_t*)ops[p],
+                                                          h->dev_status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_tc_kernel");
   }
@@ -704,6 +816,7 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
   auto kern = mode == pgld::kModePairs
                   ? band_tc_kernel<1, pgld::kModePairs>
                   : (P == 1 ? band_tc_kernel<1, pgld::kModeBinned> : band_tc_kernel<2, pgld::kModeBinned>);
+  if (mode == pgld::kModeWindows) kern = band_tc_kernel<1, pgld::kModeWindows>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc smem attribute");
   kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(maps[0], maps[1], prm);
@@ -720,4 +833,111 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
 int pgld_tc_pairs(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
                   cudaStream_t st) {
   return tc_launch(h, panel, a, pgld::kModePairs, st);
+}
+
+namespace pgld {
+namespace tc {
+// 64-SNP tiles per window (upper triangle); bad ranges get none and set the status
+__global__ void tc_window_tiles_kernel(const long long* __restrict__ wb,
+                                       const long long* __restrict__ we, int n_win, long long n_idx,
+                                       long long* __restrict__ tiles, int32_t* __restrict__ status) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_win; w += gridDim.x * blockDim.x) {
+    const long long lo = wb[w], hi = we[w];
+    long long T = 0;
+    if (lo < 0 || hi < lo || hi > n_idx)
+      atomicCAS(status, 0, 3100);
+    else
+      T = (hi - lo + kTileSnp - 1) / kTileSnp;
+    tiles[w] = T * (T + 1) / 2;
+  }
+}
+}  // namespace tc
+}  // namespace pgld
+
+int pgld_site_freqs(pgld_context* h, const uint32_t* planes, const uint32_t* valid, int W,
+                    long long n_snp, float4* site, cudaStream_t st);
+
+// Per-window sums on the tensor cores (one population, <= 2048 haplotypes, no
+// validity plane): the operand is built over the index list so that each
+// window is a contiguous range of operand rows.
+int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t* idx,
+                    long long n_idx, const long long* wb, const long long* we, int n_win,
+                    double* sums, unsigned long long* counts, cudaStream_t st) {
+  using namespace pgld::tc;
+  int rc = get_encode(h);
+  if (rc) return rc;
+  const long long n = panel->n_snp;
+  const int W = panel->n_words[0];
+  if (2 * n_idx > 2147483647LL - 256)
+    return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core windows: too many SNPs");
+  const int k_pad = ((W * 32 + kKChunk - 1) / kKChunk) * kKChunk;
+  const size_t op_bytes = (size_t)2 * std::max<long long>(n_idx, 1) * k_pad;
+  const size_t sb = pgld::scan_scratch_bytes(n_win);
+  auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+  const size_t off_tiles = 0, off_scan = al((size_t)(n_win + 1) * 8), off_op = off_scan + al(sb),
+               off_site = off_op + al(op_bytes),
+               total = off_site + al((size_t)std::max<long long>(n, 1) * 16);
+  void* ws = nullptr;
+  rc = pgld_workspace(h, total, &ws);
+  if (rc) return rc;
+  char* w = (char*)ws;
+  long long* tiles = (long long*)(w + off_tiles);
+  unsigned char* op = (unsigned char*)(w + off_op);
+  float4* site = (float4*)(w + off_site);
+  {
+    const unsigned gb = (unsigned)std::max<long long>(1, std::min<long long>((n_win + 255) / 256, h->n_sm * 4LL));
+    tc_window_tiles_kernel<<<gb, 256, 0, st>>>(wb, we, n_win, n_idx, tiles, h->dev_status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "tc_window_tiles_kernel");
+  }
+  rc = pgld::exclusive_scan_i64(h, tiles, n_win, w + off_scan, sb, st);
+  if (rc) return rc;
+  if (n > 0) {
+    rc = pgld_site_freqs(h, panel->planes[0], nullptr, W, n, site, st);
+    if (rc) return rc;
+  }
+  if (n_idx > 0) {
+    const long long words = 2 * n_idx * (long long)(k_pad / 4);
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>((words + 255) / 256, h->n_sm * 16LL));
+    pack_tc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, n_idx, idx, k_pad, (uint32_t*)op,
+                                           h->dev_status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_tc_kernel");
+  }
+  CUtensorMap map;
+  rc = make_map(h, &map, op, 2 * std::max<long long>(n_idx, 1), k_pad);
+  if (rc) return rc;
+  Params prm{};
+  prm.n_pops = 1;
+  prm.kchunks[0] = k_pad / kKChunk;
+  prm.n_snp = n_idx;
+  prm.n_bins = 0;
+  prm.status = h->dev_status;
+  prm.nmax = 32 * W;
+  prm.win_begin = wb;
+  prm.win_end = we;
+  prm.n_win = n_win;
+  prm.tile_off = tiles;
+  prm.idx = idx;
+  prm.n_panel = n;
+  prm.site = site;
+  prm.wsums = sums;
+  prm.wcnt = counts;
+  prm.ipos = nullptr;  // positions play no part in windows mode
+  prm.ipos_bad = nullptr;
+  const size_t fixed = sizeof(Ctrl) + (pgld::kMaxBins + 1) * 8 + (pgld::kMaxBins + 2) * 4 +
+                       (size_t)4 * (prm.nmax + 1) * sizeof(float) + 1024;
+  int max_smem = 0;
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  const int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStageBytes);
+  if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core windows: shared memory");
+  prm.stages = stages;
+  const size_t smem = (size_t)stages * kStageBytes + fixed;
+  auto kern = band_tc_kernel<1, pgld::kModeWindows>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "tc windows smem attribute");
+  kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map, map, prm);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc_kernel (windows)");
+  return PGLD_OK;
 }

@@ -19,6 +19,7 @@
 #include "pgld_epilogue.cuh"
 #include "pgld_internal.cuh"
 #include "pgld_scan.cuh"
+#include "pgld_window.cuh"
 
 using pgld::i64;
 
@@ -42,8 +43,8 @@ struct Args {
   const i64* win_end;
   int n_win;
   const i64* tile_off;     // [n_win + 1] prefix of tiles per window
-  const int32_t* dac;      // per-SNP carrier count among the valid
-  const int32_t* nvs;      // per-SNP valid count
+  const float4* site;      // per-SNP (dac, nv, 1 / nv, 1 / pq) of site_freq
+  int nmax;                // largest valid n (reciprocal tables 0..nmax)
   double* sums;            // [n_win][kCols]
   unsigned long long* cnt; // [n_win][kCnts]
   int32_t* status;
@@ -66,10 +67,10 @@ __global__ void window_tiles_kernel(const i64* __restrict__ win_begin,
   }
 }
 
-// per-SNP allele counts: dac = carriers, nv = valid (carrier or reference)
-__global__ void site_counts_kernel(const uint32_t* __restrict__ planes,
-                                   const uint32_t* __restrict__ valid, int W, i64 n_snp,
-                                   int32_t* __restrict__ dac, int32_t* __restrict__ nvs) {
+// per-SNP site_freq: carriers and valid haplotypes (carrier or reference)
+__global__ void site_freq_kernel(const uint32_t* __restrict__ planes,
+                                 const uint32_t* __restrict__ valid, int W, i64 n_snp,
+                                 float4* __restrict__ site) {
   for (i64 s = (i64)blockIdx.x * blockDim.x + threadIdx.x; s < n_snp;
        s += (i64)gridDim.x * blockDim.x) {
     int d = 0, v = 0;
@@ -78,8 +79,7 @@ __global__ void site_counts_kernel(const uint32_t* __restrict__ planes,
       d += __popc(c);
       v += valid ? __popc(valid[s * W + w]) : __popc(c | z);
     }
-    dac[s] = d;
-    nvs[s] = v;
+    site[s] = site_freq(d, v);
   }
 }
 
@@ -111,7 +111,15 @@ struct __align__(16) Smem {
 
 __global__ void __launch_bounds__(kThreads) window_kernel(Args a) {
   __shared__ Smem sm;
+  extern __shared__ float tabs[];  // 1/n and 1/(n(n-1)(n-2)(n-3)), n = 0..nmax
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float* tinv = tabs;
+  float* tr4 = tabs + (a.nmax + 1);
+  for (int x = threadIdx.x; x <= a.nmax; x += kThreads) {
+    float r2, r3;
+    fast::recip_entry(x, tinv + x, &r2, &r3, tr4 + x);
+  }
+  __syncthreads();
   i64 n_items = a.tile_off[a.n_win];
   for (i64 item = blockIdx.x; item < n_items; item += gridDim.x) {
     // window of the item, then its tile (bi, bj), bj >= bi, in row-major order
@@ -182,46 +190,11 @@ __global__ void __launch_bounds__(kThreads) window_kernel(Args a) {
       const fast::Pop p = fast::make(c1, c2, c3, c4);
       const int n = a.valid ? nv[q] : p.n;
       ++n_pairs;
-      // r^2 = x^2 / (pA qA pB qB) on the pair's counts (NaN where undefined)
-      const float rden = fast::x2_value(fast::x2_prod(p.pA * p.qA, p.pB * p.qB));
-      if (rden > 0.f) {
-        acc[0] += fast::x2_value(fast::x2_prod(p.x, p.x)) / rden;
-        ++n_r2;
-      }
-      // the moments statistics with the pair's n; divisions in float32
-      if (n >= 4) {
-        const float d4 = (float)((long long)n * (n - 1) * (n - 2) * (n - 3));
-        const float dd = fast::dd_num(p), pi = fast::pi2_num(p);
-        ++n_four;
-        if (pi != 0.f) acc[1] += dd / pi;
-        acc[2] += dd / d4;
-        acc[3] += fast::dz_num(p) / d4;
-        acc[4] += pi / d4;
-      }
-      // naive r^2 with per-site frequencies (_tile_r2_naive): D = c1/n - p_i p_j
-      // (p_AB = 0 where no haplotype is valid at both), over pq_i pq_j
-      {
-        const i64 si = a.idx ? (i64)a.idx[ia] : ia, sj = a.idx ? (i64)a.idx[jb] : jb;
-        if (si >= 0 && si < a.n_snp && sj >= 0 && sj < a.n_snp) {
-          const float di = (float)a.dac[si], vi = (float)a.nvs[si];
-          const float dj = (float)a.dac[sj], vj = (float)a.nvs[sj];
-          if (vi > 0.f && vj > 0.f) {
-            const float pqi = (di * (vi - di)) / (vi * vi), pqj = (dj * (vj - dj)) / (vj * vj);
-            if (pqi * pqj > 0.f) {
-              float D;
-              if (n > 0) {
-                // exact numerator c1 vi vj - n di dj, then one rounding
-                fast::X2 num = fast::x2_prod(c1, vi * vj);
-                fast::x2_add_prod(num, -(float)n, di * dj);
-                D = fast::x2_value(num) / ((float)n * (vi * vj));
-              } else {
-                D = -(di * dj) / (vi * vj);
-              }
-              acc[5] += (D * D) / (pqi * pqj);
-            }
-          }
-        }
-      }
+      const i64 si = a.idx ? (i64)a.idx[ia] : ia, sj = a.idx ? (i64)a.idx[jb] : jb;
+      const bool sok = si >= 0 && si < a.n_snp && sj >= 0 && sj < a.n_snp;
+      const float4 fi = sok ? a.site[si] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 fj = sok ? a.site[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
+      window_pair(p, n, c1, tinv[n], tr4[n], fi, fj, acc, n_r2, n_four);
     }
     // warp totals, one atomic per statistic per warp
 #pragma unroll
@@ -245,10 +218,24 @@ __global__ void __launch_bounds__(kThreads) window_kernel(Args a) {
 }  // namespace win
 }  // namespace pgld
 
+int pgld_site_freqs(pgld_context* h, const uint32_t* planes, const uint32_t* valid, int W,
+                    long long n_snp, float4* site, cudaStream_t st) {
+  const unsigned b = (unsigned)std::max<i64>(1, std::min<i64>((n_snp + 255) / 256, h->n_sm * 8));
+  pgld::win::site_freq_kernel<<<b, 256, 0, st>>>(planes, valid, W, n_snp, site);
+  PGLD_CHECK_CUDA(h, cudaGetLastError());
+  return PGLD_OK;
+}
+
+int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel);
+int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t* idx,
+                    long long n_idx, const long long* wb, const long long* we, int n_win,
+                    double* sums, unsigned long long* counts, cudaStream_t st);
+
 extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
                                     const int32_t* snp_idx, int64_t n_idx,
                                     const int64_t* win_begin, const int64_t* win_end,
-                                    int32_t n_win, double* sums, int64_t* counts, void* stream) {
+                                    int32_t n_win, double* sums, int64_t* counts, int32_t form,
+                                    void* stream) {
   PGLD_REQUIRE(h, h != nullptr, "pgld_hap_window_sums: NULL handle");
   PGLD_REQUIRE(h, panel != nullptr && panel->n_pops == 1,
                "pgld_hap_window_sums: one population per call");
@@ -257,6 +244,10 @@ extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
   PGLD_REQUIRE(h, snp_idx != nullptr || n_idx == panel->n_snp,
                "pgld_hap_window_sums: without an index list n_idx must be n_snp");
   PGLD_REQUIRE(h, n_idx >= 0, "pgld_hap_window_sums: n_idx < 0");
+  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC, "pgld_hap_window_sums: form");
+  if (form == PGLD_FORM_TC && !pgld_tc_supported(h, panel))
+    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "pgld_hap_window_sums: tensor-core form needs "
+                     "<= 2048 haplotypes and no separate validity plane");
   if (n_win == 0) return PGLD_OK;
   PGLD_REQUIRE(h, win_begin && win_end && sums && counts, "pgld_hap_window_sums: NULL buffer");
   PGLD_REQUIRE(h, panel->planes[0] != nullptr || panel->n_snp == 0,
@@ -267,17 +258,25 @@ extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
   const int W = panel->n_words[0];
   PGLD_CHECK_CUDA(h, cudaMemsetAsync(sums, 0, (size_t)n_win * pgld::win::kCols * 8, st));
   PGLD_CHECK_CUDA(h, cudaMemsetAsync(counts, 0, (size_t)n_win * pgld::win::kCnts * 8, st));
+  if (form == PGLD_FORM_TC) {
+    int rc = pgld_tc_windows(h, panel, snp_idx, n_idx, reinterpret_cast<const i64*>(win_begin),
+                             reinterpret_cast<const i64*>(win_end), n_win, sums,
+                             reinterpret_cast<unsigned long long*>(counts), st);
+    if (rc) return rc;
+    // the workspace holds the tile offsets and the operand: finish before reuse
+    PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    return PGLD_OK;
+  }
   const size_t sb = pgld::scan_scratch_bytes(n_win);
   const size_t tiles_b = ((size_t)(n_win + 1) * 8 + 255) & ~size_t(255);
-  const size_t site_b = ((size_t)std::max<i64>(n, 1) * 4 + 255) & ~size_t(255);
+  const size_t site_b = ((size_t)std::max<i64>(n, 1) * 16 + 255) & ~size_t(255);
   void* ws = nullptr;
-  int rc = pgld_workspace(h, tiles_b + 2 * site_b + sb + 256, &ws);
+  int rc = pgld_workspace(h, tiles_b + site_b + sb + 256, &ws);
   if (rc) return rc;
   char* wp = (char*)ws;
   i64* tiles = (i64*)wp;
-  int32_t* dac = (int32_t*)(wp + tiles_b);
-  int32_t* nvs = (int32_t*)(wp + tiles_b + site_b);
-  char* scratch = wp + tiles_b + 2 * site_b;
+  float4* site = (float4*)(wp + tiles_b);
+  char* scratch = wp + tiles_b + site_b;
   const unsigned gb = (unsigned)std::max<i64>(1, std::min<i64>((n_win + 255) / 256, h->n_sm * 4));
   const i64* wb = reinterpret_cast<const i64*>(win_begin);
   const i64* we = reinterpret_cast<const i64*>(win_end);
@@ -288,8 +287,8 @@ extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
   if (rc) return rc;
   if (n > 0) {
     const unsigned sbk = (unsigned)std::max<i64>(1, std::min<i64>((n + 255) / 256, h->n_sm * 8));
-    pgld::win::site_counts_kernel<<<sbk, 256, 0, st>>>(panel->planes[0], panel->valid[0], W, n,
-                                                        dac, nvs);
+    pgld::win::site_freq_kernel<<<sbk, 256, 0, st>>>(panel->planes[0], panel->valid[0], W, n,
+                                                      site);
     PGLD_CHECK_CUDA(h, cudaGetLastError());
   }
   pgld::win::Args a{};
@@ -302,16 +301,19 @@ extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
   a.win_end = we;
   a.n_win = n_win;
   a.tile_off = tiles;
-  a.dac = dac;
-  a.nvs = nvs;
+  a.site = site;
+  a.nmax = 32 * W;
   a.sums = sums;
   a.cnt = reinterpret_cast<unsigned long long*>(counts);
   a.status = h->dev_status;
+  const size_t tab_b = (size_t)2 * (a.nmax + 1) * sizeof(float);
+  PGLD_CHECK_CUDA(h, cudaFuncSetAttribute(pgld::win::window_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_b));
   int per_sm = 0;
   PGLD_CHECK_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &per_sm, pgld::win::window_kernel, pgld::win::kThreads, 0));
-  pgld::win::window_kernel<<<(unsigned)(h->n_sm * std::max(1, per_sm)), pgld::win::kThreads, 0,
-                             st>>>(a);
+                         &per_sm, pgld::win::window_kernel, pgld::win::kThreads, tab_b));
+  pgld::win::window_kernel<<<(unsigned)(h->n_sm * std::max(1, per_sm)), pgld::win::kThreads,
+                             tab_b, st>>>(a);
   PGLD_CHECK_CUDA(h, cudaGetLastError());
   // the tile offsets and site counts live in the workspace: finish before reuse
   PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));

@@ -1,0 +1,61 @@
+// Per-pair statistics of the window sums, shared by the plain and the
+// tensor-core window kernels.
+//
+// Per pair: r^2 on the pair's counts (where defined), sigma_D^2 = the DD over
+// the pi2 numerator (n >= 4, 0 where the pi2 numerator is 0), the moments DD,
+// Dz, pi2 (0 below n = 4) and the naive r^2 of _tile_r2_naive
+// (ld_statistics.py:299-308) from per-site allele frequencies.  Numerators
+// come from the exact float32 features of pgld_epilogue.cuh; the divisions
+// use the fast reciprocal (relative error of a few ulp per pair, far inside
+// the window sums' float32 accumulation), the moments denominators the
+// per-n reciprocal tables.
+#pragma once
+#include "pgld_epilogue.cuh"
+
+namespace pgld {
+namespace win {
+
+// per-site (dac, nv, 1 / nv, 1 / (p (1 - p))) with p = dac / nv; the last
+// entry is 0 where the site is monomorphic among its valid haplotypes or has
+// none
+__device__ __forceinline__ float4 site_freq(int dac, int nv) {
+  if (nv <= 0) return make_float4(0.f, 0.f, 0.f, 0.f);
+  const float d = (float)dac, v = (float)nv;
+  const float pq_num = d * (v - d);  // exact: below 2^24 for nv <= 4096
+  return make_float4(d, v, 1.0f / v, pq_num > 0.f ? (v * v) / pq_num : 0.f);
+}
+
+// accumulate one pair: acc = r^2, sigma_D^2, DD, Dz, pi2, naive r^2
+__device__ __forceinline__ void window_pair(const fast::Pop& p, int n, float c1, float inv_n,
+                                            float r4n, float4 si, float4 sj, float (&acc)[6],
+                                            int& n_r2, int& n_four) {
+  const float rden = fast::x2_value(fast::x2_prod(p.pA * p.qA, p.pB * p.qB));
+  if (rden > 0.f) {
+    acc[0] += __fdividef(fast::x2_value(fast::x2_prod(p.x, p.x)), rden);
+    ++n_r2;
+  }
+  if (n >= 4) {
+    const float dd = fast::dd_num(p), pi = fast::pi2_num(p);
+    ++n_four;
+    if (pi != 0.f) acc[1] += __fdividef(dd, pi);
+    acc[2] += dd * r4n;
+    acc[3] += fast::dz_num(p) * r4n;
+    acc[4] += pi * r4n;
+  }
+  if (si.w > 0.f && sj.w > 0.f) {
+    // D = c1 / n - p_i p_j from the exact integer c1 v_i v_j - n d_i d_j, so
+    // that the cancellation costs nothing (p_AB = 0 where n = 0)
+    float D;
+    if (n > 0) {
+      fast::X2 num = fast::x2_prod(c1, si.y * sj.y);
+      fast::x2_add_prod(num, -(float)n, si.x * sj.x);
+      D = fast::x2_value(num) * inv_n * si.z * sj.z;
+    } else {
+      D = -(si.x * si.z) * (sj.x * sj.z);
+    }
+    acc[5] += (D * D) * (si.w * sj.w);
+  }
+}
+
+}  // namespace win
+}  // namespace pgld

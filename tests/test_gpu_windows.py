@@ -32,8 +32,9 @@ def copying_model(rng, H, M, F, switch, missing=0.0, flip=1e-3):
     return hap.astype(np.int8)
 
 
-@pytest.mark.parametrize("H", [33, 400])
-def test_window_sums_match_oracle(H):
+@pytest.mark.parametrize("H,form", [(33, "plain"), (400, "plain"), (33, "tc"), (400, "tc"),
+                                    (2000, "tc")])
+def test_window_sums_match_oracle(H, form):
     rng = np.random.default_rng(H)
     M = 900
     hap = copying_model(rng, H, M, 12, 2e-3, missing=0.02)
@@ -44,7 +45,7 @@ def test_window_sums_match_oracle(H):
     e = np.minimum(np.array([0, 1, 5, 37, 300, 131 + 64, 700, ns, 200], np.int64), ns)
     assert ns > 300
     pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
-    sums, cnt = _ops.window_sums(pk, torch.as_tensor(seg, device="cuda"), b, e)
+    sums, cnt = _ops.window_sums(pk, torch.as_tensor(seg, device="cuda"), b, e, form=form)
     ref, rcnt = O.window_sums(hap, seg, b, e)
     assert np.array_equal(cnt.cpu().numpy(), rcnt)
     got = sums.cpu().numpy()
@@ -89,9 +90,12 @@ def test_zns_matches_reference(golden):
         O.zns_window(z["hap"], 0, z["hap"].shape[1], False), rel=1e-5)
 
 
-def test_window_errors():
+@pytest.mark.parametrize("form", ["plain", "tc"])
+def test_window_errors(form):
     pk = _ops.pack(np.zeros((8, 10), np.int8))
     with pytest.raises(IndexError):
-        _ops.window_sums(pk, torch.arange(10, dtype=torch.int32, device="cuda"), [0], [11])
+        _ops.window_sums(pk, torch.arange(10, dtype=torch.int32, device="cuda"), [0], [11],
+                         form=form)
     with pytest.raises(IndexError):
-        _ops.window_sums(pk, torch.tensor([0, 3, 99], dtype=torch.int32, device="cuda"), [0], [3])
+        _ops.window_sums(pk, torch.tensor([0, 3, 99], dtype=torch.int32, device="cuda"), [0], [3],
+                         form=form)
