@@ -7,18 +7,25 @@
 // magnitude < 2^24, so it is formed exactly in float32 -- on the float32
 // pipes, with no integer-to-float conversions.
 //
-// Numerators whose terms can cancel are evaluated exactly as an unevaluated
-// sum s + e of two float32 (error-free products via fma and error-free sums,
-// "TwoProduct" / "TwoSum"): every term is an integer, so the low parts are
-// small integers that add exactly and s + e rounds once.  64-bit integer
-// multiplies would run at the float64 rate on GB300.  Products of exact
-// integers that cannot cancel are formed directly in float32.  Denominators
-// come from per-CTA tables of reciprocals indexed by the valid sample size n
-// (1/n, 1/(n(n-1)), 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3)), each the IEEE
-// reciprocal of the exact integer rounded once to float32), so each statistic
-// carries at most six roundings (< 4e-7 relative).  The formulas are the case
-// formulas of ld_statistics.py (1116-1617) for the population patterns of the
-// moments tables of one and two populations (ld_pipeline.py:357-457).
+// Every numerator is rewritten as (at most) two products of such exact
+// integers -- e.g. DD: x (x + c2 + c3 - 1) - c1c4 (n - 2), pi2:
+// c1c4 (n^2 - 4n + 2) + x (x + n - 1 - (n - 2)(c1 + c4)) -- and evaluated
+// with Kahan's algorithm for a*b + c*d (the rounding error of c*d recovered
+// exactly by an fma, one fma and one addition more), whose relative error is
+// at most 2u even under cancellation (Jeannerod, Louvet and Muller, "Further
+// analysis of Kahan's algorithm for the accurate computation of 2x2
+// determinants", Math. Comp. 82, 2013).  The one numerator with three
+// products, pi2(i,j,i,j), sums its two cubic products exactly as s + t
+// (TwoProduct / TwoSum: the low parts are integers below 2^22 and add exactly)
+// before one fma adds the quartic product, so it carries at most 3u.
+// 64-bit integer multiplies would run at the float64 rate on GB300.
+// Denominators come from per-CTA tables of reciprocals indexed by the valid
+// sample size n (1/n, 1/(n(n-1)), 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3)), each
+// the IEEE reciprocal of the exact integer rounded once to float32), so each
+// statistic is within 10u (< 6e-7) relative of its exact value.  The formulas
+// are the case formulas of ld_statistics.py (1116-1617) for the population
+// patterns of the moments tables of one and two populations
+// (ld_pipeline.py:357-457).
 #pragma once
 #include <stdint.h>
 
@@ -93,6 +100,14 @@ PGLD_HD void x2_add_prod(X2& acc, float a, float b) {
 
 PGLD_HD float x2_value(const X2& v) { return fadd(v.s, v.e); }
 
+// a*b + c*d (exact float32 integers) with relative error <= 2u: Kahan's
+// algorithm
+PGLD_HD float dot2(float a, float b, float c, float d) {
+  const float w = fmul(c, d);
+  const float e = fmaf(c, d, -w);
+  return fadd(fmaf(a, b, w), e);
+}
+
 // reciprocal tables, entries 0..nmax (0 where the integer is 0)
 struct Recip {
   const float* inv;  // 1/n
@@ -115,7 +130,8 @@ struct Pop {
   float pA, qA, pB, qB;
   float a, b, x;    // c1c4, c2c3, c1c4 - c2c3
   float dA, dB, e;  // qA - pA, qB - pB, (c2+c3) - (c1+c4)
-  int n;            // c1 + c2 + c3 + c4 (the pairwise valid n of 0/1/-1 data)
+  float s, t, ns;   // c2 + c3, c1 + c4, c1 + c2 + c3 + c4
+  int n;            // ns as an int (the pairwise valid n of 0/1/-1 data)
 };
 
 PGLD_HD Pop make(float c1, float c2, float c3, float c4) {
@@ -123,48 +139,52 @@ PGLD_HD Pop make(float c1, float c2, float c3, float c4) {
   p.c1 = c1; p.c2 = c2; p.c3 = c3; p.c4 = c4;
   p.pA = c1 + c2; p.qA = c3 + c4; p.pB = c1 + c3; p.qB = c2 + c4;
   p.a = c1 * c4; p.b = c2 * c3; p.x = p.a - p.b;
-  p.dA = p.qA - p.pA; p.dB = p.qB - p.pB; p.e = (c2 + c3) - (c1 + c4);
-  p.n = f2i_small(p.pA + p.qA);
+  p.dA = p.qA - p.pA; p.dB = p.qB - p.pB;
+  p.s = c2 + c3; p.t = c1 + c4; p.e = p.s - p.t;
+  p.ns = p.pA + p.qA;
+  p.n = f2i_small(p.ns);
   return p;
 }
 
-// c1(c1-1)c4(c4-1) + c2(c2-1)c3(c3-1) - 2c1c2c3c4 = x^2 - a(c1+c4-1) - b(c2+c3-1)
-PGLD_HD float dd_num(const Pop& p) {
-  X2 v = x2_prod(p.x, p.x);
-  x2_add_prod(v, p.a, 1.0f - p.c1 - p.c4);
-  x2_add_prod(v, p.b, 1.0f - p.c2 - p.c3);
-  return x2_value(v);
-}
+// c1(c1-1)c4(c4-1) + c2(c2-1)c3(c3-1) - 2c1c2c3c4
+//   = x^2 - a(c1+c4-1) - b(c2+c3-1) = x (x + c2 + c3 - 1) + a (2 - n)
+// (n = the sum of the four counts; b = a - x)
+PGLD_HD float dd_num(const Pop& p) { return dot2(p.x, (p.x + p.s) - 1.0f, p.a, 2.0f - p.ns); }
 // x*(dA*dB + e) + 2(a+b): the fma rounds once, and whenever the two terms can
 // cancel the product is below 2^24 and exact
 PGLD_HD float dz_num(const Pop& p) { return fmaf(p.x, p.dA * p.dB + p.e, 2.0f * (p.a + p.b)); }
+// pA pB qA qB - a(3c2 + 3c3 + c1 + c4 - 1) - b(3c1 + 3c4 + c2 + c3 - 1)
+//   = a (n^2 - 4n + 2) + x (x + n - 1 - (n - 2)(c1 + c4))
+// (pA pB = n c1 - x and qA qB = n c4 - x)
 PGLD_HD float pi2_num(const Pop& p) {
-  X2 v = x2_prod(p.pA * p.pB, p.qB * p.qA);
-  x2_add_prod(v, p.a, 1.0f - p.c1 - 3.0f * p.c2 - 3.0f * p.c3 - p.c4);
-  x2_add_prod(v, p.b, 1.0f - 3.0f * p.c1 - p.c2 - p.c3 - 3.0f * p.c4);
-  return x2_value(v);
+  const float pn = fmaf(p.ns, p.ns - 4.0f, 2.0f);
+  const float w = fmaf(2.0f - p.ns, p.t, p.x + (p.ns - 1.0f));
+  return dot2(p.a, pn, p.x, w);
 }
 // pi2 with population t three times and s once, times 2
 PGLD_HD float triple_num2(const Pop& t, const Pop& s) {
-  X2 v = x2_prod(t.pA * t.qA, t.qB * s.pB + t.pB * s.qB - 2.0f * s.qB);
-  x2_add_prod(v, t.pA * t.c4 + t.c2 * t.qA, s.qB - s.pB);
-  return x2_value(v);
+  return dot2(t.pA * t.qA, t.qB * s.pB + t.pB * s.qB - 2.0f * s.qB, t.pA * t.c4 + t.c2 * t.qA,
+              s.qB - s.pB);
 }
 // pi2(i,j,i,j) times 4 (symmetric in the two populations).  The quartic and
 // cubic polynomial of the reference (ld_statistics.py:1349-1402) equals
 //   H_A H_B + (1 - n_A - n_B) K - x_A e_B - x_B e_A
-// with H_A = qA_A pA_B + pA_A qA_B, H_B = qB_A pB_B + pB_A qB_B and
-// K = c1_A c4_B + c2_A c3_B + c3_A c2_B + c4_A c1_B (an algebraic identity,
-// checked term by term against the oracle in tests/test_epilogue_cpu.py).
+//   = K m_A m_B + x_B (m_A e_A) + x_A (m_B e_B + 4 x_B)
+// with H_A = qA_A pA_B + pA_A qA_B, H_B = qB_A pB_B + pB_A qB_B,
+// K = c1_A c4_B + c2_A c3_B + c3_A c2_B + c4_A c1_B and m = n - 1 (algebraic
+// identities, checked against the oracle in tests/test_epilogue_cpu.py).  The
+// two cubic products are summed exactly as s + t; K m_A m_B + s rounds once in
+// the fma and t (an integer below 2^22) is added last.
 PGLD_HD float ijij_num4(const Pop& A, const Pop& B) {
-  const float HA = A.qA * B.pA + A.pA * B.qA;
-  const float HB = A.qB * B.pB + A.pB * B.qB;
   const float K = A.c1 * B.c4 + A.c2 * B.c3 + A.c3 * B.c2 + A.c4 * B.c1;
-  X2 v = x2_prod(HA, HB);
-  x2_add_prod(v, 1.0f - (A.pA + A.qA) - (B.pA + B.qA), K);
-  x2_add_prod(v, -A.x, B.e);
-  x2_add_prod(v, -B.x, A.e);
-  return x2_value(v);
+  const float mA = A.ns - 1.0f, mB = B.ns - 1.0f;
+  const float y1 = mA * A.e, y2 = fmaf(mB, B.e, 4.0f * B.x);
+  const float p1 = fmul(B.x, y1), e1 = fmaf(B.x, y1, -p1);
+  const float p2 = fmul(A.x, y2), e2 = fmaf(A.x, y2, -p2);
+  const float s = fadd(p1, p2);
+  const float bb = fsub(s, p1);
+  const float t = fadd(fadd(fsub(p1, fsub(s, bb)), fsub(p2, bb)), fadd(e1, e2));
+  return fadd(fmaf(K, fmul(mA, mB), s), t);
 }
 
 // DD, Dz, pi2 of one population (moments order for one population)

@@ -2,9 +2,9 @@
 // float2 operands, so that every addition, multiplication and fused
 // multiply-add is one packed sm_100+ instruction (FADD2 / FMUL2 / FFMA2) for
 // two SNP pairs.  The arithmetic of each lane is exactly that of the scalar
-// code: the same exact integer features, the same error-free TwoProduct /
-// TwoSum numerators and the same reciprocal-table divisions, so each lane's
-// statistics equal the scalar epilogue's bit for bit.
+// code: the same exact integer features, the same two-product numerators
+// (Kahan's algorithm, TwoProduct / TwoSum) and the same reciprocal-table
+// divisions, so each lane's statistics equal the scalar epilogue's bit for bit.
 #pragma once
 #include "pgld_epilogue.cuh"
 
@@ -36,30 +36,19 @@ PGLD_HD V vs(float a) { return make_float2(a, a); }
 // exactly like a correctly rounded subtraction
 PGLD_HD V vsub(V a, V b) { return vfma(b, vs(-1.0f), a); }
 
-struct X2 {
-  V s, e;
-};
-
-PGLD_HD X2 x2_prod(V a, V b) {
-  const V p = vmul(a, b);
-  return {p, vfma(a, b, vneg(p))};
+// a*b + c*d with relative error <= 2u (Kahan's algorithm, as fast::dot2)
+PGLD_HD V dot2(V a, V b, V c, V d) {
+  const V w = vmul(c, d);
+  const V e = vfma(c, d, vneg(w));
+  return vadd(vfma(a, b, w), e);
 }
-PGLD_HD void x2_add_prod(X2& acc, V a, V b) {
-  const V p = vmul(a, b);
-  const V pe = vfma(a, b, vneg(p));
-  const V s = vadd(acc.s, p);
-  const V bb = vsub(s, acc.s);
-  const V t = vadd(vsub(acc.s, vsub(s, bb)), vsub(p, bb));
-  acc.s = s;
-  acc.e = vadd(acc.e, vadd(pe, t));
-}
-PGLD_HD V x2_value(const X2& v) { return vadd(v.s, v.e); }
 
 struct Pop {
   V c1, c2, c3, c4;
   V pA, qA, pB, qB;
   V a, b, x;
   V dA, dB, e;
+  V s, t, ns;
   int n0, n1;  // valid n of each lane
 };
 
@@ -71,45 +60,38 @@ PGLD_HD Pop make(V c1, V c2, V c3, V c4) {
   p.pA = vadd(c1, c2); p.qA = vadd(c3, c4); p.pB = vadd(c1, c3); p.qB = vadd(c2, c4);
   p.a = vmul(c1, c4); p.b = vmul(c2, c3); p.x = vsub(p.a, p.b);
   p.dA = vsub(p.qA, p.pA); p.dB = vsub(p.qB, p.pB);
-  p.e = vsub(vadd(c2, c3), vadd(c1, c4));
-  const V n = vadd(p.pA, p.qA);
-  p.n0 = f2i(n.x);
-  p.n1 = f2i(n.y);
+  p.s = vadd(c2, c3); p.t = vadd(c1, c4); p.e = vsub(p.s, p.t);
+  p.ns = vadd(p.pA, p.qA);
+  p.n0 = f2i(p.ns.x);
+  p.n1 = f2i(p.ns.y);
   return p;
 }
 
 PGLD_HD V dd_num(const Pop& p) {
-  X2 v = x2_prod(p.x, p.x);
-  x2_add_prod(v, p.a, vsub(vsub(vs(1.0f), p.c1), p.c4));
-  x2_add_prod(v, p.b, vsub(vsub(vs(1.0f), p.c2), p.c3));
-  return x2_value(v);
+  return dot2(p.x, vsub(vadd(p.x, p.s), vs(1.0f)), p.a, vsub(vs(2.0f), p.ns));
 }
 PGLD_HD V dz_num(const Pop& p) {
   return vfma(p.x, vfma(p.dA, p.dB, p.e), vmul(vs(2.0f), vadd(p.a, p.b)));
 }
 PGLD_HD V pi2_num(const Pop& p) {
-  X2 v = x2_prod(vmul(p.pA, p.pB), vmul(p.qB, p.qA));
-  // 1 - c1 - 3 c2 - 3 c3 - c4 and 1 - 3 c1 - c2 - c3 - 3 c4
-  const V s23 = vadd(p.c2, p.c3), s14 = vadd(p.c1, p.c4);
-  x2_add_prod(v, p.a, vsub(vfma(vs(-3.0f), s23, vs(1.0f)), s14));
-  x2_add_prod(v, p.b, vsub(vfma(vs(-3.0f), s14, vs(1.0f)), s23));
-  return x2_value(v);
+  const V pn = vfma(p.ns, vsub(p.ns, vs(4.0f)), vs(2.0f));
+  const V w = vfma(vsub(vs(2.0f), p.ns), p.t, vadd(p.x, vsub(p.ns, vs(1.0f))));
+  return dot2(p.a, pn, p.x, w);
 }
 PGLD_HD V triple_num2(const Pop& t, const Pop& s) {
-  X2 v = x2_prod(vmul(t.pA, t.qA),
-                 vfma(vs(-2.0f), s.qB, vfma(t.qB, s.pB, vmul(t.pB, s.qB))));
-  x2_add_prod(v, vfma(t.pA, t.c4, vmul(t.c2, t.qA)), vsub(s.qB, s.pB));
-  return x2_value(v);
+  return dot2(vmul(t.pA, t.qA), vfma(vs(-2.0f), s.qB, vfma(t.qB, s.pB, vmul(t.pB, s.qB))),
+              vfma(t.pA, t.c4, vmul(t.c2, t.qA)), vsub(s.qB, s.pB));
 }
 PGLD_HD V ijij_num4(const Pop& A, const Pop& B) {
-  const V HA = vfma(A.qA, B.pA, vmul(A.pA, B.qA));
-  const V HB = vfma(A.qB, B.pB, vmul(A.pB, B.qB));
   const V K = vfma(A.c1, B.c4, vfma(A.c2, B.c3, vfma(A.c3, B.c2, vmul(A.c4, B.c1))));
-  X2 v = x2_prod(HA, HB);
-  x2_add_prod(v, vsub(vsub(vs(1.0f), vadd(A.pA, A.qA)), vadd(B.pA, B.qA)), K);
-  x2_add_prod(v, vneg(A.x), B.e);
-  x2_add_prod(v, vneg(B.x), A.e);
-  return x2_value(v);
+  const V mA = vsub(A.ns, vs(1.0f)), mB = vsub(B.ns, vs(1.0f));
+  const V y1 = vmul(mA, A.e), y2 = vfma(mB, B.e, vmul(vs(4.0f), B.x));
+  const V p1 = vmul(B.x, y1), e1 = vfma(B.x, y1, vneg(p1));
+  const V p2 = vmul(A.x, y2), e2 = vfma(A.x, y2, vneg(p2));
+  const V s = vadd(p1, p2);
+  const V bb = vsub(s, p1);
+  const V t = vadd(vadd(vsub(p1, vsub(s, bb)), vsub(p2, bb)), vadd(e1, e2));
+  return vadd(vfma(K, vmul(mA, mB), s), t);
 }
 
 PGLD_HD V tab(const float* t, int n0, int n1) { return make_float2(t[n0], t[n1]); }

@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && !*abort_flag; ++p) {
           const CUtensorMap* map = p == 0 ? &map0 : &map1;
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+            if (!mbar_wait_idle(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
               set_abort(ctrl, a.status, 3002);
               break;
             }
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
+        if (!mbar_wait_idle(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }

@@ -63,6 +63,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile
   }
   return false;
 }
+// the same bounded wait for the producer and MMA roles, which mostly wait on the
+// epilogue: between polls the thread sleeps (32 ns doubling to 256 ns), so that
+// its spinning takes no issue slots from the epilogue warps of its SM
+// sub-partition
+__device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity,
+                                               volatile int* abort_flag) {
+  const long long t0 = clock64();
+  unsigned ns = 32;
+  for (long long k = 0; k < kSpinLimit; ++k) {
+    if (mbar_try(b, parity)) return true;
+    if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
+    __nanosleep(ns);
+    if (ns < 256) ns <<= 1;
+  }
+  return false;
+}
 // drain wait: bounded by time only
 __device__ __forceinline__ void mbar_wait_drain(uint64_t* b, uint32_t parity) {
   const long long t0 = clock64();
