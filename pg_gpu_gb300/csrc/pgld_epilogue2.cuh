@@ -13,6 +13,9 @@ struct float2 {
   float x, y;
 };
 inline float2 make_float2(float x, float y) { return {x, y}; }
+struct alignas(16) float4 {
+  float x, y, z, w;
+};
 #endif
 
 namespace pgld {
@@ -96,14 +99,30 @@ PGLD_HD V ijij_num4(const Pop& A, const Pop& B) {
 
 PGLD_HD V tab(const float* t, int n0, int n1) { return make_float2(t[n0], t[n1]); }
 
+// the reciprocal factors of the valid n of two lanes: 1/n, 1/(n(n-1)),
+// 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3))
+struct R2 {
+  V inv, r2, r3, r4;
+};
+// from four separate tables (eight loads)
+PGLD_HD R2 recip(const fast::Recip& T, int n0, int n1) {
+  return {tab(T.inv, n0, n1), tab(T.r2, n0, n1), tab(T.r3, n0, n1), tab(T.r4, n0, n1)};
+}
+// from one interleaved table of float4 {1/n, 1/(n(n-1)), ...} (two loads)
+PGLD_HD R2 recip(const float4* T4, int n0, int n1) {
+  const float4 a = T4[n0], b = T4[n1];
+  return {make_float2(a.x, b.x), make_float2(a.y, b.y), make_float2(a.z, b.z),
+          make_float2(a.w, b.w)};
+}
 
 // the 15 two-population statistics in moments ld_names(2) order, two pairs;
 // each value goes to sink(k, value) as soon as it is formed, so a caller that
 // only accumulates never holds all fifteen
-template <class Sink>
-PGLD_HD void stats2_to(const Pop& p, const Pop& q, const fast::Recip& T, Sink&& sink) {
-  const V r4p = tab(T.r4, p.n0, p.n1), r4q = tab(T.r4, q.n0, q.n1);
-  const V r22 = vmul(tab(T.r2, p.n0, p.n1), tab(T.r2, q.n0, q.n1));
+template <class Tab, class Sink>
+PGLD_HD void stats2_to(const Pop& p, const Pop& q, const Tab& T, Sink&& sink) {
+  const R2 rp = recip(T, p.n0, p.n1), rq = recip(T, q.n0, q.n1);
+  const V r4p = rp.r4, r4q = rq.r4;
+  const V r22 = vmul(rp.r2, rq.r2);
   sink(0, vmul(dd_num(p), r4p));
   sink(1, vmul(vmul(p.x, q.x), r22));
   sink(2, vmul(dd_num(q), r4q));
@@ -116,27 +135,29 @@ PGLD_HD void stats2_to(const Pop& p, const Pop& q, const fast::Recip& T, Sink&& 
   sink(11, vmul(vfma(vmul(p.pA, p.qA), vmul(q.pB, q.qB), vmul(vmul(q.pA, q.qA), vmul(p.pB, p.qB))),
                 vmul(vs(0.5f), r22)));
   sink(12, vmul(ijij_num4(p, q), vmul(vs(0.25f), r22)));
-  const V h31p = vmul(vs(0.5f), vmul(tab(T.r3, p.n0, p.n1), tab(T.inv, q.n0, q.n1)));
+  const V h31p = vmul(vs(0.5f), vmul(rp.r3, rq.inv));
   sink(4, vmul(vmul(p.x, vfma(p.dA, q.dB, vmul(p.dB, q.dA))), h31p));
   sink(10, vmul(triple_num2(p, q), h31p));
-  const V h31q = vmul(vs(0.5f), vmul(tab(T.r3, q.n0, q.n1), tab(T.inv, p.n0, p.n1)));
+  const V h31q = vmul(vs(0.5f), vmul(rq.r3, rp.inv));
   sink(7, vmul(vmul(q.x, vfma(q.dA, p.dB, vmul(q.dB, p.dA))), h31q));
   sink(13, vmul(triple_num2(q, p), h31q));
 }
 
-PGLD_HD void stats2(const Pop& p, const Pop& q, const fast::Recip& T, V o[15]) {
+template <class Tab>
+PGLD_HD void stats2(const Pop& p, const Pop& q, const Tab& T, V o[15]) {
   stats2_to(p, q, T, [&](int k, V v) { o[k] = v; });
 }
 
-template <class Sink>
-PGLD_HD void stats1_to(const Pop& p, const fast::Recip& T, Sink&& sink) {
-  const V r4 = tab(T.r4, p.n0, p.n1);
+template <class Tab, class Sink>
+PGLD_HD void stats1_to(const Pop& p, const Tab& T, Sink&& sink) {
+  const V r4 = recip(T, p.n0, p.n1).r4;
   sink(0, vmul(dd_num(p), r4));
   sink(1, vmul(dz_num(p), r4));
   sink(2, vmul(pi2_num(p), r4));
 }
 
-PGLD_HD void stats1(const Pop& p, const fast::Recip& T, V o[3]) {
+template <class Tab>
+PGLD_HD void stats1(const Pop& p, const Tab& T, V o[3]) {
   stats1_to(p, T, [&](int k, V v) { o[k] = v; });
 }
 

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         const int yi = (int)(lo * kRows), yj = (int)((lo + (item - a.item_off[lo])) * kRows);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait_idle(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+          if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
             set_abort(ctrl, a.status, 4002);
             break;
           }
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait_idle(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
+        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
           set_abort(ctrl, a.status, 4003);
           break;
         }

@@ -158,16 +158,49 @@ __device__ __forceinline__ void kahan_add(float2* slot, float v) {
   slot->y = __fadd_rn(slot->y, err);
 }
 
-// every lane receives the warp total of each statistic; lane s keeps stat s
+// warp totals of S <= 16 values by recursive halving (16 shuffles for S = 15
+// where a butterfly per value takes 75): each step sends the half of the values
+// that the partner lane keeps; lane l ends with the total of value
+// l >> totals_shift<S>()
 template <int S>
-__device__ __forceinline__ float warp_totals_pick(const float (&v)[S], int lane) {
-  float mine = 0.f;
+__host__ __device__ constexpr int totals_width() {
+  return S <= 1 ? 1 : S <= 2 ? 2 : S <= 4 ? 4 : S <= 8 ? 8 : 16;
+}
+template <int S>
+__host__ __device__ constexpr int totals_shift() {
+  return totals_width<S>() == 16 ? 1 : totals_width<S>() == 8 ? 2 : totals_width<S>() == 4 ? 3
+                                                               : totals_width<S>() == 2 ? 4 : 5;
+}
+template <int S>
+__device__ __forceinline__ float warp_totals(const float (&v)[S], int lane) {
+  constexpr int K = totals_width<S>();
+  static_assert(S <= 16, "at most 16 values");
+  float w[K];
 #pragma unroll
-  for (int s = 0; s < S; ++s) {
-    const float t = warp_sum(v[s]);
-    if (lane == s) mine = t;
+  for (int k = 0; k < K; ++k) w[k] = k < S ? v[k] : 0.f;
+  int off = 16;
+#pragma unroll
+  for (int h = K / 2; h >= 1; h >>= 1, off >>= 1) {
+    const bool up = (lane & off) != 0;
+#pragma unroll
+    for (int k = 0; k < h; ++k) {
+      const float send = up ? w[k] : w[k + h];
+      const float keep = up ? w[k + h] : w[k];
+      w[k] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
   }
-  return mine;
+  float t = w[0];
+#pragma unroll
+  for (; off >= 1; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+  return t;
+}
+// the warp's totals of v added to slot[0..S) (one lane per value)
+template <int S>
+__device__ __forceinline__ void warp_totals_add(const float (&v)[S], int lane, float2* slot) {
+  const float tot = warp_totals<S>(v, lane);
+  constexpr int sh = totals_shift<S>();
+  const int k = lane >> sh;
+  if ((lane & ((1 << sh) - 1)) == 0 && k < S) kahan_add(slot + k, tot);
 }
 
 // MODE kModeBinned: distance-binned moments sums of P populations;
@@ -189,12 +222,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   float2* kacc = reinterpret_cast<float2*>(thr + (kMaxBins + 2));  // [kEpiWarps][n_bins][S]
   unsigned long long* kcnt =
       reinterpret_cast<unsigned long long*>(kacc + kEpiWarps * a.n_bins * S);  // [kEpiWarps][n_bins]
-  float* tables = reinterpret_cast<float*>(kcnt + kEpiWarps * a.n_bins);     // 4 x (nmax + 1)
+  // reciprocal tables by n, 4 x (nmax + 1) floats: four arrays (1/n,
+  // 1/(n(n-1)), 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3))) for the per-pair and
+  // window modes, one interleaved float4 array for the binned mode (one load
+  // per population and pair)
+  unsigned char* tables_u8 = reinterpret_cast<unsigned char*>(kcnt + kEpiWarps * a.n_bins);
+  tables_u8 += (16 - (smem_u32(tables_u8) & 15)) & 15;  // 16-byte aligned for float4 loads
+  float* tables = reinterpret_cast<float*>(tables_u8);
   fast::Recip T;
   T.inv = tables;
   T.r2 = tables + (a.nmax + 1);
   T.r3 = tables + 2 * (a.nmax + 1);
   T.r4 = tables + 3 * (a.nmax + 1);
+  const float4* T4 = reinterpret_cast<const float4*>(tables);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_bins = a.n_bins;
@@ -227,8 +267,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) kacc[x] = make_float2(0.f, 0.f);
     for (int x = t; x < kEpiWarps * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
     for (int x = t; x <= a.nmax; x += kEpiThreads)
-      fast::recip_entry(x, tables + x, tables + (a.nmax + 1) + x, tables + 2 * (a.nmax + 1) + x,
-                        tables + 3 * (a.nmax + 1) + x);
+      if constexpr (MODE == kModeBinned)
+        fast::recip_entry(x, tables + 4 * x, tables + 4 * x + 1, tables + 4 * x + 2,
+                          tables + 4 * x + 3);
+      else
+        fast::recip_entry(x, tables + x, tables + (a.nmax + 1) + x, tables + 2 * (a.nmax + 1) + x,
+                          tables + 3 * (a.nmax + 1) + x);
     for (int x = t; MODE == kModeBinned && x <= n_bins; x += kEpiThreads) {
       const double b = a.bins[x];
       sbins[x] = b;
@@ -259,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && !*abort_flag; ++p) {
           const CUtensorMap* map = p == 0 ? &map0 : &map1;
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait_idle(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+            if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
               set_abort(ctrl, a.status, 3002);
               break;
             }
@@ -300,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait_idle(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
+        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }
@@ -513,7 +557,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         // counts of this lane's four pairs of the chunk, as exact float32:
         // plane 0 rows hold (n11, n10) of every j, plane 1 rows (n01, n00), so
-        // partner lanes swap halves and each lane owns whole pairs
+        // partner lanes swap halves and each lane owns whole pairs.  Each lane
+        // takes (c1, c2, c3, c4) = (own row, partner row): (n11, n10, n01, n00)
+        // on plane 0 and (n01, n00, n11, n10) on plane 1 -- the same pair with
+        // the alleles of SNP i relabelled in every population, under which
+        // every moments statistic (and its float32 evaluation's error bound)
+        // is invariant
         float cf[4][P][4];
 #pragma unroll
         for (int q = 0; q < 4; ++q)
@@ -521,14 +570,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int p = 0; p < P; ++p) {
             const uint32_t s0 = plane ? r[p][4 * q] : r[p][4 * q + 2];
             const uint32_t s1 = plane ? r[p][4 * q + 1] : r[p][4 * q + 3];
-            const float g0 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
-            const float g1 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
-            const float m0 = __uint_as_float(plane ? r[p][4 * q + 2] : r[p][4 * q]);
-            const float m1 = __uint_as_float(plane ? r[p][4 * q + 3] : r[p][4 * q + 1]);
-            cf[q][p][0] = plane ? g0 : m0;
-            cf[q][p][1] = plane ? g1 : m1;
-            cf[q][p][2] = plane ? m0 : g0;
-            cf[q][p][3] = plane ? m1 : g1;
+            cf[q][p][2] = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
+            cf[q][p][3] = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
+            cf[q][p][0] = __uint_as_float(plane ? r[p][4 * q + 2] : r[p][4 * q]);
+            cf[q][p][1] = __uint_as_float(plane ? r[p][4 * q + 3] : r[p][4 * q + 1]);
           }
         // two pairs per iteration (packed float2 arithmetic) over rotating
         // arrays: the statistics code is emitted once (instruction cache)
@@ -548,8 +593,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
               for (int m = 0; m < 4; ++m) cf[k][p][m] = cf[k + 2][p][m];
           float2 st[S];
-          if constexpr (P == 1) fast2::stats1(p0, T, st);
-          else fast2::stats2(p0, p1, T, st);
+          if constexpr (P == 1) fast2::stats1(p0, T4, st);
+          else fast2::stats2(p0, p1, T4, st);
           if (mode == 0) {
 #pragma unroll
             for (int s = 0; s < S; ++s) acc_lo[s] += st[s].x + st[s].y;
@@ -590,8 +635,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 float v[S];
 #pragma unroll
                 for (int s = 0; s < S; ++s) v[s] = mine ? (h ? st[s].y : st[s].x) : 0.f;
-                const float tot = warp_totals_pick<S>(v, lane);
-                if (lane < S) kahan_add(my_acc + bb * S + lane, tot);
+                warp_totals_add<S>(v, lane, my_acc + bb * S);
                 if (lane == 31) my_cnt[bb] += (unsigned long long)__popc(grp);
                 pending &= ~grp;
               }
@@ -600,12 +644,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       if (mode <= 1) {
-        const float tot = warp_totals_pick<S>(acc_lo, lane);
-        if (lane < S) kahan_add(my_acc + b0 * S + lane, tot);
+        warp_totals_add<S>(acc_lo, lane, my_acc + b0 * S);
         const int hi_total = __reduce_add_sync(0xffffffffu, n_hi);
         if (mode == 1) {
-          const float tot_hi = warp_totals_pick<S>(acc_hi, lane);
-          if (lane < S) kahan_add(my_acc + (b0 + 1) * S + lane, tot_hi);
+          warp_totals_add<S>(acc_hi, lane, my_acc + (b0 + 1) * S);
         }
         if (lane == 31) {
           my_cnt[b0] += (unsigned long long)(512 - hi_total);

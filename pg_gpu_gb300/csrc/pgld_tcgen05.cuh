@@ -43,39 +43,27 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+// try_wait that may suspend the thread for up to ns nanoseconds; the thread
+// resumes as soon as the phase completes
+__device__ __forceinline__ bool mbar_try_for(uint64_t* b, uint32_t parity, uint32_t ns) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
       " selp.u32 %0, 1, 0, p;\n}"
       : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity)
+      : "r"(smem_u32(b)), "r"(parity), "r"(ns)
       : "memory");
   return ok != 0;
 }
-// bounded wait: false once ~2 s of SM clock passed or another role aborted
+// bounded wait: false once ~2 s of SM clock passed or another role aborted.
+// Each poll may suspend the thread until the phase completes (or 20 us pass).
 constexpr long long kWaitCycles = 4000000000ll;
+constexpr uint32_t kSuspendNs = 20000;
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
   const long long t0 = clock64();
   for (long long k = 0; k < kSpinLimit; ++k) {
-    if (mbar_try(b, parity)) return true;
-    if ((k & 63) == 63 && (*abort_flag || clock64() - t0 > kWaitCycles)) return false;
-  }
-  return false;
-}
-// the same bounded wait for the producer and MMA roles, which mostly wait on the
-// epilogue: between polls the thread sleeps (32 ns doubling to 256 ns), so that
-// its spinning takes no issue slots from the epilogue warps of its SM
-// sub-partition
-__device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity,
-                                               volatile int* abort_flag) {
-  const long long t0 = clock64();
-  unsigned ns = 32;
-  for (long long k = 0; k < kSpinLimit; ++k) {
-    if (mbar_try(b, parity)) return true;
+    if (mbar_try_for(b, parity, kSuspendNs)) return true;
     if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
-    __nanosleep(ns);
-    if (ns < 256) ns <<= 1;
   }
   return false;
 }
@@ -83,8 +71,8 @@ __device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity,
 __device__ __forceinline__ void mbar_wait_drain(uint64_t* b, uint32_t parity) {
   const long long t0 = clock64();
   for (long long k = 0; k < kSpinLimit; ++k) {
-    if (mbar_try(b, parity)) return;
-    if ((k & 63) == 63 && clock64() - t0 > kWaitCycles) return;
+    if (mbar_try_for(b, parity, kSuspendNs)) return;
+    if (clock64() - t0 > kWaitCycles) return;
   }
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x,

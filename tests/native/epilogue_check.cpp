@@ -26,16 +26,16 @@ extern "C" void pgld_check_stats(const int* counts, const int* n, int N, int P, 
   }
 }
 
-// the packed two-pair form: rows k and N-1-k share one float2 evaluation
+// the packed two-pair form: rows k and N-1-k share one float2 evaluation; the
+// reciprocals come from the interleaved float4 table of the tensor-core kernel
 extern "C" void pgld_check_stats2(const int* counts, const int* n, int N, int P, float* out) {
   using namespace pgld::fast;
   namespace f2 = pgld::fast2;
   int nmax = 0;
   for (int k = 0; k < N * 2; ++k) nmax = n[k] > nmax ? n[k] : nmax;
-  std::vector<float> tab(4 * (nmax + 1));
-  for (int v = 0; v <= nmax; ++v)
-    recip_entry(v, &tab[v], &tab[(nmax + 1) + v], &tab[2 * (nmax + 1) + v], &tab[3 * (nmax + 1) + v]);
-  Recip T{&tab[0], &tab[nmax + 1], &tab[2 * (nmax + 1)], &tab[3 * (nmax + 1)]};
+  std::vector<float4> tab(nmax + 1);
+  for (int v = 0; v <= nmax; ++v) recip_entry(v, &tab[v].x, &tab[v].y, &tab[v].z, &tab[v].w);
+  const float4* T = tab.data();
   const int S = P == 1 ? 3 : 15;
   for (int k = 0; k < N; ++k) {
     const int* a = counts + 8 * k;
