@@ -8,7 +8,7 @@
 // pipes, with no integer-to-float conversions.
 //
 // Every numerator is rewritten as (at most) two products of such exact
-// integers -- e.g. DD: x (x + c2 + c3 - 1) - c1c4 (n - 2), pi2:
+// integers -- e.g. DD: x (x + c2 + c3) - c1c4 n + (c1c4 + c2c3), pi2:
 // c1c4 (n^2 - 4n + 2) + x (x + n - 1 - (n - 2)(c1 + c4)) -- and evaluated
 // with Kahan's algorithm for a*b + c*d (the rounding error of c*d recovered
 // exactly by an fma, one fma and one addition more), whose relative error is
@@ -17,7 +17,8 @@
 // determinants", Math. Comp. 82, 2013).  The one numerator with three
 // products, pi2(i,j,i,j), sums its two cubic products exactly as s + t
 // (TwoProduct / TwoSum: the low parts are integers below 2^22 and add exactly)
-// before one fma adds the quartic product, so it carries at most 3u.
+// before one fma adds the quartic product, so it carries at most 3u (DD
+// likewise, its exact integer remainder added last).
 // 64-bit integer multiplies would run at the float64 rate on GB300.
 // Denominators come from per-CTA tables of reciprocals indexed by the valid
 // sample size n (1/n, 1/(n(n-1)), 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3)), each
@@ -147,9 +148,15 @@ PGLD_HD Pop make(float c1, float c2, float c3, float c4) {
 }
 
 // c1(c1-1)c4(c4-1) + c2(c2-1)c3(c3-1) - 2c1c2c3c4
-//   = x^2 - a(c1+c4-1) - b(c2+c3-1) = x (x + c2 + c3 - 1) + a (2 - n)
-// (n = the sum of the four counts; b = a - x)
-PGLD_HD float dd_num(const Pop& p) { return dot2(p.x, (p.x + p.s) - 1.0f, p.a, 2.0f - p.ns); }
+//   = x^2 - a(c1+c4-1) - b(c2+c3-1) = x (x + c2 + c3) - a n + (a + b)
+// (n = the sum of the four counts; b = a - x).  With w = RN(a n) and its exact
+// error e, x (x + c2 + c3) - w is an integer rounded once by the fma (exactly
+// when below 2^24) and a + b - e is exact (< 2^23), so the value is within 3u.
+PGLD_HD float dd_num(const Pop& p) {
+  const float w = fmul(p.a, p.ns);
+  const float e = fmaf(p.a, p.ns, -w);
+  return fadd(fmaf(p.x, p.x + p.s, -w), (p.a + p.b) - e);
+}
 // x*(dA*dB + e) + 2(a+b): the fma rounds once, and whenever the two terms can
 // cancel the product is below 2^24 and exact
 PGLD_HD float dz_num(const Pop& p) { return fmaf(p.x, p.dA * p.dB + p.e, 2.0f * (p.a + p.b)); }

@@ -35,9 +35,9 @@ PGLD_HD V vfma(V a, V b, V c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y
 #endif
 PGLD_HD V vneg(V a) { return make_float2(-a.x, -a.y); }
 PGLD_HD V vs(float a) { return make_float2(a, a); }
-// a - b as one fused operation: b * (-1) is exact, so the sum rounds once,
-// exactly like a correctly rounded subtraction
-PGLD_HD V vsub(V a, V b) { return vfma(b, vs(-1.0f), a); }
+// a - b: the negation is exact, so the sum rounds once, exactly like a
+// correctly rounded subtraction
+PGLD_HD V vsub(V a, V b) { return vadd(a, vneg(b)); }
 
 // a*b + c*d with relative error <= 2u (Kahan's algorithm, as fast::dot2)
 PGLD_HD V dot2(V a, V b, V c, V d) {
@@ -71,24 +71,30 @@ PGLD_HD Pop make(V c1, V c2, V c3, V c4) {
 }
 
 PGLD_HD V dd_num(const Pop& p) {
-  return dot2(p.x, vsub(vadd(p.x, p.s), vs(1.0f)), p.a, vsub(vs(2.0f), p.ns));
+  const V w = vmul(p.a, p.ns);
+  const V e = vfma(p.a, p.ns, vneg(w));
+  return vadd(vfma(p.x, vadd(p.x, p.s), vneg(w)), vsub(vadd(p.a, p.b), e));
 }
-PGLD_HD V dz_num(const Pop& p) {
-  return vfma(p.x, vfma(p.dA, p.dB, p.e), vmul(vs(2.0f), vadd(p.a, p.b)));
+// w = dA dB + e (exact), shared with the cross terms Dz(i,j,j)
+PGLD_HD V dz_num(const Pop& p, V w) {
+  const V ab = vadd(p.a, p.b);
+  return vfma(p.x, w, vadd(ab, ab));
 }
 PGLD_HD V pi2_num(const Pop& p) {
   const V pn = vfma(p.ns, vsub(p.ns, vs(4.0f)), vs(2.0f));
   const V w = vfma(vsub(vs(2.0f), p.ns), p.t, vadd(p.x, vsub(p.ns, vs(1.0f))));
   return dot2(p.a, pn, p.x, w);
 }
-PGLD_HD V triple_num2(const Pop& t, const Pop& s) {
-  return dot2(vmul(t.pA, t.qA), vfma(vs(-2.0f), s.qB, vfma(t.qB, s.pB, vmul(t.pB, s.qB))),
+// uA = pA qA of population t
+PGLD_HD V triple_num2(const Pop& t, const Pop& s, V uA) {
+  return dot2(uA, vsub(vfma(t.qB, s.pB, vmul(t.pB, s.qB)), vadd(s.qB, s.qB)),
               vfma(t.pA, t.c4, vmul(t.c2, t.qA)), vsub(s.qB, s.pB));
 }
 PGLD_HD V ijij_num4(const Pop& A, const Pop& B) {
   const V K = vfma(A.c1, B.c4, vfma(A.c2, B.c3, vfma(A.c3, B.c2, vmul(A.c4, B.c1))));
   const V mA = vsub(A.ns, vs(1.0f)), mB = vsub(B.ns, vs(1.0f));
-  const V y1 = vmul(mA, A.e), y2 = vfma(mB, B.e, vmul(vs(4.0f), B.x));
+  const V x2 = vadd(B.x, B.x);
+  const V y1 = vmul(mA, A.e), y2 = vfma(mB, B.e, vadd(x2, x2));
   const V p1 = vmul(B.x, y1), e1 = vfma(B.x, y1, vneg(p1));
   const V p2 = vmul(A.x, y2), e2 = vfma(A.x, y2, vneg(p2));
   const V s = vadd(p1, p2);
@@ -97,68 +103,60 @@ PGLD_HD V ijij_num4(const Pop& A, const Pop& B) {
   return vadd(vfma(K, vmul(mA, mB), s), t);
 }
 
-PGLD_HD V tab(const float* t, int n0, int n1) { return make_float2(t[n0], t[n1]); }
-
 // the reciprocal factors of the valid n of two lanes: 1/n, 1/(n(n-1)),
-// 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3))
+// 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3)), from one interleaved table of float4
 struct R2 {
   V inv, r2, r3, r4;
 };
-// from four separate tables (eight loads)
-PGLD_HD R2 recip(const fast::Recip& T, int n0, int n1) {
-  return {tab(T.inv, n0, n1), tab(T.r2, n0, n1), tab(T.r3, n0, n1), tab(T.r4, n0, n1)};
-}
-// from one interleaved table of float4 {1/n, 1/(n(n-1)), ...} (two loads)
 PGLD_HD R2 recip(const float4* T4, int n0, int n1) {
   const float4 a = T4[n0], b = T4[n1];
   return {make_float2(a.x, b.x), make_float2(a.y, b.y), make_float2(a.z, b.z),
           make_float2(a.w, b.w)};
 }
 
-// the 15 two-population statistics in moments ld_names(2) order, two pairs;
-// each value goes to sink(k, value) as soon as it is formed, so a caller that
-// only accumulates never holds all fifteen
-template <class Tab, class Sink>
-PGLD_HD void stats2_to(const Pop& p, const Pop& q, const Tab& T, Sink&& sink) {
-  const R2 rp = recip(T, p.n0, p.n1), rq = recip(T, q.n0, q.n1);
-  const V r4p = rp.r4, r4q = rq.r4;
+// the 15 two-population statistics in moments ld_names(2) order, two pairs:
+// statistic k = num * scale goes to sink(k, num, scale) as soon as it is
+// formed (a caller that accumulates fuses the product into its sums)
+template <class Sink>
+PGLD_HD void stats2_to(const Pop& p, const Pop& q, const float4* T4, Sink&& sink) {
+  const R2 rp = recip(T4, p.n0, p.n1), rq = recip(T4, q.n0, q.n1);
   const V r22 = vmul(rp.r2, rq.r2);
-  sink(0, vmul(dd_num(p), r4p));
-  sink(1, vmul(vmul(p.x, q.x), r22));
-  sink(2, vmul(dd_num(q), r4q));
-  sink(3, vmul(dz_num(p), r4p));
-  sink(8, vmul(dz_num(q), r4q));
-  sink(9, vmul(pi2_num(p), r4p));
-  sink(14, vmul(pi2_num(q), r4q));
-  sink(5, vmul(vmul(p.x, vfma(q.dB, q.dA, q.e)), r22));
-  sink(6, vmul(vmul(q.x, vfma(p.dB, p.dA, p.e)), r22));
-  sink(11, vmul(vfma(vmul(p.pA, p.qA), vmul(q.pB, q.qB), vmul(vmul(q.pA, q.qA), vmul(p.pB, p.qB))),
-                vmul(vs(0.5f), r22)));
-  sink(12, vmul(ijij_num4(p, q), vmul(vs(0.25f), r22)));
+  const V wp = vfma(p.dA, p.dB, p.e), wq = vfma(q.dA, q.dB, q.e);
+  sink(0, dd_num(p), rp.r4);
+  sink(1, vmul(p.x, q.x), r22);
+  sink(2, dd_num(q), rq.r4);
+  sink(3, dz_num(p, wp), rp.r4);
+  sink(8, dz_num(q, wq), rq.r4);
+  sink(9, pi2_num(p), rp.r4);
+  sink(14, pi2_num(q), rq.r4);
+  sink(5, vmul(p.x, wq), r22);
+  sink(6, vmul(q.x, wp), r22);
+  const V uAp = vmul(p.pA, p.qA), uAq = vmul(q.pA, q.qA);
+  sink(11, vfma(uAp, vmul(q.pB, q.qB), vmul(uAq, vmul(p.pB, p.qB))), vmul(vs(0.5f), r22));
+  sink(12, ijij_num4(p, q), vmul(vs(0.25f), r22));
+  const V dc = vfma(p.dA, q.dB, vmul(p.dB, q.dA));
   const V h31p = vmul(vs(0.5f), vmul(rp.r3, rq.inv));
-  sink(4, vmul(vmul(p.x, vfma(p.dA, q.dB, vmul(p.dB, q.dA))), h31p));
-  sink(10, vmul(triple_num2(p, q), h31p));
+  sink(4, vmul(p.x, dc), h31p);
+  sink(10, triple_num2(p, q, uAp), h31p);
   const V h31q = vmul(vs(0.5f), vmul(rq.r3, rp.inv));
-  sink(7, vmul(vmul(q.x, vfma(q.dA, p.dB, vmul(q.dB, p.dA))), h31q));
-  sink(13, vmul(triple_num2(q, p), h31q));
+  sink(7, vmul(q.x, dc), h31q);
+  sink(13, triple_num2(q, p, uAq), h31q);
 }
 
-template <class Tab>
-PGLD_HD void stats2(const Pop& p, const Pop& q, const Tab& T, V o[15]) {
-  stats2_to(p, q, T, [&](int k, V v) { o[k] = v; });
+PGLD_HD void stats2(const Pop& p, const Pop& q, const float4* T4, V o[15]) {
+  stats2_to(p, q, T4, [&](int k, V num, V sc) { o[k] = vmul(num, sc); });
 }
 
-template <class Tab, class Sink>
-PGLD_HD void stats1_to(const Pop& p, const Tab& T, Sink&& sink) {
-  const V r4 = recip(T, p.n0, p.n1).r4;
-  sink(0, vmul(dd_num(p), r4));
-  sink(1, vmul(dz_num(p), r4));
-  sink(2, vmul(pi2_num(p), r4));
+template <class Sink>
+PGLD_HD void stats1_to(const Pop& p, const float4* T4, Sink&& sink) {
+  const V r4 = recip(T4, p.n0, p.n1).r4;
+  sink(0, dd_num(p), r4);
+  sink(1, dz_num(p, vfma(p.dA, p.dB, p.e)), r4);
+  sink(2, pi2_num(p), r4);
 }
 
-template <class Tab>
-PGLD_HD void stats1(const Pop& p, const Tab& T, V o[3]) {
-  stats1_to(p, T, [&](int k, V v) { o[k] = v; });
+PGLD_HD void stats1(const Pop& p, const float4* T4, V o[3]) {
+  stats1_to(p, T4, [&](int k, V num, V sc) { o[k] = vmul(num, sc); });
 }
 
 }  // namespace fast2

@@ -538,121 +538,143 @@ __global__ void __launch_bounds__(kThreads, 1)
         continue;
       }
 
-      // bin accumulators of the warp's sub-tile
-      float acc_lo[S], acc_hi[S];
-#pragma unroll
-      for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
-      int n_hi = 0;
+      // the warp's sub-tile: 4 chunks of 8 SNPs j, each two steps of two
+      // pairs per lane; body(c, qq, p0, p1) gets the packed counts of a step
+      auto steps = [&](auto&& body) {
 #pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        uint32_t r[P][16];
-        const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
+        for (int c = 0; c < 4; ++c) {
+          uint32_t r[P][16];
+          const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
 #pragma unroll
-        for (int p = 0; p < P; ++p) tmem_ld16(tmem_base + lane_base + col + p * 128, r[p]);
-        tmem_wait_ld();
-        if (c == 3) {
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
-        }
-        // counts of this lane's four pairs of the chunk, as exact float32:
-        // plane 0 rows hold (n11, n10) of every j, plane 1 rows (n01, n00), so
-        // partner lanes swap halves and each lane owns whole pairs.  Each lane
-        // takes (c1, c2, c3, c4) = (own row, partner row): (n11, n10, n01, n00)
-        // on plane 0 and (n01, n00, n11, n10) on plane 1 -- the same pair with
-        // the alleles of SNP i relabelled in every population, under which
-        // every moments statistic (and its float32 evaluation's error bound)
-        // is invariant
-        float cf[4][P][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int p = 0; p < P; ++p) {
-            const uint32_t s0 = plane ? r[p][4 * q] : r[p][4 * q + 2];
-            const uint32_t s1 = plane ? r[p][4 * q + 1] : r[p][4 * q + 3];
-            cf[q][p][2] = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
-            cf[q][p][3] = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
-            cf[q][p][0] = __uint_as_float(plane ? r[p][4 * q + 2] : r[p][4 * q]);
-            cf[q][p][1] = __uint_as_float(plane ? r[p][4 * q + 3] : r[p][4 * q + 1]);
+          for (int p = 0; p < P; ++p) tmem_ld16(tmem_base + lane_base + col + p * 128, r[p]);
+          tmem_wait_ld();
+          if (c == 3) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
           }
-        // two pairs per iteration (packed float2 arithmetic) over rotating
-        // arrays: the statistics code is emitted once (instruction cache)
-#pragma unroll 1
-        for (int qq = 0; qq < 2; ++qq) {
-          const fast2::Pop p0 = fast2::make(
-              make_float2(cf[0][0][0], cf[1][0][0]), make_float2(cf[0][0][1], cf[1][0][1]),
-              make_float2(cf[0][0][2], cf[1][0][2]), make_float2(cf[0][0][3], cf[1][0][3]));
-          const fast2::Pop p1 = fast2::make(make_float2(cf[0][P - 1][0], cf[1][P - 1][0]),
-                                            make_float2(cf[0][P - 1][1], cf[1][P - 1][1]),
-                                            make_float2(cf[0][P - 1][2], cf[1][P - 1][2]),
-                                            make_float2(cf[0][P - 1][3], cf[1][P - 1][3]));
+          // counts of this lane's four pairs of the chunk, as exact float32:
+          // plane 0 rows hold (n11, n10) of every j, plane 1 rows (n01, n00),
+          // so partner lanes swap halves and each lane owns whole pairs.  Each
+          // lane takes (c1, c2, c3, c4) = (own row, partner row): (n11, n10,
+          // n01, n00) on plane 0 and (n01, n00, n11, n10) on plane 1 -- the
+          // same pair with the alleles of SNP i relabelled in every
+          // population, under which every moments statistic (and its float32
+          // evaluation's error bound) is invariant.  cf[h][p][m]: count m of
+          // population p for the lane's pairs q = 2h (.x) and q = 2h + 1 (.y)
+          float2 cf[2][P][4];
 #pragma unroll
-          for (int k = 0; k < 2; ++k)
+          for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int p = 0; p < P; ++p)
-#pragma unroll
-              for (int m = 0; m < 4; ++m) cf[k][p][m] = cf[k + 2][p][m];
-          float2 st[S];
-          if constexpr (P == 1) fast2::stats1(p0, T4, st);
-          else fast2::stats2(p0, p1, T4, st);
-          if (mode == 0) {
-#pragma unroll
-            for (int s = 0; s < S; ++s) acc_lo[s] += st[s].x + st[s].y;
-          } else if (mode == 1) {
-            const long long ja = j0 + half * 32 + c * 8 + 4 * qq + plane;
-            const bool up0 = (a.ipos[ja] - ipos_i) >= thr_mid;
-            const bool up1 = (a.ipos[ja + 2] - ipos_i) >= thr_mid;
-            const float2 fu = make_float2(up0 ? 1.f : 0.f, up1 ? 1.f : 0.f);
-            const float2 fl = make_float2(up0 ? 0.f : 1.f, up1 ? 0.f : 1.f);
-            n_hi += (up0 ? 1 : 0) + (up1 ? 1 : 0);
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-              acc_hi[s] = fmaf(fu.x, st[s].x, fmaf(fu.y, st[s].y, acc_hi[s]));
-              acc_lo[s] = fmaf(fl.x, st[s].x, fmaf(fl.y, st[s].y, acc_lo[s]));
-            }
-          } else {
-#pragma unroll 1
-            for (int h = 0; h < 2; ++h) {
-              const int jl = half * 32 + c * 8 + 2 * (2 * qq + h) + plane;
-              const long long j = j0 + jl;
-              bool ok = (i < j) && (j < a.n_snp);
-              int b = -1;
-              if (use_int) {
-                const int d = ok ? a.ipos[j] - ipos_i : 0;
-                if (ok && d <= maxd_int) b = bin_of_int(thr, n_bins, d);
-              } else if (ok) {
-                const double dp = a.pos[j] - a.pos[i];
-                if (dp <= maxd) {
-                  const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
-                  b = bin_of_f64(sbins, n_bins, d);
-                }
-              }
-              unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
-              while (pending) {
-                const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
-                const bool mine = (b == bb);
-                const unsigned grp = __ballot_sync(0xffffffffu, mine);
-                float v[S];
-#pragma unroll
-                for (int s = 0; s < S; ++s) v[s] = mine ? (h ? st[s].y : st[s].x) : 0.f;
-                warp_totals_add<S>(v, lane, my_acc + bb * S);
-                if (lane == 31) my_cnt[bb] += (unsigned long long)__popc(grp);
-                pending &= ~grp;
+            for (int p = 0; p < P; ++p) {
+              const uint32_t s0 = plane ? r[p][4 * q] : r[p][4 * q + 2];
+              const uint32_t s1 = plane ? r[p][4 * q + 1] : r[p][4 * q + 3];
+              const float v2 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
+              const float v3 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
+              const float v0 = __uint_as_float(plane ? r[p][4 * q + 2] : r[p][4 * q]);
+              const float v1 = __uint_as_float(plane ? r[p][4 * q + 3] : r[p][4 * q + 1]);
+              if (q & 1) {
+                cf[q >> 1][p][0].y = v0; cf[q >> 1][p][1].y = v1;
+                cf[q >> 1][p][2].y = v2; cf[q >> 1][p][3].y = v3;
+              } else {
+                cf[q >> 1][p][0].x = v0; cf[q >> 1][p][1].x = v1;
+                cf[q >> 1][p][2].x = v2; cf[q >> 1][p][3].x = v3;
               }
             }
+#pragma unroll
+          for (int qq = 0; qq < 2; ++qq) {
+            const fast2::Pop p0 =
+                fast2::make(cf[qq][0][0], cf[qq][0][1], cf[qq][0][2], cf[qq][0][3]);
+            const fast2::Pop p1 = fast2::make(cf[qq][P - 1][0], cf[qq][P - 1][1],
+                                              cf[qq][P - 1][2], cf[qq][P - 1][3]);
+            body(c, qq, p0, p1);
           }
         }
-      }
-      if (mode <= 1) {
+      };
+      auto stats_of = [&](const fast2::Pop& p0, const fast2::Pop& p1, float2 (&st)[S]) {
+        if constexpr (P == 1) fast2::stats1(p0, T4, st);
+        else fast2::stats2(p0, p1, T4, st);
+      };
+
+      if (mode == 0) {
+        // one bin: packed sums, each statistic's reciprocal factor fused into
+        // its running sum
+        float2 acc2[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) acc2[s] = make_float2(0.f, 0.f);
+        steps([&](int, int, const fast2::Pop& p0, const fast2::Pop& p1) {
+          auto sink = [&](int k, float2 num, float2 sc) { acc2[k] = fast2::vfma(num, sc, acc2[k]); };
+          if constexpr (P == 1) fast2::stats1_to(p0, T4, sink);
+          else fast2::stats2_to(p0, p1, T4, sink);
+        });
+        float v[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) v[s] = acc2[s].x + acc2[s].y;
+        warp_totals_add<S>(v, lane, my_acc + b0 * S);
+        if (lane == 31) my_cnt[b0] += 512ull;
+      } else if (mode == 1) {
+        // two adjacent bins split at thr_mid: weighted sums of both
+        float acc_lo[S], acc_hi[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
+        int n_hi = 0;
+        steps([&](int c, int qq, const fast2::Pop& p0, const fast2::Pop& p1) {
+          const long long ja = j0 + half * 32 + c * 8 + 4 * qq + plane;
+          const bool up0 = (a.ipos[ja] - ipos_i) >= thr_mid;
+          const bool up1 = (a.ipos[ja + 2] - ipos_i) >= thr_mid;
+          const float2 fu = make_float2(up0 ? 1.f : 0.f, up1 ? 1.f : 0.f);
+          const float2 fl = make_float2(up0 ? 0.f : 1.f, up1 ? 0.f : 1.f);
+          n_hi += (up0 ? 1 : 0) + (up1 ? 1 : 0);
+          auto sink = [&](int k, float2 num, float2 sc) {
+            const float2 st = fast2::vmul(num, sc);
+            acc_hi[k] = fmaf(fu.x, st.x, fmaf(fu.y, st.y, acc_hi[k]));
+            acc_lo[k] = fmaf(fl.x, st.x, fmaf(fl.y, st.y, acc_lo[k]));
+          };
+          if constexpr (P == 1) fast2::stats1_to(p0, T4, sink);
+          else fast2::stats2_to(p0, p1, T4, sink);
+        });
         warp_totals_add<S>(acc_lo, lane, my_acc + b0 * S);
+        warp_totals_add<S>(acc_hi, lane, my_acc + (b0 + 1) * S);
         const int hi_total = __reduce_add_sync(0xffffffffu, n_hi);
-        if (mode == 1) {
-          warp_totals_add<S>(acc_hi, lane, my_acc + (b0 + 1) * S);
-        }
         if (lane == 31) {
           my_cnt[b0] += (unsigned long long)(512 - hi_total);
-          if (mode == 1) my_cnt[b0 + 1] += (unsigned long long)hi_total;
+          my_cnt[b0 + 1] += (unsigned long long)hi_total;
         }
+      } else {
+        // general: each pair's own bin (or none)
+        steps([&](int c, int qq, const fast2::Pop& p0, const fast2::Pop& p1) {
+          float2 st[S];
+          stats_of(p0, p1, st);
+#pragma unroll 1
+          for (int h = 0; h < 2; ++h) {
+            const int jl = half * 32 + c * 8 + 2 * (2 * qq + h) + plane;
+            const long long j = j0 + jl;
+            bool ok = (i < j) && (j < a.n_snp);
+            int b = -1;
+            if (use_int) {
+              const int d = ok ? a.ipos[j] - ipos_i : 0;
+              if (ok && d <= maxd_int) b = bin_of_int(thr, n_bins, d);
+            } else if (ok) {
+              const double dp = a.pos[j] - a.pos[i];
+              if (dp <= maxd) {
+                const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
+                b = bin_of_f64(sbins, n_bins, d);
+              }
+            }
+            unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
+            while (pending) {
+              const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
+              const bool mine = (b == bb);
+              const unsigned grp = __ballot_sync(0xffffffffu, mine);
+              float v[S];
+#pragma unroll
+              for (int s = 0; s < S; ++s) v[s] = mine ? (h ? st[s].y : st[s].x) : 0.f;
+              warp_totals_add<S>(v, lane, my_acc + bb * S);
+              if (lane == 31) my_cnt[bb] += (unsigned long long)__popc(grp);
+              pending &= ~grp;
+            }
+          }
+        });
       }
     }
   }
