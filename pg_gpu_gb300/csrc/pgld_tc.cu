@@ -641,26 +641,73 @@ __global__ void __launch_bounds__(kThreads, 1)
           my_cnt[b0 + 1] += (unsigned long long)hi_total;
         }
       } else {
-        // general: each pair's own bin (or none)
+        // general (diagonal and band-edge tiles, short distances): the bins
+        // of the lane's two pairs per step (-1: none).  A step whose pairs
+        // fall in at most two adjacent bins goes to running sums of bins
+        // (key, key + 1), added to the warp's slots when the key changes; a
+        // step without any pair in a bin is skipped; other steps take one warp
+        // reduction per bin.
+        float acc_lo[S], acc_hi[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
+        int key = -1, n_lo = 0, n_hi = 0;
+        auto flush = [&]() {
+          if (key < 0) return;
+          warp_totals_add<S>(acc_lo, lane, my_acc + key * S);
+          const int tl = __reduce_add_sync(0xffffffffu, n_lo);
+          const int th = __reduce_add_sync(0xffffffffu, n_hi);
+          if (th) warp_totals_add<S>(acc_hi, lane, my_acc + (key + 1) * S);
+          if (lane == 31) {
+            my_cnt[key] += (unsigned long long)tl;
+            if (th) my_cnt[key + 1] += (unsigned long long)th;
+          }
+#pragma unroll
+          for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
+          n_lo = n_hi = 0;
+          key = -1;
+        };
+        auto bin_of = [&](long long j) -> int {
+          if (!(i < j && j < a.n_snp)) return -1;
+          if (use_int) {
+            const int d = a.ipos[j] - ipos_i;
+            return d <= maxd_int ? bin_of_int(thr, n_bins, d) : -1;
+          }
+          const double dp = a.pos[j] - a.pos[i];
+          if (!(dp <= maxd)) return -1;
+          const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
+          return bin_of_f64(sbins, n_bins, d);
+        };
         steps([&](int c, int qq, const fast2::Pop& p0, const fast2::Pop& p1) {
+          const long long jx = j0 + half * 32 + c * 8 + 4 * qq + plane;
+          const int bx = bin_of(jx), by = bin_of(jx + 2);
+          const int lo = min(bx < 0 ? 0x7fffffff : bx, by < 0 ? 0x7fffffff : by);
+          const int mn = __reduce_min_sync(0xffffffffu, lo);
+          const int mx = __reduce_max_sync(0xffffffffu, max(bx, by));
+          if (mx < 0) return;
+          if (mx - mn <= 1) {
+            if (mn != key) {
+              flush();
+              key = mn;
+            }
+            const float2 fl = make_float2(bx == key ? 1.f : 0.f, by == key ? 1.f : 0.f);
+            const float2 fu = make_float2(bx == key + 1 ? 1.f : 0.f, by == key + 1 ? 1.f : 0.f);
+            n_lo += (bx == key ? 1 : 0) + (by == key ? 1 : 0);
+            n_hi += (bx == key + 1 ? 1 : 0) + (by == key + 1 ? 1 : 0);
+            auto sink = [&](int k, float2 num, float2 sc) {
+              const float2 st = fast2::vmul(num, sc);
+              acc_hi[k] = fmaf(fu.x, st.x, fmaf(fu.y, st.y, acc_hi[k]));
+              acc_lo[k] = fmaf(fl.x, st.x, fmaf(fl.y, st.y, acc_lo[k]));
+            };
+            if constexpr (P == 1) fast2::stats1_to(p0, T4, sink);
+            else fast2::stats2_to(p0, p1, T4, sink);
+            return;
+          }
+          flush();  // (the running sums are zero while the step's values live)
           float2 st[S];
           stats_of(p0, p1, st);
 #pragma unroll 1
           for (int h = 0; h < 2; ++h) {
-            const int jl = half * 32 + c * 8 + 2 * (2 * qq + h) + plane;
-            const long long j = j0 + jl;
-            bool ok = (i < j) && (j < a.n_snp);
-            int b = -1;
-            if (use_int) {
-              const int d = ok ? a.ipos[j] - ipos_i : 0;
-              if (ok && d <= maxd_int) b = bin_of_int(thr, n_bins, d);
-            } else if (ok) {
-              const double dp = a.pos[j] - a.pos[i];
-              if (dp <= maxd) {
-                const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
-                b = bin_of_f64(sbins, n_bins, d);
-              }
-            }
+            const int b = h ? by : bx;
             unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
             while (pending) {
               const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
@@ -675,6 +722,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         });
+        flush();
       }
     }
   }
