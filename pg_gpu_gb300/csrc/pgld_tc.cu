@@ -425,7 +425,6 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       }
-      const int ipos_i = (MODE != kModeWindows && use_int && i < a.n_snp) ? a.ipos[i] : 0;
 
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
@@ -538,59 +537,48 @@ __global__ void __launch_bounds__(kThreads, 1)
         continue;
       }
 
-      // the warp's sub-tile: 4 chunks of 8 SNPs j, each two steps of two
-      // pairs per lane; body(c, qq, p0, p1) gets the packed counts of a step
+      // the warp's sub-tile (16 SNPs i x 32 SNPs j) in 8 steps of 8 x 8 SNPs,
+      // two pairs per lane.  The binned operand rows are grouped by 8 SNPs
+      // (row 16g + k: SNP 8g + k plane 0; row 16g + 8 + k: plane 1), so a
+      // 16x256b TMEM load gives thread t both planes of SNP i = t / 4 of its
+      // 8-SNP row group against SNPs j = 2 (t % 4) and 2 (t % 4) + 1 of an
+      // 8-SNP column group: (n11, n11, n01, n01) from the columns of plane 0
+      // and (n10, n10, n00, n00) from those of plane 1 -- each count already
+      // the float2 (.x: j even, .y: j odd) of the packed epilogue.
+      // body(hh, g, p0, p1): row half hh (SNPs 8 hh + t / 4), column group g
       auto steps = [&](auto&& body) {
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
+          const int hh = c & 1, gp = c >> 1;
           uint32_t r[P][16];
-          const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
+          const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32 + hh * 16) << 16) +
+                                 (uint32_t)(acc * 256 + half * 64 + gp * 32);
 #pragma unroll
-          for (int p = 0; p < P; ++p) tmem_ld16(tmem_base + lane_base + col + p * 128, r[p]);
+          for (int p = 0; p < P; ++p) tmem_ld16x256_x4(taddr + p * 128, r[p]);
           tmem_wait_ld();
           if (c == 3) {
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
           }
-          // counts of this lane's four pairs of the chunk, as exact float32:
-          // plane 0 rows hold (n11, n10) of every j, plane 1 rows (n01, n00),
-          // so partner lanes swap halves and each lane owns whole pairs.  Each
-          // lane takes (c1, c2, c3, c4) = (own row, partner row): (n11, n10,
-          // n01, n00) on plane 0 and (n01, n00, n11, n10) on plane 1 -- the
-          // same pair with the alleles of SNP i relabelled in every
-          // population, under which every moments statistic (and its float32
-          // evaluation's error bound) is invariant.  cf[h][p][m]: count m of
-          // population p for the lane's pairs q = 2h (.x) and q = 2h + 1 (.y)
-          float2 cf[2][P][4];
+          auto u2 = [](uint32_t x, uint32_t y) { return make_float2(__uint_as_float(x), __uint_as_float(y)); };
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int p = 0; p < P; ++p) {
-              const uint32_t s0 = plane ? r[p][4 * q] : r[p][4 * q + 2];
-              const uint32_t s1 = plane ? r[p][4 * q + 1] : r[p][4 * q + 3];
-              const float v2 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
-              const float v3 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
-              const float v0 = __uint_as_float(plane ? r[p][4 * q + 2] : r[p][4 * q]);
-              const float v1 = __uint_as_float(plane ? r[p][4 * q + 3] : r[p][4 * q + 1]);
-              if (q & 1) {
-                cf[q >> 1][p][0].y = v0; cf[q >> 1][p][1].y = v1;
-                cf[q >> 1][p][2].y = v2; cf[q >> 1][p][3].y = v3;
-              } else {
-                cf[q >> 1][p][0].x = v0; cf[q >> 1][p][1].x = v1;
-                cf[q >> 1][p][2].x = v2; cf[q >> 1][p][3].x = v3;
-              }
-            }
-#pragma unroll
-          for (int qq = 0; qq < 2; ++qq) {
-            const fast2::Pop p0 =
-                fast2::make(cf[qq][0][0], cf[qq][0][1], cf[qq][0][2], cf[qq][0][3]);
-            const fast2::Pop p1 = fast2::make(cf[qq][P - 1][0], cf[qq][P - 1][1],
-                                              cf[qq][P - 1][2], cf[qq][P - 1][3]);
-            body(c, qq, p0, p1);
+          for (int g = 0; g < 2; ++g) {
+            const int o = 8 * g;
+            const fast2::Pop p0 = fast2::make(u2(r[0][o], r[0][o + 1]), u2(r[0][o + 4], r[0][o + 5]),
+                                              u2(r[0][o + 2], r[0][o + 3]), u2(r[0][o + 6], r[0][o + 7]));
+            const fast2::Pop p1 =
+                fast2::make(u2(r[P - 1][o], r[P - 1][o + 1]), u2(r[P - 1][o + 4], r[P - 1][o + 5]),
+                            u2(r[P - 1][o + 2], r[P - 1][o + 3]), u2(r[P - 1][o + 6], r[P - 1][o + 7]));
+            body(hh, 2 * gp + g, p0, p1);
           }
         }
       };
+      // the lane's SNP i of row half hh and first SNP j of column group g
+      const long long ib = i0 + 16 * quarter + (lane >> 2);
+      const int ipos_b0 = (use_int && ib < a.n_snp) ? a.ipos[ib] : 0;
+      const int ipos_b1 = (use_int && ib + 8 < a.n_snp) ? a.ipos[ib + 8] : 0;
+      auto jx_of = [&](int g) { return j0 + 32 * half + 8 * g + 2 * (lane & 3); };
       auto stats_of = [&](const fast2::Pop& p0, const fast2::Pop& p1, float2 (&st)[S]) {
         if constexpr (P == 1) fast2::stats1(p0, T4, st);
         else fast2::stats2(p0, p1, T4, st);
@@ -618,10 +606,11 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
         int n_hi = 0;
-        steps([&](int c, int qq, const fast2::Pop& p0, const fast2::Pop& p1) {
-          const long long ja = j0 + half * 32 + c * 8 + 4 * qq + plane;
-          const bool up0 = (a.ipos[ja] - ipos_i) >= thr_mid;
-          const bool up1 = (a.ipos[ja + 2] - ipos_i) >= thr_mid;
+        steps([&](int hh, int g, const fast2::Pop& p0, const fast2::Pop& p1) {
+          const long long ja = jx_of(g);
+          const int ipi = hh ? ipos_b1 : ipos_b0;
+          const bool up0 = (a.ipos[ja] - ipi) >= thr_mid;
+          const bool up1 = (a.ipos[ja + 1] - ipi) >= thr_mid;
           const float2 fu = make_float2(up0 ? 1.f : 0.f, up1 ? 1.f : 0.f);
           const float2 fl = make_float2(up0 ? 0.f : 1.f, up1 ? 0.f : 1.f);
           n_hi += (up0 ? 1 : 0) + (up1 ? 1 : 0);
@@ -666,20 +655,22 @@ __global__ void __launch_bounds__(kThreads, 1)
           n_lo = n_hi = 0;
           key = -1;
         };
-        auto bin_of = [&](long long j) -> int {
-          if (!(i < j && j < a.n_snp)) return -1;
+        auto bin_of = [&](long long is, int ipi, long long j) -> int {
+          if (!(is < j && j < a.n_snp)) return -1;
           if (use_int) {
-            const int d = a.ipos[j] - ipos_i;
+            const int d = a.ipos[j] - ipi;
             return d <= maxd_int ? bin_of_int(thr, n_bins, d) : -1;
           }
-          const double dp = a.pos[j] - a.pos[i];
+          const double dp = a.pos[j] - a.pos[is];
           if (!(dp <= maxd)) return -1;
-          const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[i]) : dp;
+          const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[is]) : dp;
           return bin_of_f64(sbins, n_bins, d);
         };
-        steps([&](int c, int qq, const fast2::Pop& p0, const fast2::Pop& p1) {
-          const long long jx = j0 + half * 32 + c * 8 + 4 * qq + plane;
-          const int bx = bin_of(jx), by = bin_of(jx + 2);
+        steps([&](int hh, int g, const fast2::Pop& p0, const fast2::Pop& p1) {
+          const long long jx = jx_of(g);
+          const long long is = ib + 8 * hh;
+          const int ipi = hh ? ipos_b1 : ipos_b0;
+          const int bx = bin_of(is, ipi, jx), by = bin_of(is, ipi, jx + 1);
           const int lo = min(bx < 0 ? 0x7fffffff : bx, by < 0 ? 0x7fffffff : by);
           const int mn = __reduce_min_sync(0xffffffffu, lo);
           const int mx = __reduce_max_sync(0xffffffffu, max(bx, by));
@@ -773,25 +764,42 @@ __global__ void pos_to_int_kernel(const double* __restrict__ pos, long long n, i
 // ---------------------------------------------------------------------------
 // operand packing: bit planes -> E4M3 rows (2 per SNP), K padded to 128
 // ---------------------------------------------------------------------------
+// Row order: interleaved (row 2r + plane: SNP r) or, with grouped, by groups of
+// 8 SNPs (row 16g + 8 plane + k: SNP 8g + k; n_rows rounded up to 8, rows of
+// SNPs past n_rows zero).
 __global__ void pack_tc_kernel(const uint32_t* __restrict__ planes, int W, long long n_snp,
                                long long n_rows, const int32_t* __restrict__ idx, int k_pad,
-                               uint32_t* __restrict__ out, int32_t* __restrict__ status) {
+                               int grouped, uint32_t* __restrict__ out,
+                               int32_t* __restrict__ status) {
   // one thread writes 4 bytes (4 haplotypes) of one operand row; operand row
   // pair r holds SNP idx[r] (idx NULL: SNP r); an index outside the panel
   // gives a zero row and sets the status word
   const int words_per_row = k_pad / 4;
-  const long long total = 2 * n_rows * (long long)words_per_row;
+  const long long rows_out = grouped ? (n_rows + 7) / 8 * 8 : n_rows;
+  const long long total = 2 * rows_out * (long long)words_per_row;
   for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
     const long long rowi = x / words_per_row;
     const int wq = (int)(x - rowi * words_per_row);  // 4-haplotype group
-    long long s = idx ? (long long)idx[rowi >> 1] : (rowi >> 1);
+    long long r;
+    int plane;
+    if (grouped) {
+      r = (rowi >> 4) * 8 + (rowi & 7);
+      plane = (int)((rowi >> 3) & 1);
+      if (r >= n_rows) {
+        out[x] = 0u;
+        continue;
+      }
+    } else {
+      r = rowi >> 1;
+      plane = (int)(rowi & 1);
+    }
+    long long s = idx ? (long long)idx[r] : r;
     if (s < 0 || s >= n_snp) {
       if (status) atomicCAS(status, 0, 3102);
       out[x] = 0u;
       continue;
     }
-    const int plane = (int)(rowi & 1);
     const int h0 = wq * 4;
     const int w = h0 >> 5;
     uint32_t bits = 0;
@@ -836,11 +844,14 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
   const long long nb = (n + kTileSnp - 1) / kTileSnp;
   if (2 * (nb * kTileSnp) > 2147483647LL)
     return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: too many SNPs");
+  // the binned mode's operand rows are grouped by 8 SNPs (see pack_tc_kernel)
+  const int grouped = mode == pgld::kModeBinned ? 1 : 0;
+  const long long n_op = grouped ? (n + 7) / 8 * 8 : n;
   int k_pad[2] = {0, 0};
   size_t op_bytes[2] = {0, 0};
   for (int p = 0; p < P; ++p) {
     k_pad[p] = ((panel->n_words[p] * 32 + kKChunk - 1) / kKChunk) * kKChunk;
-    op_bytes[p] = (size_t)2 * n * k_pad[p];
+    op_bytes[p] = (size_t)2 * n_op * k_pad[p];
   }
   // the scan scratch serves both the tile list and (pairs mode) the per-SNP
   // pair offsets; the offsets live in this call's own workspace layout, since
@@ -865,11 +876,11 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
 
   // operands
   for (int p = 0; p < P; ++p) {
-    const long long words = 2 * n * (long long)(k_pad[p] / 4);
+    const long long words = 2 * n_op * (long long)(k_pad[p] / 4);
     unsigned blocks = (unsigned)std::min<long long>((words + 255) / 256, (long long)h->n_sm * 16);
     pack_tc_kernel<<<std::max(1u, blocks), 256, 0, st>>>(panel->planes[p], panel->n_words[p], n,
-                                                          n, nullptr, k_pad[p], (uint32_t*)ops[p],
-                                                          h->dev_status);
+                                                          n, nullptr, k_pad[p], grouped,
+                                                          (uint32_t*)ops[p], h->dev_status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_tc_kernel");
   }
@@ -888,7 +899,7 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
   }
   CUtensorMap maps[2];
   for (int p = 0; p < P; ++p) {
-    rc = make_map(h, &maps[p], ops[p], 2 * n, k_pad[p]);
+    rc = make_map(h, &maps[p], ops[p], 2 * n_op, k_pad[p]);
     if (rc) return rc;
   }
   if (P == 1) maps[1] = maps[0];
@@ -1011,7 +1022,7 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
   if (n_idx > 0) {
     const long long words = 2 * n_idx * (long long)(k_pad / 4);
     const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>((words + 255) / 256, h->n_sm * 16LL));
-    pack_tc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, n_idx, idx, k_pad, (uint32_t*)op,
+    pack_tc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, n_idx, idx, k_pad, 0, (uint32_t*)op,
                                            h->dev_status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_tc_kernel");
