@@ -490,36 +490,43 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
 
       if constexpr (MODE == kModePairs) {
-        // per-pair outputs: each lane owns whole pairs (i, j) after the C / Z
-        // exchange; rows k = pair_off[i] + (j - i - 1) in the reference's order
+        // per-pair outputs.  The operand rows are grouped by 8 SNPs (as in the
+        // binned mode), so a 16x256b TMEM load gives thread t all four counts
+        // of the pairs (i, j) and (i, j + 1), i = i0 + 16 quarter + 8 hh + t/4,
+        // j = j0 + 32 half + 8 g + 2 (t % 4); rows k = pair_off[i] + (j - i - 1)
+        // in the reference's order, two consecutive rows per thread
+        const long long ib = i0 + 16 * quarter + (lane >> 2);
+        const long long off0 = ib < a.n_snp ? a.pair_off[ib] : 0;
+        const long long np0 = ib < a.n_snp ? a.pair_off[ib + 1] - off0 : 0;
+        const long long off1 = ib + 8 < a.n_snp ? a.pair_off[ib + 8] : 0;
+        const long long np1 = ib + 8 < a.n_snp ? a.pair_off[ib + 9] - off1 : 0;
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
+          const int hh = c & 1, gp = c >> 1;
           uint32_t r[16];
-          const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
-          tmem_ld16(tmem_base + lane_base + col, r);
+          tmem_ld16x256_x4(tmem_base + ((uint32_t)(quarter * 32 + hh * 16) << 16) +
+                               (uint32_t)(acc * 256 + half * 64 + gp * 32),
+                           r);
           tmem_wait_ld();
           if (c == 3) {
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
           }
+          const long long is = ib + 8 * hh;
+          const long long offh = hh ? off1 : off0, nph = hh ? np1 : np0;
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const uint32_t s0 = plane ? r[4 * q] : r[4 * q + 2];
-            const uint32_t s1 = plane ? r[4 * q + 1] : r[4 * q + 3];
-            const float g0 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
-            const float g1 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
-            const float m0 = __uint_as_float(plane ? r[4 * q + 2] : r[4 * q]);
-            const float m1 = __uint_as_float(plane ? r[4 * q + 3] : r[4 * q + 1]);
-            const float c1 = plane ? g0 : m0, c2 = plane ? g1 : m1;
-            const float c3 = plane ? m0 : g0, c4 = plane ? m1 : g1;
-            const long long j = j0 + half * 32 + c * 8 + 2 * q + plane;
-            // the pair's row comes from the band offsets themselves, so a pair
-            // is written exactly when the offsets list it
-            bool ok = (i < j) && (j < a.n_snp);
-            if (ok) ok = (j - i - 1) < (a.pair_off[i + 1] - a.pair_off[i]);
-            if (ok) {
-              const long long k = a.pair_off[i] + (j - i - 1);
+          for (int g = 0; g < 2; ++g)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+              const int o = 8 * g + y;
+              const float c1 = __uint_as_float(r[o]), c2 = __uint_as_float(r[o + 4]);
+              const float c3 = __uint_as_float(r[o + 2]), c4 = __uint_as_float(r[o + 6]);
+              const long long j = j0 + 32 * half + 8 * (2 * gp + g) + 2 * (lane & 3) + y;
+              // the pair's row comes from the band offsets themselves, so a
+              // pair is written exactly when the offsets list it
+              if (!(is < j && j < a.n_snp && (j - is - 1) < nph)) continue;
+              const long long k = offh + (j - is - 1);
               const fast::Pop p = fast::make(c1, c2, c3, c4);
               reinterpret_cast<int4*>(a.counts)[k] =
                   make_int4(fast::f2i_small(c1), fast::f2i_small(c2), fast::f2i_small(c3),
@@ -532,7 +539,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                                 fast::pi2_num(p) * r4);
               }
             }
-          }
         }
         continue;
       }
@@ -844,8 +850,8 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
   const long long nb = (n + kTileSnp - 1) / kTileSnp;
   if (2 * (nb * kTileSnp) > 2147483647LL)
     return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: too many SNPs");
-  // the binned mode's operand rows are grouped by 8 SNPs (see pack_tc_kernel)
-  const int grouped = mode == pgld::kModeBinned ? 1 : 0;
+  // the operand rows are grouped by 8 SNPs (see pack_tc_kernel)
+  const int grouped = 1;
   const long long n_op = grouped ? (n + 7) / 8 * 8 : n;
   int k_pad[2] = {0, 0};
   size_t op_bytes[2] = {0, 0};
