@@ -32,8 +32,33 @@ class PackedPop:
         self.n_words = n_words
         self.n_rows = n_rows
         self.n_snp = n_snp
-        self.has_missing = has_missing
-        self.has_other = has_other
+        self._flags = None
+        self._missing = has_missing
+        self._other = has_other
+
+    @classmethod
+    def pending(cls, planes, valid, n_words, n_rows, n_snp, flags):
+        """Planes whose flags (a device int32[2] written by the packing kernel)
+        are read on first use, so that packing does not synchronise."""
+        pk = cls(planes, valid, n_words, n_rows, n_snp, None, None)
+        pk._flags = flags
+        return pk
+
+    def _resolve(self):
+        if self._flags is not None:
+            f = self._flags.cpu().numpy()
+            self._missing, self._other = bool(f[0]), bool(f[1])
+            self._flags = None
+
+    @property
+    def has_missing(self):
+        self._resolve()
+        return self._missing
+
+    @property
+    def has_other(self):
+        self._resolve()
+        return self._other
 
     @property
     def valid_for_n(self):
@@ -41,25 +66,55 @@ class PackedPop:
         return self.valid if (self.has_other and self.has_missing) else None
 
 
-def pack(hap, rows=None):
-    """Pack the rows of an int8 (H x M) device matrix into bit planes."""
+def _check_rows(rows, n_total):
+    """Population row indices as a device int32 tensor, checked against
+    n_total (on the host for host indices, one device read otherwise)."""
     torch = _torch()
-    hap = L.as_device(hap, np.int8)
+    if isinstance(rows, torch.Tensor) and rows.is_cuda:
+        rows_t = L.as_device(rows, np.int32)
+        if rows_t.numel():
+            lo, hi = (int(v) for v in torch.aminmax(rows_t))
+            if lo < 0 or hi >= n_total:
+                raise IndexError("population row index out of range")
+        return rows_t
+    r = np.asarray(rows.numpy() if isinstance(rows, torch.Tensor) else rows)
+    if r.size and (int(r.min()) < 0 or int(r.max()) >= n_total):
+        raise IndexError("population row index out of range")
+    return L.as_device(r.astype(np.int32, copy=False), np.int32)
+
+
+def _host_readable(hap):
+    """True for a contiguous int8 CPU tensor in pinned (page-locked) memory:
+    the packing kernel reads it in place over the host link."""
+    torch = _torch()
+    return (isinstance(hap, torch.Tensor) and not hap.is_cuda and hap.dtype == torch.int8
+            and hap.dim() == 2 and hap.stride(1) == 1 and hap.is_pinned())
+
+
+def pack(hap, rows=None):
+    """Pack the rows of an int8 (H x M) matrix into bit planes on the device.
+
+    hap is a device matrix (or anything as_device accepts, copied first); an
+    int8 CPU tensor in pinned memory is read in place by the packing kernel,
+    so only the packed planes are written to device memory (the call then
+    returns once the kernel is done with the host matrix)."""
+    torch = _torch()
+    if not _host_readable(hap):
+        hap = L.as_device(hap, np.int8)
     if hap.dim() != 2:
         raise ValueError("haplotypes must be 2-D (n_haplotypes, n_variants)")
     n_total, n_snp = hap.shape
     if rows is not None:
-        rows_t = L.as_device(rows, np.int32)
-        if rows_t.numel() and (int(rows_t.min()) < 0 or int(rows_t.max()) >= n_total):
-            raise IndexError("population row index out of range")
+        rows_t = _check_rows(rows, n_total)
         n_rows = rows_t.numel()
     else:
         rows_t = None
         n_rows = n_total
     W = max(1, (n_rows + 31) // 32)
-    planes = torch.empty((n_snp, 2 * W), dtype=torch.int32, device=hap.device)
-    valid = torch.empty((n_snp, W), dtype=torch.int32, device=hap.device)
-    flags = torch.zeros(2, dtype=torch.int32, device=hap.device)
+    dev = hap.device if hap.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    planes = torch.empty((n_snp, 2 * W), dtype=torch.int32, device=dev)
+    valid = torch.empty((n_snp, W), dtype=torch.int32, device=dev)
+    flags = torch.zeros(2, dtype=torch.int32, device=dev)
     if n_rows == 0:
         planes.zero_()
         valid.zero_()
@@ -68,8 +123,10 @@ def pack(hap, rows=None):
         L.check(L.lib().pgld_pack_haplotypes(h, L.ptr(hap), hap.stride(0), n_snp, L.ptr(rows_t),
                                              n_rows, L.ptr(planes), L.ptr(valid), L.ptr(flags),
                                              L.stream_ptr()), h)
-    f = flags.cpu().numpy()
-    return PackedPop(planes, valid, W, n_rows, n_snp, bool(f[0]), bool(f[1]))
+    pk = PackedPop.pending(planes, valid, W, n_rows, n_snp, flags)
+    if not hap.is_cuda:
+        pk._resolve()  # the host matrix is read in place: finish before returning
+    return pk
 
 
 def panel(pops):

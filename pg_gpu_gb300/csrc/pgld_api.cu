@@ -348,36 +348,72 @@ extern "C" int pgld_device_status(pgld_handle h, int32_t* code_out, void* stream
 // ---------------------------------------------------------------------------
 // bit-plane packing
 // ---------------------------------------------------------------------------
-// grid (ceil(n_snp/256), n_words): thread = one SNP x one 32-haplotype word.
+// block = one 32-haplotype word w x 512 SNPs.  The 32 rows x 512 bytes are
+// staged in shared memory with coalesced 16-byte (VEC) or 1-byte loads -- the
+// matrix may be pinned host memory read over the C2C link -- and each warp then
+// turns 64 SNPs into words: lane r holds row r's byte and one ballot per plane
+// gives the 32-bit word of a SNP.
+constexpr int kPackSnps = 512;
+constexpr int kPackPitch = kPackSnps + 4;  // row pitch: lanes of a column hit distinct banks
+template <bool VEC>
 __global__ void __launch_bounds__(256) pack_hap_kernel(const int8_t* __restrict__ hap, i64 ld,
                                                        i64 n_snp, const int32_t* __restrict__ rows,
                                                        int n_rows, int W, uint32_t* __restrict__ planes,
                                                        uint32_t* __restrict__ valid,
                                                        int32_t* __restrict__ flags) {
-  i64 s = (i64)blockIdx.x * 256 + threadIdx.x;
-  int w = blockIdx.y;
-  bool in = s < n_snp;
-  uint32_t cw = 0, zw = 0, vw = 0;
-  bool miss = false, other = false;
-  if (in) {
-    for (int r = 0; r < 32; ++r) {
-      int row = w * 32 + r;
-      if (row >= n_rows) break;
-      i64 hr = rows ? (i64)__ldg(rows + row) : (i64)row;
-      int8_t v = __ldg(hap + hr * ld + s);
-      cw |= (uint32_t)(v == 1) << r;
-      zw |= (uint32_t)(v == 0) << r;
-      vw |= (uint32_t)(v >= 0) << r;
-      miss |= (v == -1);
-      other |= (v != -1 && v != 0 && v != 1);
+  __shared__ __align__(16) int8_t tile[32 * kPackPitch];
+  const int w = blockIdx.y;
+  const i64 s0 = (i64)blockIdx.x * kPackSnps;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // load: warp k stages rows 4k .. 4k+3 of the word
+  for (int rr = 0; rr < 4; ++rr) {
+    const int r = warp * 4 + rr;
+    const int row = w * 32 + r;
+    int8_t* dst = tile + r * kPackPitch;
+    if (row >= n_rows) continue;
+    const i64 hr = rows ? (i64)__ldg(rows + row) : (i64)row;
+    const int8_t* src = hap + hr * ld + s0;
+    if (VEC && s0 + kPackSnps <= n_snp) {
+      const int4 v = __ldg(reinterpret_cast<const int4*>(src) + lane);
+      // kPackPitch is not a multiple of 16: store as four words
+      int* d4 = reinterpret_cast<int*>(dst + 16 * lane);
+      d4[0] = v.x; d4[1] = v.y; d4[2] = v.z; d4[3] = v.w;
+    } else {
+      for (int k = lane; k < kPackSnps; k += 32)
+        dst[k] = (s0 + k < n_snp) ? __ldg(src + k) : (int8_t)0;
     }
-    planes[s * 2 * W + w] = cw;
-    planes[s * 2 * W + W + w] = zw;
-    if (valid) valid[s * W + w] = vw;
   }
-  unsigned m = __ballot_sync(0xffffffffu, miss);
-  unsigned o = __ballot_sync(0xffffffffu, other);
-  if ((threadIdx.x & 31) == 0) {
+  __syncthreads();
+  const bool live = w * 32 + lane < n_rows;
+  const int8_t* mine = tile + lane * kPackPitch;
+  bool miss = false, other = false;
+  for (int c = warp * 64; c < warp * 64 + 64; c += 32) {
+    // 32 SNPs: lane k keeps the words of SNP c + k and stores them
+    uint32_t mc = 0, mz = 0, mv = 0;
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) {
+      const int v = live ? (int)mine[c + k] : -1;
+      const uint32_t cw = __ballot_sync(0xffffffffu, live && v == 1);
+      const uint32_t zw = __ballot_sync(0xffffffffu, live && v == 0);
+      const uint32_t vw = __ballot_sync(0xffffffffu, live && v >= 0);
+      miss |= live && v == -1 && s0 + c + k < n_snp;
+      other |= live && v != -1 && v != 0 && v != 1 && s0 + c + k < n_snp;
+      if (lane == k) {
+        mc = cw;
+        mz = zw;
+        mv = vw;
+      }
+    }
+    const i64 s = s0 + c + lane;
+    if (s < n_snp) {
+      planes[s * 2 * W + w] = mc;
+      planes[s * 2 * W + W + w] = mz;
+      if (valid) valid[s * W + w] = mv;
+    }
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, miss);
+  const unsigned o = __ballot_sync(0xffffffffu, other);
+  if (lane == 0) {
     if (m) atomicOr(flags, 1);
     if (o) atomicOr(flags + 1, 1);
   }
@@ -396,9 +432,14 @@ extern "C" int pgld_pack_haplotypes(pgld_handle h, const int8_t* hap, int64_t ld
   if (n_snp == 0 || W == 0) return PGLD_OK;
   PGLD_REQUIRE(h, W <= 65535, "pgld_pack_haplotypes: too many rows");
   PGLD_CHECK_CUDA(h, cudaSetDevice(h->device));
-  dim3 grid((unsigned)((n_snp + 255) / 256), (unsigned)W);
-  pack_hap_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(hap, ld, n_snp, rows, n_rows, W, planes,
-                                                           valid, flags);
+  dim3 grid((unsigned)((n_snp + kPackSnps - 1) / kPackSnps), (unsigned)W);
+  const bool vec = ((uintptr_t)hap % 16 == 0) && (ld % 16 == 0);
+  if (vec)
+    pack_hap_kernel<true><<<grid, 256, 0, (cudaStream_t)stream>>>(hap, ld, n_snp, rows, n_rows, W,
+                                                                  planes, valid, flags);
+  else
+    pack_hap_kernel<false><<<grid, 256, 0, (cudaStream_t)stream>>>(hap, ld, n_snp, rows, n_rows, W,
+                                                                   planes, valid, flags);
   PGLD_CHECK_CUDA(h, cudaGetLastError());
   return PGLD_OK;
 }

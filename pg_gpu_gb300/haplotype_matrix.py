@@ -37,7 +37,16 @@ class HaplotypeMatrix:
             raise ValueError("genotypes cannot be empty")
         if len(positions) == 0:
             raise ValueError("positions cannot be empty")
-        if g_dev:
+        # a pinned int8 CPU tensor stays on the host: the LD methods pack it in
+        # place (the packing kernel reads it over the host link); other
+        # methods copy it to the device on first use, like a numpy matrix
+        self._pinned = genotypes if _ops._host_readable(genotypes) else None
+        if self._pinned is not None:
+            self._device = "CPU"
+            self._haplotypes = genotypes.numpy()
+            self._positions = np.asarray(positions.cpu().numpy() if _is_torch(positions)
+                                         else positions)
+        elif g_dev:
             self._device = "GPU"
             self._haplotypes = L.as_device(genotypes, np.int8)
             self._positions = L.as_device(positions)
@@ -64,6 +73,7 @@ class HaplotypeMatrix:
     @haplotypes.setter
     def haplotypes(self, value):
         self._haplotypes = value
+        self._pinned = None
         self._packed = {}
 
     @property
@@ -229,11 +239,14 @@ class HaplotypeMatrix:
 
     def packed(self, pop=None):
         """Cached bit planes of a population (None: every haplotype)."""
-        self.transfer_to_gpu()
+        src = self._pinned if (self._device == "CPU" and self._pinned is not None) else None
+        if src is None:
+            self.transfer_to_gpu()
+            src = self._haplotypes
         key = pop
         if key not in self._packed:
             rows = self._pop_rows(pop)
-            self._packed[key] = _ops.pack(self._haplotypes, rows)
+            self._packed[key] = _ops.pack(src, rows)
         return self._packed[key]
 
     # ------------------------------------------------------------ LD methods

@@ -151,6 +151,57 @@ def test_binned_sums_match_moments_golden(golden):
     _near(s, z["ld_sums"], a)
 
 
+def _planes_oracle(hap, rows):
+    """Carrier / reference / validity words of the rows (bit r of word w: row 32w + r)."""
+    sub = hap[rows]
+    H, M = sub.shape
+    W = (H + 31) // 32
+    cw = np.zeros((M, W), np.uint32)
+    zw = np.zeros((M, W), np.uint32)
+    vw = np.zeros((M, W), np.uint32)
+    for r in range(H):
+        w, b = divmod(r, 32)
+        cw[:, w] |= (sub[r] == 1).astype(np.uint32) << np.uint32(b)
+        zw[:, w] |= (sub[r] == 0).astype(np.uint32) << np.uint32(b)
+        vw[:, w] |= (sub[r] >= 0).astype(np.uint32) << np.uint32(b)
+    return np.concatenate([cw, zw], 1), vw, bool((sub == -1).any()), \
+        bool(((sub != -1) & (sub != 0) & (sub != 1)).any())
+
+
+@pytest.mark.parametrize("M", [1040, 1037, 511])
+def test_pack_tiles_and_pinned_host(M):
+    """Packing: full 512-SNP tiles with 16-byte loads (row stride a multiple of
+    16), byte loads otherwise, ragged row subsets, other codes; a pinned host
+    matrix is read in place and gives the same planes."""
+    rng = np.random.default_rng(M)
+    hap = rng.choice(np.array([-1, 0, 1, 2], np.int8), size=(70, M), p=[0.05, 0.5, 0.44, 0.01])
+    rows = np.sort(rng.choice(70, 45, replace=False)).astype(np.int32)
+    want_p, want_v, miss, other = _planes_oracle(hap, rows)
+    host = torch.as_tensor(hap).pin_memory()
+    for src in (torch.as_tensor(hap, device="cuda"), host):
+        pk = _ops.pack(src, rows)
+        assert np.array_equal(np_(pk.planes).view(np.uint32), want_p)
+        assert np.array_equal(np_(pk.valid).view(np.uint32), want_v)
+        assert (pk.has_missing, pk.has_other) == (miss, other)
+
+
+def test_pinned_host_matrix_binned_equals_device():
+    from pg_gpu_gb300.haplotype_matrix import HaplotypeMatrix
+    rng = np.random.default_rng(17)
+    hap = copying_model(rng, 96, 1200, 8, 2e-3, missing=0.02)
+    pos = np.sort(rng.choice(600_000, 1200, replace=False)).astype(np.int64)
+    bins = np.logspace(3, 5, 9)
+    sets = {"a": list(range(48)), "b": list(range(48, 96))}
+    host = torch.as_tensor(hap).pin_memory()
+    hm_h = HaplotypeMatrix(host, pos, sample_sets=sets)
+    assert hm_h.device == "CPU"
+    got = hm_h.compute_ld_statistics_gpu_two_pops(bins, "a", "b", raw=True, ac_filter=False)
+    assert hm_h.device == "CPU"  # packed in place, not copied
+    hm_d = HaplotypeMatrix(torch.as_tensor(hap, device="cuda"), pos, sample_sets=sets)
+    want = hm_d.compute_ld_statistics_gpu_two_pops(bins, "a", "b", raw=True, ac_filter=False)
+    assert got == want
+
+
 # --------------------------------------------------------------------------
 # oracle comparisons: sizes, ragged word counts, large samples
 # --------------------------------------------------------------------------
