@@ -772,48 +772,50 @@ __global__ void pos_to_int_kernel(const double* __restrict__ pos, long long n, i
 // ---------------------------------------------------------------------------
 // Row order: interleaved (row 2r + plane: SNP r) or, with grouped, by groups of
 // 8 SNPs (row 16g + 8 plane + k: SNP 8g + k; n_rows rounded up to 8, rows of
-// SNPs past n_rows zero).
-__global__ void pack_tc_kernel(const uint32_t* __restrict__ planes, int W, long long n_snp,
-                               long long n_rows, const int32_t* __restrict__ idx, int k_pad,
-                               int grouped, uint32_t* __restrict__ out,
-                               int32_t* __restrict__ status) {
-  // one thread writes 4 bytes (4 haplotypes) of one operand row; operand row
-  // pair r holds SNP idx[r] (idx NULL: SNP r); an index outside the panel
-  // gives a zero row and sets the status word
-  const int words_per_row = k_pad / 4;
-  const long long rows_out = grouped ? (n_rows + 7) / 8 * 8 : n_rows;
-  const long long total = 2 * rows_out * (long long)words_per_row;
-  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
-       x += (long long)gridDim.x * blockDim.x) {
-    const long long rowi = x / words_per_row;
-    const int wq = (int)(x - rowi * words_per_row);  // 4-haplotype group
-    long long r;
-    int plane;
-    if (grouped) {
-      r = (rowi >> 4) * 8 + (rowi & 7);
-      plane = (int)((rowi >> 3) & 1);
-      if (r >= n_rows) {
-        out[x] = 0u;
-        continue;
-      }
-    } else {
-      r = rowi >> 1;
-      plane = (int)(rowi & 1);
-    }
-    long long s = idx ? (long long)idx[r] : r;
+// SNPs past n_rows zero).  A block writes 8 operand rows, a warp one row in
+// 16-byte chunks (16 haplotypes: one nibble-to-bytes lookup per 4).
+__global__ void __launch_bounds__(256) pack_tc_kernel(const uint32_t* __restrict__ planes, int W,
+                                                      long long n_snp, long long n_rows,
+                                                      const int32_t* __restrict__ idx, int k_pad,
+                                                      int grouped, uint32_t* __restrict__ out,
+                                                      int32_t* __restrict__ status) {
+  const long long rows_out = 2 * (grouped ? (n_rows + 7) / 8 * 8 : n_rows);
+  const long long rowi = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (rowi >= rows_out) return;
+  const int chunks = k_pad / 16;
+  uint4* dst = reinterpret_cast<uint4*>(out) + rowi * chunks;
+  long long r;
+  int plane;
+  if (grouped) {
+    r = (rowi >> 4) * 8 + (rowi & 7);
+    plane = (int)((rowi >> 3) & 1);
+  } else {
+    r = rowi >> 1;
+    plane = (int)(rowi & 1);
+  }
+  long long s = -1;
+  if (r < n_rows) {
+    s = idx ? (long long)idx[r] : r;
     if (s < 0 || s >= n_snp) {
-      if (status) atomicCAS(status, 0, 3102);
-      out[x] = 0u;
-      continue;
+      if (status && lane == 0) atomicCAS(status, 0, 3102);
+      s = -1;
     }
-    const int h0 = wq * 4;
+  }
+  const uint32_t* src = planes + (s < 0 ? 0 : s) * 2 * W + plane * W;
+  for (int c = lane; c < chunks; c += 32) {
+    const int h0 = 16 * c;
     const int w = h0 >> 5;
-    uint32_t bits = 0;
-    if (w < W) bits = (__ldg(planes + s * 2 * W + plane * W + w) >> (h0 & 31)) & 0xF;
-    uint32_t v = 0;
+    const uint32_t bits = (s >= 0 && w < W) ? (__ldg(src + w) >> (h0 & 31)) & 0xFFFFu : 0u;
+    uint32_t v[4];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) v |= ((bits >> b) & 1u) * (kOne << (8 * b));
-    out[x] = v;
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t nib = (bits >> (4 * q)) & 0xFu;
+      // byte b of v[q] = E4M3 1.0 where bit b of the nibble is set
+      v[q] = (nib & 1u ? kOne : 0u) | (nib & 2u ? kOne << 8 : 0u) | (nib & 4u ? kOne << 16 : 0u) |
+             (nib & 8u ? kOne << 24 : 0u);
+    }
+    dst[c] = make_uint4(v[0], v[1], v[2], v[3]);
   }
 }
 
@@ -882,8 +884,7 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
 
   // operands
   for (int p = 0; p < P; ++p) {
-    const long long words = 2 * n_op * (long long)(k_pad[p] / 4);
-    unsigned blocks = (unsigned)std::min<long long>((words + 255) / 256, (long long)h->n_sm * 16);
+    const unsigned blocks = (unsigned)((2 * n_op + 7) / 8);
     pack_tc_kernel<<<std::max(1u, blocks), 256, 0, st>>>(panel->planes[p], panel->n_words[p], n,
                                                           n, nullptr, k_pad[p], grouped,
                                                           (uint32_t*)ops[p], h->dev_status);
@@ -1026,8 +1027,7 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
     if (rc) return rc;
   }
   if (n_idx > 0) {
-    const long long words = 2 * n_idx * (long long)(k_pad / 4);
-    const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>((words + 255) / 256, h->n_sm * 16LL));
+    const unsigned blocks = (unsigned)((2 * n_idx + 7) / 8);
     pack_tc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, n_idx, idx, k_pad, 0, (uint32_t*)op,
                                            h->dev_status);
     cudaError_t e = cudaGetLastError();
