@@ -288,32 +288,38 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 // operand rows: row 128 * (s / 32) + 32 * plane + s % 32 holds, for plane 0..2,
 // the individuals with dosage == plane at SNP s, and for plane 3 the valid
-// ones; one thread writes 4 bytes (4 individuals)
-__global__ void pack_gtc_kernel(const uint32_t* __restrict__ planes, int W, long long n_snp,
-                                long long n_blocks, int k_pad, uint32_t* __restrict__ out) {
-  const int words_per_row = k_pad / 4;
-  const long long total = n_blocks * kRows * (long long)words_per_row;
-  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
-       x += (long long)gridDim.x * blockDim.x) {
-    const long long row = x / words_per_row;
-    const int wq = (int)(x - row * words_per_row);
-    const long long blk = row >> 7;
-    const int within = (int)(row & 127);
-    const int plane = within >> 5;
-    const long long s = blk * kTileSnp + (within & 31);
-    const int h0 = wq * 4;
+// ones.  A block writes 8 rows, a warp one row in 16-byte chunks (16
+// individuals, one nibble-to-bytes step per 4).
+__global__ void __launch_bounds__(256) pack_gtc_kernel(const uint32_t* __restrict__ planes, int W,
+                                                       long long n_snp, long long n_blocks,
+                                                       int k_pad, uint32_t* __restrict__ out) {
+  const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n_blocks * kRows) return;
+  const int chunks = k_pad / 16;
+  uint4* dst = reinterpret_cast<uint4*>(out) + row * chunks;
+  const long long blk = row >> 7;
+  const int within = (int)(row & 127);
+  const int plane = within >> 5;
+  const long long s = blk * kTileSnp + (within & 31);
+  const uint32_t* ps = planes + (s < n_snp ? s : 0) * 3 * W;
+  for (int c = lane; c < chunks; c += 32) {
+    const int h0 = 16 * c;
     const int w = h0 >> 5;
     uint32_t bits = 0;
     if (s < n_snp && w < W) {
-      const uint32_t* ps = planes + s * 3 * W;
       const uint32_t word = plane < 3 ? __ldg(ps + plane * W + w)
                                       : (__ldg(ps + w) | __ldg(ps + W + w) | __ldg(ps + 2 * W + w));
-      bits = (word >> (h0 & 31)) & 0xF;
+      bits = (word >> (h0 & 31)) & 0xFFFFu;
     }
-    uint32_t v = 0;
+    uint32_t v[4];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) v |= ((bits >> b) & 1u) * (kOne << (8 * b));
-    out[x] = v;
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t nib = (bits >> (4 * q)) & 0xFu;
+      v[q] = (nib & 1u ? kOne : 0u) | (nib & 2u ? kOne << 8 : 0u) | (nib & 4u ? kOne << 16 : 0u) |
+             (nib & 8u ? kOne << 24 : 0u);
+    }
+    dst[c] = make_uint4(v[0], v[1], v[2], v[3]);
   }
 }
 
@@ -349,9 +355,7 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
   rc = pgld_band_offsets(h, pos, n, max_dist, poff, w + off_scan, sb, st);
   if (rc) return rc;
   {
-    const long long words = (long long)nb * kRows * (k_pad / 4);
-    const unsigned blocks =
-        (unsigned)std::max<long long>(1, std::min<long long>((words + 255) / 256, h->n_sm * 16LL));
+    const unsigned blocks = (unsigned)std::max<long long>(1, (nb * kRows + 7) / 8);
     pack_gtc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, nb, k_pad, (uint32_t*)op);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_gtc_kernel");
