@@ -327,6 +327,22 @@ int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel, const int32
                          int32_t n_win, double* sums, int64_t* counts, int32_t form,
                          void* stream);
 
+/* Per-SNP row and column sums of one window statistic, for Kim and Nielsen's
+ * omega over batched windows (one launch).  Windows as pgld_hap_window_sums
+ * (they may overlap).  For every pair of list positions a < b of window w
+ * (a, b relative to win_begin[w]), the pair's value of column stat (0..5 of
+ * pgld_hap_window_sums: 1 = sigma_D^2 = DD / pi2 numerators, 5 = naive r^2)
+ * is added to row_sums[out_off[w] + a] and col_sums[out_off[w] + b] (float64,
+ * n_out entries each, zeroed by the call; out_off device int64, window w
+ * owning win_end[w] - win_begin[w] entries).  The prefix sums of these give
+ * the within / between block sums of every split point of
+ * ld_statistics.omega (ld_statistics.py:761-862) without the m x m matrix.
+ * Plain (AND + popcount) counts.  Synchronises. */
+int pgld_hap_window_snp_sums(pgld_handle h, const pgld_hap_panel* panel, const int32_t* snp_idx,
+                             int64_t n_idx, const int64_t* win_begin, const int64_t* win_end,
+                             int32_t n_win, const int64_t* out_off, int32_t stat,
+                             double* row_sums, double* col_sums, int64_t n_out, void* stream);
+
 /* pgld_hap_binned_sums for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers of this library cannot call
  * cudaMalloc: a host application that hands every byte of the device to its

@@ -1087,3 +1087,79 @@ def zns_window(hap, s, e, projection=True):
     if projection:
         return sums[0, 1] / cnts[0, 2] if cnts[0, 2] > 0 else 0.0
     return sums[0, 5] / cnts[0, 0]
+
+
+# ---------------------------------------------------------------------------
+# Kim and Nielsen's omega  (ld_statistics.py:734-862)
+# ---------------------------------------------------------------------------
+def pair_stat_matrix(hap, stat):
+    """Square matrix of one window statistic over all site pairs of hap
+    (zero diagonal): stat 1 = sigma_D^2 = DD / pi2 numerators (n >= 4 and a
+    nonzero pi2 numerator, else 0; _build_sigma_d2_matrix,
+    ld_statistics.py:734-758), 5 = naive r^2 of per-site frequencies
+    (HaplotypeMatrix.pairwise_r2, haplotype_matrix.py:1138-1170)."""
+    h = np.asarray(hap)
+    m = h.shape[1]
+    out = np.zeros((m, m))
+    if m < 2:
+        return out
+    a, b = np.triu_indices(m, 1)
+    c, nv = counts_for_pairs(h, a, b)
+    n = c.astype(I64).sum(1)
+    if stat == 1:
+        p = Pop(c, n)
+        dd_n, _ = dd_ii(p)
+        pi_n, _ = pi2_iiii(p)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            v = np.where((n >= 4) & (pi_n != 0), dd_n / np.where(pi_n != 0, pi_n, 1), 0.0)
+    elif stat == 5:
+        dac = (h == 1).sum(0).astype(np.int64)
+        nvs = (h >= 0).sum(0).astype(np.int64)
+        pi_ = dac[a] / np.maximum(nvs[a], 1)
+        pj_ = dac[b] / np.maximum(nvs[b], 1)
+        pab = np.where(n > 0, c[:, 0] / np.maximum(n, 1), 0.0)
+        D = pab - pi_ * pj_
+        den = pi_ * (1 - pi_) * pj_ * (1 - pj_)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            v = np.where(den > 0, D * D / np.where(den > 0, den, 1), 0.0)
+    else:
+        raise ValueError("stat 1 or 5")
+    out[a, b] = v
+    out[b, a] = v
+    return out
+
+
+def omega_matrix(r2):
+    """omega of a square LD matrix: for splits l = 3 .. m-2 the mean of the
+    upper triangle within [0, l) and [l, m) over the mean across, maximised
+    (the 2-D prefix-sum form of ld_statistics.py:813-862); 0.0 below 5 sites."""
+    r2 = np.asarray(r2, np.float64)
+    m = r2.shape[0]
+    if m < 5:
+        return 0.0
+    S = np.cumsum(np.cumsum(np.triu(r2, 1), axis=0), axis=1)
+    l = np.arange(3, m - 1)
+    left = S[l - 1, l - 1]
+    total = S[m - 1, m - 1]
+    cross = S[l - 1, m - 1] - left
+    right = total - left - cross
+    n_within = l * (l - 1) // 2 + (m - l) * (m - l - 1) // 2
+    n_cross = l * (m - l)
+    valid = (n_within > 0) & (n_cross > 0) & (cross > 0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        mw = np.where(n_within > 0, (left + right) / n_within, 0.0)
+        mc = np.where(n_cross > 0, cross / n_cross, 1.0)
+        vals = np.where(valid, mw / mc, 0.0)
+    return float(vals.max()) if vals.size else 0.0
+
+
+def omega_hap(hap, estimator="sigma_d2", missing_data="include"):
+    """omega of a haplotype matrix over its segregating sites (after dropping
+    sites with missing calls for missing_data 'exclude'), ld_statistics.py:761-862."""
+    h = np.asarray(hap)
+    if missing_data == "exclude":
+        h = h[:, (h < 0).sum(0) == 0]
+    h = h[:, segregating(h)]
+    if h.shape[1] < 2:
+        return 0.0
+    return omega_matrix(pair_stat_matrix(h, 1 if estimator == "sigma_d2" else 5))

@@ -108,6 +108,9 @@ _SIGS = {
                              ctypes.c_int),
     "pgld_hap_binned_sums_noalloc": ([ctypes.c_int, ctypes.POINTER(HapPanel), _P, _D, _P, _P, _I32,
                                       _P, _P, _P], ctypes.c_int),
+    "pgld_hap_window_snp_sums": ([_P, ctypes.POINTER(HapPanel), _P, _I64, _P, _P, _I32, _P, _I32,
+                                  _P, _P, _I64, _P],
+                                 ctypes.c_int),
 }
 
 _lib = None

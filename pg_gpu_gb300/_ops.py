@@ -322,6 +322,70 @@ def window_sums(pk, idx, win_begin, win_end, form="auto"):
     return sums, cnt
 
 
+def window_snp_sums(pk, idx, win_begin, win_end, stat):
+    """Per-SNP row and column sums (float64, one entry per list position of
+    each window, windows concatenated) of window statistic column stat
+    (WINDOW_COLUMNS) over the pairs a < b of each window, and the offsets of
+    the windows' entries (host int64, n_win + 1)."""
+    torch = _torch()
+    dev = pk.planes.device
+    wb_h = np.asarray(win_begin, np.int64)
+    we_h = np.asarray(win_end, np.int64)
+    if wb_h.shape != we_h.shape:
+        raise ValueError("win_begin and win_end must have the same shape")
+    n_win = wb_h.size
+    lens = np.maximum(we_h - wb_h, 0)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    n_out = int(off[-1])
+    rows = torch.empty(max(n_out, 1), dtype=torch.float64, device=dev)
+    cols = torch.empty(max(n_out, 1), dtype=torch.float64, device=dev)
+    if n_win == 0:
+        return rows[:0], cols[:0], off
+    ii = None if idx is None else L.as_device(idx, np.int32)
+    n_idx = pk.n_snp if ii is None else ii.numel()
+    wb, we = L.as_device(wb_h, np.int64), L.as_device(we_h, np.int64)
+    off_d = L.as_device(off[:-1].copy(), np.int64)
+    h = L.handle()
+    L.check(L.lib().pgld_hap_window_snp_sums(h, ctypes.byref(panel([pk])), L.ptr(ii), n_idx,
+                                             L.ptr(wb), L.ptr(we), n_win, L.ptr(off_d), int(stat),
+                                             L.ptr(rows), L.ptr(cols), n_out, L.stream_ptr()), h)
+    st = torch.zeros(1, dtype=torch.int32)
+    L.check(L.lib().pgld_device_status(h, ctypes.cast(st.data_ptr(), ctypes.POINTER(
+        ctypes.c_int32)), L.stream_ptr()), h)
+    if int(st[0]):
+        raise IndexError(f"window or SNP index out of range (device status {int(st[0])})")
+    return rows[:n_out], cols[:n_out], off
+
+
+def omega_from_sums(row, col):
+    """Kim and Nielsen's omega of m sites from the row sums row[i] = sum over
+    j > i and column sums col[j] = sum over i < j of the pair statistic (the
+    upper triangle): for every split l = 3 .. m-2 the mean within the blocks
+    [0, l) and [l, m) over the mean across them (ld_statistics.py:810-862);
+    0.0 below 5 sites or where no split is defined."""
+    row = np.asarray(row, np.float64)
+    col = np.asarray(col, np.float64)
+    m = row.size
+    if m < 5:
+        return 0.0
+    A = np.cumsum(row)          # pairs with i < l: A[l - 1]
+    left_all = np.cumsum(col)   # pairs with j < l: left_all[l - 1]
+    total = A[-1]
+    l = np.arange(3, m - 1)
+    left = left_all[l - 1]
+    cross = A[l - 1] - left
+    right = total - A[l - 1]
+    n_left = l * (l - 1) // 2
+    n_right = (m - l) * (m - l - 1) // 2
+    n_cross = l * (m - l)
+    n_within = n_left + n_right
+    valid = (n_within > 0) & (n_cross > 0) & (cross > 0)
+    within = np.where(n_within > 0, (left + right) / np.maximum(n_within, 1), 0.0)
+    across = np.where(n_cross > 0, cross / np.maximum(n_cross, 1), 1.0)
+    vals = np.where(valid, within / np.where(valid, across, 1.0), 0.0)
+    return float(vals.max()) if vals.size else 0.0
+
+
 def tc_applies(pops):
     """The tensor-core form takes 1-2 populations of <= 2048 haplotypes (0/1/-1 codes)."""
     return len(pops) <= 2 and all(pk.n_words <= 64 and pk.valid_for_n is None for pk in pops)

@@ -48,6 +48,13 @@ struct Args {
   double* sums;            // [n_win][kCols]
   unsigned long long* cnt; // [n_win][kCnts]
   int32_t* status;
+  // per-SNP mode (window_kernel<true>): statistic snp_stat of every pair
+  // (a, b), a < b list positions of window w, added to row_sums[snp_off[w] +
+  // a - begin] and col_sums[snp_off[w] + b - begin]
+  int snp_stat;
+  const i64* snp_off;
+  double* row_sums;
+  double* col_sums;
 };
 
 // tiles per window; a window outside [0, n_idx] or with a negative length
@@ -109,6 +116,7 @@ struct __align__(16) Smem {
   uint32_t vi[kKW][kPad], vj[kKW][kPad];
 };
 
+template <bool SNP>
 __global__ void __launch_bounds__(kThreads) window_kernel(Args a) {
   __shared__ Smem sm;
   extern __shared__ float tabs[];  // 1/n and 1/(n(n-1)(n-2)(n-3)), n = 0..nmax
@@ -179,6 +187,36 @@ __global__ void __launch_bounds__(kThreads) window_kernel(Args a) {
       __syncthreads();
     }
 
+    if constexpr (SNP) {
+      // row totals of the warp's 4 rows, column totals of its lane's column
+      float colv = 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const i64 ia = a0 + wid + 8 * q, jb = b0 + lane;
+        float x = 0.f;
+        if (ia < jb && jb < end) {
+          const float c1 = (float)c[q][0], c2 = (float)c[q][1], c3 = (float)c[q][2],
+                      c4 = (float)c[q][3];
+          const fast::Pop p = fast::make(c1, c2, c3, c4);
+          const int n = a.valid ? nv[q] : p.n;
+          const i64 si = a.idx ? (i64)a.idx[ia] : ia, sj = a.idx ? (i64)a.idx[jb] : jb;
+          const bool sok = si >= 0 && si < a.n_snp && sj >= 0 && sj < a.n_snp;
+          const float4 fi = sok ? a.site[si] : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 fj = sok ? a.site[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
+          x = pair_stat(a.snp_stat, p, n, c1, tinv[n], tr4[n], fi, fj);
+        }
+        colv += x;
+        float rv = x;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rv += __shfl_xor_sync(0xffffffffu, rv, o);
+        if (lane == 0 && rv != 0.f && ia < end)
+          atomicAdd(a.row_sums + a.snp_off[w] + (ia - base), (double)rv);
+      }
+      if (colv != 0.f && b0 + lane < end)
+        atomicAdd(a.col_sums + a.snp_off[w] + (b0 + lane - base), (double)colv);
+      continue;
+    }
+
     float acc[kCols] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int n_pairs = 0, n_r2 = 0, n_four = 0;
 #pragma unroll
@@ -231,42 +269,15 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
                     long long n_idx, const long long* wb, const long long* we, int n_win,
                     double* sums, unsigned long long* counts, cudaStream_t st);
 
-extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
-                                    const int32_t* snp_idx, int64_t n_idx,
-                                    const int64_t* win_begin, const int64_t* win_end,
-                                    int32_t n_win, double* sums, int64_t* counts, int32_t form,
-                                    void* stream) {
-  PGLD_REQUIRE(h, h != nullptr, "pgld_hap_window_sums: NULL handle");
-  PGLD_REQUIRE(h, panel != nullptr && panel->n_pops == 1,
-               "pgld_hap_window_sums: one population per call");
-  PGLD_REQUIRE(h, panel->n_words[0] >= 1 && panel->n_snp >= 0, "pgld_hap_window_sums: panel");
-  PGLD_REQUIRE(h, n_win >= 0, "pgld_hap_window_sums: n_win < 0");
-  PGLD_REQUIRE(h, snp_idx != nullptr || n_idx == panel->n_snp,
-               "pgld_hap_window_sums: without an index list n_idx must be n_snp");
-  PGLD_REQUIRE(h, n_idx >= 0, "pgld_hap_window_sums: n_idx < 0");
-  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC, "pgld_hap_window_sums: form");
-  if (form == PGLD_FORM_TC && !pgld_tc_supported(h, panel))
-    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "pgld_hap_window_sums: tensor-core form needs "
-                     "<= 2048 haplotypes and no separate validity plane");
-  if (n_win == 0) return PGLD_OK;
-  PGLD_REQUIRE(h, win_begin && win_end && sums && counts, "pgld_hap_window_sums: NULL buffer");
-  PGLD_REQUIRE(h, panel->planes[0] != nullptr || panel->n_snp == 0,
-               "pgld_hap_window_sums: NULL planes");
-  PGLD_CHECK_CUDA(h, cudaSetDevice(h->device));
-  cudaStream_t st = (cudaStream_t)stream;
+// the plain window kernel over windows [wb[w], we[w]) of the index list:
+// window sums (snp_stat < 0) or per-SNP row / column sums of statistic
+// snp_stat; synchronises (the workspace holds the tile list and site counts)
+static int window_run(pgld_context* h, const pgld_hap_panel* panel, const int32_t* snp_idx,
+                      i64 n_idx, const i64* wb, const i64* we, int n_win, double* sums,
+                      unsigned long long* counts, int snp_stat, const i64* snp_off,
+                      double* row_sums, double* col_sums, cudaStream_t st) {
   const i64 n = panel->n_snp;
   const int W = panel->n_words[0];
-  PGLD_CHECK_CUDA(h, cudaMemsetAsync(sums, 0, (size_t)n_win * pgld::win::kCols * 8, st));
-  PGLD_CHECK_CUDA(h, cudaMemsetAsync(counts, 0, (size_t)n_win * pgld::win::kCnts * 8, st));
-  if (form == PGLD_FORM_TC) {
-    int rc = pgld_tc_windows(h, panel, snp_idx, n_idx, reinterpret_cast<const i64*>(win_begin),
-                             reinterpret_cast<const i64*>(win_end), n_win, sums,
-                             reinterpret_cast<unsigned long long*>(counts), st);
-    if (rc) return rc;
-    // the workspace holds the tile offsets and the operand: finish before reuse
-    PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));
-    return PGLD_OK;
-  }
   const size_t sb = pgld::scan_scratch_bytes(n_win);
   const size_t tiles_b = ((size_t)(n_win + 1) * 8 + 255) & ~size_t(255);
   const size_t site_b = ((size_t)std::max<i64>(n, 1) * 16 + 255) & ~size_t(255);
@@ -278,8 +289,6 @@ extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
   float4* site = (float4*)(wp + tiles_b);
   char* scratch = wp + tiles_b + site_b;
   const unsigned gb = (unsigned)std::max<i64>(1, std::min<i64>((n_win + 255) / 256, h->n_sm * 4));
-  const i64* wb = reinterpret_cast<const i64*>(win_begin);
-  const i64* we = reinterpret_cast<const i64*>(win_end);
   pgld::win::window_tiles_kernel<<<gb, 256, 0, st>>>(wb, we, n_win, n_idx, tiles,
                                                       h->dev_status);
   PGLD_CHECK_CUDA(h, cudaGetLastError());
@@ -304,18 +313,91 @@ extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
   a.site = site;
   a.nmax = 32 * W;
   a.sums = sums;
-  a.cnt = reinterpret_cast<unsigned long long*>(counts);
+  a.cnt = counts;
   a.status = h->dev_status;
+  a.snp_stat = snp_stat;
+  a.snp_off = snp_off;
+  a.row_sums = row_sums;
+  a.col_sums = col_sums;
   const size_t tab_b = (size_t)2 * (a.nmax + 1) * sizeof(float);
-  PGLD_CHECK_CUDA(h, cudaFuncSetAttribute(pgld::win::window_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_b));
+  auto kern = snp_stat >= 0 ? pgld::win::window_kernel<true> : pgld::win::window_kernel<false>;
+  PGLD_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)tab_b));
   int per_sm = 0;
-  PGLD_CHECK_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &per_sm, pgld::win::window_kernel, pgld::win::kThreads, tab_b));
-  pgld::win::window_kernel<<<(unsigned)(h->n_sm * std::max(1, per_sm)), pgld::win::kThreads,
-                             tab_b, st>>>(a);
+  PGLD_CHECK_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern,
+                                                                   pgld::win::kThreads, tab_b));
+  kern<<<(unsigned)(h->n_sm * std::max(1, per_sm)), pgld::win::kThreads, tab_b, st>>>(a);
   PGLD_CHECK_CUDA(h, cudaGetLastError());
   // the tile offsets and site counts live in the workspace: finish before reuse
   PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));
   return PGLD_OK;
+}
+
+extern "C" int pgld_hap_window_sums(pgld_handle h, const pgld_hap_panel* panel,
+                                    const int32_t* snp_idx, int64_t n_idx,
+                                    const int64_t* win_begin, const int64_t* win_end,
+                                    int32_t n_win, double* sums, int64_t* counts, int32_t form,
+                                    void* stream) {
+  PGLD_REQUIRE(h, h != nullptr, "pgld_hap_window_sums: NULL handle");
+  PGLD_REQUIRE(h, panel != nullptr && panel->n_pops == 1,
+               "pgld_hap_window_sums: one population per call");
+  PGLD_REQUIRE(h, panel->n_words[0] >= 1 && panel->n_snp >= 0, "pgld_hap_window_sums: panel");
+  PGLD_REQUIRE(h, n_win >= 0, "pgld_hap_window_sums: n_win < 0");
+  PGLD_REQUIRE(h, snp_idx != nullptr || n_idx == panel->n_snp,
+               "pgld_hap_window_sums: without an index list n_idx must be n_snp");
+  PGLD_REQUIRE(h, n_idx >= 0, "pgld_hap_window_sums: n_idx < 0");
+  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC, "pgld_hap_window_sums: form");
+  if (form == PGLD_FORM_TC && !pgld_tc_supported(h, panel))
+    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "pgld_hap_window_sums: tensor-core form needs "
+                     "<= 2048 haplotypes and no separate validity plane");
+  if (n_win == 0) return PGLD_OK;
+  PGLD_REQUIRE(h, win_begin && win_end && sums && counts, "pgld_hap_window_sums: NULL buffer");
+  PGLD_REQUIRE(h, panel->planes[0] != nullptr || panel->n_snp == 0,
+               "pgld_hap_window_sums: NULL planes");
+  PGLD_CHECK_CUDA(h, cudaSetDevice(h->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  PGLD_CHECK_CUDA(h, cudaMemsetAsync(sums, 0, (size_t)n_win * pgld::win::kCols * 8, st));
+  PGLD_CHECK_CUDA(h, cudaMemsetAsync(counts, 0, (size_t)n_win * pgld::win::kCnts * 8, st));
+  if (form == PGLD_FORM_TC) {
+    int rc = pgld_tc_windows(h, panel, snp_idx, n_idx, reinterpret_cast<const i64*>(win_begin),
+                             reinterpret_cast<const i64*>(win_end), n_win, sums,
+                             reinterpret_cast<unsigned long long*>(counts), st);
+    if (rc) return rc;
+    // the workspace holds the tile offsets and the operand: finish before reuse
+    PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    return PGLD_OK;
+  }
+  return window_run(h, panel, snp_idx, n_idx, reinterpret_cast<const i64*>(win_begin),
+                    reinterpret_cast<const i64*>(win_end), n_win, sums,
+                    reinterpret_cast<unsigned long long*>(counts), -1, nullptr, nullptr, nullptr,
+                    st);
+}
+
+extern "C" int pgld_hap_window_snp_sums(pgld_handle h, const pgld_hap_panel* panel,
+                                        const int32_t* snp_idx, int64_t n_idx,
+                                        const int64_t* win_begin, const int64_t* win_end,
+                                        int32_t n_win, const int64_t* out_off, int32_t stat,
+                                        double* row_sums, double* col_sums, int64_t n_out,
+                                        void* stream) {
+  PGLD_REQUIRE(h, h != nullptr, "pgld_hap_window_snp_sums: NULL handle");
+  PGLD_REQUIRE(h, panel != nullptr && panel->n_pops == 1,
+               "pgld_hap_window_snp_sums: one population per call");
+  PGLD_REQUIRE(h, panel->n_words[0] >= 1 && panel->n_snp >= 0, "pgld_hap_window_snp_sums: panel");
+  PGLD_REQUIRE(h, n_win >= 0 && n_idx >= 0 && n_out >= 0, "pgld_hap_window_snp_sums: sizes");
+  PGLD_REQUIRE(h, snp_idx != nullptr || n_idx == panel->n_snp,
+               "pgld_hap_window_snp_sums: without an index list n_idx must be n_snp");
+  PGLD_REQUIRE(h, stat >= 0 && stat < pgld::win::kCols, "pgld_hap_window_snp_sums: stat %d",
+               (int)stat);
+  if (n_win == 0) return PGLD_OK;
+  PGLD_REQUIRE(h, win_begin && win_end && out_off && row_sums && col_sums,
+               "pgld_hap_window_snp_sums: NULL buffer");
+  PGLD_REQUIRE(h, panel->planes[0] != nullptr || panel->n_snp == 0,
+               "pgld_hap_window_snp_sums: NULL planes");
+  PGLD_CHECK_CUDA(h, cudaSetDevice(h->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  PGLD_CHECK_CUDA(h, cudaMemsetAsync(row_sums, 0, (size_t)n_out * 8, st));
+  PGLD_CHECK_CUDA(h, cudaMemsetAsync(col_sums, 0, (size_t)n_out * 8, st));
+  return window_run(h, panel, snp_idx, n_idx, reinterpret_cast<const i64*>(win_begin),
+                    reinterpret_cast<const i64*>(win_end), n_win, nullptr, nullptr, (int)stat,
+                    reinterpret_cast<const i64*>(out_off), row_sums, col_sums, st);
 }

@@ -57,5 +57,35 @@ __device__ __forceinline__ void window_pair(const fast::Pop& p, int n, float c1,
   }
 }
 
+// the value of one statistic of a pair (column stat of window_pair, 0 where
+// window_pair adds nothing), the same arithmetic as window_pair
+__device__ __forceinline__ float pair_stat(int stat, const fast::Pop& p, int n, float c1,
+                                           float inv_n, float r4n, float4 si, float4 sj) {
+  if (stat == 0) {
+    const float rden = fast::x2_value(fast::x2_prod(p.pA * p.qA, p.pB * p.qB));
+    return rden > 0.f ? __fdividef(fast::x2_value(fast::x2_prod(p.x, p.x)), rden) : 0.f;
+  }
+  if (stat <= 4) {
+    if (n < 4) return 0.f;
+    if (stat == 1) {
+      const float pi = fast::pi2_num(p);
+      return pi != 0.f ? __fdividef(fast::dd_num(p), pi) : 0.f;
+    }
+    if (stat == 2) return fast::dd_num(p) * r4n;
+    if (stat == 3) return fast::dz_num(p) * r4n;
+    return fast::pi2_num(p) * r4n;
+  }
+  if (!(si.w > 0.f && sj.w > 0.f)) return 0.f;
+  float D;
+  if (n > 0) {
+    fast::X2 num = fast::x2_prod(c1, si.y * sj.y);
+    fast::x2_add_prod(num, -(float)n, si.x * sj.x);
+    D = fast::x2_value(num) * inv_n * si.z * sj.z;
+  } else {
+    D = -(si.x * si.z) * (sj.x * sj.z);
+  }
+  return (D * D) * (si.w * sj.w);
+}
+
 }  // namespace win
 }  // namespace pgld

@@ -18,7 +18,8 @@ from . import _ops
 from .ld_pipeline import case_of
 
 __all__ = ["dd", "dz", "pi2", "dd_within", "dd_between", "r", "r_squared", "d_prime",
-           "compute_ld_statistics", "rogers_huff_r", "rogers_huff_r_squared"]
+           "compute_ld_statistics", "rogers_huff_r", "rogers_huff_r_squared", "zns",
+           "windowed_zns", "omega", "windowed_omega"]
 
 
 def _counts(counts):
@@ -253,3 +254,90 @@ def zns(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
     if m < 2:
         return 0.0
     return float((r2.sum() - torch.trace(r2)) / (m * (m - 1)))
+
+
+# --------------------------------------------------------------------------
+# Kim and Nielsen's omega (ld_statistics.py:734-862, windowed_analysis.py:2051)
+# --------------------------------------------------------------------------
+def _omega_estimator(estimator, is_hm):
+    """'auto' -> sigma_d2 for a HaplotypeMatrix (ld_statistics.py:344-363)."""
+    if estimator == "auto":
+        return "sigma_d2" if is_hm else "rogers_huff"
+    if estimator not in ("r2", "sigma_d2", "rogers_huff"):
+        raise ValueError(f"Unknown estimator: {estimator!r} "
+                         "(expected one of 'auto', 'r2', 'sigma_d2', 'rogers_huff')")
+    return estimator
+
+
+def _omega_windows(hm, win_start, win_stop, column):
+    """omega of each SNP window [win_start[w], win_stop[w]) of hm over its
+    segregating sites, one launch for all windows: the per-site row and
+    column sums of the pair statistic (window column `column`) give every
+    split point's block sums."""
+    hm.transfer_to_gpu()
+    seg = _segregating_index(hm.haplotypes)
+    seg_np = seg.cpu().numpy()
+    b = np.searchsorted(seg_np, np.asarray(win_start, np.int64), side="left").astype(np.int64)
+    e = np.searchsorted(seg_np, np.asarray(win_stop, np.int64), side="left").astype(np.int64)
+    rows, cols, off = _ops.window_snp_sums(hm.packed(None), seg, b, e, column)
+    rows, cols = rows.cpu().numpy(), cols.cpu().numpy()
+    return np.array([_ops.omega_from_sums(rows[off[w]:off[w + 1]], cols[off[w]:off[w + 1]])
+                     for w in range(len(b))])
+
+
+def omega(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
+    """Kim and Nielsen's omega: the largest ratio of the mean LD within the two
+    blocks of a split of the sites to the mean LD across them, over splits
+    l = 3 .. m-2 of the upper triangle (ld_statistics.py:761-862).
+
+    A HaplotypeMatrix uses its segregating sites (after dropping sites with
+    missing calls for missing_data="exclude") and the unbiased sigma_D^2 =
+    DD / pi2 numerators by default ("auto"), or naive r^2 ("r2",
+    "rogers_huff"); the pair statistics are reduced on the device to per-site
+    row and column sums (no m x m matrix).  A precomputed square r^2 matrix is
+    used as given.  0.0 below 5 sites."""
+    from .haplotype_matrix import HaplotypeMatrix
+    is_hm = isinstance(r2_matrix_or_matrix, HaplotypeMatrix)
+    estimator = _omega_estimator(estimator, is_hm)
+    if estimator == "sigma_d2" and not is_hm:
+        raise ValueError("estimator='sigma_d2' requires a HaplotypeMatrix")
+    if is_hm:
+        hm = r2_matrix_or_matrix
+        hm.transfer_to_gpu()
+        if missing_data == "exclude":
+            keep = ((hm.haplotypes < 0).sum(0) == 0).nonzero().flatten()
+            hm = hm.get_subset(keep)
+        column = 1 if estimator == "sigma_d2" else 5
+        return float(_omega_windows(hm, [0], [hm.num_variants], column)[0])
+    if hasattr(r2_matrix_or_matrix, "genotypes"):
+        raise NotImplementedError("omega of a GenotypeMatrix (diploid r^2 matrix) is not built")
+    import torch
+    r2 = L.as_device(r2_matrix_or_matrix, np.float64)
+    if r2.dim() != 2 or r2.shape[0] != r2.shape[1]:
+        raise ValueError("omega needs a square r^2 matrix")
+    up = torch.triu(r2, diagonal=1)
+    return _ops.omega_from_sums(up.sum(1).cpu().numpy(), up.sum(0).cpu().numpy())
+
+
+def windowed_omega(matrix, win_start, win_stop, missing_data="include", estimator="auto"):
+    """Per-window omega of SNP windows [win_start[w], win_stop[w]) of a
+    HaplotypeMatrix in one launch: the omega column of windowed_analysis
+    (windowed_analysis.py:2014-2062), NaN for windows of fewer than 4 SNPs."""
+    estimator = _omega_estimator(estimator, True)
+    hm = matrix
+    ws = np.asarray(win_start, np.int64)
+    we = np.asarray(win_stop, np.int64)
+    if ws.shape != we.shape:
+        raise ValueError("win_start and win_stop must have the same shape")
+    if missing_data == "exclude":
+        hm.transfer_to_gpu()
+        keep = ((hm.haplotypes < 0).sum(0) == 0).nonzero().flatten()
+        keep_np = keep.cpu().numpy()
+        ws2 = np.searchsorted(keep_np, ws, side="left")
+        we2 = np.searchsorted(keep_np, we, side="left")
+        hm = hm.get_subset(keep)
+    else:
+        ws2, we2 = ws, we
+    out = _omega_windows(hm, ws2, we2, 1 if estimator == "sigma_d2" else 5)
+    out[(we - ws) < 4] = np.nan
+    return out

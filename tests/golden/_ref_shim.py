@@ -179,7 +179,8 @@ def _make_cupy():
                  "tile", "nonzero", "argsort", "sort", "count_nonzero", "fill_diagonal",
                  "asnumpy", "nansum", "nanmean", "dot", "matmul", "einsum", "bincount",
                  "logical_and", "logical_or", "logical_not", "floor", "ceil", "round",
-                 "minimum", "maximum", "prod", "cumprod", "max", "min", "float_"):
+                 "minimum", "maximum", "prod", "cumprod", "max", "min", "float_", "triu",
+                 "tril", "argmax"):
         if hasattr(np, name):
             fn = getattr(np, name)
             setattr(cp, name, _wrapped(fn) if callable(fn) else fn)
@@ -230,6 +231,28 @@ def load_reference_modules():
         setattr(pkg, mod, m)
         _LOADED[mod] = m
     return _LOADED
+
+
+def load_haplotype_matrix():
+    """The reference's HaplotypeMatrix class (haplotype_matrix.py), with empty
+    stand-ins for its unused imports allel and tskit (absent here)."""
+    if "haplotype_matrix" in _LOADED:
+        return _LOADED["haplotype_matrix"].HaplotypeMatrix
+    load_reference_modules()
+    for name in ("allel", "tskit"):
+        stub = sys.modules.setdefault(name, types.ModuleType(name))
+        if name == "tskit" and not hasattr(stub, "TreeSequence"):
+            stub.TreeSequence = type("TreeSequence", (), {})  # annotation only
+    pkg = sys.modules["pg_gpu"]
+    for mod in ("accessible", "haplotype_matrix"):
+        path = os.path.join(REF_ROOT, "pg_gpu", mod + ".py")
+        spec = importlib.util.spec_from_file_location("pg_gpu." + mod, path)
+        m = importlib.util.module_from_spec(spec)
+        sys.modules["pg_gpu." + mod] = m
+        spec.loader.exec_module(m)
+        setattr(pkg, mod, m)
+        _LOADED[mod] = m
+    return _LOADED["haplotype_matrix"].HaplotypeMatrix
 
 
 def garr(x):

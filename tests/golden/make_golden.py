@@ -377,6 +377,29 @@ def gen_windows(M):
                         zns_proj=np.array(zp, np.float64), zns_naive=np.array(zn, np.float64))
 
 
+def gen_omega(M):
+    """Kim and Nielsen's omega from the reference (ld_statistics.omega,
+    ld_statistics.py:761-862) on HaplotypeMatrix inputs: the default sigma_D^2
+    estimator, naive r^2, missing_data 'exclude'; and on a precomputed r^2
+    matrix (the reference's own pairwise_r2)."""
+    ls = M["ld_statistics"]
+    HM = S.load_haplotype_matrix()
+    out = {}
+    for k, (H, m, F, sw, miss) in enumerate([(40, 100, 6, 0.02, 0.0), (64, 180, 8, 0.01, 0.03),
+                                             (30, 60, 4, 0.05, 0.05)]):
+        rng = np.random.default_rng(20261210 + k)
+        hap = copying_model(rng, H, m, F, sw, missing=miss)
+        pos = np.arange(m, dtype=np.int64) * 1000
+        out[f"hap{k}"] = hap
+        out[f"omega_sd2_{k}"] = ls.omega(HM(hap.copy(), pos.copy()))
+        out[f"omega_r2_{k}"] = ls.omega(HM(hap.copy(), pos.copy()), estimator="r2")
+        out[f"omega_sd2_excl_{k}"] = ls.omega(HM(hap.copy(), pos.copy()), missing_data="exclude")
+        r2 = np.asarray(HM(hap.copy(), pos.copy()).pairwise_r2())
+        out[f"r2_{k}"] = r2
+        out[f"omega_arr_{k}"] = ls.omega(S.garr(r2))
+    np.savez_compressed(os.path.join(HERE, "omega.npz"), **out)
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -387,6 +410,7 @@ def main():
     gen_geno_stats(M)
     gen_geno_binned(M)
     gen_windows(M)
+    gen_omega(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

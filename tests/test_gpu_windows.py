@@ -99,3 +99,48 @@ def test_window_errors(form):
     with pytest.raises(IndexError):
         _ops.window_sums(pk, torch.tensor([0, 3, 99], dtype=torch.int32, device="cuda"), [0], [3],
                          form=form)
+
+
+def test_omega_matches_reference(golden):
+    """omega of a HaplotypeMatrix from per-site row / column sums on the device
+    equals the reference's omega (sigma_D^2, naive r^2, missing_data
+    'exclude', precomputed r^2 matrix)."""
+    z = golden("omega")
+    for k in range(3):
+        h = z[f"hap{k}"]
+        pos = np.arange(h.shape[1], dtype=np.int64) * 1000
+        hm = lambda: HaplotypeMatrix(h.copy(), pos.copy())  # noqa: E731
+        np.testing.assert_allclose(ld_statistics.omega(hm()), z[f"omega_sd2_{k}"], rtol=1e-5)
+        np.testing.assert_allclose(ld_statistics.omega(hm(), estimator="r2"), z[f"omega_r2_{k}"],
+                                   rtol=1e-5)
+        np.testing.assert_allclose(ld_statistics.omega(hm(), missing_data="exclude"),
+                                   z[f"omega_sd2_excl_{k}"], rtol=1e-5, atol=1e-12)
+        np.testing.assert_allclose(ld_statistics.omega(z[f"r2_{k}"]), z[f"omega_arr_{k}"],
+                                   rtol=1e-12)
+    with pytest.raises(ValueError, match="HaplotypeMatrix"):
+        ld_statistics.omega(z["r2_0"], estimator="sigma_d2")
+    with pytest.raises(ValueError, match="Unknown estimator"):
+        ld_statistics.omega(z["r2_0"], estimator="nonsense")
+    assert ld_statistics.omega(np.zeros((4, 4))) == 0.0
+
+
+@pytest.mark.parametrize("H", [40, 300])
+def test_windowed_omega_matches_oracle(H):
+    rng = np.random.default_rng(H + 7)
+    M = 400
+    hap = copying_model(rng, H, M, 6, 0.01, missing=0.02)
+    pos = np.arange(M, dtype=np.int64) * 100
+    ws = np.array([0, 10, 50, 50, 200, 390, 100])
+    we = np.array([3, 60, 130, 400, 330, 400, 102])
+    hm = HaplotypeMatrix(hap, pos)
+    for est in ("sigma_d2", "r2"):
+        got = ld_statistics.windowed_omega(hm, ws, we, estimator=est)
+        for w in range(len(ws)):
+            if we[w] - ws[w] < 4:
+                assert np.isnan(got[w])
+                continue
+            want = O.omega_hap(hap[:, ws[w]:we[w]], est)
+            np.testing.assert_allclose(got[w], want, rtol=2e-5, atol=1e-12)
+    # one window and the single-matrix call agree
+    one = ld_statistics.windowed_omega(hm, [0], [M])[0]
+    np.testing.assert_allclose(one, ld_statistics.omega(HaplotypeMatrix(hap, pos)), rtol=1e-12)

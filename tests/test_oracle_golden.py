@@ -229,3 +229,17 @@ def test_window_zns_matches_reference(golden):
     for k, (s, e) in enumerate(zip(b[:-1], b[1:])):
         assert O.zns_window(z["hap"], s, e, True) == pytest.approx(z["zns_proj"][k], rel=1e-12)
         assert O.zns_window(z["hap"], s, e, False) == pytest.approx(z["zns_naive"][k], rel=1e-12)
+
+
+def test_omega_matches_reference(golden):
+    """Kim and Nielsen's omega (ld_statistics.py:761-862): sigma_D^2 and naive
+    r^2 over segregating sites, missing_data 'exclude', and a precomputed r^2
+    matrix, against the reference's own results."""
+    z = golden("omega")
+    for k in range(3):
+        h = z[f"hap{k}"]
+        np.testing.assert_allclose(O.omega_hap(h), z[f"omega_sd2_{k}"], rtol=1e-12)
+        np.testing.assert_allclose(O.omega_hap(h, "r2"), z[f"omega_r2_{k}"], rtol=1e-12)
+        np.testing.assert_allclose(O.omega_hap(h, missing_data="exclude"),
+                                   z[f"omega_sd2_excl_{k}"], rtol=1e-12)
+        np.testing.assert_allclose(O.omega_matrix(z[f"r2_{k}"]), z[f"omega_arr_{k}"], rtol=1e-12)
