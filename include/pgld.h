@@ -343,6 +343,18 @@ int pgld_hap_window_snp_sums(pgld_handle h, const pgld_hap_panel* panel, const i
                              int32_t n_win, const int64_t* out_off, int32_t stat,
                              double* row_sums, double* col_sums, int64_t n_out, void* stream);
 
+/* locate_unlinked pruning on the host (as the reference's): sliding windows
+ * of `size` variants advanced by `step`; within a window, for still-active
+ * variants i < j in order, j is dropped when r2 of the pair (i, j) exceeds
+ * threshold.  r2: HOST float64 values of the band pairs j - i < size in row
+ * order (row i at pair_off[i], pair k of it j = i + 1 + k, as
+ * pgld_count_pairs_within / pgld_pairs_within over positions 0..n_snp-1 with
+ * max_dist size - 1); pair_off: HOST int64 [n_snp + 1].  loc: HOST uint8
+ * [n_snp] out, 1 = kept.  Replaces the pruning loop of
+ * HaplotypeMatrix.locate_unlinked (haplotype_matrix.py:1172-1233). */
+int pgld_prune_unlinked(pgld_handle h, const double* r2, const int64_t* pair_off, int64_t n_snp,
+                        int32_t size, int32_t step, double threshold, uint8_t* loc);
+
 /* pgld_hap_binned_sums for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers of this library cannot call
  * cudaMalloc: a host application that hands every byte of the device to its

@@ -1163,3 +1163,28 @@ def omega_hap(hap, estimator="sigma_d2", missing_data="include"):
     if h.shape[1] < 2:
         return 0.0
     return omega_matrix(pair_stat_matrix(h, 1 if estimator == "sigma_d2" else 5))
+
+
+# ---------------------------------------------------------------------------
+# locate_unlinked  (haplotype_matrix.py:1172-1233)
+# ---------------------------------------------------------------------------
+def locate_unlinked(hap, size=100, step=20, threshold=0.1):
+    """Sliding windows of `size` variants advanced by `step`; within a window,
+    for active variants i < j in order, j is dropped when naive r^2(i, j) >
+    threshold (naive r^2 of pair_stat_matrix column 5 on the active subset)."""
+    h = np.asarray(hap)
+    m = h.shape[1]
+    loc = np.ones(m, dtype=bool)
+    for ws in range(0, m, step):
+        we = min(ws + size, m)
+        act = np.where(loc[ws:we])[0] + ws
+        if len(act) <= 1:
+            continue
+        r2 = pair_stat_matrix(h[:, act], 5)
+        for a in range(len(act)):
+            if not loc[act[a]]:
+                continue
+            for b in range(a + 1, len(act)):
+                if loc[act[b]] and r2[a, b] > threshold:
+                    loc[act[b]] = False
+    return loc

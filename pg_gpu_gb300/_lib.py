@@ -111,6 +111,7 @@ _SIGS = {
     "pgld_hap_window_snp_sums": ([_P, ctypes.POINTER(HapPanel), _P, _I64, _P, _P, _I32, _P, _I32,
                                   _P, _P, _I64, _P],
                                  ctypes.c_int),
+    "pgld_prune_unlinked": ([_P, _P, _P, _I64, _I32, _I32, _D, _P], ctypes.c_int),
 }
 
 _lib = None

@@ -779,3 +779,47 @@ extern "C" int pgld_pairs_within(pgld_handle h, const double* pos, int64_t n_snp
   PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));
   return PGLD_OK;
 }
+
+// ---------------------------------------------------------------------------
+// locate_unlinked pruning (host): sliding windows of `size` variants advanced
+// by `step`; within a window, for active variants i < j in order, j is
+// dropped when r2[pair (i, j)] > threshold.  r2 holds the band pairs j - i <
+// size in row order (row i at pair_off[i], j = i + 1 + k), as the band pair
+// list of positions 0..n_snp-1 within size - 1.  Follows
+// HaplotypeMatrix.locate_unlinked (haplotype_matrix.py:1172-1233), whose
+// pruning also runs on the host.
+// ---------------------------------------------------------------------------
+extern "C" int pgld_prune_unlinked(pgld_handle h, const double* r2, const int64_t* pair_off,
+                                   int64_t n_snp, int32_t size, int32_t step, double threshold,
+                                   uint8_t* loc) {
+  PGLD_REQUIRE(h, h != nullptr, "pgld_prune_unlinked: NULL handle");
+  PGLD_REQUIRE(h, size >= 1 && step >= 1, "pgld_prune_unlinked: size %d, step %d", (int)size,
+               (int)step);
+  PGLD_REQUIRE(h, n_snp >= 0, "pgld_prune_unlinked: n_snp < 0");
+  if (n_snp == 0) return PGLD_OK;
+  PGLD_REQUIRE(h, pair_off && loc && (r2 || pair_off[n_snp] == 0),
+               "pgld_prune_unlinked: NULL buffer");
+  for (int64_t s = 0; s < n_snp; ++s) loc[s] = 1;
+  std::vector<int64_t> act;
+  act.reserve((size_t)size);
+  for (int64_t ws = 0; ws < n_snp; ws += step) {
+    const int64_t we = std::min<int64_t>(ws + size, n_snp);
+    act.clear();
+    for (int64_t s = ws; s < we; ++s)
+      if (loc[s]) act.push_back(s);
+    if (act.size() <= 1) continue;
+    for (size_t a = 0; a < act.size(); ++a) {
+      const int64_t i = act[a];
+      if (!loc[i]) continue;
+      const int64_t row = pair_off[i], row_n = pair_off[i + 1] - row;
+      for (size_t b = a + 1; b < act.size(); ++b) {
+        const int64_t j = act[b];
+        if (!loc[j]) continue;
+        PGLD_REQUIRE(h, j - i - 1 < row_n, "pgld_prune_unlinked: pair (%lld, %lld) not in the band",
+                     (long long)i, (long long)j);
+        if (r2[row + (j - i - 1)] > threshold) loc[j] = 0;
+      }
+    }
+  }
+  return PGLD_OK;
+}

@@ -358,6 +358,50 @@ class HaplotypeMatrix:
         r2.fill_diagonal_(0)
         return r2
 
+    def locate_unlinked(self, size=100, step=20, threshold=0.1):
+        """Variants in approximate linkage equilibrium (haplotype_matrix.py:1172-1233):
+        windows of `size` variants advanced by `step`; within a window an
+        active variant j is dropped when its naive r^2 with an earlier active
+        variant i exceeds threshold.  The naive r^2 of every pair closer than
+        `size` variants comes from one band-pair call on the device (D =
+        n11 / n - p_i p_j over the pair's valid haplotypes, p per site); the
+        greedy pruning runs on the host, as in the reference."""
+        import ctypes
+        import torch
+        size, step = int(size), int(step)
+        if size < 1 or step < 1:
+            raise ValueError("size and step must be positive")
+        m = self.num_variants
+        pk = self.packed(None)
+        if pk.has_other:
+            raise NotImplementedError("locate_unlinked of non-biallelic codes")
+        dev = pk.planes.device
+        pos_d = torch.arange(m, dtype=torch.float64, device=dev)
+        off, n = _ops.band_offsets(pos_d, size - 1)
+        counts, nv, _ = _ops.band_pairs(pk, pos_d, size - 1, with_stats=False)
+        h = self._pinned if (self._device == "CPU" and self._pinned is not None) else None
+        h = L.as_device(self._haplotypes if h is None else h, np.int8)
+        dac = (h == 1).sum(0).to(torch.float64)
+        nvs = (h >= 0).sum(0).to(torch.float64)
+        p = torch.where(nvs > 0, dac / torch.where(nvs > 0, nvs, 1.0), 0.0)
+        rows = torch.repeat_interleave(torch.arange(m, device=dev), off[1:] - off[:-1])
+        k = torch.arange(n, device=dev)
+        cols = rows + 1 + (k - off[:-1][rows])
+        c = counts.to(torch.float64)
+        nn = nv.to(torch.float64) if pk.has_missing else c.sum(1)
+        D = torch.where(nn > 0, c[:, 0] / torch.where(nn > 0, nn, 1.0), 0.0) - p[rows] * p[cols]
+        den = p[rows] * (1 - p[rows]) * p[cols] * (1 - p[cols])
+        r2 = torch.where(den > 0, D * D / torch.where(den > 0, den, 1.0), 0.0)
+        r2_h = np.ascontiguousarray(r2.cpu().numpy())
+        off_h = np.ascontiguousarray(off.cpu().numpy())
+        loc = np.zeros(m, dtype=np.uint8)
+        hd = L.handle()
+        L.check(L.lib().pgld_prune_unlinked(hd, r2_h.ctypes.data_as(ctypes.c_void_p),
+                                            off_h.ctypes.data_as(ctypes.c_void_p), m, size, step,
+                                            float(threshold),
+                                            loc.ctypes.data_as(ctypes.c_void_p)), hd)
+        return loc.astype(bool)
+
     def pairwise_LD_v(self):
         D, _ = self._pairwise_ld_core()
         D.fill_diagonal_(0)

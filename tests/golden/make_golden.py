@@ -400,6 +400,25 @@ def gen_omega(M):
     np.savez_compressed(os.path.join(HERE, "omega.npz"), **out)
 
 
+def gen_unlinked(M):
+    """HaplotypeMatrix.locate_unlinked (haplotype_matrix.py:1172-1233) from the
+    reference: sliding windows, greedy pruning on naive r^2."""
+    HM = S.load_haplotype_matrix()
+    out = {}
+    for k, (H, m, F, sw, miss, size, step, thr) in enumerate(
+            [(40, 300, 6, 0.05, 0.0, 100, 20, 0.1), (64, 500, 8, 0.02, 0.03, 50, 10, 0.2),
+             (30, 120, 3, 0.2, 0.05, 7, 3, 0.05)]):
+        rng = np.random.default_rng(20261211 + k)
+        hap = copying_model(rng, H, m, F, sw, missing=miss)
+        pos = np.arange(m, dtype=np.int64) * 100
+        loc = HM(hap.copy(), pos.copy()).locate_unlinked(size=size, step=step, threshold=thr)
+        out[f"hap{k}"] = hap
+        out[f"args{k}"] = np.array([size, step], np.int64)
+        out[f"thr{k}"] = np.float64(thr)
+        out[f"loc{k}"] = np.asarray(loc, bool)
+    np.savez_compressed(os.path.join(HERE, "unlinked.npz"), **out)
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -411,6 +430,7 @@ def main():
     gen_geno_binned(M)
     gen_windows(M)
     gen_omega(M)
+    gen_unlinked(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -144,3 +144,21 @@ def test_windowed_omega_matches_oracle(H):
     # one window and the single-matrix call agree
     one = ld_statistics.windowed_omega(hm, [0], [M])[0]
     np.testing.assert_allclose(one, ld_statistics.omega(HaplotypeMatrix(hap, pos)), rtol=1e-12)
+
+
+def test_locate_unlinked_matches_reference(golden):
+    """Greedy pruning on naive r^2 of every pair closer than `size` variants
+    (band pairs on the device, pruning on the host) equals the reference."""
+    z = golden("unlinked")
+    for k in range(3):
+        size, step = (int(v) for v in z[f"args{k}"])
+        h = z[f"hap{k}"]
+        hm = HaplotypeMatrix(h, np.arange(h.shape[1], dtype=np.int64) * 100)
+        got = hm.locate_unlinked(size=size, step=step, threshold=float(z[f"thr{k}"]))
+        assert np.array_equal(got, z[f"loc{k}"])
+    rng = np.random.default_rng(3)
+    h = copying_model(rng, 300, 700, 5, 0.02, missing=0.02)
+    hm = HaplotypeMatrix(h, np.arange(700, dtype=np.int64))
+    assert np.array_equal(hm.locate_unlinked(64, 16, 0.3), O.locate_unlinked(h, 64, 16, 0.3))
+    with pytest.raises(ValueError):
+        hm.locate_unlinked(0, 1)

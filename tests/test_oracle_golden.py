@@ -243,3 +243,11 @@ def test_omega_matches_reference(golden):
         np.testing.assert_allclose(O.omega_hap(h, missing_data="exclude"),
                                    z[f"omega_sd2_excl_{k}"], rtol=1e-12)
         np.testing.assert_allclose(O.omega_matrix(z[f"r2_{k}"]), z[f"omega_arr_{k}"], rtol=1e-12)
+
+
+def test_locate_unlinked_matches_reference(golden):
+    z = golden("unlinked")
+    for k in range(3):
+        size, step = (int(v) for v in z[f"args{k}"])
+        got = O.locate_unlinked(z[f"hap{k}"], size, step, float(z[f"thr{k}"]))
+        assert np.array_equal(got, z[f"loc{k}"])
