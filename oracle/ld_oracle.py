@@ -1188,3 +1188,43 @@ def locate_unlinked(hap, size=100, step=20, threshold=0.1):
                 if loc[act[b]] and r2[a, b] > threshold:
                     loc[act[b]] = False
     return loc
+
+
+# ---------------------------------------------------------------------------
+# diploid dosage r^2, ZnS and omega of a GenotypeMatrix  (ld_statistics.py:973-1020)
+# ---------------------------------------------------------------------------
+def r2_matrix_diploid(geno):
+    """Squared dosage correlation: per-site means over valid individuals,
+    centred dosages with missing entries zeroed, cov = gn^T gn over
+    sqrt(var_i var_j) (0 where the denominator is 0), zero diagonal."""
+    g = np.asarray(geno)
+    valid = (g >= 0).astype(np.float64)
+    gc = np.where(g >= 0, g, 0).astype(np.float64)
+    nv = valid.sum(0)
+    mean = np.where(nv > 0, gc.sum(0) / np.maximum(nv, 1), 0.0)
+    gn = (gc - mean[None, :]) * valid
+    var = (gn ** 2).sum(0)
+    cov = gn.T @ gn
+    den = np.sqrt(np.outer(var, var))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r2 = np.where(den > 0, (cov / np.where(den > 0, den, 1)) ** 2, 0.0)
+    np.fill_diagonal(r2, 0.0)
+    return r2
+
+
+def zns_diploid(geno, missing_data="include"):
+    g = np.asarray(geno)
+    if missing_data == "exclude":
+        g = g[:, (g < 0).sum(0) == 0]
+    m = g.shape[1]
+    if m < 2:
+        return 0.0
+    r2 = r2_matrix_diploid(g)
+    return float((r2.sum() - np.trace(r2)) / (m * (m - 1)))
+
+
+def omega_diploid(geno, missing_data="include"):
+    g = np.asarray(geno)
+    if missing_data == "exclude":
+        g = g[:, (g < 0).sum(0) == 0]
+    return omega_matrix(r2_matrix_diploid(g))

@@ -19,7 +19,7 @@ from .ld_pipeline import case_of
 
 __all__ = ["dd", "dz", "pi2", "dd_within", "dd_between", "r", "r_squared", "d_prime",
            "compute_ld_statistics", "rogers_huff_r", "rogers_huff_r_squared", "zns",
-           "windowed_zns", "omega", "windowed_omega"]
+           "windowed_zns", "omega", "windowed_omega", "zns_diploid", "omega_diploid"]
 
 
 def _counts(counts):
@@ -230,7 +230,10 @@ def zns(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
     A HaplotypeMatrix takes the unbiased sigma_D^2 estimator by default
     ("auto"), or naive r^2 ("r2"), over its segregating sites (missing_data
     "exclude" first drops sites with missing calls), in one device pass; a
-    precomputed square r^2 matrix gives its mean off-diagonal value.
+    GenotypeMatrix the squared dosage correlation of all its sites
+    (_r2_matrix_diploid, ld_statistics.py:973-1020) from the 9-way joint
+    genotype counts; a precomputed square r^2 matrix gives its mean
+    off-diagonal value.
     """
     from .haplotype_matrix import HaplotypeMatrix
     is_hm = isinstance(r2_matrix_or_matrix, HaplotypeMatrix)
@@ -248,12 +251,83 @@ def zns(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
     if estimator == "sigma_d2":
         raise ValueError("estimator='sigma_d2' requires a HaplotypeMatrix, "
                          "not a pre-computed r² array")
+    if _is_genotype_matrix(r2_matrix_or_matrix):
+        row, _ = _diploid_row_col_sums(r2_matrix_or_matrix, missing_data)
+        m = row.size
+        return float(2.0 * row.sum() / (m * (m - 1))) if m >= 2 else 0.0
     import torch
     r2 = L.as_device(r2_matrix_or_matrix, np.float64)
     m = r2.shape[0]
     if m < 2:
         return 0.0
     return float((r2.sum() - torch.trace(r2)) / (m * (m - 1)))
+
+
+# --------------------------------------------------------------------------
+# diploid dosage r^2 of a GenotypeMatrix (ld_statistics.py:973-1020)
+# --------------------------------------------------------------------------
+def _is_genotype_matrix(x):
+    from .genotype_matrix import GenotypeMatrix
+    return isinstance(x, GenotypeMatrix)
+
+
+def _diploid_row_col_sums(gm, missing_data="include", chunk_pairs=1 << 24):
+    """Per-site row and column sums of the upper triangle of the squared
+    dosage-correlation matrix of _r2_matrix_diploid, from the 9-way joint
+    genotype counts of every site pair (pgld_geno_counts_pairs): with per-site
+    means mu and variances var over the valid individuals, the covariance of
+    centred dosages with missing entries zeroed is sum_ab (a - mu_i)(b - mu_j)
+    n_ab over the jointly valid individuals.  Returns (row, col) float64 on the
+    host; pairs are processed in chunks of about chunk_pairs."""
+    import torch
+    gm.transfer_to_gpu()
+    g = L.as_device(gm.genotypes, np.int8)
+    if missing_data == "exclude":
+        keep = ((g < 0).sum(0) == 0).nonzero().flatten()
+        gm = gm.get_subset(keep)
+        g = L.as_device(gm.genotypes, np.int8)
+    m = g.shape[1]
+    dev = g.device
+    row = torch.zeros(m, dtype=torch.float64, device=dev)
+    col = torch.zeros(m, dtype=torch.float64, device=dev)
+    if m < 2:
+        return row.cpu().numpy(), col.cpu().numpy()
+    pk = gm.packed(None)
+    if pk.has_other:
+        raise NotImplementedError("diploid r^2 of dosages above 2")
+    valid = g >= 0
+    gc = torch.where(valid, g, torch.zeros_like(g)).to(torch.float64)
+    nvs = valid.sum(0).to(torch.float64)
+    mu = torch.where(nvs > 0, gc.sum(0) / torch.where(nvs > 0, nvs, 1.0), 0.0)
+    var = (((gc - mu[None, :]) * valid) ** 2).sum(0)
+    av = torch.tensor([0., 0., 0., 1., 1., 1., 2., 2., 2.], dtype=torch.float64, device=dev)
+    bv = torch.tensor([0., 1., 2.] * 3, dtype=torch.float64, device=dev)
+    per_row = (m - 1 - torch.arange(m, device=dev)).cpu().numpy()
+    r0 = 0
+    while r0 < m - 1:
+        # rows [r0, r1) with about chunk_pairs pairs
+        cum = np.cumsum(per_row[r0:])
+        r1 = r0 + max(1, int(np.searchsorted(cum, chunk_pairs, side="right")))
+        r1 = min(r1, m - 1)
+        cnt = torch.as_tensor(per_row[r0:r1], device=dev)
+        ii = torch.repeat_interleave(torch.arange(r0, r1, device=dev), cnt)
+        start = torch.cumsum(cnt, 0) - cnt
+        k = torch.arange(ii.numel(), device=dev)
+        jj = ii + 1 + (k - torch.repeat_interleave(start, cnt))
+        c, _ = _ops.geno_counts_pairs(pk, ii.to(torch.int32), jj.to(torch.int32))
+        c = c.to(torch.float64)
+        s_ab = c @ (av * bv)
+        s_a = c @ av
+        s_b = c @ bv
+        n_ij = c.sum(1)
+        mi, mj = mu[ii], mu[jj]
+        cov = s_ab - mj * s_a - mi * s_b + mi * mj * n_ij
+        den = var[ii] * var[jj]
+        r2 = torch.where(den > 0, cov * cov / torch.where(den > 0, den, 1.0), 0.0)
+        row.index_add_(0, ii, r2)
+        col.index_add_(0, jj, r2)
+        r0 = r1
+    return row.cpu().numpy(), col.cpu().numpy()
 
 
 # --------------------------------------------------------------------------
@@ -294,8 +368,9 @@ def omega(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
     missing calls for missing_data="exclude") and the unbiased sigma_D^2 =
     DD / pi2 numerators by default ("auto"), or naive r^2 ("r2",
     "rogers_huff"); the pair statistics are reduced on the device to per-site
-    row and column sums (no m x m matrix).  A precomputed square r^2 matrix is
-    used as given.  0.0 below 5 sites."""
+    row and column sums (no m x m matrix).  A GenotypeMatrix uses the squared
+    dosage correlation of all its sites (as zns).  A precomputed square r^2
+    matrix is used as given.  0.0 below 5 sites."""
     from .haplotype_matrix import HaplotypeMatrix
     is_hm = isinstance(r2_matrix_or_matrix, HaplotypeMatrix)
     estimator = _omega_estimator(estimator, is_hm)
@@ -309,8 +384,8 @@ def omega(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
             hm = hm.get_subset(keep)
         column = 1 if estimator == "sigma_d2" else 5
         return float(_omega_windows(hm, [0], [hm.num_variants], column)[0])
-    if hasattr(r2_matrix_or_matrix, "genotypes"):
-        raise NotImplementedError("omega of a GenotypeMatrix (diploid r^2 matrix) is not built")
+    if _is_genotype_matrix(r2_matrix_or_matrix):
+        return _ops.omega_from_sums(*_diploid_row_col_sums(r2_matrix_or_matrix, missing_data))
     import torch
     r2 = L.as_device(r2_matrix_or_matrix, np.float64)
     if r2.dim() != 2 or r2.shape[0] != r2.shape[1]:
@@ -341,3 +416,8 @@ def windowed_omega(matrix, win_start, win_stop, missing_data="include", estimato
     out = _omega_windows(hm, ws2, we2, 1 if estimator == "sigma_d2" else 5)
     out[(we - ws) < 4] = np.nan
     return out
+
+
+# the reference's diploid names are aliases (ld_statistics.py:1026-1027)
+zns_diploid = zns
+omega_diploid = omega

@@ -180,7 +180,7 @@ def _make_cupy():
                  "asnumpy", "nansum", "nanmean", "dot", "matmul", "einsum", "bincount",
                  "logical_and", "logical_or", "logical_not", "floor", "ceil", "round",
                  "minimum", "maximum", "prod", "cumprod", "max", "min", "float_", "triu",
-                 "tril", "argmax"):
+                 "tril", "argmax", "trace"):
         if hasattr(np, name):
             fn = getattr(np, name)
             setattr(cp, name, _wrapped(fn) if callable(fn) else fn)
@@ -244,7 +244,7 @@ def load_haplotype_matrix():
         if name == "tskit" and not hasattr(stub, "TreeSequence"):
             stub.TreeSequence = type("TreeSequence", (), {})  # annotation only
     pkg = sys.modules["pg_gpu"]
-    for mod in ("accessible", "haplotype_matrix"):
+    for mod in ("accessible", "haplotype_matrix", "genotype_matrix"):
         path = os.path.join(REF_ROOT, "pg_gpu", mod + ".py")
         spec = importlib.util.spec_from_file_location("pg_gpu." + mod, path)
         m = importlib.util.module_from_spec(spec)

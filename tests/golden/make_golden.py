@@ -419,6 +419,29 @@ def gen_unlinked(M):
     np.savez_compressed(os.path.join(HERE, "unlinked.npz"), **out)
 
 
+def gen_diploid_ld(M):
+    """ZnS and omega of a GenotypeMatrix (zns_diploid / omega_diploid: the
+    dosage-correlation r^2 matrix of _r2_matrix_diploid, ld_statistics.py:
+    973-1020, then zns / omega of it), from the reference."""
+    ls = M["ld_statistics"]
+    S.load_haplotype_matrix()
+    GM = sys.modules["pg_gpu.genotype_matrix"].GenotypeMatrix
+    out = {}
+    for k, (n, m, miss) in enumerate([(30, 80, 0.0), (50, 120, 0.03), (20, 9, 0.1)]):
+        rng = np.random.default_rng(20261212 + k)
+        h = copying_model(rng, 2 * n, m, 6, 0.02)
+        g = (h[0::2] + h[1::2]).astype(np.int8)
+        g[rng.random(g.shape) < miss] = -1
+        pos = np.arange(m, dtype=np.int64) * 100
+        out[f"geno{k}"] = g
+        out[f"r2_{k}"] = np.asarray(ls._r2_matrix_diploid(S.garr(g)))
+        out[f"zns_{k}"] = ls.zns(GM(g.copy(), pos.copy()))
+        out[f"omega_{k}"] = ls.omega(GM(g.copy(), pos.copy()))
+        out[f"zns_excl_{k}"] = ls.zns(GM(g.copy(), pos.copy()), missing_data="exclude")
+        out[f"omega_excl_{k}"] = ls.omega(GM(g.copy(), pos.copy()), missing_data="exclude")
+    np.savez_compressed(os.path.join(HERE, "diploid_ld.npz"), **out)
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -431,6 +454,7 @@ def main():
     gen_windows(M)
     gen_omega(M)
     gen_unlinked(M)
+    gen_diploid_ld(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

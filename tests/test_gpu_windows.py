@@ -162,3 +162,27 @@ def test_locate_unlinked_matches_reference(golden):
     assert np.array_equal(hm.locate_unlinked(64, 16, 0.3), O.locate_unlinked(h, 64, 16, 0.3))
     with pytest.raises(ValueError):
         hm.locate_unlinked(0, 1)
+
+
+def test_diploid_zns_omega_match_reference(golden):
+    """zns / omega of a GenotypeMatrix (squared dosage correlation from 9-way
+    counts, pairs in chunks) equal the reference's zns_diploid / omega_diploid."""
+    from pg_gpu_gb300.genotype_matrix import GenotypeMatrix
+    z = golden("diploid_ld")
+    for k in range(3):
+        g = z[f"geno{k}"]
+        pos = np.arange(g.shape[1], dtype=np.int64) * 100
+        gm = lambda: GenotypeMatrix(g.copy(), pos.copy())  # noqa: E731
+        np.testing.assert_allclose(ld_statistics.zns_diploid(gm()), z[f"zns_{k}"], rtol=1e-10)
+        np.testing.assert_allclose(ld_statistics.omega_diploid(gm()), z[f"omega_{k}"], rtol=1e-10)
+        np.testing.assert_allclose(ld_statistics.zns(gm(), missing_data="exclude"),
+                                   z[f"zns_excl_{k}"], rtol=1e-10, atol=1e-15)
+        np.testing.assert_allclose(ld_statistics.omega(gm(), missing_data="exclude"),
+                                   z[f"omega_excl_{k}"], rtol=1e-10)
+    # chunked pair enumeration gives the same sums as one chunk
+    from pg_gpu_gb300.ld_statistics import _diploid_row_col_sums
+    g = z["geno1"]
+    a = _diploid_row_col_sums(GenotypeMatrix(g, np.arange(g.shape[1])), chunk_pairs=97)
+    b = _diploid_row_col_sums(GenotypeMatrix(g, np.arange(g.shape[1])))
+    np.testing.assert_allclose(a[0], b[0], rtol=1e-12)
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-12)

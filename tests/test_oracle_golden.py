@@ -251,3 +251,16 @@ def test_locate_unlinked_matches_reference(golden):
         size, step = (int(v) for v in z[f"args{k}"])
         got = O.locate_unlinked(z[f"hap{k}"], size, step, float(z[f"thr{k}"]))
         assert np.array_equal(got, z[f"loc{k}"])
+
+
+def test_diploid_zns_omega_match_reference(golden):
+    z = golden("diploid_ld")
+    for k in range(3):
+        g = z[f"geno{k}"]
+        np.testing.assert_allclose(O.r2_matrix_diploid(g), z[f"r2_{k}"], rtol=1e-12, atol=1e-15)
+        np.testing.assert_allclose(O.zns_diploid(g), z[f"zns_{k}"], rtol=1e-12)
+        np.testing.assert_allclose(O.omega_diploid(g), z[f"omega_{k}"], rtol=1e-12)
+        np.testing.assert_allclose(O.zns_diploid(g, "exclude"), z[f"zns_excl_{k}"], rtol=1e-12,
+                                   atol=1e-15)
+        np.testing.assert_allclose(O.omega_diploid(g, "exclude"), z[f"omega_excl_{k}"],
+                                   rtol=1e-12)
