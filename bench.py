@@ -144,6 +144,18 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def tc_roofline(pairs_per_s, ops_per_pair, basis):
+    """Tensor-pipe roofline of a tensor-core workload: ops_per_pair int8-
+    equivalent operations per pair (the algorithmic contraction), against 2 x
+    the measured bf16 dense rate (the E4M3 rate); basis names the timed region."""
+    peaks, src = measured_peaks()
+    peak = 2.0 * float(peaks["bf16_tflops"])
+    achieved = pairs_per_s * ops_per_pair / 1e12
+    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None, "ops_per_pair": ops_per_pair,
+            "peak_source": f"2 x {src} bf16_tflops (dense fp8 rate)", "timed": basis}
+
+
 def profile_traffic(form, workload):
     """dram bytes per launch of the dominant kernel from a committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "traffic.txt")
@@ -504,6 +516,7 @@ def run_windows(args):
         "dtype": "e4m3", "data": "synthetic (copying model, seed per window)",
         "config": {"workload": "windows512", "haplotypes": 400, "windows": 512,
                    "n_snp": int(sizes.sum()), "pairs": n_pairs, "form": "tc"},
+        "roofline": tc_roofline(n_pairs / (t_one / 1e3), 8 * 400, "whole call, wall clock"),
         "plain_one_launch": {"ms_per_step": t_plain, "value": n_pairs / (t_plain / 1e3)},
         "plain_per_window_launches": {"ms_per_step": t_per, "value": n_pairs / (t_per / 1e3),
                                       "ratio_tc_one_launch_over_this": t_per / t_one}}),
@@ -562,6 +575,7 @@ def run_geno_band(args):
         "config": {"workload": "geno_band", "individuals": 1000, "n_snp": M,
                    "max_dist_bp": 200_000, "pairs": n_pairs, "form": "tc",
                    "per_pair_bytes_written": (36 if args.geno_counts else 0) + 4 + 16},
+        "roofline": tc_roofline(n_pairs / (ms / 1e3), 9 * 2 * 1000, "whole call, wall clock"),
         "compare": {"form": "plain", "ms_per_step": res["plain"],
                     "value": n_pairs / (res["plain"] / 1e3),
                     "ratio_tc_over_plain": res["plain"] / ms}}), flush=True)
@@ -612,6 +626,7 @@ def run_hap_band(args):
         "data": "synthetic (copying model, 2 % missing)",
         "config": {"workload": "hap_band", "haplotypes": 2000, "n_snp": M,
                    "max_dist_bp": 100_000, "pairs": n_pairs, "per_pair_bytes_written": 36},
+        "roofline": tc_roofline(n_pairs / (res["tc"] / 1e3), 8 * 2000, "whole call, wall clock"),
         "compare": {"form": "plain", "ms_per_step": res["plain"],
                     "value": n_pairs / (res["plain"] / 1e3),
                     "ratio_tc_over_plain": res["plain"] / res["tc"]}}), flush=True)
