@@ -81,6 +81,7 @@ struct Params {
 // j0, the end of its range, and (windows mode) its window
 struct TileRef {
   long long i0, j0, end, bi, bj;
+  long long begin;  // first list position of the window (windows mode)
   int w;
 };
 
@@ -93,8 +94,11 @@ __device__ __forceinline__ TileRef decode_item(const Params& a, long long item) 
       const int mid = (lo + hi) >> 1;
       if (a.tile_off[mid] <= item) lo = mid; else hi = mid;
     }
-    const long long base = a.win_begin[lo], m = a.win_end[lo] - base;
-    const long long T = (m + kTileSnp - 1) / kTileSnp;
+    // tiles start at the window's first list position rounded down to a
+    // multiple of 8 (the operand rows are grouped by 8 positions); pairs
+    // before the window are masked
+    const long long base = a.win_begin[lo] & ~7ll, m = a.win_end[lo] - base;
+    const long long T = a.win_end[lo] > a.win_begin[lo] ? (m + kTileSnp - 1) / kTileSnp : 0;
     const long long t = item - a.tile_off[lo];
     long long rlo = 0, rhi = T;  // row bi starts at bi*T - bi(bi-1)/2
     while (rhi - rlo > 1) {
@@ -106,6 +110,7 @@ __device__ __forceinline__ TileRef decode_item(const Params& a, long long item) 
     r.i0 = base + r.bi * kTileSnp;
     r.j0 = base + r.bj * kTileSnp;
     r.end = base + m;
+    r.begin = a.win_begin[lo];
     r.w = lo;
   } else {
     long long lo = 0, hi = a.n_blocks;
@@ -118,6 +123,7 @@ __device__ __forceinline__ TileRef decode_item(const Params& a, long long item) 
     r.i0 = r.bi * kTileSnp;
     r.j0 = r.bj * kTileSnp;
     r.end = a.n_snp;
+    r.begin = 0;
     r.w = 0;
   }
   return r;
@@ -389,9 +395,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int e = warp - 4;
     const int quarter = warp & 3;
     const int half = e >> 2;
-    const int row = quarter * 32 + lane;  // D row: SNP i = row/2, plane = row&1
-    const int il = row >> 1, plane = row & 1;
-    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
     const bool use_int = MODE != kModeWindows && (a.bcoord == nullptr) && (*a.ipos_bad == 0);
@@ -405,7 +408,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       const long long bi = tr.bi, bj = tr.bj;
       const long long i0 = tr.i0, j0 = tr.j0;
       const long long si0 = i0 + 16 * quarter, sj0 = j0 + 32 * half;
-      const long long i = i0 + il;
 
       // classify the warp's sub-tile: 0 one bin, 1 two adjacent bins, 2 general
       int mode = 2, b0 = -1, thr_mid = 0;
@@ -436,42 +438,48 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc_fence_after();
 
       if constexpr (MODE == kModeWindows) {
-        // per-window sums: every pair of list positions a < b < end of the
-        // item's window (the statistics of pgld_hap_window_sums)
+        // per-window sums: every pair of list positions begin <= a < b < end
+        // of the item's window (the statistics of pgld_hap_window_sums).  The
+        // operand rows are grouped by 8 list positions, so a 16x256b TMEM load
+        // gives thread t all four counts of the pairs (a, b) and (a, b + 1),
+        // a = i0 + 16 quarter + 8 hh + t / 4, b = j0 + 32 half + 8 g + 2 (t % 4)
         float ws[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         int np = 0, nr2 = 0, nfour = 0;
+        const long long ib = i0 + 16 * quarter + (lane >> 2);
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
+          const int hh = c & 1, gp = c >> 1;
           uint32_t r[16];
-          const uint32_t col = (uint32_t)(acc * 256 + half * 64 + c * 16);
-          tmem_ld16(tmem_base + lane_base + col, r);
+          tmem_ld16x256_x4(tmem_base + ((uint32_t)(quarter * 32 + hh * 16) << 16) +
+                               (uint32_t)(acc * 256 + half * 64 + gp * 32),
+                           r);
           tmem_wait_ld();
           if (c == 3) {
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
           }
-#pragma unroll 1
-          for (int q = 0; q < 4; ++q) {
-            const uint32_t s0 = plane ? r[4 * q] : r[4 * q + 2];
-            const uint32_t s1 = plane ? r[4 * q + 1] : r[4 * q + 3];
-            const float g0 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s0, 1));
-            const float g1 = __uint_as_float(__shfl_xor_sync(0xffffffffu, s1, 1));
-            const float m0 = __uint_as_float(plane ? r[4 * q + 2] : r[4 * q]);
-            const float m1 = __uint_as_float(plane ? r[4 * q + 3] : r[4 * q + 1]);
-            const float c1 = plane ? g0 : m0, c2 = plane ? g1 : m1;
-            const float c3 = plane ? m0 : g0, c4 = plane ? m1 : g1;
-            const long long j = j0 + half * 32 + c * 8 + 2 * q + plane;
-            if (!(i < j && j < tr.end)) continue;
-            const fast::Pop p = fast::make(c1, c2, c3, c4);
-            ++np;
-            const long long si = a.idx ? (long long)a.idx[i] : i;
-            const long long sj = a.idx ? (long long)a.idx[j] : j;
-            const bool sok = si >= 0 && si < a.n_panel && sj >= 0 && sj < a.n_panel;
-            const float4 fi = sok ? a.site[si] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 fj = sok ? a.site[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
-            win::window_pair(p, p.n, c1, T.inv[p.n], T.r4[p.n], fi, fj, ws, nr2, nfour);
-          }
+          const long long is = ib + 8 * hh;
+          const bool iok = is >= tr.begin && is < tr.end;
+          const long long si = iok ? (a.idx ? (long long)a.idx[is] : is) : -1;
+          const float4 fi = (si >= 0 && si < a.n_panel) ? a.site[si] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int g = 0; g < 2; ++g)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+              const int o = 8 * g + y;
+              const long long j = j0 + 32 * half + 8 * (2 * gp + g) + 2 * (lane & 3) + y;
+              if (!(iok && is < j && j < tr.end)) continue;
+              const float c1 = __uint_as_float(r[o]), c2 = __uint_as_float(r[o + 4]);
+              const float c3 = __uint_as_float(r[o + 2]), c4 = __uint_as_float(r[o + 6]);
+              const fast::Pop p = fast::make(c1, c2, c3, c4);
+              ++np;
+              const long long sj = a.idx ? (long long)a.idx[j] : j;
+              const bool sok = si >= 0 && si < a.n_panel && sj >= 0 && sj < a.n_panel;
+              const float4 fj = sok ? a.site[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
+              win::window_pair(p, p.n, c1, T.inv[p.n], T.r4[p.n], sok ? fi : make_float4(0.f, 0.f, 0.f, 0.f),
+                               fj, ws, nr2, nfour);
+            }
         }
 #pragma unroll
         for (int s2 = 0; s2 < 6; ++s2) {
@@ -976,8 +984,8 @@ __global__ void tc_window_tiles_kernel(const long long* __restrict__ wb,
     long long T = 0;
     if (lo < 0 || hi < lo || hi > n_idx)
       atomicCAS(status, 0, 3100);
-    else
-      T = (hi - lo + kTileSnp - 1) / kTileSnp;
+    else if (hi > lo)
+      T = (hi - (lo & ~7ll) + kTileSnp - 1) / kTileSnp;  // origin rounded down to 8
     tiles[w] = T * (T + 1) / 2;
   }
 }
@@ -1001,7 +1009,9 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
   if (2 * n_idx > 2147483647LL - 256)
     return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core windows: too many SNPs");
   const int k_pad = ((W * 32 + kKChunk - 1) / kKChunk) * kKChunk;
-  const size_t op_bytes = (size_t)2 * std::max<long long>(n_idx, 1) * k_pad;
+  // operand rows grouped by 8 list positions (see pack_tc_kernel)
+  const long long n_op = (std::max<long long>(n_idx, 1) + 7) / 8 * 8;
+  const size_t op_bytes = (size_t)2 * n_op * k_pad;
   const size_t sb = pgld::scan_scratch_bytes(n_win);
   auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
   const size_t off_tiles = 0, off_scan = al((size_t)(n_win + 1) * 8), off_op = off_scan + al(sb),
@@ -1027,14 +1037,14 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
     if (rc) return rc;
   }
   if (n_idx > 0) {
-    const unsigned blocks = (unsigned)((2 * n_idx + 7) / 8);
-    pack_tc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, n_idx, idx, k_pad, 0, (uint32_t*)op,
+    const unsigned blocks = (unsigned)((2 * n_op + 7) / 8);
+    pack_tc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, n_idx, idx, k_pad, 1, (uint32_t*)op,
                                            h->dev_status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_tc_kernel");
   }
   CUtensorMap map;
-  rc = make_map(h, &map, op, 2 * std::max<long long>(n_idx, 1), k_pad);
+  rc = make_map(h, &map, op, 2 * n_op, k_pad);
   if (rc) return rc;
   Params prm{};
   prm.n_pops = 1;
