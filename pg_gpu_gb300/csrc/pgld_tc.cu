@@ -523,30 +523,46 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           const long long is = ib + 8 * hh;
           const long long offh = hh ? off1 : off0, nph = hh ? np1 : np0;
+          auto u2 = [](uint32_t x, uint32_t y) {
+            return make_float2(__uint_as_float(x), __uint_as_float(y));
+          };
 #pragma unroll
-          for (int g = 0; g < 2; ++g)
+          for (int g = 0; g < 2; ++g) {
+            // the pairs (is, j) and (is, j + 1), two lanes of the packed epilogue
+            const int o = 8 * g;
+            const long long j = j0 + 32 * half + 8 * (2 * gp + g) + 2 * (lane & 3);
+            // a pair's row comes from the band offsets themselves, so a pair
+            // is written exactly when the offsets list it
+            const bool ok0 = is < j && j < a.n_snp && (j - is - 1) < nph;
+            const bool ok1 = is < j + 1 && j + 1 < a.n_snp && (j - is) < nph;
+            if (!ok0 && !ok1) continue;
+            const fast2::Pop p = fast2::make(u2(r[o], r[o + 1]), u2(r[o + 4], r[o + 5]),
+                                             u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
+            const long long k = offh + (j - is - 1);  // row of (is, j); (is, j + 1) follows
+            float4 st[2];
+            if (a.stats) {
+              const float2 r4 = make_float2(T.r4[p.n0], T.r4[p.n1]);
+              const float2 dd = fast2::vmul(fast2::dd_num(p), r4);
+              const float2 dz = fast2::vmul(fast2::dz_num(p, fast2::vfma(p.dA, p.dB, p.e)), r4);
+              const float2 pi = fast2::vmul(fast2::pi2_num(p), r4);
+              const float2 num = fast2::vmul(p.x, p.x);
+              const float2 den = fast2::vmul(fast2::vmul(p.pA, p.qA), fast2::vmul(p.pB, p.qB));
+              st[0] = make_float4(den.x > 0.f ? num.x / den.x : NAN, dd.x, dz.x, pi.x);
+              st[1] = make_float4(den.y > 0.f ? num.y / den.y : NAN, dd.y, dz.y, pi.y);
+            }
 #pragma unroll
             for (int y = 0; y < 2; ++y) {
-              const int o = 8 * g + y;
-              const float c1 = __uint_as_float(r[o]), c2 = __uint_as_float(r[o + 4]);
-              const float c3 = __uint_as_float(r[o + 2]), c4 = __uint_as_float(r[o + 6]);
-              const long long j = j0 + 32 * half + 8 * (2 * gp + g) + 2 * (lane & 3) + y;
-              // the pair's row comes from the band offsets themselves, so a
-              // pair is written exactly when the offsets list it
-              if (!(is < j && j < a.n_snp && (j - is - 1) < nph)) continue;
-              const long long k = offh + (j - is - 1);
-              const fast::Pop p = fast::make(c1, c2, c3, c4);
-              reinterpret_cast<int4*>(a.counts)[k] =
-                  make_int4(fast::f2i_small(c1), fast::f2i_small(c2), fast::f2i_small(c3),
-                            fast::f2i_small(c4));
-              if (a.nvalid) a.nvalid[k] = p.n;
-              if (a.stats) {
-                const float r4 = T.r4[p.n];
-                reinterpret_cast<float4*>(a.stats)[k] =
-                    make_float4(fast::r2_of(p), fast::dd_num(p) * r4, fast::dz_num(p) * r4,
-                                fast::pi2_num(p) * r4);
-              }
+              if (!(y ? ok1 : ok0)) continue;
+              const int q = o + y;
+              reinterpret_cast<int4*>(a.counts)[k + y] =
+                  make_int4(fast::f2i_small(__uint_as_float(r[q])),
+                            fast::f2i_small(__uint_as_float(r[q + 4])),
+                            fast::f2i_small(__uint_as_float(r[q + 2])),
+                            fast::f2i_small(__uint_as_float(r[q + 6])));
+              if (a.nvalid) a.nvalid[k + y] = y ? p.n1 : p.n0;
+              if (a.stats) reinterpret_cast<float4*>(a.stats)[k + y] = st[y];
             }
+          }
         }
         continue;
       }
