@@ -384,20 +384,23 @@ __global__ void __launch_bounds__(256) pack_hap_kernel(const int8_t* __restrict_
     }
   }
   __syncthreads();
-  const bool live = w * 32 + lane < n_rows;
+  // rows of the word that exist (the staged bytes of the others are not read
+  // into any word); bytes past n_snp are staged as 0
+  const int n_live = n_rows - w * 32;
+  const uint32_t live = n_live >= 32 ? 0xffffffffu : ((1u << n_live) - 1u);
   const int8_t* mine = tile + lane * kPackPitch;
-  bool miss = false, other = false;
+  uint32_t any_miss = 0, any_other = 0;
   for (int c = warp * 64; c < warp * 64 + 64; c += 32) {
     // 32 SNPs: lane k keeps the words of SNP c + k and stores them
     uint32_t mc = 0, mz = 0, mv = 0;
 #pragma unroll 8
     for (int k = 0; k < 32; ++k) {
-      const int v = live ? (int)mine[c + k] : -1;
-      const uint32_t cw = __ballot_sync(0xffffffffu, live && v == 1);
-      const uint32_t zw = __ballot_sync(0xffffffffu, live && v == 0);
-      const uint32_t vw = __ballot_sync(0xffffffffu, live && v >= 0);
-      miss |= live && v == -1 && s0 + c + k < n_snp;
-      other |= live && v != -1 && v != 0 && v != 1 && s0 + c + k < n_snp;
+      const int v = (int)mine[c + k];
+      const uint32_t cw = __ballot_sync(0xffffffffu, v == 1) & live;
+      const uint32_t zw = __ballot_sync(0xffffffffu, v == 0) & live;
+      const uint32_t vw = __ballot_sync(0xffffffffu, v >= 0) & live;
+      any_miss |= __ballot_sync(0xffffffffu, v == -1);
+      any_other |= __ballot_sync(0xffffffffu, (unsigned)(v + 1) > 2u);
       if (lane == k) {
         mc = cw;
         mz = zw;
@@ -411,11 +414,9 @@ __global__ void __launch_bounds__(256) pack_hap_kernel(const int8_t* __restrict_
       if (valid) valid[s * W + w] = mv;
     }
   }
-  const unsigned m = __ballot_sync(0xffffffffu, miss);
-  const unsigned o = __ballot_sync(0xffffffffu, other);
   if (lane == 0) {
-    if (m) atomicOr(flags, 1);
-    if (o) atomicOr(flags + 1, 1);
+    if (any_miss & live) atomicOr(flags, 1);
+    if (any_other & live) atomicOr(flags + 1, 1);
   }
 }
 
