@@ -443,9 +443,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         // operand rows are grouped by 8 list positions, so a 16x256b TMEM load
         // gives thread t all four counts of the pairs (a, b) and (a, b + 1),
         // a = i0 + 16 quarter + 8 hh + t / 4, b = j0 + 32 half + 8 g + 2 (t % 4)
-        float ws[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float2 ws2[6];
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2) ws2[s2] = make_float2(0.f, 0.f);
         int np = 0, nr2 = 0, nfour = 0;
         const long long ib = i0 + 16 * quarter + (lane >> 2);
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto site_of = [&](long long pos) {
+          const long long sp = a.idx ? (long long)a.idx[pos] : pos;
+          return (sp >= 0 && sp < a.n_panel) ? a.site[sp] : zero4;
+        };
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
           const int hh = c & 1, gp = c >> 1;
@@ -461,26 +468,26 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           const long long is = ib + 8 * hh;
           const bool iok = is >= tr.begin && is < tr.end;
-          const long long si = iok ? (a.idx ? (long long)a.idx[is] : is) : -1;
-          const float4 fi = (si >= 0 && si < a.n_panel) ? a.site[si] : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 fi = iok ? site_of(is) : zero4;
+          auto u2 = [](uint32_t x, uint32_t y) {
+            return make_float2(__uint_as_float(x), __uint_as_float(y));
+          };
 #pragma unroll
-          for (int g = 0; g < 2; ++g)
-#pragma unroll
-            for (int y = 0; y < 2; ++y) {
-              const int o = 8 * g + y;
-              const long long j = j0 + 32 * half + 8 * (2 * gp + g) + 2 * (lane & 3) + y;
-              if (!(iok && is < j && j < tr.end)) continue;
-              const float c1 = __uint_as_float(r[o]), c2 = __uint_as_float(r[o + 4]);
-              const float c3 = __uint_as_float(r[o + 2]), c4 = __uint_as_float(r[o + 6]);
-              const fast::Pop p = fast::make(c1, c2, c3, c4);
-              ++np;
-              const long long sj = a.idx ? (long long)a.idx[j] : j;
-              const bool sok = si >= 0 && si < a.n_panel && sj >= 0 && sj < a.n_panel;
-              const float4 fj = sok ? a.site[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
-              win::window_pair(p, p.n, c1, T.inv[p.n], T.r4[p.n], sok ? fi : make_float4(0.f, 0.f, 0.f, 0.f),
-                               fj, ws, nr2, nfour);
-            }
+          for (int g = 0; g < 2; ++g) {
+            const int o = 8 * g;
+            const long long j = j0 + 32 * half + 8 * (2 * gp + g) + 2 * (lane & 3);
+            const bool l0 = iok && is < j && j < tr.end;
+            const bool l1 = iok && is < j + 1 && j + 1 < tr.end;
+            if (!(l0 || l1)) continue;
+            const fast2::Pop p = fast2::make(u2(r[o], r[o + 1]), u2(r[o + 4], r[o + 5]),
+                                             u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
+            win::window_pair2(p, u2(r[o], r[o + 1]), T, fi, l0 ? site_of(j) : zero4,
+                              l1 ? site_of(j + 1) : zero4, l0, l1, ws2, np, nr2, nfour);
+          }
         }
+        float ws[6];
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2) ws[s2] = ws2[s2].x + ws2[s2].y;
 #pragma unroll
         for (int s2 = 0; s2 < 6; ++s2) {
           const float v = warp_sum(ws[s2]);

@@ -11,6 +11,7 @@
 // per-n reciprocal tables.
 #pragma once
 #include "pgld_epilogue.cuh"
+#include "pgld_epilogue2.cuh"
 
 namespace pgld {
 namespace win {
@@ -54,6 +55,50 @@ __device__ __forceinline__ void window_pair(const fast::Pop& p, int n, float c1,
       D = -(si.x * si.z) * (sj.x * sj.z);
     }
     acc[5] += (D * D) * (si.w * sj.w);
+  }
+}
+
+// window_pair for two pairs (i, j0) and (i, j1) at once on packed float2
+// features (the tensor-core window kernel): the same statistics, with the
+// naive-r^2 numerator c1 v_i v_j - n d_i d_j by Kahan's two-product
+// algorithm; live.x / live.y select the pairs that belong to the window
+__device__ __forceinline__ void window_pair2(const fast2::Pop& p, float2 c1, const fast::Recip& T,
+                                             float4 si, float4 sj0, float4 sj1, bool live0,
+                                             bool live1, float2 (&acc)[6], int& n_pairs,
+                                             int& n_r2, int& n_four) {
+  using namespace fast2;
+  n_pairs += (live0 ? 1 : 0) + (live1 ? 1 : 0);
+  const V rden = vmul(vmul(p.pA, p.qA), vmul(p.pB, p.qB));
+  const V xx = vmul(p.x, p.x);
+  const bool r0 = live0 && rden.x > 0.f, r1 = live1 && rden.y > 0.f;
+  n_r2 += (r0 ? 1 : 0) + (r1 ? 1 : 0);
+  acc[0] = vadd(acc[0], make_float2(r0 ? __fdividef(xx.x, rden.x) : 0.f,
+                                    r1 ? __fdividef(xx.y, rden.y) : 0.f));
+  const bool f0 = live0 && p.n0 >= 4, f1 = live1 && p.n1 >= 4;
+  n_four += (f0 ? 1 : 0) + (f1 ? 1 : 0);
+  if (f0 || f1) {
+    const V dd = dd_num(p), pi = pi2_num(p);
+    const V dz = dz_num(p, vfma(p.dA, p.dB, p.e));
+    const V r4 = make_float2(f0 ? T.r4[p.n0] : 0.f, f1 ? T.r4[p.n1] : 0.f);
+    acc[1] = vadd(acc[1], make_float2(f0 && pi.x != 0.f ? __fdividef(dd.x, pi.x) : 0.f,
+                                      f1 && pi.y != 0.f ? __fdividef(dd.y, pi.y) : 0.f));
+    acc[2] = vfma(dd, r4, acc[2]);
+    acc[3] = vfma(dz, r4, acc[3]);
+    acc[4] = vfma(pi, r4, acc[4]);
+  }
+  const bool s0 = live0 && si.w > 0.f && sj0.w > 0.f, s1 = live1 && si.w > 0.f && sj1.w > 0.f;
+  if (s0 || s1) {
+    // D = c1 / n - p_i p_j from the integer c1 v_i v_j - n d_i d_j
+    const V ns = p.ns;
+    const V vv = make_float2(si.y * sj0.y, si.y * sj1.y), dd2 = make_float2(si.x * sj0.x, si.x * sj1.x);
+    const V num = dot2(c1, vv, vneg(ns), dd2);
+    const V inv = make_float2(T.inv[p.n0], T.inv[p.n1]);
+    const V zz = make_float2(si.z * sj0.z, si.z * sj1.z);
+    const V neg0 = make_float2(-(si.x * si.z) * (sj0.x * sj0.z), -(si.x * si.z) * (sj1.x * sj1.z));
+    const V Dv = vmul(vmul(num, inv), zz);
+    const float D0 = p.n0 > 0 ? Dv.x : neg0.x, D1 = p.n1 > 0 ? Dv.y : neg0.y;
+    const V ww = make_float2(s0 ? si.w * sj0.w : 0.f, s1 ? si.w * sj1.w : 0.f);
+    acc[5] = vfma(vmul(make_float2(D0, D1), make_float2(D0, D1)), ww, acc[5]);
   }
 }
 
