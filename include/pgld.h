@@ -355,6 +355,19 @@ int pgld_hap_window_snp_sums(pgld_handle h, const pgld_hap_panel* panel, const i
 int pgld_prune_unlinked(pgld_handle h, const double* r2, const int64_t* pair_off, int64_t n_snp,
                         int32_t size, int32_t step, double threshold, uint8_t* loc);
 
+/* VCF GT reading on the host (no device, no handle).  pgld_vcf_scan counts
+ * the samples of the #CHROM header line and the data records of a VCF text
+ * (already decompressed).  pgld_vcf_parse_gt writes the GT alleles of the
+ * selected samples (sample_cols: n_sel column indices into the VCF samples,
+ * NULL = all, n_sel = n_samples) as the int8 haplotype matrix of
+ * HaplotypeMatrix.from_vcf (haplotype_matrix.py:293-404): row k = first
+ * allele of selected sample k, row n_sel + k = its second allele, n_records
+ * columns; '.' or an empty allele is -1, a haploid call's second allele -1,
+ * allele numbers clipped to 127; pos: int64 [n_records] POS column. */
+int pgld_vcf_scan(const char* text, int64_t len, int32_t* n_samples, int64_t* n_records);
+int pgld_vcf_parse_gt(const char* text, int64_t len, int32_t n_samples, int64_t n_records,
+                      const int32_t* sample_cols, int32_t n_sel, int8_t* hap, int64_t* pos);
+
 /* pgld_hap_binned_sums for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers of this library cannot call
  * cudaMalloc: a host application that hands every byte of the device to its

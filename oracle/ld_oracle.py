@@ -1228,3 +1228,59 @@ def omega_diploid(geno, missing_data="include"):
     if missing_data == "exclude":
         g = g[:, (g < 0).sum(0) == 0]
     return omega_matrix(r2_matrix_diploid(g))
+
+
+# ---------------------------------------------------------------------------
+# VCF GT reading  (haplotype_matrix.py:293-404 through allel.read_vcf)
+# ---------------------------------------------------------------------------
+def read_vcf_gt(text, samples=None):
+    """(sample names, int8 haplotypes (2 n, M), int64 POS) of a VCF text.
+
+    The layout of HaplotypeMatrix.from_vcf (haplotype_matrix.py:324-328): row
+    k is the first allele of sample k, row n + k its second.  GT semantics of
+    allel.read_vcf's calldata/GT: the first ':' subfield, alleles split at
+    '/' or '|', '.' or empty -> -1, a haploid call's second allele -1; allele
+    numbers above 127 are clipped to 127 (int8)."""
+    names, gts, pos = None, [], []
+    for line in text.split("\n"):
+        line = line.rstrip("\r")
+        if not line or line.startswith("##"):
+            continue
+        parts = line.split("\t")
+        if line.startswith("#CHROM"):
+            names = parts[9:]
+            continue
+        if line.startswith("#"):
+            continue
+        pos.append(int(parts[1]))
+        row = []
+        for g in parts[9:9 + len(names)]:
+            gt = g.split(":")[0].replace("/", "|").split("|")
+
+            def al(s):
+                return -1 if s in (".", "") else min(int(s), 127)
+            row.append((al(gt[0]), al(gt[1]) if len(gt) > 1 else -1))
+        gts.append(row)
+    cols = list(range(len(names))) if samples is None else [names.index(s) for s in samples]
+    gt = np.asarray(gts, np.int8).reshape(len(gts), len(names), 2)[:, cols, :]
+    n = len(cols)
+    hap = np.empty((2 * n, gt.shape[0]), np.int8)
+    hap[:n] = gt[:, :, 0].T
+    hap[n:] = gt[:, :, 1].T
+    return [names[c] for c in cols], hap, np.asarray(pos, np.int64)
+
+
+def vcf_dosages(text):
+    """(names, int8 dosages (n, M'), POS) of GenotypeMatrix.from_vcf
+    (genotype_matrix.py:359-380): alt-allele counts of the sites allel's
+    count_alleles().is_biallelic_01() keeps (alleles 0 and 1 both observed,
+    nothing above 1), -1 where either allele is missing."""
+    names, hap, pos = read_vcf_gt(text)
+    n = len(names)
+    gt = np.stack([hap[:n].T, hap[n:].T], axis=2)          # (M, n, 2)
+    keep = np.array([(0 in set(r.ravel())) and (1 in set(r.ravel())) and r.max() <= 1
+                     for r in gt])
+    gt = gt[keep]
+    g = gt.sum(axis=2).astype(np.int8)
+    g[(gt < 0).any(axis=2)] = -1
+    return names, g.T.copy(), pos[keep]

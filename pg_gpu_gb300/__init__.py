@@ -6,5 +6,8 @@ compute is libpgld (``include/pgld.h``), hand-written CUDA for sm_103a, called
 through ctypes on CUDA device pointers.  There is no CPU path.
 """
 from ._lib import PgldError  # noqa: F401
+from . import ld_statistics  # noqa: F401
+from .genotype_matrix import GenotypeMatrix  # noqa: F401
+from .haplotype_matrix import HaplotypeMatrix  # noqa: F401
 
 __version__ = "0.1.0"

@@ -57,7 +57,7 @@ def build(verbose=False, force=False):
             list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         tmp = LIB + ".tmp"
-        run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -112,6 +112,8 @@ _SIGS = {
                                   _P, _P, _I64, _P],
                                  ctypes.c_int),
     "pgld_prune_unlinked": ([_P, _P, _P, _I64, _I32, _I32, _D, _P], ctypes.c_int),
+    "pgld_vcf_scan": ([_P, _I64, _P, _P], ctypes.c_int),
+    "pgld_vcf_parse_gt": ([_P, _I64, _I32, _I64, _P, _I32, _P, _P], ctypes.c_int),
 }
 
 _lib = None

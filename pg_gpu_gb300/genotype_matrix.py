@@ -6,8 +6,6 @@ missing), its positions and population sample sets (genotype_matrix.py:
 """
 from __future__ import annotations
 
-import gzip
-
 import numpy as np
 
 from . import _lib as L
@@ -145,32 +143,22 @@ class GenotypeMatrix:
 
     @classmethod
     def from_vcf(cls, path, include_invariant=False, accessible_bed=None):
-        """GT dosages of a plain or gzipped VCF (alt allele count, -1 if any allele missing)."""
-        opener = gzip.open if str(path).endswith(".gz") else open
-        names, rows, pos = None, [], []
-        with opener(path, "rt") as f:
-            for line in f:
-                if line.startswith("##"):
-                    continue
-                parts = line.rstrip("\n").split("\t")
-                if line.startswith("#CHROM"):
-                    names = parts[9:]
-                    continue
-                pos.append(int(parts[1]))
-                row = []
-                for g in parts[9:]:
-                    gt = g.split(":")[0].replace("/", "|").split("|")
-                    if any(a in (".", "") for a in gt):
-                        row.append(-1)
-                    else:
-                        row.append(sum(int(a) for a in gt))
-                rows.append(row)
-        if not rows:
-            raise ValueError(f"No variants found in {path}")
-        g = np.ascontiguousarray(np.asarray(rows, dtype=np.int8).T)
-        pos = np.asarray(pos, np.int64)
-        return cls(g, pos, int(pos[0]), int(pos[-1]), samples=list(names),
-                   n_total_sites=len(pos) if include_invariant else None)
+        """Alt-allele dosages of a plain or gzipped VCF through the native GT
+        reader, kept to the sites whose called alleles are exactly {0, 1}
+        (allel's is_biallelic_01); -1 where either allele is missing
+        (genotype_matrix.py:343-391)."""
+        from .haplotype_matrix import read_vcf_gt
+        names, hap, pos = read_vcf_gt(path)
+        n = len(names)
+        a, b = hap[:n], hap[n:]
+        keep = (hap == 0).any(0) & (hap == 1).any(0) & ~(hap > 1).any(0)
+        a, b, pos = a[:, keep], b[:, keep], pos[keep]
+        g = (a.astype(np.int16) + b).astype(np.int8)
+        g[(a < 0) | (b < 0)] = -1
+        if g.shape[1] == 0:
+            raise ValueError(f"No biallelic variants found in {path}")
+        return cls(np.ascontiguousarray(g), pos, int(pos[0]), int(pos[-1]), samples=list(names),
+                   n_total_sites=g.shape[1] if include_invariant else None)
 
     def load_pop_file(self, pop_file, pops=None):
         """Population sample sets from a sample / pop file (genotype_matrix.py:475-504)."""

@@ -8,6 +8,7 @@ tensor; packed bit planes of each population are cached after first use.
 """
 from __future__ import annotations
 
+import ctypes
 import gzip
 from collections import OrderedDict
 
@@ -23,6 +24,77 @@ def _is_torch(x):
         return isinstance(x, torch.Tensor)
     except ImportError:
         return False
+
+
+def _parse_region(region):
+    """('chrom', start or None, end or None) of 'chrom[:start[-end]]'."""
+    chrom, _, rng = region.partition(":")
+    lo = hi = None
+    if rng:
+        a, _, b = rng.partition("-")
+        lo = int(a.replace(",", "")) if a else None
+        hi = int(b.replace(",", "")) if b else None
+    return chrom, lo, hi
+
+
+def _vcf_region(data, region):
+    """The VCF text with only the header lines and the records of region."""
+    chrom, lo, hi = _parse_region(region)
+    c = chrom.encode()
+    keep = []
+    for line in data.split(b"\n"):
+        if line.startswith(b"#"):
+            keep.append(line)
+            continue
+        f = line.split(b"\t", 2)
+        if len(f) < 2 or f[0] != c:
+            continue
+        p = int(f[1])
+        if (lo is None or p >= lo) and (hi is None or p <= hi):
+            keep.append(line)
+    return b"\n".join(keep)
+
+
+def _vcf_sample_names(data):
+    """Sample names of the #CHROM header line."""
+    i = data.find(b"#CHROM")
+    line = data[i:data.find(b"\n", i) if data.find(b"\n", i) >= 0 else len(data)]
+    return [x.decode() for x in line.rstrip(b"\r").split(b"\t")[9:]]
+
+
+def read_vcf_gt(path, region=None, samples=None):
+    """(sample names, int8 haplotypes (2 n, M), int64 POS) of a plain or
+    gzipped VCF through the native GT reader (pgld_vcf_scan /
+    pgld_vcf_parse_gt): row k = first allele of sample k, row n + k its
+    second, -1 = missing (the calldata/GT layout of allel.read_vcf that
+    haplotype_matrix.py:317-328 reshapes)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:2] == b"\x1f\x8b":
+        data = gzip.decompress(data)
+    if region is not None:
+        data = _vcf_region(data, region)
+    ns, nr = ctypes.c_int32(0), ctypes.c_int64(0)
+    L.check(L.lib().pgld_vcf_scan(data, len(data), ctypes.byref(ns), ctypes.byref(nr)))
+    names = _vcf_sample_names(data)
+    if nr.value == 0:
+        raise ValueError(f"No variants found in {path}"
+                         + (f" for region {region}" if region else ""))
+    cols = None
+    if samples is not None:
+        missing = [s for s in samples if s not in names]
+        if missing:
+            raise ValueError(f"samples not in {path}: {missing}")
+        cols = np.ascontiguousarray([names.index(s) for s in samples], np.int32)
+        names = list(samples)
+    n_sel = len(names)
+    hap = np.empty((2 * n_sel, nr.value), np.int8)
+    pos = np.empty(nr.value, np.int64)
+    L.check(L.lib().pgld_vcf_parse_gt(
+        data, len(data), ns.value, nr.value,
+        None if cols is None else cols.ctypes.data_as(ctypes.c_void_p), n_sel,
+        hap.ctypes.data_as(ctypes.c_void_p), pos.ctypes.data_as(ctypes.c_void_p)))
+    return names, hap, pos
 
 
 class HaplotypeMatrix:
@@ -166,44 +238,20 @@ class HaplotypeMatrix:
     @classmethod
     def from_vcf(cls, path, region=None, samples=None, include_invariant=False,
                  accessible_bed=None):
-        """Phased GT of a plain or gzipped VCF; rows = all hap-0 then all hap-1
-        (haplotype_matrix.py:324-328)."""
+        """GT of a plain or gzipped VCF through the native reader; rows = all
+        hap-0 then all hap-1 (haplotype_matrix.py:293-356).
+
+        ``region`` ('chrom', 'chrom:start-end', 1-based inclusive) keeps the
+        records inside it by a linear scan (no tabix index needed) and sets
+        chrom_start / chrom_end from its bounds, as the reference does."""
+        names, hap, pos = read_vcf_gt(path, region, samples)
+        start, end = int(pos[0]), int(pos[-1])
         if region is not None:
-            raise NotImplementedError("region queries need a tabix reader")
-        opener = gzip.open if str(path).endswith(".gz") else open
-        names, gts, pos = None, [], []
-        with opener(path, "rt") as f:
-            for line in f:
-                if line.startswith("##"):
-                    continue
-                parts = line.rstrip("\n").split("\t")
-                if line.startswith("#CHROM"):
-                    names = parts[9:]
-                    continue
-                pos.append(int(parts[1]))
-                row = []
-                for g in parts[9:]:
-                    gt = g.split(":")[0].replace("/", "|").split("|")
-                    a = -1 if gt[0] in (".", "") else int(gt[0])
-                    b = -1 if len(gt) < 2 or gt[1] in (".", "") else int(gt[1])
-                    row.append((a, b))
-                gts.append(row)
-        if not gts:
-            raise ValueError(f"No variants found in {path}")
-        gt = np.asarray(gts, dtype=np.int8)
-        keep_s = np.arange(gt.shape[1])
-        if samples is not None:
-            keep_s = np.array([names.index(s) for s in samples])
-            names = list(samples)
-        gt = gt[:, keep_s, :]
-        n = gt.shape[1]
-        hap = np.empty((gt.shape[0], 2 * n), np.int8)
-        hap[:, :n] = gt[:, :, 0]
-        hap[:, n:] = gt[:, :, 1]
-        pos = np.asarray(pos, np.int64)
-        return cls(np.ascontiguousarray(hap.T), pos, int(pos[0]), int(pos[-1]),
-                   samples=list(names),
-                   n_total_sites=gt.shape[0] if include_invariant else None)
+            _, lo, hi = _parse_region(region)
+            start = lo if lo is not None else start
+            end = hi if hi is not None else end
+        return cls(hap, pos, start, end, samples=names,
+                   n_total_sites=len(pos) if include_invariant else None)
 
     def load_pop_file(self, pop_file, pops=None):
         """Sample sets from a sample / pop file; sample i owns haplotype rows i and

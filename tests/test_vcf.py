@@ -1,0 +1,157 @@
+"""Native VCF GT reader (pgld_vcf_scan / pgld_vcf_parse_gt) against the oracle's
+restatement of allel.read_vcf's GT layout, and HaplotypeMatrix.from_vcf end to
+end (haplotype_matrix.py:293-356).  Host code only: no GPU."""
+import gzip
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ld_oracle as O
+
+pytest.importorskip("torch")
+from pg_gpu_gb300 import _lib as L  # noqa: E402
+
+pytestmark = pytest.mark.skipif(not os.path.exists(L.LIB_PATH), reason="libpgld.so not built")
+
+HEADER = "##fileformat=VCFv4.2\n##contig=<ID=chr1>\n"
+COLS = "#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO\tFORMAT"
+
+
+def _vcf(names, records, eol="\n"):
+    lines = HEADER.rstrip("\n").split("\n") + [COLS + "".join("\t" + n for n in names)]
+    for chrom, pos, fmt, gts in records:
+        lines.append("\t".join([chrom, str(pos), ".", "A", "T", ".", "PASS", ".", fmt] + gts))
+    return eol.join(lines) + eol
+
+
+def _edge_text(eol="\n"):
+    names = ["s0", "s1", "s2", "s3"]
+    recs = [
+        ("chr1", 100, "GT", ["0|1", "1|1", "0|0", "1|0"]),
+        ("chr1", 250, "GT:DP:GQ", ["0/1:12:99", "./.:0:0", "1/1:3:20", "0|.:4:5"]),
+        ("chr1", 300, "GT", [".|.", "0", "1", "."]),         # missing and haploid calls
+        ("chr1", 1000, "GT:AD", ["2|0:1,2", "0|3:4,5", "12|1:0,0", "0|200:1,1"]),
+        ("chr2", 50, "GT", ["1|1", "0|0", "1|0", "0|1"]),
+    ]
+    return names, _vcf(names, recs, eol)
+
+
+def _native(text, samples=None):
+    import ctypes
+    data = text.encode()
+    ns, nr = ctypes.c_int32(0), ctypes.c_int64(0)
+    L.check(L.lib().pgld_vcf_scan(data, len(data), ctypes.byref(ns), ctypes.byref(nr)))
+    from pg_gpu_gb300.haplotype_matrix import _vcf_sample_names
+    names = _vcf_sample_names(data)
+    cols = None if samples is None else np.array([names.index(s) for s in samples], np.int32)
+    n_sel = ns.value if cols is None else len(cols)
+    hap = np.full((2 * n_sel, nr.value), 99, np.int8)
+    pos = np.zeros(nr.value, np.int64)
+    rc = L.lib().pgld_vcf_parse_gt(data, len(data), ns.value, nr.value,
+                                   None if cols is None else cols.ctypes.data_as(ctypes.c_void_p),
+                                   n_sel, hap.ctypes.data_as(ctypes.c_void_p),
+                                   pos.ctypes.data_as(ctypes.c_void_p))
+    L.check(rc)
+    return hap, pos
+
+
+@pytest.mark.parametrize("eol", ["\n", "\r\n"])
+def test_native_gt_matches_oracle_edge_cases(eol):
+    names, text = _edge_text(eol)
+    ref_names, ref_hap, ref_pos = O.read_vcf_gt(text)
+    hap, pos = _native(text)
+    assert ref_names == names
+    assert np.array_equal(hap, ref_hap) and np.array_equal(pos, ref_pos)
+    # spot values: missing, haploid, multi-digit and clipped alleles
+    assert hap[1, 1] == -1 and hap[5, 1] == -1          # "./."
+    assert hap[1, 2] == 0 and hap[5, 2] == -1           # "0" (haploid)
+    assert hap[2, 3] == 12 and hap[7, 3] == 127         # "12|1", "0|200"
+
+
+def test_native_sample_subset_matches_oracle():
+    _, text = _edge_text()
+    sub = ["s3", "s0"]
+    ref_names, ref_hap, _ = O.read_vcf_gt(text, samples=sub)
+    hap, _ = _native(text, samples=sub)
+    assert ref_names == sub and np.array_equal(hap, ref_hap)
+
+
+def test_native_rejects_malformed_text():
+    import ctypes
+    ns, nr = ctypes.c_int32(0), ctypes.c_int64(0)
+    data = b"##fileformat=VCFv4.2\nchr1\t1\t.\tA\tT\t.\t.\t.\tGT\t0|1\n"   # no #CHROM line
+    assert L.lib().pgld_vcf_scan(data, len(data), ctypes.byref(ns), ctypes.byref(nr)) != 0
+    names, text = _edge_text()
+    short = text.replace("\t1|0\n", "\n", 1).encode()                     # a record short a sample
+    L.check(L.lib().pgld_vcf_scan(short, len(short), ctypes.byref(ns), ctypes.byref(nr)))
+    hap = np.zeros((2 * ns.value, nr.value), np.int8)
+    pos = np.zeros(nr.value, np.int64)
+    assert L.lib().pgld_vcf_parse_gt(short, len(short), ns.value, nr.value, None, ns.value,
+                                     hap.ctypes.data_as(ctypes.c_void_p),
+                                     pos.ctypes.data_as(ctypes.c_void_p)) != 0
+    bad = np.array([7], np.int32)                                          # sample out of range
+    assert L.lib().pgld_vcf_parse_gt(short, len(short), ns.value, nr.value,
+                                     bad.ctypes.data_as(ctypes.c_void_p), 1,
+                                     hap.ctypes.data_as(ctypes.c_void_p),
+                                     pos.ctypes.data_as(ctypes.c_void_p)) != 0
+
+
+def test_from_vcf_gzip_region_and_samples(tmp_path):
+    from pg_gpu_gb300 import HaplotypeMatrix
+    names, text = _edge_text()
+    p = tmp_path / "edge.vcf.gz"
+    with gzip.open(p, "wt") as f:
+        f.write(text)
+    hm = HaplotypeMatrix.from_vcf(str(p))
+    _, ref_hap, ref_pos = O.read_vcf_gt(text)
+    assert np.array_equal(np.asarray(hm.haplotypes), ref_hap)
+    assert np.array_equal(np.asarray(hm.positions), ref_pos) and hm.samples == names
+    assert (hm.chrom_start, hm.chrom_end) == (100, 50)    # first and last record
+    # region: chr1 records in [200, 1000], bounds from the region string
+    hm = HaplotypeMatrix.from_vcf(str(p), region="chr1:200-1,000", samples=["s2", "s1"])
+    _, ref_hap, ref_pos = O.read_vcf_gt(text, samples=["s2", "s1"])
+    keep = np.array([False, True, True, True, False])
+    assert np.array_equal(np.asarray(hm.haplotypes), ref_hap[:, keep])
+    assert np.array_equal(np.asarray(hm.positions), ref_pos[keep])
+    assert (hm.chrom_start, hm.chrom_end) == (200, 1000) and hm.samples == ["s2", "s1"]
+    with pytest.raises(ValueError):
+        HaplotypeMatrix.from_vcf(str(p), region="chr3")
+    with pytest.raises(ValueError):
+        HaplotypeMatrix.from_vcf(str(p), samples=["nope"])
+
+
+def test_from_vcf_round_trips_moments_im_haplotypes(golden, tmp_path):
+    """The im-parsing-example haplotypes of the moments golden fixture written
+    back as phased VCF text read back identically."""
+    from pg_gpu_gb300 import HaplotypeMatrix
+    z = golden("moments_im")
+    hap, pos = z["hap"], z["pos"]
+    n = hap.shape[0] // 2
+    names = [f"tsk_{k}" for k in range(n)]
+    al = lambda a: "." if a < 0 else str(int(a))  # noqa: E731
+    recs = [("1", int(pos[j]), "GT", [al(hap[k, j]) + "|" + al(hap[n + k, j]) for k in range(n)])
+            for j in range(hap.shape[1])]
+    p = tmp_path / "im.vcf"
+    p.write_text(_vcf(names, recs))
+    hm = HaplotypeMatrix.from_vcf(str(p))
+    assert np.array_equal(np.asarray(hm.haplotypes), hap)
+    assert np.array_equal(np.asarray(hm.positions), pos) and hm.samples == names
+
+
+def test_genotype_from_vcf_matches_oracle(tmp_path):
+    from pg_gpu_gb300 import GenotypeMatrix
+    names, text = _edge_text()
+    # add a monomorphic site, an all-missing site and a biallelic site with a missing call
+    extra = _vcf(names, [("chr2", 60, "GT", ["0|0", "0/0", "0|0", "0|0"]),
+                         ("chr2", 70, "GT", [".|.", "./.", ".", ".|."]),
+                         ("chr2", 80, "GT", ["0|1", "./1", "1|1", "0"])])
+    text += extra.split(COLS)[1].split("\n", 1)[1]
+    p = tmp_path / "g.vcf"
+    p.write_text(text)
+    gm = GenotypeMatrix.from_vcf(str(p))
+    ref_names, ref_g, ref_pos = O.vcf_dosages(text)
+    assert gm.samples == ref_names
+    assert np.array_equal(np.asarray(gm.genotypes), ref_g)
+    assert np.array_equal(np.asarray(gm.positions), ref_pos)
+    assert list(ref_pos) == [100, 250, 300, 50, 80]   # 1000 (alleles 2..), 60, 70 dropped
