@@ -442,14 +442,9 @@ __global__ void __launch_bounds__(kThreads) geno_band_kernel(BandArgs a) {
           }
           if (a.nvalid) a.nvalid[k] = (int32_t)P[0].n;
           if (a.stats) {
-            // only the requested columns are evaluated (the polynomials are
-            // the bulk of the per-pair work); the others are written as 0
-            float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (a.stat_mask & 1) o.x = rh2_f32(cc[0]);
-            if (a.stat_mask & 2) o.y = gv_f32(dd_single(P[0]));
-            if (a.stat_mask & 4) o.z = gv_f32(dz_single(P[0]));
-            if (a.stat_mask & 8) o.w = gv_f32(pi2_single(P[0]));
-            reinterpret_cast<float4*>(a.stats)[k] = o;
+            // only the requested columns are evaluated; the others are 0
+            reinterpret_cast<float4*>(a.stats)[k] =
+                gmom::stats_f32(gmom::from_counts(cc[0]), a.stat_mask);
           }
         }
       } else {

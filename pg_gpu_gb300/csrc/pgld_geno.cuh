@@ -14,7 +14,7 @@
 #pragma once
 #include <stdint.h>
 
-#include "pgld_geno_tables.cuh"
+#include "pgld_geno_mom.cuh"
 #include "pgld_internal.cuh"
 
 namespace pgld {
@@ -96,9 +96,20 @@ struct GV {
 __host__ __device__ __forceinline__ GV gv(i64 num, i64 den, bool ok) { return {num, den, ok, true}; }
 __host__ __device__ __forceinline__ GV gv_ieee(i64 num, i64 den) { return {num, den, true, false}; }
 
+// The single-population DD, Dz and pi2 through the centred moments of the
+// pair (pgld_geno_mom.cuh): the same exact numerators as the reference's
+// degree-4 polynomials in the nine counts, in a few dozen integer operations.
+__host__ __device__ __forceinline__ gmom::Mom mom_of(const GPop& p) {
+  int c[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) c[k] = p.g[8 - k];
+  return gmom::from_counts(c);
+}
+
 // ---- DD (genotype_kernels.py:27-83) ----
 __host__ __device__ __forceinline__ GV dd_single(const GPop& p) {
-  return gv(16 * dd_poly(p.g) + p.D16 * p.D16, 64 * d4(p.ns), p.ns >= 4);
+  const gmom::Mom o = mom_of(p);
+  return gv(gmom::dd_num(o, gmom::terms(o)), 4 * d4(p.ns), p.ns >= 4);
 }
 __host__ __device__ __forceinline__ GV dd_between(const GPop& A, const GPop& B) {
   const i64 den = A.n * (A.n - 1) * B.n * (B.n - 1);
@@ -107,7 +118,8 @@ __host__ __device__ __forceinline__ GV dd_between(const GPop& A, const GPop& B) 
 
 // ---- Dz (genotype_kernels.py:176-276, cases of compute_all_dz_geno) ----
 __host__ __device__ __forceinline__ GV dz_single(const GPop& p) {
-  return gv(4 * dz_quartic(p.g) + p.a * p.b * p.D16, 8 * d4(p.ns), p.ns >= 4);
+  const gmom::Mom o = mom_of(p);
+  return gv(gmom::dz_num(o, gmom::terms(o)), 2 * d4(p.ns), p.ns >= 4);
 }
 __host__ __device__ __forceinline__ GV dz_iik(const GPop& I, const GPop& K) {
   return gv_ieee(u16(I) * K.a, 8 * K.n * I.n * (I.n - 1) * (I.n - 2));
@@ -124,7 +136,8 @@ __host__ __device__ __forceinline__ GV dz_ijk(const GPop& I, const GPop& J, cons
 
 // ---- pi2 (genotype_kernels.py:279-398, cases of compute_all_pi2_geno) ----
 __host__ __device__ __forceinline__ i64 pi2_single_num(const GPop& p) {
-  return p.P2 * p.Q2 * p.S2 * p.R2 + pi2_corr(p.g);
+  const gmom::Mom o = mom_of(p);
+  return gmom::pi2_num(o, gmom::terms(o));
 }
 __host__ __device__ __forceinline__ GV pi2_single(const GPop& p) {
   return gv(pi2_single_num(p), 16 * d4(p.ns), p.ns >= 4);
@@ -199,9 +212,11 @@ __host__ __device__ __forceinline__ GV pi2_alldiff(const GPop& I, const GPop& J,
 // DD / pi2 of one population (genotype_kernels.py:91-169): NaN unless n >= 4
 // and the pi2 numerator is positive
 __host__ __device__ __forceinline__ GV sigma_d2(const GPop& p) {
-  const i64 pn = pi2_single_num(p);
-  GV v = gv(16 * dd_poly(p.g) + p.D16 * p.D16, 4 * pn, p.ns >= 4 && pn > 0);
-  return v;
+  const gmom::Mom o = mom_of(p);
+  const gmom::Terms t = gmom::terms(o);
+  const i64 pn = gmom::pi2_num(o, t);
+  // DD / pi2 = [dd_num / (4 d4)] / [pn / (16 d4)] = 4 dd_num / pn
+  return gv(4 * gmom::dd_num(o, t), pn, p.ns >= 4 && pn > 0);
 }
 
 // Rogers-Huff r: exact moments of the individuals valid at both SNPs; with no

@@ -1,21 +1,27 @@
 // tcgen05 tensor-core form of the genotype distance-band pairs (sm_103a).
 //
-// The 9-way counts of a SNP pair are dot products of 0/1 indicator vectors
-// over the individuals: with A = the planes (g == 0, g == 1, g == 2, g >= 0)
-// of 32 SNPs i and B the same for 32 SNPs j, D = A B^T holds n_ab for every
-// a, b of all 1,024 pairs of the tile.  The operand rows are plane-major
-// within a 32-SNP block (row = 128 * block + 32 * plane + SNP), so D[32 a +
-// i][32 b + j] = n_ab(i, j).  Operands are E4M3 bytes (0x38 = 1.0) in
-// K-major rows padded to 128 bytes; the float32 accumulators hold integers
-// below 2^24, so the counts are exact.
+// Everything a single-population pair needs -- the 9-way counts, the
+// pairwise-valid n, Rogers-Huff r^2 and the moments DD, Dz, pi2 -- follows
+// from the nine centred moments m[3 x + y] = sum c_i^x c_j^y over the
+// individuals valid at both SNPs, c = dosage - 1 in {-1, 0, 1}
+// (pgld_geno_mom.cuh).  Those are dot products over the individuals: with A =
+// the planes (valid, c, c^2) of 32 SNPs i and B the same for 32 SNPs j,
+// D = A B^T holds m[3 x + y] for all 1,024 pairs of the tile.  The operand
+// rows are plane-major within a 32-SNP block (row = 128 * block + 32 * plane
+// + SNP; plane 3 is zero), so D[32 x + i][32 y + j] = m[3 x + y](i, j).
+// Operands are E4M3 bytes (0x38 = 1.0, 0xB8 = -1.0) in K-major rows padded to
+// 128 bytes; the float32 accumulators hold integers of magnitude below 2^24,
+// so the moments are exact.
 //
 // One CTA per SM:
 //   warp 0      TMA producer (128-row x 128-byte boxes, SWIZZLE_128B)
-//   warp 1      allocates 256 TMEM columns; one lane issues M=128 N=128 K=32
-//               kind::f8f6f4 MMAs into accumulator stage t % 2
+//   warp 1      allocates 256 TMEM columns; one lane issues M=128 N=96 K=32
+//               kind::f8f6f4 MMAs (the B rows of planes 0-2) into
+//               accumulator stage t % 2
 //   warps 4-11  epilogue: the warps of TMEM lane quarters 0-2 (planes 0-2)
-//               copy the 3 x 3 count blocks to shared memory, then all eight
-//               warps turn 1,024 pairs into outputs (4 per thread)
+//               copy the 3 x 3 moment blocks to shared memory (48 columns
+//               each), then all eight warps turn 1,024 pairs into outputs (4
+//               per thread)
 // Every mbarrier wait is bounded; the epilogue warps meet at one named
 // barrier per tile and agree on aborting after it.
 #include <cuda.h>
@@ -25,7 +31,7 @@
 
 #include "pgld_band.cuh"
 #include "pgld_epilogue.cuh"
-#include "pgld_geno.cuh"
+#include "pgld_geno_mom.cuh"
 #include "pgld_internal.cuh"
 #include "pgld_scan.cuh"
 #include "pgld_tcgen05.cuh"
@@ -40,7 +46,18 @@ constexpr int kEpiWarps = 8;
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kThreads = (4 + kEpiWarps) * 32;
 constexpr uint32_t kTmemCols = 256;   // two accumulator stages of 128 columns
-constexpr int kCntPitch = 97;         // int pitch of the 96 x 96 count block
+constexpr int kCntPitch = 97;         // int pitch of the 96 x 96 moment block
+// instruction descriptor: D f32, A/B E4M3, both K-major, N = 96, M = 128
+constexpr uint32_t kIdescN96 = (1u << 4) | ((96u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_f8_n96(uint32_t dtmem, uint64_t a, uint64_t b,
+                                           uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(kIdescN96), "r"(accum)
+      : "memory");
+}
 
 struct Params {
   int kchunks;
@@ -171,7 +188,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint64_t da = smem_desc(sa), db = smem_desc(sa + kBoxBytes);
 #pragma unroll
           for (int k = 0; k < kKChunk / 32; ++k)
-            mma_f8(d, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), (kc | k) != 0);
+            mma_f8_n96(d, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), (kc | k) != 0);
           mma_commit(&ctrl->empty[stage]);
           any = true;
           *(volatile int*)&ctrl->consumed = ++consumed;
@@ -192,14 +209,43 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---------------- epilogue ----------------
     const int e = warp - 4;
     const int quarter = warp & 3;  // TMEM lanes 32q..32q+31 = plane q of the 32 SNPs i
-    const int half = e >> 2;       // columns 64h..64h+63 = planes 2h, 2h+1 of the SNPs j
+    const int half = e >> 2;       // columns 48h..48h+47 of the 96 (planes 0-2 of the SNPs j)
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const int t_epi = threadIdx.x - 128;
+    long long lo = 0;  // row block of the current item: items ascend, so it only moves forward
     int t = 0;
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
       const int acc = t & 1;
       const uint32_t aph = (uint32_t)((t >> 1) & 1);
       int* buf = cnt + acc * 96 * kCntPitch;
+      // locate the item before waiting for its accumulator, so the loads'
+      // latency overlaps the MMAs: two warp-wide steps forward from the last
+      // row block (32 offsets per step), then a binary search for long jumps
+      {
+        bool found = false;
+#pragma unroll 1
+        for (int round = 0; round < 2 && !found; ++round) {
+          const long long idx = lo + 1 + lane;
+          const bool le = idx <= a.n_blocks && a.item_off[idx] <= item;
+          const unsigned bal = __ballot_sync(0xffffffffu, le);
+          lo += __popc(bal);
+          found = bal != 0xffffffffu;
+        }
+        if (!found) {
+          long long l2 = lo, h2 = a.n_blocks;
+          while (h2 - l2 > 1) {
+            const long long mid = (l2 + h2) >> 1;
+            if (a.item_off[mid] <= item) l2 = mid; else h2 = mid;
+          }
+          lo = l2;
+        }
+      }
+      const long long i0 = lo * kTileSnp, j0 = (lo + (item - a.item_off[lo])) * kTileSnp;
+      // band offsets of the tile's 32 rows: lane l holds row i0 + l
+      const long long ri = i0 + lane < a.n_snp ? i0 + lane : a.n_snp;
+      const long long off_lo = a.pair_off[ri];
+      const long long off_n = (ri < a.n_snp ? a.pair_off[ri + 1] : off_lo) - off_lo;
+
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
       ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
@@ -209,9 +255,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_after();
         if (quarter < 3) {
 #pragma unroll 1
-          for (int c = 0; c < 4; ++c) {
-            const int col0 = half * 64 + c * 16;
-            if (col0 >= 96) break;  // plane 3 of the SNPs j is not needed
+          for (int c = 0; c < 3; ++c) {
+            const int col0 = half * 48 + c * 16;
             uint32_t r[16];
             tmem_ld16(tmem_base + lane_base + (uint32_t)(acc * 128 + col0), r);
             tmem_wait_ld();
@@ -237,40 +282,30 @@ __global__ void __launch_bounds__(kThreads, 1)
           : "memory");
       if (any_abort) break;
 
-      long long lo = 0, hi = a.n_blocks;
-      while (hi - lo > 1) {
-        const long long mid = (lo + hi) >> 1;
-        if (a.item_off[mid] <= item) lo = mid; else hi = mid;
-      }
-      const long long i0 = lo * kTileSnp, j0 = (lo + (item - a.item_off[lo])) * kTileSnp;
 #pragma unroll 1
       for (int k = 0; k < 4; ++k) {
         const int il = (t_epi >> 5) + 8 * k, jl = lane;
+        const long long row_off = __shfl_sync(0xffffffffu, off_lo, il);
+        const long long row_n = __shfl_sync(0xffffffffu, off_n, il);
         const long long i = i0 + il, j = j0 + jl;
-        bool ok = (i < j) && (j < a.n_snp);
-        if (ok) ok = (j - i - 1) < (a.pair_off[i + 1] - a.pair_off[i]);
-        if (!ok) continue;
-        int c9[9];
+        // j < i + 1 + row_n keeps j inside the band and below n_snp
+        if (!(i < j && j - i - 1 < row_n)) continue;
+        gmom::Mom mo;
 #pragma unroll
         for (int x = 0; x < 3; ++x)
 #pragma unroll
-          for (int y = 0; y < 3; ++y) c9[3 * x + y] = buf[(x * 32 + il) * kCntPitch + y * 32 + jl];
-        const long long kk = a.pair_off[i] + (j - i - 1);
-        const geno::GPop P = geno::make_gpop(c9, -1);
+          for (int y = 0; y < 3; ++y)
+            mo.m[3 * x + y] = buf[(x * 32 + il) * kCntPitch + y * 32 + jl];
+        const long long kk = row_off + (j - i - 1);
         if (a.counts) {
+          int c9[9];
+          gmom::to_counts(mo, c9);
           int32_t* o = a.counts + kk * 9;
 #pragma unroll
           for (int x = 0; x < 9; ++x) o[x] = c9[x];
         }
-        if (a.nvalid) a.nvalid[kk] = (int32_t)P.ns;
-        if (a.stats) {
-          float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (a.stat_mask & 1) o.x = geno::rh2_f32(c9);
-          if (a.stat_mask & 2) o.y = geno::gv_f32(geno::dd_single(P));
-          if (a.stat_mask & 4) o.z = geno::gv_f32(geno::dz_single(P));
-          if (a.stat_mask & 8) o.w = geno::gv_f32(geno::pi2_single(P));
-          reinterpret_cast<float4*>(a.stats)[kk] = o;
-        }
+        if (a.nvalid) a.nvalid[kk] = mo.m[0];
+        if (a.stats) reinterpret_cast<float4*>(a.stats)[kk] = gmom::stats_f32(mo, a.stat_mask);
       }
     }
   }
@@ -286,10 +321,20 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// operand rows: row 128 * (s / 32) + 32 * plane + s % 32 holds, for plane 0..2,
-// the individuals with dosage == plane at SNP s, and for plane 3 the valid
-// ones.  A block writes 8 rows, a warp one row in 16-byte chunks (16
-// individuals, one nibble-to-bytes step per 4).
+// operand rows: row 128 * (s / 32) + 32 * plane + s % 32 holds, per
+// individual, plane 0: 1 if the dosage at SNP s is known, plane 1: c = dosage
+// - 1 (+1, 0, -1; 0 if missing), plane 2: c^2; plane 3 is zero.  A block
+// writes 8 rows, a warp one row in 16-byte chunks (16 individuals, one
+// nibble-to-bytes step per 4).
+__device__ __forceinline__ uint32_t e4m3_nibble(uint32_t mag, uint32_t neg) {
+  // byte q = (bit q of mag ? 1.0 : 0) with the sign bit from neg
+  uint32_t v = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    v |= ((mag >> q & 1u) ? kOne : 0u) << (8 * q) | ((neg >> q & 1u) ? 0x80u : 0u) << (8 * q);
+  return v;
+}
+
 __global__ void __launch_bounds__(256) pack_gtc_kernel(const uint32_t* __restrict__ planes, int W,
                                                        long long n_snp, long long n_blocks,
                                                        int k_pad, uint32_t* __restrict__ out) {
@@ -306,19 +351,16 @@ __global__ void __launch_bounds__(256) pack_gtc_kernel(const uint32_t* __restric
   for (int c = lane; c < chunks; c += 32) {
     const int h0 = 16 * c;
     const int w = h0 >> 5;
-    uint32_t bits = 0;
-    if (s < n_snp && w < W) {
-      const uint32_t word = plane < 3 ? __ldg(ps + plane * W + w)
-                                      : (__ldg(ps + w) | __ldg(ps + W + w) | __ldg(ps + 2 * W + w));
-      bits = (word >> (h0 & 31)) & 0xFFFFu;
+    uint32_t mag = 0, neg = 0;
+    if (plane < 3 && s < n_snp && w < W) {
+      const uint32_t g0 = __ldg(ps + w), g2 = __ldg(ps + 2 * W + w);
+      const uint32_t word = plane == 0 ? (g0 | __ldg(ps + W + w) | g2) : (g0 | g2);
+      mag = (word >> (h0 & 31)) & 0xFFFFu;
+      if (plane == 1) neg = (g0 >> (h0 & 31)) & 0xFFFFu;
     }
     uint32_t v[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const uint32_t nib = (bits >> (4 * q)) & 0xFu;
-      v[q] = (nib & 1u ? kOne : 0u) | (nib & 2u ? kOne << 8 : 0u) | (nib & 4u ? kOne << 16 : 0u) |
-             (nib & 8u ? kOne << 24 : 0u);
-    }
+    for (int q = 0; q < 4; ++q) v[q] = e4m3_nibble(mag >> (4 * q), neg >> (4 * q));
     dst[c] = make_uint4(v[0], v[1], v[2], v[3]);
   }
 }

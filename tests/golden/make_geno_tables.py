@@ -11,9 +11,12 @@ through the CPU shim), expands each with sympy into canonical monomials, and
 writes
 
   oracle/geno_tables.py                     (the oracle's exact evaluation)
-  pg_gpu_gb300/csrc/pgld_geno_tables.cuh    (the CUDA kernels' tables)
 
-Both files are committed; this script runs only where the reference checkout
+The CUDA kernels evaluate the same numerators through the centred moments of
+the pair (pg_gpu_gb300/csrc/pgld_geno_mom.cuh), checked against these tables
+by tests/test_geno_mom_cpu.py.
+
+The table is committed; this script runs only where the reference checkout
 exists and is not needed to build or test.
 """
 import os
@@ -74,49 +77,14 @@ def main():
           "(coefficient, (a, b, c)): coefficient * g[a] * g[b] * g[c] with g the",
           "moments-order counts g1..g9 at indices 0..8 and g[9] = 1.",
           '"""', ""]
-    cu = ["// The single-population genotype estimators of moments: the DD numerator",
-          "// polynomial, the Dz quartic and 16 x the pi2 correction (genotype_kernels.py:",
-          "// 27-71, 235-279, 364-398), expanded into canonical monomials over the",
-          "// moments-order counts g1..g9 (g[0..8]; g[9] = 1) and regrouped as",
-          "//   sum_a g[a] * (sum_b g[b] * (sum_c coef_abc * g[c])),",
-          "// innermost sums in 32-bit and outer sums in 64-bit integers: exact for",
-          "// populations below 32,768 individuals.  Generated by",
-          "// tests/golden/make_geno_tables.py.",
-          "#pragma once", "", "namespace pgld {", "namespace geno {", ""]
     for name, mono in tables.items():
         py.append(f"{name} = [")
         for c, (a, b, d) in mono:
             py.append(f"    ({c}, ({a}, {b}, {d})),")
         py.append("]")
         py.append("")
-        fname = name.lower()
-        groups = {}
-        for c, (a, b, d) in mono:
-            groups.setdefault(a, {}).setdefault(b, []).append((c, d))
-        cu.append(f"__host__ __device__ __forceinline__ long long {fname}(const int* g) {{")
-        outer = []
-        for a in sorted(groups):
-            inner = []
-            for b in sorted(groups[a]):
-                lin = " + ".join(f"{c} * g[{d}]" if d != 9 else f"{c}" for c, d in groups[a][b])
-                lin = lin.replace("+ -", "- ")
-                if b == 9:
-                    inner.append(f"(long long)({lin})")
-                else:
-                    inner.append(f"(long long)g[{b}] * ({lin})")
-            body = " +\n        ".join(inner)
-            if a == 9:
-                outer.append(f"({body})")
-            else:
-                outer.append(f"(long long)g[{a}] * (\n        {body})")
-        cu.append("  return " + " +\n      ".join(outer) + ";")
-        cu.append("}")
-        cu.append("")
-    cu += ["}  // namespace geno", "}  // namespace pgld", ""]
     with open(os.path.join(ROOT, "oracle", "geno_tables.py"), "w") as f:
         f.write("\n".join(py))
-    with open(os.path.join(ROOT, "pg_gpu_gb300", "csrc", "pgld_geno_tables.cuh"), "w") as f:
-        f.write("\n".join(cu))
     for name, mono in tables.items():
         print(name, len(mono), "monomials, max |coef|", max(abs(c) for c, _ in mono))
 
