@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(kThreads) geno_band_kernel(BandArgs a) {
           if (a.stats) {
             // only the requested columns are evaluated; the others are 0
             reinterpret_cast<float4*>(a.stats)[k] =
-                gmom::stats_f32(gmom::from_counts(cc[0]), a.stat_mask);
+                gmom::stats_f32<-1>(gmom::from_counts(cc[0]), a.stat_mask);
           }
         }
       } else {

@@ -147,14 +147,19 @@ PGLD_GM_HD RHm rh(const Mom& o) {
 #ifdef __CUDACC__
 // float32 per-pair outputs of the band kernels: x = Rogers-Huff r^2 (NaN
 // where a SNP has no variance among the pairwise-valid individuals), y, z, w
-// = DD, Dz, pi2 (0 below 4 individuals); bit k of mask selects component k,
-// the others stay 0.  Populations up to 8,192 individuals: the Rogers-Huff
-// moments n m4 - m1 m3, n m6 - m3^2, n m2 - m1^2 are then 32-bit integers
-// below 2^27, converted once each (relative error 2^-24), so r^2 carries at
-// most 8 roundings; the 64-bit numerators convert with at most two roundings
-// and share one reciprocal of d4 (__fdividef: 2 ulp): every output is within
-// 1e-6 relative of its exact value.
-__device__ __forceinline__ float4 stats_f32(const Mom& o, int mask) {
+// = DD, Dz, pi2 (0 below 4 individuals); bit k of the mask selects component
+// k, the others stay 0.  MASK >= 0 fixes the mask at compile time, -1 takes
+// mask_rt; both evaluate the same operations, so the values are identical.
+// Everything is computed unconditionally and the gates are selects (no
+// divergent branches).  Populations up to 8,192 individuals: the
+// Rogers-Huff moments n m4 - m1 m3, n m6 - m3^2, n m2 - m1^2 are then 32-bit
+// integers below 2^27, converted once each (relative error 2^-24), so r^2
+// carries at most 8 roundings; the 64-bit numerators convert with at most two
+// roundings and share one reciprocal of d4 (__fdividef: 2 ulp): every output
+// is within 1e-6 relative of its exact value.
+template <int MASK>
+__device__ __forceinline__ float4 stats_f32(const Mom& o, int mask_rt) {
+  const int mask = MASK >= 0 ? MASK : mask_rt;
   float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
   const int* m = o.m;
   const int n = m[0];
@@ -163,15 +168,16 @@ __device__ __forceinline__ float4 stats_f32(const Mom& o, int mask) {
     const int vi = n * m[6] - m[3] * m[3];
     const int vj = n * m[2] - m[1] * m[1];
     const float fc = (float)cov;
-    out.x = (vi <= 0 || vj <= 0) ? __int_as_float(0x7fc00000)
-                                 : __fdividef(fc * fc, (float)vi * (float)vj);
+    const float v = __fdividef(fc * fc, (float)vi * (float)vj);
+    out.x = (vi > 0 && vj > 0) ? v : __int_as_float(0x7fc00000);
   }
-  if ((mask & 14) && n >= 4) {
+  if (mask & 14) {
     const Terms t = terms(o);
-    const float r = __fdividef(1.0f, pgld::ll2f(d4(n)));
-    if (mask & 2) out.y = pgld::ll2f(dd_num(o, t)) * (0.25f * r);
-    if (mask & 4) out.z = pgld::ll2f(dz_num(o, t)) * (0.5f * r);
-    if (mask & 8) out.w = pgld::ll2f(pi2_num(o, t)) * (0.0625f * r);
+    const bool ok = n >= 4;
+    const float r = __fdividef(1.0f, pgld::ll2f(d4(n)));  // unused where !ok
+    if (mask & 2) out.y = ok ? pgld::ll2f(dd_num(o, t)) * (0.25f * r) : 0.f;
+    if (mask & 4) out.z = ok ? pgld::ll2f(dz_num(o, t)) * (0.5f * r) : 0.f;
+    if (mask & 8) out.w = ok ? pgld::ll2f(pi2_num(o, t)) * (0.0625f * r) : 0.f;
   }
   return out;
 }

@@ -7,23 +7,26 @@
 // (pgld_geno_mom.cuh).  Those are dot products over the individuals: with A =
 // the planes (valid, c, c^2) of 32 SNPs i and B the same for 32 SNPs j,
 // D = A B^T holds m[3 x + y] for all 1,024 pairs of the tile.  The operand
-// rows are plane-major within a 32-SNP block (row = 128 * block + 32 * plane
-// + SNP; plane 3 is zero), so D[32 x + i][32 y + j] = m[3 x + y](i, j).
+// rows are plane-major within a 32-SNP block (row = 96 * block + 32 * plane
+// + SNP), so D[32 x + i][32 y + j] = m[3 x + y](i, j); the A tile's rows
+// 96..127 (M = 128) are zero rows kept in shared memory.
 // Operands are E4M3 bytes (0x38 = 1.0, 0xB8 = -1.0) in K-major rows padded to
 // 128 bytes; the float32 accumulators hold integers of magnitude below 2^24,
 // so the moments are exact.
 //
 // One CTA per SM:
-//   warp 0      TMA producer (128-row x 128-byte boxes, SWIZZLE_128B)
+//   warp 0      TMA producer (96-row x 128-byte boxes, SWIZZLE_128B; 28 KB
+//               stages, so six are in flight)
 //   warp 1      allocates 256 TMEM columns; one lane issues M=128 N=96 K=32
 //               kind::f8f6f4 MMAs (the B rows of planes 0-2) into
 //               accumulator stage t % 2
-//   warps 4-11  epilogue: the warps of TMEM lane quarters 0-2 (planes 0-2)
-//               copy the 3 x 3 moment blocks to shared memory (48 columns
-//               each), then all eight warps turn 1,024 pairs into outputs (4
-//               per thread)
-// Every mbarrier wait is bounded; the epilogue warps meet at one named
-// barrier per tile and agree on aborting after it.
+//   warps 4-11  epilogue: two groups of four warps on alternate tiles
+//               (accumulator stage and moment buffer per group); in a group
+//               the warps of TMEM lane quarters 0-2 (planes 0-2) copy the
+//               3 x 3 moment blocks to shared memory, then all four turn
+//               1,024 pairs into outputs (8 per thread)
+// Every mbarrier wait is bounded; the warps of an epilogue group meet at
+// their named barrier twice per tile and agree on aborting at the first.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -43,10 +46,13 @@ using namespace pgld::tc;
 
 constexpr int kTileSnp = 32;          // SNPs per tile side (4 planes = 128 rows)
 constexpr int kEpiWarps = 8;
-constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kThreads = (4 + kEpiWarps) * 32;
 constexpr uint32_t kTmemCols = 256;   // two accumulator stages of 128 columns
-constexpr int kCntPitch = 97;         // int pitch of the 96 x 96 moment block
+constexpr int kBlkRows = 96;          // operand rows of a 32-SNP block (3 planes)
+constexpr int kABytes = kBoxBytes;     // A: 96 loaded rows + 32 zero rows (M = 128)
+constexpr int kBBytes = kBlkRows * kKChunk;  // B: 96 rows (N = 96)
+constexpr int kGStageBytes = kABytes + kBBytes;  // 28 KB
+constexpr int kCntPitch = 98;         // int16 pitch of the 96 x 96 moment block (49 words: odd)
 // instruction descriptor: D f32, A/B E4M3, both K-major, N = 96, M = 128
 constexpr uint32_t kIdescN96 = (1u << 4) | ((96u >> 3) << 17) | ((128u >> 4) << 24);
 
@@ -73,15 +79,16 @@ struct Params {
   int stages;
 };
 
-template <int DUMMY>
+// MASK: the statistic columns when fixed at compile time (-1: a.stat_mask)
+template <int MASK>
 __global__ void __launch_bounds__(kThreads, 1)
     gtc_pairs_kernel(const __grid_constant__ CUtensorMap map, Params a) {
   extern __shared__ unsigned char smem_dyn[];
   unsigned char* base = smem_dyn + ((1024 - (smem_u32(smem_dyn) & 1023)) & 1023);
   const int stages = a.stages;
   unsigned char* ring = base;
-  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kStageBytes);
-  int* cnt = reinterpret_cast<int*>(ctrl + 1);  // [2][96][kCntPitch]
+  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kGStageBytes);
+  int16_t* cnt = reinterpret_cast<int16_t*>(ctrl + 1);  // [2][96][kCntPitch]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int* abort_flag = &ctrl->abort_flag;
 
@@ -92,7 +99,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&ctrl->tfull[s], 1);
-      mbar_init(&ctrl->tempty[s], kEpiWarps);
+      mbar_init(&ctrl->tempty[s], kEpiWarps / 2);  // the four warps of epilogue group s
     }
     mbar_init(&ctrl->drain, 1);
     ctrl->abort_flag = 0;
@@ -106,6 +113,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  // rows 96..127 of every A stage (the last 4 KB: whole 1 KB swizzle atoms)
+  // stay zero: TMA writes only the 96 operand rows
+  for (int s = 0; s < stages; ++s) {
+    uint4* z = reinterpret_cast<uint4*>(ring + (size_t)s * kGStageBytes + kBlkRows * kKChunk);
+    for (int k = threadIdx.x; k < (kABytes - kBlkRows * kKChunk) / 16; k += blockDim.x)
+      z[k] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -129,16 +144,17 @@ __global__ void __launch_bounds__(kThreads, 1)
           const long long mid = (lo + hi) >> 1;
           if (a.item_off[mid] <= item) lo = mid; else hi = mid;
         }
-        const int yi = (int)(lo * kRows), yj = (int)((lo + (item - a.item_off[lo])) * kRows);
+        const int yi = (int)(lo * kBlkRows),
+                  yj = (int)((lo + (item - a.item_off[lo])) * kBlkRows);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+          if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
             set_abort(ctrl, a.status, 4002);
             break;
           }
-          mbar_expect_tx(&ctrl->full[stage], kStageBytes);
-          unsigned char* sa = ring + (size_t)stage * kStageBytes;
+          mbar_expect_tx(&ctrl->full[stage], 2 * kBBytes);
+          unsigned char* sa = ring + (size_t)stage * kGStageBytes;
           tma_load_2d(sa, &map, &ctrl->full[stage], kc * kKChunk, yi);
-          tma_load_2d(sa + kBoxBytes, &map, &ctrl->full[stage], kc * kKChunk, yj);
+          tma_load_2d(sa + kABytes, &map, &ctrl->full[stage], kc * kKChunk, yj);
           ++issued;
           if (++stage == stages) {
             stage = 0;
@@ -170,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
+        if (!mbar_wait_poll(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
           set_abort(ctrl, a.status, 4003);
           break;
         }
@@ -178,14 +194,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         const uint32_t d = tmem_base + (uint32_t)(acc * 128);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait(&ctrl->full[stage], phase, abort_flag)) {
+          if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag)) {
             set_abort(ctrl, a.status, 4004);
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t sa = smem_u32(ring + (size_t)stage * kStageBytes);
-          const uint64_t da = smem_desc(sa), db = smem_desc(sa + kBoxBytes);
+          const uint32_t sa = smem_u32(ring + (size_t)stage * kGStageBytes);
+          const uint64_t da = smem_desc(sa), db = smem_desc(sa + kABytes);
 #pragma unroll
           for (int k = 0; k < kKChunk / 32; ++k)
             mma_f8_n96(d, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), (kc | k) != 0);
@@ -207,106 +223,133 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp >= 4) {
     // ---------------- epilogue ----------------
+    // Two groups of four warps take alternate tiles (group g: tiles g, g + 2,
+    // ... of this CTA, accumulator stage g, moment buffer g), so one group's
+    // copy and the other's statistics overlap.  Within a group the warp of
+    // TMEM lane quarter q < 3 copies plane q's 96 moment columns, and all four
+    // warps turn the 1,024 pairs into outputs (8 per thread).
     const int e = warp - 4;
-    const int quarter = warp & 3;  // TMEM lanes 32q..32q+31 = plane q of the 32 SNPs i
-    const int half = e >> 2;       // columns 48h..48h+47 of the 96 (planes 0-2 of the SNPs j)
-    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-    const int t_epi = threadIdx.x - 128;
-    long long lo = 0;  // row block of the current item: items ascend, so it only moves forward
-    int t = 0;
-    for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
-      const int acc = t & 1;
-      const uint32_t aph = (uint32_t)((t >> 1) & 1);
-      int* buf = cnt + acc * 96 * kCntPitch;
-      // locate the item before waiting for its accumulator, so the loads'
-      // latency overlaps the MMAs: two warp-wide steps forward from the last
-      // row block (32 offsets per step), then a binary search for long jumps
-      {
-        bool found = false;
-#pragma unroll 1
-        for (int round = 0; round < 2 && !found; ++round) {
-          const long long idx = lo + 1 + lane;
-          const bool le = idx <= a.n_blocks && a.item_off[idx] <= item;
-          const unsigned bal = __ballot_sync(0xffffffffu, le);
-          lo += __popc(bal);
-          found = bal != 0xffffffffu;
-        }
-        if (!found) {
+    const int grp = e >> 2;
+    const int wq = warp & 3;  // TMEM lanes 32q..32q+31 = plane q of the 32 SNPs i
+    const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+    const uint32_t bar_id = 1u + (uint32_t)grp;
+    int16_t* buf = cnt + grp * 96 * kCntPitch;
+    const long long stride = 2LL * gridDim.x;
+    long long item = blockIdx.x + (long long)grp * gridDim.x;
+
+    // tile location: items ascend, so the row block lo only moves forward;
+    // nv holds item_off[lo + 1 + lane], loaded one tile ahead
+    long long lo = 0;
+    long long nv = 1 + lane <= a.n_blocks ? a.item_off[1 + lane] : LLONG_MAX;
+    long long i0 = 0, j0 = 0, off_lo = 0;
+    int off_n = 0;
+    auto locate = [&](long long it) {
+      unsigned bal = __ballot_sync(0xffffffffu, nv <= it);
+      lo += __popc(bal);
+      if (bal == 0xffffffffu) {
+        const long long idx = lo + 1 + lane;
+        bal = __ballot_sync(0xffffffffu, idx <= a.n_blocks && a.item_off[idx] <= it);
+        lo += __popc(bal);
+        if (bal == 0xffffffffu) {
           long long l2 = lo, h2 = a.n_blocks;
           while (h2 - l2 > 1) {
             const long long mid = (l2 + h2) >> 1;
-            if (a.item_off[mid] <= item) l2 = mid; else h2 = mid;
+            if (a.item_off[mid] <= it) l2 = mid; else h2 = mid;
           }
           lo = l2;
         }
       }
-      const long long i0 = lo * kTileSnp, j0 = (lo + (item - a.item_off[lo])) * kTileSnp;
+      i0 = lo * kTileSnp;
+      j0 = (lo + (it - a.item_off[lo])) * kTileSnp;
       // band offsets of the tile's 32 rows: lane l holds row i0 + l
       const long long ri = i0 + lane < a.n_snp ? i0 + lane : a.n_snp;
-      const long long off_lo = a.pair_off[ri];
-      const long long off_n = (ri < a.n_snp ? a.pair_off[ri + 1] : off_lo) - off_lo;
+      off_lo = a.pair_off[ri];
+      off_n = (int)((ri < a.n_snp ? a.pair_off[ri + 1] : off_lo) - off_lo);
+    };
+    if (item < n_items) locate(item);
 
+    for (int u = 0; item < n_items; item += stride, ++u) {
       bool ready = true;
-      if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
+      if (lane == 0) ready = mbar_wait(&ctrl->tfull[grp], (uint32_t)(u & 1), abort_flag);
       ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
       if (!ready && lane == 0) set_abort(ctrl, a.status, 4005);
-      const uint32_t local_abort = ready ? 0u : 1u;
-      if (ready) {
-        tc_fence_after();
-        if (quarter < 3) {
-#pragma unroll 1
-          for (int c = 0; c < 3; ++c) {
-            const int col0 = half * 48 + c * 16;
-            uint32_t r[16];
-            tmem_ld16(tmem_base + lane_base + (uint32_t)(acc * 128 + col0), r);
-            tmem_wait_ld();
-            int* row = buf + (quarter * 32 + lane) * kCntPitch + col0;
-#pragma unroll
-            for (int v = 0; v < 16; ++v) row[v] = fast::f2i_small(__uint_as_float(r[v]));
-          }
-        }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
-      }
-      // all epilogue warps meet once per tile and take one decision on
-      // aborting: the barrier ORs every thread's view (its own wait failed,
-      // or the control block's flag is set), so no warp is left waiting
+      // the group meets before overwriting its buffer (every warp is done
+      // reading the previous tile) and takes one decision on aborting: the
+      // barrier ORs every thread's view (its own wait failed, or the control
+      // block's flag is set), so no warp is left waiting
       uint32_t any_abort = 0;
-      const uint32_t mine = local_abort | (uint32_t)(*abort_flag != 0);
+      const uint32_t mine = (ready ? 0u : 1u) | (uint32_t)(*abort_flag != 0);
       asm volatile(
           "{\n .reg .pred pin, pout;\n setp.ne.u32 pin, %1, 0;\n"
-          " bar.red.or.pred pout, 1, %2, pin;\n selp.u32 %0, 1, 0, pout;\n}"
+          " bar.red.or.pred pout, %2, 128, pin;\n selp.u32 %0, 1, 0, pout;\n}"
           : "=r"(any_abort)
-          : "r"(mine), "r"(kEpiThreads)
+          : "r"(mine), "r"(bar_id)
           : "memory");
       if (any_abort) break;
-
+      tc_fence_after();
+      if (wq < 3) {
+        int16_t* row = buf + (wq * 32 + lane) * kCntPitch;
 #pragma unroll 1
-      for (int k = 0; k < 4; ++k) {
-        const int il = (t_epi >> 5) + 8 * k, jl = lane;
-        const long long row_off = __shfl_sync(0xffffffffu, off_lo, il);
-        const long long row_n = __shfl_sync(0xffffffffu, off_n, il);
-        const long long i = i0 + il, j = j0 + jl;
-        // j < i + 1 + row_n keeps j inside the band and below n_snp
-        if (!(i < j && j - i - 1 < row_n)) continue;
+        for (int h = 0; h < 2; ++h) {
+          uint32_t r[3][16];
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            tmem_ld16(tmem_base + lane_base + (uint32_t)(grp * 128 + 48 * h + 16 * c), r[c]);
+          tmem_wait_ld();
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int v = 0; v < 16; ++v)
+              row[48 * h + 16 * c + v] = (int16_t)fast::f2i_small(__uint_as_float(r[c][v]));
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&ctrl->tempty[grp]);
+      asm volatile("bar.sync %0, 128;" ::"r"(bar_id) : "memory");
+
+      // this tile's location; the next tile's offsets load during the pairs
+      const long long ti0 = i0, tj0 = j0, toff = off_lo;
+      const int tn = off_n;
+      const long long next = item + stride;
+      if (next < n_items) nv = lo + 1 + lane <= a.n_blocks ? a.item_off[lo + 1 + lane] : LLONG_MAX;
+
+      // eight pairs per thread; every value is computed and only the stores
+      // depend on the pair lying in the band.  The outputs go out as
+      // streaming global stores (st.global.cs): they are not re-read, and
+      // being global-space they cannot alias the shared-memory moments, so
+      // the loads of later pairs may move ahead of earlier pairs' stores.
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int il = wq + 4 * k, jl = lane;
+        const long long row_off = __shfl_sync(0xffffffffu, toff, il);
+        const int row_n = __shfl_sync(0xffffffffu, tn, il);
+        const int d = (int)(tj0 - ti0) + jl - il - 1;  // j - i - 1
+        // d < row_n keeps j inside the band and below n_snp
+        const bool ok = d >= 0 && d < row_n;
         gmom::Mom mo;
 #pragma unroll
         for (int x = 0; x < 3; ++x)
 #pragma unroll
           for (int y = 0; y < 3; ++y)
             mo.m[3 * x + y] = buf[(x * 32 + il) * kCntPitch + y * 32 + jl];
-        const long long kk = row_off + (j - i - 1);
+        const long long kk = row_off + d;
         if (a.counts) {
           int c9[9];
           gmom::to_counts(mo, c9);
-          int32_t* o = a.counts + kk * 9;
+          if (ok) {
+            int32_t* o = a.counts + kk * 9;
 #pragma unroll
-          for (int x = 0; x < 9; ++x) o[x] = c9[x];
+            for (int x = 0; x < 9; ++x) __stcs(o + x, c9[x]);
+          }
         }
-        if (a.nvalid) a.nvalid[kk] = mo.m[0];
-        if (a.stats) reinterpret_cast<float4*>(a.stats)[kk] = gmom::stats_f32(mo, a.stat_mask);
+        if (a.nvalid && ok) __stcs(a.nvalid + kk, mo.m[0]);
+        if (a.stats) {
+          const float4 o = gmom::stats_f32<MASK>(mo, a.stat_mask);
+          if (ok) __stcs(reinterpret_cast<float4*>(a.stats) + kk, o);
+        }
       }
+      if (next < n_items) locate(next);
     }
   }
 
@@ -321,9 +364,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// operand rows: row 128 * (s / 32) + 32 * plane + s % 32 holds, per
+// operand rows: row 96 * (s / 32) + 32 * plane + s % 32 holds, per
 // individual, plane 0: 1 if the dosage at SNP s is known, plane 1: c = dosage
-// - 1 (+1, 0, -1; 0 if missing), plane 2: c^2; plane 3 is zero.  A block
+// - 1 (+1, 0, -1; 0 if missing), plane 2: c^2.  A block
 // writes 8 rows, a warp one row in 16-byte chunks (16 individuals, one
 // nibble-to-bytes step per 4).
 __device__ __forceinline__ uint32_t e4m3_nibble(uint32_t mag, uint32_t neg) {
@@ -340,11 +383,11 @@ __global__ void __launch_bounds__(256) pack_gtc_kernel(const uint32_t* __restric
                                                        int k_pad, uint32_t* __restrict__ out) {
   const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (row >= n_blocks * kRows) return;
+  if (row >= n_blocks * kBlkRows) return;
   const int chunks = k_pad / 16;
   uint4* dst = reinterpret_cast<uint4*>(out) + row * chunks;
-  const long long blk = row >> 7;
-  const int within = (int)(row & 127);
+  const long long blk = row / kBlkRows;
+  const int within = (int)(row - blk * kBlkRows);
   const int plane = within >> 5;
   const long long s = blk * kTileSnp + (within & 31);
   const uint32_t* ps = planes + (s < n_snp ? s : 0) * 3 * W;
@@ -352,7 +395,7 @@ __global__ void __launch_bounds__(256) pack_gtc_kernel(const uint32_t* __restric
     const int h0 = 16 * c;
     const int w = h0 >> 5;
     uint32_t mag = 0, neg = 0;
-    if (plane < 3 && s < n_snp && w < W) {
+    if (s < n_snp && w < W) {
       const uint32_t g0 = __ldg(ps + w), g2 = __ldg(ps + 2 * W + w);
       const uint32_t word = plane == 0 ? (g0 | __ldg(ps + W + w) | g2) : (g0 | g2);
       mag = (word >> (h0 & 31)) & 0xFFFFu;
@@ -379,10 +422,10 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
   const long long n = panel->n_snp;
   const int W = panel->n_words[0];
   const long long nb = (n + kTileSnp - 1) / kTileSnp;
-  if (nb * kRows > 2147483647LL)
+  if (nb * kBlkRows > 2147483647LL)
     return pgld_fail(h, PGLD_ERR_TOO_LARGE, "genotype tensor-core form: too many SNPs");
   const int k_pad = ((W * 32 + kKChunk - 1) / kKChunk) * kKChunk;
-  const size_t op_bytes = (size_t)nb * kRows * k_pad;
+  const size_t op_bytes = (size_t)nb * kBlkRows * k_pad;
   const size_t sb = pgld::scan_scratch_bytes(std::max<long long>(nb, n));
   auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
   const size_t off_items = 0, off_scan = al((nb + 1) * 8), off_op = off_scan + al(sb),
@@ -397,7 +440,7 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
   rc = pgld_band_offsets(h, pos, n, max_dist, poff, w + off_scan, sb, st);
   if (rc) return rc;
   {
-    const unsigned blocks = (unsigned)std::max<long long>(1, (nb * kRows + 7) / 8);
+    const unsigned blocks = (unsigned)std::max<long long>(1, (nb * kBlkRows + 7) / 8);
     pack_gtc_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, n, nb, k_pad, (uint32_t*)op);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_gtc_kernel");
@@ -405,7 +448,7 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
   rc = pgld::band_schedule(h, pos, n, max_dist, items, w + off_scan, sb, st, kTileSnp);
   if (rc) return rc;
   CUtensorMap map;
-  rc = pgld::tchost::make_map(h, &map, op, nb * kRows, k_pad);
+  rc = pgld::tchost::make_map(h, &map, op, nb * kBlkRows, k_pad, kBlkRows);
   if (rc) return rc;
   Params prm{};
   prm.kchunks = k_pad / kKChunk;
@@ -418,15 +461,19 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
   prm.stats = stats;
   prm.stat_mask = stat_mask;
   prm.status = h->dev_status;
-  const size_t fixed = sizeof(pgld::tc::Ctrl) + (size_t)2 * 96 * kCntPitch * 4 + 1024;
+  const size_t fixed = sizeof(pgld::tc::Ctrl) + (size_t)2 * 96 * kCntPitch * 2 + 1024;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
   const int stages =
-      (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStageBytes);
+      (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kGStageBytes);
   if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "genotype tensor-core form: shared memory");
   prm.stages = stages;
-  const size_t smem = (size_t)stages * kStageBytes + fixed;
-  auto kern = gtc_pairs_kernel<0>;
+  const size_t smem = (size_t)stages * kGStageBytes + fixed;
+  // the two column sets of the band workloads get their own instantiation
+  auto kern = !stats ? gtc_pairs_kernel<0>
+              : stat_mask == 3 ? gtc_pairs_kernel<3>
+              : stat_mask == 15 ? gtc_pairs_kernel<15>
+                                : gtc_pairs_kernel<-1>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "gtc smem attribute");
   kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map, prm);

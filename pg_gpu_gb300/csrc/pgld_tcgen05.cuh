@@ -67,6 +67,29 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile
   }
   return false;
 }
+// non-blocking probe of a phase
+__device__ __forceinline__ bool mbar_test(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded polling wait for the single producer / MMA threads, whose stages
+// are short: reacts to a completed phase within a few cycles (no suspension);
+// false once ~2 s of SM clock passed or another role aborted
+__device__ __forceinline__ bool mbar_wait_poll(uint64_t* b, uint32_t parity,
+                                               volatile int* abort_flag) {
+  const long long t0 = clock64();
+  for (long long k = 0; k < kSpinLimit; ++k) {
+    if (mbar_test(b, parity)) return true;
+    if ((k & 63) == 63 && (*abort_flag || clock64() - t0 > kWaitCycles)) return false;
+  }
+  return false;
+}
 // drain wait: bounded by time only
 __device__ __forceinline__ void mbar_wait_drain(uint64_t* b, uint32_t parity) {
   const long long t0 = clock64();
@@ -176,12 +199,13 @@ inline int get_encode(pgld_context* h) {
   return PGLD_OK;
 }
 
-// rows x k_pad bytes, row-major, k_pad a multiple of 128
+// rows x k_pad bytes, row-major, k_pad a multiple of 128; boxes of box_rows
+// rows x 128 bytes
 inline int make_map(pgld_context* h, CUtensorMap* map, const void* base, long long rows,
-                    int k_pad) {
+                    int k_pad, int box_rows = pgld::tc::kRows) {
   cuuint64_t dims[2] = {(cuuint64_t)k_pad, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)k_pad};
-  cuuint32_t box[2] = {(cuuint32_t)pgld::tc::kKChunk, (cuuint32_t)pgld::tc::kRows};
+  cuuint32_t box[2] = {(cuuint32_t)pgld::tc::kKChunk, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims,
                            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
