@@ -79,15 +79,56 @@ struct Params {
   int stages;
 };
 
-// MASK: the statistic columns when fixed at compile time (-1: a.stat_mask)
-template <int MASK>
+constexpr int kChunkItems = 16;  // consecutive tiles a CTA takes per turn (resident form)
+
+// control block: the stage / accumulator barriers, plus the resident form's
+// B barriers and the per-stage tile flags the producer hands the MMA issuer
+struct GCtrl : Ctrl {
+  uint64_t bfull, bempty;
+  int meta[8];  // first stage of a tile: bit 0 = first tile of a strip, bit 1 = last
+};
+
+// the t-th tile of this CTA: turns of `chunk` consecutive items, round robin
+// over the CTAs (chunk 1: item blockIdx.x + t * gridDim.x)
+__device__ __forceinline__ long long tile_item(int t, int chunk) {
+  return ((long long)blockIdx.x + (long long)(t / chunk) * gridDim.x) * chunk + t % chunk;
+}
+
+// row block of an item, moving forward from lo (the items a thread visits
+// ascend): a few steps, then a binary search
+__device__ __forceinline__ long long advance_block(const long long* item_off, long long n_blocks,
+                                                   long long lo, long long item) {
+#pragma unroll 1
+  for (int s = 0; s < 4; ++s) {
+    if (lo + 1 >= n_blocks || item_off[lo + 1] > item) return lo;
+    ++lo;
+  }
+  long long hi = n_blocks;
+  while (hi - lo > 1) {
+    const long long mid = (lo + hi) >> 1;
+    if (item_off[mid] <= item) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// MASK: the statistic columns when fixed at compile time (-1: a.stat_mask).
+// RES: the resident form -- the row block's 96 operand rows (every K chunk)
+// stay in shared memory as the B operand (N = 96) for a strip of consecutive
+// tiles of that row block, and only the column block streams (A, M = 128 with
+// 32 zero rows); the accumulator is then transposed (lanes: planes of the
+// SNPs j, columns: planes of the SNPs i).  Otherwise both blocks stream per
+// K chunk (A = row block, B = column block).
+template <int MASK, bool RES>
 __global__ void __launch_bounds__(kThreads, 1)
     gtc_pairs_kernel(const __grid_constant__ CUtensorMap map, Params a) {
   extern __shared__ unsigned char smem_dyn[];
   unsigned char* base = smem_dyn + ((1024 - (smem_u32(smem_dyn) & 1023)) & 1023);
   const int stages = a.stages;
+  constexpr int kStage = RES ? kABytes : kGStageBytes;
+  const int chunk = RES ? kChunkItems : 1;
   unsigned char* ring = base;
-  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kGStageBytes);
+  unsigned char* bres = ring + (size_t)stages * kStage;  // resident B (RES only)
+  GCtrl* ctrl = reinterpret_cast<GCtrl*>(bres + (RES ? (size_t)a.kchunks * kBBytes : 0));
   int16_t* cnt = reinterpret_cast<int16_t*>(ctrl + 1);  // [2][96][kCntPitch]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int* abort_flag = &ctrl->abort_flag;
@@ -102,6 +143,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&ctrl->tempty[s], kEpiWarps / 2);  // the four warps of epilogue group s
     }
     mbar_init(&ctrl->drain, 1);
+    mbar_init(&ctrl->bfull, 1);
+    mbar_init(&ctrl->bempty, 1);
     ctrl->abort_flag = 0;
     ctrl->consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -116,7 +159,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   // rows 96..127 of every A stage (the last 4 KB: whole 1 KB swizzle atoms)
   // stay zero: TMA writes only the 96 operand rows
   for (int s = 0; s < stages; ++s) {
-    uint4* z = reinterpret_cast<uint4*>(ring + (size_t)s * kGStageBytes + kBlkRows * kKChunk);
+    uint4* z = reinterpret_cast<uint4*>(ring + (size_t)s * kStage + kBlkRows * kKChunk);
     for (int k = threadIdx.x; k < (kABytes - kBlkRows * kKChunk) / 16; k += blockDim.x)
       z[k] = make_uint4(0u, 0u, 0u, 0u);
   }
@@ -137,30 +180,58 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
-      int issued = 0;
-      for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x) {
-        long long lo = 0, hi = a.n_blocks;
-        while (hi - lo > 1) {
-          const long long mid = (lo + hi) >> 1;
-          if (a.item_off[mid] <= item) lo = mid; else hi = mid;
+      int issued = 0, strips = 0;
+      long long item = tile_item(0, chunk);
+      long long lo = item < n_items ? advance_block(a.item_off, a.n_blocks, 0, item) : 0;
+      long long lo_prev = -1;
+      for (int t = 0; item < n_items && !*abort_flag; ++t) {
+        const long long jb = lo + (item - a.item_off[lo]);
+        const long long next = tile_item(t + 1, chunk);
+        const long long lo_next =
+            next < n_items ? advance_block(a.item_off, a.n_blocks, lo, next) : -1;
+        const bool first = lo != lo_prev, last = lo_next != lo;
+        bool ok = true;
+        if (RES && first) {
+          // a new strip: its row block replaces the resident B once the MMAs
+          // of the previous strip are done with it
+          if (strips > 0 && !mbar_wait_poll(&ctrl->bempty, (uint32_t)((strips - 1) & 1),
+                                            abort_flag)) {
+            set_abort(ctrl, a.status, 4006);
+            break;
+          }
+          mbar_expect_tx(&ctrl->bfull, (uint32_t)(a.kchunks * kBBytes));
+          for (int kc = 0; kc < a.kchunks; ++kc)
+            tma_load_2d(bres + (size_t)kc * kBBytes, &map, &ctrl->bfull, kc * kKChunk,
+                        (int)(lo * kBlkRows));
+          ++strips;
         }
-        const int yi = (int)(lo * kBlkRows),
-                  yj = (int)((lo + (item - a.item_off[lo])) * kBlkRows);
         for (int kc = 0; kc < a.kchunks; ++kc) {
           if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
             set_abort(ctrl, a.status, 4002);
+            ok = false;
             break;
           }
-          mbar_expect_tx(&ctrl->full[stage], 2 * kBBytes);
-          unsigned char* sa = ring + (size_t)stage * kGStageBytes;
-          tma_load_2d(sa, &map, &ctrl->full[stage], kc * kKChunk, yi);
-          tma_load_2d(sa + kABytes, &map, &ctrl->full[stage], kc * kKChunk, yj);
+          if (kc == 0) ctrl->meta[stage] = (first ? 1 : 0) | (last ? 2 : 0);
+          unsigned char* sa = ring + (size_t)stage * kStage;
+          if (RES) {
+            mbar_expect_tx(&ctrl->full[stage], kBBytes);
+            tma_load_2d(sa, &map, &ctrl->full[stage], kc * kKChunk, (int)(jb * kBlkRows));
+          } else {
+            mbar_expect_tx(&ctrl->full[stage], 2 * kBBytes);
+            tma_load_2d(sa, &map, &ctrl->full[stage], kc * kKChunk, (int)(lo * kBlkRows));
+            tma_load_2d(sa + kABytes, &map, &ctrl->full[stage], kc * kKChunk,
+                        (int)(jb * kBlkRows));
+          }
           ++issued;
           if (++stage == stages) {
             stage = 0;
             phase ^= 1;
           }
         }
+        if (!ok) break;
+        lo_prev = lo;
+        lo = lo_next;
+        item = next;
       }
       if (*abort_flag) {
         // drain: every issued copy lands before the CTA may exit
@@ -174,6 +245,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             ph2 ^= 1;
           }
         }
+        if (RES && strips > 0) mbar_wait_drain(&ctrl->bfull, (uint32_t)((strips - 1) & 1));
       }
     }
   } else if (warp == 1) {
@@ -181,9 +253,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
-      int t = 0, consumed = 0;
+      int consumed = 0, strips = 0;
       bool any = false;
-      for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
+      for (int t = 0; !*abort_flag; ++t) {
+        if (tile_item(t, chunk) >= n_items) break;
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
         if (!mbar_wait_poll(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
@@ -191,7 +264,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         tc_fence_after();
-        bool ok = true;
+        bool ok = true, last = false;
         const uint32_t d = tmem_base + (uint32_t)(acc * 128);
         for (int kc = 0; kc < a.kchunks; ++kc) {
           if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag)) {
@@ -199,9 +272,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             ok = false;
             break;
           }
+          if (kc == 0) {
+            const int m = ctrl->meta[stage];
+            last = (m & 2) != 0;
+            if (RES && (m & 1)) {
+              if (!mbar_wait_poll(&ctrl->bfull, (uint32_t)(strips & 1), abort_flag)) {
+                set_abort(ctrl, a.status, 4007);
+                ok = false;
+                break;
+              }
+              ++strips;
+            }
+          }
           tc_fence_after();
-          const uint32_t sa = smem_u32(ring + (size_t)stage * kGStageBytes);
-          const uint64_t da = smem_desc(sa), db = smem_desc(sa + kABytes);
+          const uint32_t sa = smem_u32(ring + (size_t)stage * kStage);
+          const uint64_t da = smem_desc(sa);
+          const uint64_t db =
+              smem_desc(RES ? smem_u32(bres + (size_t)kc * kBBytes) : sa + kABytes);
 #pragma unroll
           for (int k = 0; k < kKChunk / 32; ++k)
             mma_f8_n96(d, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), (kc | k) != 0);
@@ -215,6 +302,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (!ok) break;
         mma_commit(&ctrl->tfull[acc]);
+        if (RES && last) mma_commit(&ctrl->bempty);  // the strip's MMAs are all issued
       }
       if (*abort_flag && any) {
         mma_commit(&ctrl->drain);
@@ -230,12 +318,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     // warps turn the 1,024 pairs into outputs (8 per thread).
     const int e = warp - 4;
     const int grp = e >> 2;
-    const int wq = warp & 3;  // TMEM lanes 32q..32q+31 = plane q of the 32 SNPs i
+    const int wq = warp & 3;  // TMEM lanes 32q..32q+31: plane q of the SNPs i (j if RES)
     const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
     const uint32_t bar_id = 1u + (uint32_t)grp;
     int16_t* buf = cnt + grp * 96 * kCntPitch;
-    const long long stride = 2LL * gridDim.x;
-    long long item = blockIdx.x + (long long)grp * gridDim.x;
+    int t = grp;
+    long long item = tile_item(t, chunk);
 
     // tile location: items ascend, so the row block lo only moves forward;
     // nv holds item_off[lo + 1 + lane], loaded one tile ahead
@@ -268,7 +356,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     };
     if (item < n_items) locate(item);
 
-    for (int u = 0; item < n_items; item += stride, ++u) {
+    for (int u = 0; item < n_items; ++u) {
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[grp], (uint32_t)(u & 1), abort_flag);
       ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
@@ -311,7 +399,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       // this tile's location; the next tile's offsets load during the pairs
       const long long ti0 = i0, tj0 = j0, toff = off_lo;
       const int tn = off_n;
-      const long long next = item + stride;
+      t += 2;
+      const long long next = tile_item(t, chunk);
       if (next < n_items) nv = lo + 1 + lane <= a.n_blocks ? a.item_off[lo + 1 + lane] : LLONG_MAX;
 
       // eight pairs per thread; every value is computed and only the stores
@@ -332,7 +421,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int x = 0; x < 3; ++x)
 #pragma unroll
           for (int y = 0; y < 3; ++y)
-            mo.m[3 * x + y] = buf[(x * 32 + il) * kCntPitch + y * 32 + jl];
+            mo.m[3 * x + y] = RES ? buf[(y * 32 + jl) * kCntPitch + x * 32 + il]
+                                  : buf[(x * 32 + il) * kCntPitch + y * 32 + jl];
         const long long kk = row_off + d;
         if (a.counts) {
           int c9[9];
@@ -349,7 +439,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (ok) __stcs(reinterpret_cast<float4*>(a.stats) + kk, o);
         }
       }
-      if (next < n_items) locate(next);
+      item = next;
+      if (item < n_items) locate(item);
     }
   }
 
@@ -461,19 +552,34 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
   prm.stats = stats;
   prm.stat_mask = stat_mask;
   prm.status = h->dev_status;
-  const size_t fixed = sizeof(pgld::tc::Ctrl) + (size_t)2 * 96 * kCntPitch * 2 + 1024;
+  const size_t fixed = sizeof(GCtrl) + (size_t)2 * 96 * kCntPitch * 2 + 1024;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-  const int stages =
-      (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kGStageBytes);
+  // the resident form when the row block (every K chunk) fits beside at
+  // least four 16 KB A stages: up to 1,280 individuals
+  const long long res_bytes = (long long)prm.kchunks * kBBytes;
+  const long long res_stages =
+      std::min<long long>(8, ((long long)max_smem - (long long)fixed - res_bytes) / kABytes);
+  const bool res = res_stages >= 4;
+  const int stages = res ? (int)res_stages
+                         : (int)std::min<long long>(
+                               8, ((long long)max_smem - (long long)fixed) / kGStageBytes);
   if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "genotype tensor-core form: shared memory");
   prm.stages = stages;
-  const size_t smem = (size_t)stages * kGStageBytes + fixed;
+  const size_t smem =
+      res ? (size_t)stages * kABytes + (size_t)res_bytes + fixed : (size_t)stages * kGStageBytes + fixed;
   // the two column sets of the band workloads get their own instantiation
-  auto kern = !stats ? gtc_pairs_kernel<0>
-              : stat_mask == 3 ? gtc_pairs_kernel<3>
-              : stat_mask == 15 ? gtc_pairs_kernel<15>
-                                : gtc_pairs_kernel<-1>;
+  void (*kern)(CUtensorMap, Params);
+  if (res)
+    kern = !stats ? gtc_pairs_kernel<0, true>
+           : stat_mask == 3 ? gtc_pairs_kernel<3, true>
+           : stat_mask == 15 ? gtc_pairs_kernel<15, true>
+                             : gtc_pairs_kernel<-1, true>;
+  else
+    kern = !stats ? gtc_pairs_kernel<0, false>
+           : stat_mask == 3 ? gtc_pairs_kernel<3, false>
+           : stat_mask == 15 ? gtc_pairs_kernel<15, false>
+                             : gtc_pairs_kernel<-1, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "gtc smem attribute");
   kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map, prm);
