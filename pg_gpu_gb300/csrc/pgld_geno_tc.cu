@@ -81,6 +81,20 @@ struct Params {
 
 constexpr int kChunkItems = 16;  // consecutive tiles a CTA takes per turn (resident form)
 
+// streaming global stores under a predicate, without a branch around them
+__device__ __forceinline__ void st_cs_if(bool p, int32_t* ptr, int v) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n @q st.global.cs.b32 [%1], %2;\n}" ::"r"(
+          (int)p),
+      "l"(ptr), "r"(v));
+}
+__device__ __forceinline__ void st_cs_if(bool p, float4* ptr, float4 v) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n"
+      " @q st.global.cs.v4.f32 [%1], {%2, %3, %4, %5};\n}" ::"r"((int)p),
+      "l"(ptr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
+}
+
 // control block: the stage / accumulator barriers, plus the resident form's
 // B barriers and the per-stage tile flags the producer hands the MMA issuer
 struct GCtrl : Ctrl {
@@ -396,6 +410,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (lane == 0) mbar_arrive(&ctrl->tempty[grp]);
       asm volatile("bar.sync %0, 128;" ::"r"(bar_id) : "memory");
 
+      const bool want_nv = a.nvalid != nullptr;
       // this tile's location; the next tile's offsets load during the pairs
       const long long ti0 = i0, tj0 = j0, toff = off_lo;
       const int tn = off_n;
@@ -433,10 +448,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int x = 0; x < 9; ++x) __stcs(o + x, c9[x]);
           }
         }
-        if (a.nvalid && ok) __stcs(a.nvalid + kk, mo.m[0]);
+        st_cs_if(ok && want_nv, a.nvalid + kk, mo.m[0]);
         if (a.stats) {
           const float4 o = gmom::stats_f32<MASK>(mo, a.stat_mask);
-          if (ok) __stcs(reinterpret_cast<float4*>(a.stats) + kk, o);
+          st_cs_if(ok, reinterpret_cast<float4*>(a.stats) + kk, o);
         }
       }
       item = next;
