@@ -117,3 +117,29 @@ def test_tc_band_pairs_match_oracle(H, M):
     assert (np.abs(st[m] - ref[m]) / np.abs(ref[m])).max() <= 1e-6
     z = ref == 0
     assert np.all(st[z] == 0)
+
+
+@pytest.mark.parametrize("form", ["tc", "plain"])
+def test_sharded_binned_sums_add_up(form):
+    # the multi-rank partition (pg_gpu_gb300/shard.py) run as three shards on
+    # one device: the partials' sum is the oracle's whole-panel result
+    from pg_gpu_gb300 import shard as S
+    rng = np.random.default_rng(77)
+    H, M = 300, 2_500
+    hap = copying_model(rng, 2 * H, M, 20, 2e-3, missing=0.02)
+    pos = np.sort(rng.choice(2_000_000, M, replace=False)).astype(np.int64)
+    bins = np.array([0.0, 1e3, 1e4, 5e4, 1e5])
+    rows = [np.arange(0, H), np.arange(H, 2 * H)]
+    hap_d = torch.as_tensor(hap, device="cuda")
+    pops = [_ops.pack(hap_d, r) for r in rows]
+    pos_d = _ops.positions_f64(pos)
+    compute = S.slice_binned_sums(pops, pos_d, bins, form=form)
+    acc_s, acc_c = 0.0, 0
+    for sh in S.plan_shards(pos, bins[-1], 3):
+        part = S.shard_partial(compute, sh)
+        acc_s = acc_s + part[0].cpu().numpy()
+        acc_c = acc_c + part[1].cpu().numpy()
+    ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True)
+    assert np.array_equal(acc_c, ref_cnt)
+    # each shard's sums carry the float32 per-pair error of the halo pairs twice
+    assert np.all(np.abs(acc_s - ref) <= 3 * SUM_TOL * ref_abs + 1e-300)
