@@ -14,7 +14,8 @@ from . import _ops
 __all__ = ["estimate_ld_chunk_size", "iter_pairs_within_distance", "compute_counts_for_pairs",
            "compute_genotype_counts_for_pairs", "compute_two_pop_statistics_batch",
            "compute_single_pop_statistics_batch", "ld_names", "het_names",
-           "generate_stat_specs", "PopData"]
+           "generate_stat_specs", "PopData", "pairs_within_distance_statistics",
+           "genotype_pairs_within_distance_statistics"]
 
 
 def estimate_ld_chunk_size(n_haplotypes_per_pop, available_memory_bytes=None, num_pops=2):
@@ -89,6 +90,35 @@ def _pc(counts):
 
 def _nv(n_valid):
     return None if n_valid is None else L.as_device(n_valid, np.int32)
+
+
+def pairs_within_distance_statistics(haplotypes, positions, max_dist, pop_indices=None,
+                                     with_stats=True):
+    """Every pair (i < j, pos[j] - pos[i] <= max_dist) of one population, fused
+    on the device: the loop of iter_pairs_within_distance +
+    compute_counts_for_pairs + compute_ld_statistics (ld_pipeline.py:57-175,
+    ld_statistics.py:13-246) in one call, pairs in iter_pairs_within_distance
+    order.  Returns (counts (N,4) int32, n_valid (N,) int32, stats (N,4)
+    float32 = r^2, DD, Dz, pi2, or None)."""
+    pk = _ops.pack(haplotypes, pop_indices)
+    return _ops.band_pairs(pk, _ops.positions_f64(positions), float(max_dist),
+                           with_stats=with_stats)
+
+
+def genotype_pairs_within_distance_statistics(genotypes, positions, max_dist, pop_indices=None,
+                                              statistics=("r2", "dd", "dz", "pi2"),
+                                              with_counts=True):
+    """Every pair (i < j, pos[j] - pos[i] <= max_dist) of one population of
+    dosages, fused on the device: the loop of iter_pairs_within_distance +
+    compute_genotype_counts_for_pairs + the single-population genotype DD /
+    Dz / pi2 (genotype_kernels.py:27-71, 235-279, 364-398) and Rogers-Huff
+    r^2 over the pairwise-valid individuals, pairs in
+    iter_pairs_within_distance order.  Returns (counts (N,9) int32 or None,
+    n_valid (N,) int32, stats (N,4) float32 = r^2, DD, Dz, pi2; columns not
+    in `statistics` hold 0)."""
+    pk = _ops.pack_geno(genotypes, pop_indices)
+    return _ops.geno_band_pairs(pk, _ops.positions_f64(positions), float(max_dist),
+                                with_counts=with_counts, columns=tuple(statistics))
 
 
 def compute_two_pop_statistics_batch(counts_pop1, counts_pop2, n_valid1, n_valid2,

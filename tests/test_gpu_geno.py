@@ -226,3 +226,26 @@ def test_edge_cases_and_errors():
         assert np.array_equal(np_(counts), rc)
     with pytest.raises(PgldError):
         _ops.geno_binned_sums([pk], _ops.positions_f64(pos), np.linspace(0, 1, 200))
+
+
+def test_public_fused_pair_statistics_match_the_chunked_loop():
+    # ld_pipeline's fused band calls give the reference loop's pairs, in its order
+    from pg_gpu_gb300 import ld_pipeline as LP
+    rng = np.random.default_rng(31)
+    g = dosages(rng, 200, 400, 12, 2e-3, missing=0.03)
+    hap = (rng.random((64, 400)) < 0.4).astype(np.int8)
+    hap[rng.random(hap.shape) < 0.02] = -1
+    pos = np.sort(rng.choice(200_000, 400, replace=False)).astype(np.int64)
+    ii, jj = O.pairs_within_distance(pos, 20_000)
+    c, nv, st = LP.genotype_pairs_within_distance_statistics(
+        torch.as_tensor(g, device="cuda"), pos, 20_000, statistics=("r2", "dd"))
+    rc, rnv = O.genotype_counts_for_pairs(g, ii, jj)
+    assert np.array_equal(np_(c), rc) and np.array_equal(np_(nv), rnv)
+    ref = O.geno_dd((0, 0), [O.GenoPop(rc, rnv)])
+    got = np_(st)[:, 1].astype(np.float64)
+    m = np.abs(ref) > 1e-30
+    assert np.all(np.abs(got[m] - ref[m]) <= 1e-6 * np.abs(ref[m])) and np.all(np_(st)[:, 2:] == 0)
+    c4, nv4, st4 = LP.pairs_within_distance_statistics(torch.as_tensor(hap, device="cuda"), pos,
+                                                       20_000)
+    rc4 = O.counts_for_pairs(hap, ii, jj)[0]
+    assert np.array_equal(np_(c4), rc4) and st4.shape == (len(ii), 4)
