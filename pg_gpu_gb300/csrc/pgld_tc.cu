@@ -85,8 +85,12 @@ struct TileRef {
   int w;
 };
 
+// row_hint: the row block of this thread's previous item (its items ascend),
+// from which the band modes step forward -- a load or two per tile instead of
+// a binary search -- falling back to a binary search for long jumps
 template <int MODE>
-__device__ __forceinline__ TileRef decode_item(const Params& a, long long item) {
+__device__ __forceinline__ TileRef decode_item(const Params& a, long long item,
+                                               long long& row_hint) {
   TileRef r;
   if constexpr (MODE == kModeWindows) {
     int lo = 0, hi = a.n_win;
@@ -113,11 +117,20 @@ __device__ __forceinline__ TileRef decode_item(const Params& a, long long item) 
     r.begin = a.win_begin[lo];
     r.w = lo;
   } else {
-    long long lo = 0, hi = a.n_blocks;
-    while (hi - lo > 1) {
-      const long long mid = (lo + hi) >> 1;
-      if (a.item_off[mid] <= item) lo = mid; else hi = mid;
+    long long lo = row_hint;
+    int steps = 0;
+    while (lo + 1 < a.n_blocks && a.item_off[lo + 1] <= item && steps < 4) {
+      ++lo;
+      ++steps;
     }
+    if (steps == 4) {
+      long long hi = a.n_blocks;
+      while (hi - lo > 1) {
+        const long long mid = (lo + hi) >> 1;
+        if (a.item_off[mid] <= item) lo = mid; else hi = mid;
+      }
+    }
+    row_hint = lo;
     r.bi = lo;
     r.bj = lo + (item - a.item_off[lo]);
     r.i0 = r.bi * kTileSnp;
@@ -303,8 +316,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       int stage = 0;
       uint32_t phase = 0;
       int issued = 0;
+      long long row_hint = 0;
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x) {
-        const TileRef tr = decode_item<MODE>(a, item);
+        const TileRef tr = decode_item<MODE>(a, item, row_hint);
         const int yi = (int)(2 * tr.i0), yj = (int)(2 * tr.j0);
         for (int p = 0; p < P && !*abort_flag; ++p) {
           const CUtensorMap* map = p == 0 ? &map0 : &map1;
@@ -401,10 +415,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     float2* my_acc = kacc + (size_t)e * n_bins * S;
     unsigned long long* my_cnt = kcnt + (size_t)e * n_bins;
     int t = 0;
+    long long row_hint = 0;
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
       const int acc = t & 1;
       const uint32_t aph = (uint32_t)((t >> 1) & 1);
-      const TileRef tr = decode_item<MODE>(a, item);
+      const TileRef tr = decode_item<MODE>(a, item, row_hint);
       const long long bi = tr.bi, bj = tr.bj;
       const long long i0 = tr.i0, j0 = tr.j0;
       const long long si0 = i0 + 16 * quarter, sj0 = j0 + 32 * half;
