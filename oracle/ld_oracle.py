@@ -548,7 +548,7 @@ def bin_index(distances, bins):
 
 
 def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
-                pair_block=2_000_000, abs_sums=False):
+                pair_block=2_000_000, abs_sums=False, anchor_stop=None):
     """(n_bins, n_stats) float64 sums of the per-pair statistics, plus pair counts.
 
     ``pop_rows``: list of row-index arrays, one per population (1..4).
@@ -556,6 +556,8 @@ def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
     a genetic map in Morgans for the recombination-distance mode).
     With ``abs_sums`` the sums of |stat| are returned as a third value
     (the scale that bounds the float32 rounding of the GPU sums).
+    ``anchor_stop``: only the pairs whose first SNP lies below it (a sample of
+    a large panel's pairs).
     """
     pos = np.asarray(positions)
     coord = pos.astype(np.float64) if coords is None else np.asarray(coords, np.float64)
@@ -564,7 +566,13 @@ def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
     P = len(pop_rows)
     if max_dist is None:
         max_dist = float(bins[-1])
+    if anchor_stop is not None:
+        jend = np.searchsorted(pos, pos[:anchor_stop] + max_dist, side="right")
+        pos = pos[:int(jend.max()) if anchor_stop > 0 else 0]
     ii, jj = pairs_within_distance(pos, max_dist)
+    if anchor_stop is not None:
+        keep = ii < anchor_stop
+        ii, jj = ii[keep], jj[keep]
     specs = stat_specs(P)
     sums = np.zeros((n_bins, len(specs)))
     asums = np.zeros((n_bins, len(specs)))

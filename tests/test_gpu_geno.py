@@ -249,3 +249,50 @@ def test_public_fused_pair_statistics_match_the_chunked_loop():
                                                        20_000)
     rc4 = O.counts_for_pairs(hap, ii, jj)[0]
     assert np.array_equal(np_(c4), rc4) and st4.shape == (len(ii), 4)
+
+
+def test_full_size_geno_band():
+    # the unphased-genotype workload at full size: 1,000 diploids x 500,000
+    # SNPs over 50 Mb, 3 % missing, every pair within 200 kb (~1e9 pairs; the
+    # n / r^2 / DD outputs, 20 GB).  On all pairs: the pair count equals the
+    # one from the positions, 4 <= n <= 1,000 where DD is nonzero, r^2 in
+    # [0, 1] or NaN; the first ~1e6 pairs equal the oracle's
+    rng = np.random.default_rng(20261505)
+    N, M, D = 1000, 500_000, 200_000
+    p = rng.beta(0.3, 0.3, size=M)
+    f = (rng.random((60, M)) < p).astype(np.int8)
+    g = np.zeros((N, M), np.int8)
+    for b in range(0, M, 2_000):  # each haplotype copies a founder per 2,000-SNP block
+        for _ in range(2):
+            g[:, b:b + 2_000] += f[rng.integers(0, 60, N), b:b + 2_000]
+    g[rng.random(g.shape) < 0.03] = -1
+    pos = np.sort(rng.choice(50_000_000, M, replace=False)).astype(np.int64)
+    g_d = torch.as_tensor(g, device="cuda")
+    pk = _ops.pack_geno(g_d)
+    pos_d = _ops.positions_f64(pos)
+    _, nv, st = _ops.geno_band_pairs(pk, pos_d, D, with_counts=False, columns=("r2", "dd"))
+    pf = pos.astype(np.float64)
+    n_exact = int((np.searchsorted(pf, pf + D, side="right") - np.arange(M) - 1).sum())
+    assert nv.shape[0] == n_exact
+    assert int(nv.max()) <= N and int(nv.min()) >= 0
+    r2 = st[:, 0]
+    assert bool((torch.isnan(r2) | ((r2 >= 0) & (r2 <= 1 + 1e-6))).all())
+    assert bool(((st[:, 1] == 0) | (nv >= 4)).all()) and bool((st[:, 2:] == 0).all())
+    del st
+    A = 500  # anchors of the sampled pairs (~1e6 pairs)
+    ext = np.searchsorted(pf, pf[:A] + D, side="right")
+    ii, jj = O.pairs_within_distance(pos[:int(ext.max())], D)
+    sel = ii < A
+    ii, jj = ii[sel], jj[sel]
+    parts = [O.genotype_counts_for_pairs(g, ii[s:s + 200_000], jj[s:s + 200_000])
+             for s in range(0, len(ii), 200_000)]
+    rc = np.concatenate([q[0] for q in parts])
+    rnv = np.concatenate([q[1] for q in parts])
+    c_gpu, _ = ld_pipeline.compute_genotype_counts_for_pairs(g_d, ii, jj)
+    assert np.array_equal(np_(c_gpu), rc) and np.array_equal(np_(nv[:len(ii)]), rnv)
+    _, _, st = _ops.geno_band_pairs(pk, pos_d, D, with_counts=False, columns=("r2", "dd"))
+    got = np_(st[:len(ii), :2]).astype(np.float64)
+    ref = np.stack([O.rogers_huff_r_counts(rc) ** 2, O.geno_dd((0, 0), [O.GenoPop(rc, rnv)])], 1)
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    m = ~np.isnan(ref) & (np.abs(ref) > 1e-30)
+    assert (np.abs(got[m] - ref[m]) / np.abs(ref[m])).max() <= 1e-6

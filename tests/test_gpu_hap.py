@@ -300,3 +300,54 @@ def test_edge_cases_and_errors():
     assert float(s.abs().sum()) == 0.0 and int(n.sum()) == 0
     with pytest.raises(PgldError):
         _ops.binned_sums([pk], _ops.positions_f64([1.0]), np.linspace(0, 1, 200))
+
+
+def _block_copies(rng, n, M, F, block):
+    """n haplotypes copying one of F founders per block of SNPs (a coarse
+    copying model that generates full-size panels quickly)."""
+    p = rng.beta(0.3, 0.3, size=M)
+    f = (rng.random((F, M)) < p).astype(np.int8)
+    nb = (M + block - 1) // block
+    pick = rng.integers(0, F, size=(n, nb))
+    out = np.empty((n, M), np.int8)
+    for b in range(nb):
+        s, e = b * block, min(M, (b + 1) * block)
+        out[:, s:e] = f[pick[:, b], s:e]
+    return out
+
+
+def test_full_size_band_pairs():
+    # the per-pair workload at full size: 2,000 haplotypes x 100,000 SNPs over
+    # 10 Mb, 2 % missing, every pair within 100 kb (~1e8 pairs).  On all pairs:
+    # the pair count equals the one from the positions, n = n11+n10+n01+n00,
+    # r^2 in [0, 1] or NaN; the first ~1e6 pairs equal the oracle's
+    rng = np.random.default_rng(20261502)
+    H, M, D = 2000, 100_000, 100_000
+    hap = _block_copies(rng, H, M, 50, 2_000)
+    hap[rng.random(hap.shape) < 0.02] = -1
+    pos = np.sort(rng.choice(10_000_000, M, replace=False)).astype(np.int64)
+    pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
+    counts, nv, st = _ops.band_pairs(pk, _ops.positions_f64(pos), D, form="tc")
+    pf = pos.astype(np.float64)
+    n_exact = int((np.searchsorted(pf, pf + D, side="right") - np.arange(M) - 1).sum())
+    assert counts.shape[0] == n_exact
+    assert torch.equal(counts.sum(1, dtype=torch.int32), nv)
+    r2 = st[:, 0]
+    ok = torch.isnan(r2) | ((r2 >= 0) & (r2 <= 1 + 1e-6))
+    assert bool(ok.all())
+    A = 1000  # anchors of the sampled pairs (~1e6 pairs)
+    ext = np.searchsorted(pf, pf[:A] + D, side="right")
+    ii, jj = O.pairs_within_distance(pos[:int(ext.max())], D)
+    sel = ii < A
+    ii, jj = ii[sel], jj[sel]
+    parts = [O.counts_for_pairs(hap, ii[s:s + 200_000], jj[s:s + 200_000])
+             for s in range(0, len(ii), 200_000)]
+    rc = np.concatenate([p[0] for p in parts])
+    rnv = np.concatenate([p[1] for p in parts])
+    assert np.array_equal(np_(counts[:len(ii)]), rc) and np.array_equal(np_(nv[:len(ii)]), rnv)
+    ref = np.stack([O.r_squared(rc, rnv), O.dd(rc, None, rnv), O.dz(rc, None, rnv),
+                    O.pi2(rc, None, rnv)], axis=1)
+    got = np_(st[:len(ii)]).astype(np.float64)
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    m = ~np.isnan(ref) & (np.abs(ref) > 1e-30)
+    assert (np.abs(got[m] - ref[m]) / np.abs(ref[m])).max() <= 1e-6

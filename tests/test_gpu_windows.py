@@ -186,3 +186,49 @@ def test_diploid_zns_omega_match_reference(golden):
     b = _diploid_row_col_sums(GenotypeMatrix(g, np.arange(g.shape[1])))
     np.testing.assert_allclose(a[0], b[0], rtol=1e-12)
     np.testing.assert_allclose(a[1], b[1], rtol=1e-12)
+
+
+def test_full_size_windows():
+    # the batched-window workload at full size: 400 haplotypes, 512 windows of
+    # log-uniform 500..20,000 SNPs (each its own copying panel; 1.3e10 pairs).
+    # On all windows: the pair counts are n (n - 1) / 2, every pair has n >= 4
+    # (no missing data), and the tensor-core and popcount forms count alike;
+    # the three smallest windows equal the oracle's sums
+    rng = np.random.default_rng(20261504)
+    H = 400
+    sizes = np.exp(rng.uniform(np.log(500), np.log(20_000), 512)).astype(np.int64)
+    we = np.cumsum(sizes)
+    wb = we - sizes
+    M = int(we[-1])
+    hap = np.empty((H, M), np.int8)
+    for w in range(len(sizes)):
+        s, e = int(wb[w]), int(we[w])
+        p = rng.beta(0.3, 0.3, size=e - s)
+        f = (rng.random((40, e - s)) < p).astype(np.int8)
+        for b in range(s, e, 1_000):  # a founder per haplotype per 1,000-SNP block
+            hap[:, b:min(e, b + 1_000)] = f[rng.integers(0, 40, H), b - s:min(e, b + 1_000) - s]
+    pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
+    sums, cnt = _ops.window_sums(pk, None, wb, we, form="tc")
+    _, cnt_pl = _ops.window_sums(pk, None, wb, we, form="plain")
+    c = cnt.cpu().numpy()
+    assert np.array_equal(c[:, 0], sizes * (sizes - 1) // 2)
+    assert np.array_equal(c[:, 2], c[:, 0]) and np.all(c[:, 1] <= c[:, 0])
+    assert np.array_equal(c, cnt_pl.cpu().numpy())
+    got = sums.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    for w in np.argsort(sizes)[:3]:
+        s, e = int(wb[w]), int(we[w])
+        ref, rcnt = O.window_sums(hap[:, s:e], np.arange(e - s), [0], [e - s])
+        assert np.array_equal(c[w], rcnt[0])
+        sel = np.arange(s, e)
+        a_, b_ = np.triu_indices(len(sel), 1)
+        cc, nv = O.counts_for_pairs(hap, sel[a_], sel[b_])
+        n = cc.astype(np.int64).sum(1)
+        p_ = O.Pop(cc, n)
+        ddn, _ = O.dd_ii(p_)
+        pin, _ = O.pi2_iiii(p_)
+        ok = (n >= 4) & (pin != 0)
+        scale = np.array([np.nansum(np.abs(O.r_squared(cc, nv))), np.abs(ddn[ok] / pin[ok]).sum(),
+                          np.abs(O.dd(cc, None, n)).sum(), np.abs(O.dz(cc, None, n)).sum(),
+                          np.abs(O.pi2(cc, None, n)).sum(), abs(ref[0, 5])])
+        assert np.all(np.abs(got[w] - ref[0]) <= 2e-6 * scale + 1e-12), (w, got[w], ref[0])
