@@ -81,20 +81,6 @@ struct Params {
 
 constexpr int kChunkItems = 16;  // consecutive tiles a CTA takes per turn (resident form)
 
-// streaming global stores under a predicate, without a branch around them
-__device__ __forceinline__ void st_cs_if(bool p, int32_t* ptr, int v) {
-  asm volatile(
-      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n @q st.global.cs.b32 [%1], %2;\n}" ::"r"(
-          (int)p),
-      "l"(ptr), "r"(v));
-}
-__device__ __forceinline__ void st_cs_if(bool p, float4* ptr, float4 v) {
-  asm volatile(
-      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n"
-      " @q st.global.cs.v4.f32 [%1], {%2, %3, %4, %5};\n}" ::"r"((int)p),
-      "l"(ptr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
-}
-
 // control block: the stage / accumulator barriers, plus the resident form's
 // B barriers and the per-stage tile flags the producer hands the MMA issuer
 struct GCtrl : Ctrl {

@@ -574,15 +574,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
 #pragma unroll
             for (int y = 0; y < 2; ++y) {
-              if (!(y ? ok1 : ok0)) continue;
+              const bool oky = y ? ok1 : ok0;
               const int q = o + y;
-              reinterpret_cast<int4*>(a.counts)[k + y] =
-                  make_int4(fast::f2i_small(__uint_as_float(r[q])),
-                            fast::f2i_small(__uint_as_float(r[q + 4])),
-                            fast::f2i_small(__uint_as_float(r[q + 2])),
-                            fast::f2i_small(__uint_as_float(r[q + 6])));
-              if (a.nvalid) a.nvalid[k + y] = y ? p.n1 : p.n0;
-              if (a.stats) reinterpret_cast<float4*>(a.stats)[k + y] = st[y];
+              st_cs_if(oky, reinterpret_cast<int4*>(a.counts) + (k + y),
+                       make_int4(fast::f2i_small(__uint_as_float(r[q])),
+                                 fast::f2i_small(__uint_as_float(r[q + 4])),
+                                 fast::f2i_small(__uint_as_float(r[q + 2])),
+                                 fast::f2i_small(__uint_as_float(r[q + 6]))));
+              if (a.nvalid) st_cs_if(oky, a.nvalid + (k + y), y ? p.n1 : p.n0);
+              if (a.stats) st_cs_if(oky, reinterpret_cast<float4*>(a.stats) + (k + y), st[y]);
             }
           }
         }

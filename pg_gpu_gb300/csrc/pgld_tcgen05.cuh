@@ -161,6 +161,28 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// streaming (evict-first) global stores of per-pair outputs under a
+// predicate, without a branch around them; global-space stores cannot alias
+// shared-memory loads, so later loads may be scheduled ahead of them
+__device__ __forceinline__ void st_cs_if(bool p, int32_t* ptr, int v) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n @q st.global.cs.b32 [%1], %2;\n}" ::"r"(
+          (int)p),
+      "l"(ptr), "r"(v));
+}
+__device__ __forceinline__ void st_cs_if(bool p, float4* ptr, float4 v) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n"
+      " @q st.global.cs.v4.f32 [%1], {%2, %3, %4, %5};\n}" ::"r"((int)p),
+      "l"(ptr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
+}
+__device__ __forceinline__ void st_cs_if(bool p, int4* ptr, int4 v) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n"
+      " @q st.global.cs.v4.b32 [%1], {%2, %3, %4, %5};\n}" ::"r"((int)p),
+      "l"(ptr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w));
+}
+
 struct Ctrl {
   uint64_t full[8], empty[8], tfull[2], tempty[2], drain;
   uint32_t tmem_base;
