@@ -146,7 +146,8 @@ def test_band_pairs_fp32_outputs():
     assert np.all(st2[:, 2:] == 0)
 
 
-@pytest.mark.parametrize("n_ind,M", [(1, 90), (31, 200), (33, 333), (130, 257), (1000, 300)])
+@pytest.mark.parametrize("n_ind,M", [(1, 90), (31, 200), (33, 333), (130, 257), (1000, 300),
+                                     (1281, 200), (3000, 150)])
 def test_tc_band_pairs_match_plain_and_oracle(n_ind, M):
     # the tensor-core genotype form: counts bit-exact, statistics bit-identical
     # to the plain form (the same float32 epilogue on the same counts)
