@@ -96,10 +96,17 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, ValueError):
             self.proc = None
+        if self.proc is not None:
+            # wait (up to 3 s) for the first sample, so that the sampler is
+            # running when the timed region starts; that sample is not kept
+            import select
+            ready, _, _ = select.select([self.proc.stdout], [], [], 3.0)
+            if ready:
+                self.proc.stdout.readline()
         return self
 
     def __exit__(self, *a):
@@ -635,7 +642,7 @@ def run_hap_band(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="tc", choices=["plain", "tc"])
