@@ -85,19 +85,30 @@ struct TileRef {
   int w;
 };
 
-// row_hint: the row block of this thread's previous item (its items ascend),
-// from which the band modes step forward -- a load or two per tile instead of
-// a binary search -- falling back to a binary search for long jumps
+// row_hint: the row block (windows mode: the window) of this thread's previous
+// item (its items ascend), from which the search steps forward -- a load or
+// two per tile instead of a binary search -- falling back to a binary search
+// for long jumps
 template <int MODE>
 __device__ __forceinline__ TileRef decode_item(const Params& a, long long item,
                                                long long& row_hint) {
   TileRef r;
   if constexpr (MODE == kModeWindows) {
-    int lo = 0, hi = a.n_win;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (a.tile_off[mid] <= item) lo = mid; else hi = mid;
+    // the window: forward from the previous item's window, like the rows below
+    int lo = (int)row_hint;
+    int steps = 0;
+    while (lo + 1 < a.n_win && a.tile_off[lo + 1] <= item && steps < 4) {
+      ++lo;
+      ++steps;
     }
+    if (steps == 4) {
+      int hi = a.n_win;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (a.tile_off[mid] <= item) lo = mid; else hi = mid;
+      }
+    }
+    row_hint = lo;
     // tiles start at the window's first list position rounded down to a
     // multiple of 8 (the operand rows are grouped by 8 positions); pairs
     // before the window are masked
