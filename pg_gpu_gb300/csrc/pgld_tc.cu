@@ -454,6 +454,26 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
 
+      // windows mode: the naive-r^2 site terms of the thread's SNPs, loaded
+      // before the accumulator wait so that their latency overlaps it
+      float4 wfi[2], wfj[8];
+      if constexpr (MODE == kModeWindows) {
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto site_at = [&](long long pos) {
+          if (pos < tr.begin || pos >= tr.end) return zero4;
+          const long long sp = a.idx ? (long long)a.idx[pos] : pos;
+          return (sp >= 0 && sp < a.n_panel) ? a.site[sp] : zero4;
+        };
+        const long long ib = i0 + 16 * quarter + (lane >> 2);
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) wfi[hh] = site_at(ib + 8 * hh);
+#pragma unroll
+        for (int gg = 0; gg < 4; ++gg)
+#pragma unroll
+          for (int y = 0; y < 2; ++y)
+            wfj[2 * gg + y] = site_at(j0 + 32 * half + 8 * gg + 2 * (lane & 3) + y);
+      }
+
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
       ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
@@ -475,11 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         int np = 0, nr2 = 0, nfour = 0;
         const long long ib = i0 + 16 * quarter + (lane >> 2);
         const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        auto site_of = [&](long long pos) {
-          const long long sp = a.idx ? (long long)a.idx[pos] : pos;
-          return (sp >= 0 && sp < a.n_panel) ? a.site[sp] : zero4;
-        };
-#pragma unroll 1
+#pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int hh = c & 1, gp = c >> 1;
           uint32_t r[16];
@@ -494,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           const long long is = ib + 8 * hh;
           const bool iok = is >= tr.begin && is < tr.end;
-          const float4 fi = iok ? site_of(is) : zero4;
+          const float4 fi = wfi[hh];
           auto u2 = [](uint32_t x, uint32_t y) {
             return make_float2(__uint_as_float(x), __uint_as_float(y));
           };
@@ -507,8 +523,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!(l0 || l1)) continue;
             const fast2::Pop p = fast2::make(u2(r[o], r[o + 1]), u2(r[o + 4], r[o + 5]),
                                              u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
-            win::window_pair2(p, u2(r[o], r[o + 1]), T, fi, l0 ? site_of(j) : zero4,
-                              l1 ? site_of(j + 1) : zero4, l0, l1, ws2, np, nr2, nfour);
+            const int gg = 2 * gp + g;
+            win::window_pair2(p, u2(r[o], r[o + 1]), T, fi, l0 ? wfj[2 * gg] : zero4,
+                              l1 ? wfj[2 * gg + 1] : zero4, l0, l1, ws2, np, nr2, nfour);
           }
         }
         float ws[6];
