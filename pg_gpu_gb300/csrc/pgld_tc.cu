@@ -474,6 +474,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             wfj[2 * gg + y] = site_at(j0 + 32 * half + 8 * gg + 2 * (lane & 3) + y);
       }
 
+      // binned mode with integer positions: the positions of the thread's
+      // SNPs (rows ib, ib + 8; columns j0 + 32 half + 8 g + 2 (lane % 4) + y),
+      // loaded before the accumulator wait for the sub-tiles that bin per pair
+      int bp_i0 = 0, bp_i1 = 0, bp_j[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) bp_j[q] = 0;
+      if (MODE == kModeBinned && use_int && mode != 0) {
+        const long long ibp = i0 + 16 * quarter + (lane >> 2);
+        bp_i0 = ibp < a.n_snp ? a.ipos[ibp] : 0;
+        bp_i1 = ibp + 8 < a.n_snp ? a.ipos[ibp + 8] : 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const long long jq = j0 + 32 * half + 8 * (q >> 1) + 2 * (lane & 3) + (q & 1);
+          bp_j[q] = jq < a.n_snp ? a.ipos[jq] : 0;
+        }
+      }
+
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
       ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
@@ -656,9 +673,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       };
       // the lane's SNP i of row half hh and first SNP j of column group g
       const long long ib = i0 + 16 * quarter + (lane >> 2);
-      const int ipos_b0 = (use_int && ib < a.n_snp) ? a.ipos[ib] : 0;
-      const int ipos_b1 = (use_int && ib + 8 < a.n_snp) ? a.ipos[ib + 8] : 0;
+      const int ipos_b0 = bp_i0;
+      const int ipos_b1 = bp_i1;
       auto jx_of = [&](int g) { return j0 + 32 * half + 8 * g + 2 * (lane & 3); };
+      // the prefetched position of column j = jx_of(g) + y (g runtime: selects)
+      auto jpos = [&](int g, int y) {
+        const int a0 = y ? bp_j[1] : bp_j[0], a1 = y ? bp_j[3] : bp_j[2];
+        const int a2 = y ? bp_j[5] : bp_j[4], a3 = y ? bp_j[7] : bp_j[6];
+        return g == 0 ? a0 : g == 1 ? a1 : g == 2 ? a2 : a3;
+      };
       auto stats_of = [&](const fast2::Pop& p0, const fast2::Pop& p1, float2 (&st)[S]) {
         if constexpr (P == 1) fast2::stats1(p0, T4, st);
         else fast2::stats2(p0, p1, T4, st);
@@ -687,10 +710,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int s = 0; s < S; ++s) acc_lo[s] = acc_hi[s] = 0.f;
         int n_hi = 0;
         steps([&](int hh, int g, const fast2::Pop& p0, const fast2::Pop& p1) {
-          const long long ja = jx_of(g);
           const int ipi = hh ? ipos_b1 : ipos_b0;
-          const bool up0 = (a.ipos[ja] - ipi) >= thr_mid;
-          const bool up1 = (a.ipos[ja + 1] - ipi) >= thr_mid;
+          const bool up0 = (jpos(g, 0) - ipi) >= thr_mid;
+          const bool up1 = (jpos(g, 1) - ipi) >= thr_mid;
           const float2 fu = make_float2(up0 ? 1.f : 0.f, up1 ? 1.f : 0.f);
           const float2 fl = make_float2(up0 ? 0.f : 1.f, up1 ? 0.f : 1.f);
           n_hi += (up0 ? 1 : 0) + (up1 ? 1 : 0);
@@ -735,10 +757,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           n_lo = n_hi = 0;
           key = -1;
         };
-        auto bin_of = [&](long long is, int ipi, long long j) -> int {
+        auto bin_of = [&](long long is, int ipi, long long j, int jp) -> int {
           if (!(is < j && j < a.n_snp)) return -1;
           if (use_int) {
-            const int d = a.ipos[j] - ipi;
+            const int d = jp - ipi;
             return d <= maxd_int ? bin_of_int(thr, n_bins, d) : -1;
           }
           const double dp = a.pos[j] - a.pos[is];
@@ -750,7 +772,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const long long jx = jx_of(g);
           const long long is = ib + 8 * hh;
           const int ipi = hh ? ipos_b1 : ipos_b0;
-          const int bx = bin_of(is, ipi, jx), by = bin_of(is, ipi, jx + 1);
+          const int bx = bin_of(is, ipi, jx, jpos(g, 0)), by = bin_of(is, ipi, jx + 1, jpos(g, 1));
           const int lo = min(bx < 0 ? 0x7fffffff : bx, by < 0 ? 0x7fffffff : by);
           const int mn = __reduce_min_sync(0xffffffffu, lo);
           const int mx = __reduce_max_sync(0xffffffffu, max(bx, by));
