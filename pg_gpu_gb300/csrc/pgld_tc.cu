@@ -491,6 +491,21 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
 
+      // pairs mode: the band offsets of the thread's two rows, loaded before
+      // the accumulator wait
+      long long pf_off0 = 0, pf_np0 = 0, pf_off1 = 0, pf_np1 = 0;
+      if constexpr (MODE == kModePairs) {
+        const long long ibp = i0 + 16 * quarter + (lane >> 2);
+        if (ibp < a.n_snp) {
+          pf_off0 = a.pair_off[ibp];
+          pf_np0 = a.pair_off[ibp + 1] - pf_off0;
+        }
+        if (ibp + 8 < a.n_snp) {
+          pf_off1 = a.pair_off[ibp + 8];
+          pf_np1 = a.pair_off[ibp + 9] - pf_off1;
+        }
+      }
+
       bool ready = true;
       if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
       ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
@@ -571,10 +586,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // j = j0 + 32 half + 8 g + 2 (t % 4); rows k = pair_off[i] + (j - i - 1)
         // in the reference's order, two consecutive rows per thread
         const long long ib = i0 + 16 * quarter + (lane >> 2);
-        const long long off0 = ib < a.n_snp ? a.pair_off[ib] : 0;
-        const long long np0 = ib < a.n_snp ? a.pair_off[ib + 1] - off0 : 0;
-        const long long off1 = ib + 8 < a.n_snp ? a.pair_off[ib + 8] : 0;
-        const long long np1 = ib + 8 < a.n_snp ? a.pair_off[ib + 9] - off1 : 0;
+        const long long off0 = pf_off0, np0 = pf_np0, off1 = pf_off1, np1 = pf_np1;
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
           const int hh = c & 1, gp = c >> 1;
