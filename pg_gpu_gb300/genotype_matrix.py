@@ -157,8 +157,16 @@ class GenotypeMatrix:
         g[(a < 0) | (b < 0)] = -1
         if g.shape[1] == 0:
             raise ValueError(f"No biallelic variants found in {path}")
-        return cls(np.ascontiguousarray(g), pos, int(pos[0]), int(pos[-1]), samples=list(names),
-                   n_total_sites=g.shape[1] if include_invariant else None)
+        gm = cls(np.ascontiguousarray(g), pos, int(pos[0]), int(pos[-1]), samples=list(names),
+                 n_total_sites=g.shape[1] if include_invariant else None)
+        if accessible_bed is not None:
+            # variants at inaccessible positions are dropped (the reference
+            # masks them by the first record's chromosome)
+            from .accessible import accessible_variants
+            from .haplotype_matrix import vcf_first_chrom
+            keep = accessible_variants(pos, accessible_bed, vcf_first_chrom(path))
+            gm = gm.get_subset(np.nonzero(keep)[0])
+        return gm
 
     def load_pop_file(self, pop_file, pops=None):
         """Population sample sets from a sample / pop file (genotype_matrix.py:475-504)."""

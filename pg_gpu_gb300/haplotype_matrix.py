@@ -55,6 +55,18 @@ def _vcf_region(data, region):
     return b"\n".join(keep)
 
 
+def vcf_first_chrom(path):
+    """CHROM of the first data record of a plain or gzipped VCF (or None)."""
+    with open(path, "rb") as f:
+        gz = f.read(2) == b"\x1f\x8b"
+    opener = gzip.open if gz else open
+    with opener(path, "rb") as f:
+        for line in f:
+            if not line.startswith(b"#") and line.strip():
+                return line.split(b"\t", 1)[0].decode()
+    return None
+
+
 def _vcf_sample_names(data):
     """Sample names of the #CHROM header line."""
     i = data.find(b"#CHROM")
@@ -250,8 +262,16 @@ class HaplotypeMatrix:
             _, lo, hi = _parse_region(region)
             start = lo if lo is not None else start
             end = hi if hi is not None else end
-        return cls(hap, pos, start, end, samples=names,
-                   n_total_sites=len(pos) if include_invariant else None)
+        hm = cls(hap, pos, start, end, samples=names,
+                 n_total_sites=len(pos) if include_invariant else None)
+        if accessible_bed is not None:
+            # variants at inaccessible positions are dropped (the reference
+            # hides them behind a mask of the region's chromosome)
+            from .accessible import accessible_variants
+            chrom = _parse_region(region)[0] if region is not None else vcf_first_chrom(path)
+            keep = accessible_variants(pos, accessible_bed, chrom or None)
+            hm = hm.get_subset(np.nonzero(keep)[0])
+        return hm
 
     def load_pop_file(self, pop_file, pops=None):
         """Sample sets from a sample / pop file; sample i owns haplotype rows i and

@@ -18,6 +18,17 @@ from .ld_pipeline import het_names as _het_names
 from .ld_pipeline import ld_names as _ld_names
 
 
+def _accessible(mat, accessible_bed):
+    """The variants at accessible positions of the BED file (all of its
+    chromosomes, as the reference's set_accessible_mask(path) without a
+    chromosome; moments_ld.py:136-137, 159-160)."""
+    if accessible_bed is None:
+        return mat
+    from .accessible import accessible_variants
+    keep = accessible_variants(mat._pos_np(), accessible_bed)
+    return mat.get_subset(np.nonzero(keep)[0])
+
+
 def compute_ld_statistics(vcf_file=None, rec_map_file=None, pop_file=None, pops=None,
                           r_bins=None, bp_bins=None, use_genotypes=False, report=True,
                           ac_filter=True, haplotype_matrix=None, genotype_matrix=None,
@@ -31,8 +42,6 @@ def compute_ld_statistics(vcf_file=None, rec_map_file=None, pop_file=None, pops=
         raise ValueError("1-4 populations supported")
     if r_bins is None and bp_bins is None:
         raise ValueError("Either r_bins or bp_bins must be provided")
-    if accessible_bed is not None:
-        raise NotImplementedError("accessible_bed masks are outside the LD library")
 
     if use_genotypes:
         if genotype_matrix is not None:
@@ -50,6 +59,7 @@ def compute_ld_statistics(vcf_file=None, rec_map_file=None, pop_file=None, pops=
             mat.load_pop_file(pop_file, pops=pops)
             if ac_filter:
                 mat = mat.apply_biallelic_filter()
+        mat = _accessible(mat, accessible_bed)
         mat.transfer_to_gpu()
         if report:
             print(f"  {mat.num_individuals} individuals, {mat.num_variants:,} variants")
@@ -67,6 +77,7 @@ def compute_ld_statistics(vcf_file=None, rec_map_file=None, pop_file=None, pops=
             mat.load_pop_file(pop_file, pops=pops)
             if ac_filter:
                 mat = mat.apply_biallelic_filter()
+        mat = _accessible(mat, accessible_bed)
         mat.transfer_to_gpu()
         if report:
             print(f"  {mat.num_haplotypes} hap, {mat.num_variants:,} variants")

@@ -206,6 +206,27 @@ def test_moments_ld_genotype_and_haplotype_paths(golden):
     np.testing.assert_allclose(res_g["sums"][-1], [het[h] for h in res_g["stats"][1]], rtol=1e-12)
 
 
+def test_moments_ld_accessible_bed(golden, tmp_path):
+    # accessible_bed: the variants outside the BED intervals are dropped
+    # before the statistics (moments_ld.py:99-101, 159-160)
+    z = golden("moments_im")
+    sets = {"deme0": list(map(int, z["rows0"])), "deme1": list(map(int, z["rows1"]))}
+    pos = z["pos"]
+    lo, hi = int(pos[len(pos) // 4]), int(pos[3 * len(pos) // 4])
+    bed = tmp_path / "acc.bed"
+    bed.write_text(f"1\t{lo}\t{hi}\n")
+    hm = HaplotypeMatrix(z["hap"], pos, sample_sets=sets)
+    res = moments_ld.compute_ld_statistics(haplotype_matrix=hm, pops=["deme0", "deme1"],
+                                           bp_bins=z["bins"], report=False,
+                                           accessible_bed=str(bed))
+    inside = np.nonzero((pos > lo) & (pos <= hi))[0]
+    ref = moments_ld.compute_ld_statistics(
+        haplotype_matrix=HaplotypeMatrix(z["hap"][:, inside], pos[inside], sample_sets=sets),
+        pops=["deme0", "deme1"], bp_bins=z["bins"], report=False)
+    np.testing.assert_array_equal(np.array(res["sums"][:-1]), np.array(ref["sums"][:-1]))
+    np.testing.assert_allclose(res["sums"][-1], ref["sums"][-1], rtol=1e-12)
+
+
 def test_edge_cases_and_errors():
     c, nv = ld_pipeline.compute_genotype_counts_for_pairs(np.zeros((4, 1), np.int8),
                                                           np.zeros(0, np.int32),

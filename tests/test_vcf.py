@@ -155,3 +155,50 @@ def test_genotype_from_vcf_matches_oracle(tmp_path):
     assert np.array_equal(np.asarray(gm.genotypes), ref_g)
     assert np.array_equal(np.asarray(gm.positions), ref_pos)
     assert list(ref_pos) == [100, 250, 300, 50, 80]   # 1000 (alleles 2..), 60, 70 dropped
+
+
+def _accessible_loop(pos, intervals, chrom=None):
+    """Direct restatement of the reference's BED mask (accessible.py:167-197):
+    (start, end) covers the 1-based positions start + 1 .. end."""
+    out = []
+    for p in pos:
+        out.append(any(s + 1 <= p <= e for c, s, e in intervals if chrom is None or c == chrom))
+    return np.array(out, bool)
+
+
+def test_accessible_filter_matches_loop(tmp_path):
+    from pg_gpu_gb300 import accessible as A
+    rng = np.random.default_rng(3)
+    bed = tmp_path / "acc.bed"
+    iv = []
+    for c in ("chr1", "chr2"):
+        starts = np.sort(rng.choice(10_000, 40, replace=False))
+        for s in starts:
+            iv.append((c, int(s), int(s + rng.integers(0, 300))))
+    with open(bed, "w") as f:
+        f.write("track name=acc\n# comment\n")
+        for c, s, e in iv:
+            f.write(f"{c}\t{s}\t{e}\textra\n")
+    assert A.parse_bed(str(bed)) == iv
+    pos = np.sort(rng.choice(np.arange(1, 10_500), 2_000, replace=False))
+    for chrom in (None, "chr1", "chr2", "chr9"):
+        assert np.array_equal(A.accessible_variants(pos, str(bed), chrom),
+                              _accessible_loop(pos, iv, chrom))
+
+
+def test_from_vcf_accessible_bed(tmp_path):
+    from pg_gpu_gb300 import GenotypeMatrix, HaplotypeMatrix
+    names, text = _edge_text()
+    p = tmp_path / "e.vcf"
+    p.write_text(text)
+    bed = tmp_path / "a.bed"
+    bed.write_text("chr1\t99\t100\nchr1\t299\t1000\nchr2\t0\t60\n")
+    hm = HaplotypeMatrix.from_vcf(str(p), accessible_bed=str(bed))
+    # the mask is built from the intervals of the first record's chromosome
+    # (chr1): POS 100, 300 and 1000 are accessible, 250 is not, and the chr2
+    # record at POS 50 is not covered by a chr1 interval
+    assert list(np.asarray(hm.positions)) == [100, 300, 1000]
+    gm = GenotypeMatrix.from_vcf(str(p), accessible_bed=str(bed))
+    assert list(np.asarray(gm.positions)) == [100, 300]  # 1000 is multi-allelic
+    hm = HaplotypeMatrix.from_vcf(str(p), region="chr2", accessible_bed=str(bed))
+    assert list(np.asarray(hm.positions)) == [50]
