@@ -1292,3 +1292,53 @@ def vcf_dosages(text):
     g = gt.sum(axis=2).astype(np.int8)
     g[(gt < 0).any(axis=2)] = -1
     return names, g.T.copy(), pos[keep]
+
+
+# ---------------------------------------------------------------------------
+# mu_LD  (ld_statistics.py:865-918, diversity.py:1310-1360)
+# ---------------------------------------------------------------------------
+def cluster_haplotypes(h):
+    """Greedy clustering with -1 as a wildcard: each haplotype joins the first
+    cluster whose representative (its first member) it matches at every site
+    where both are called; without missing data, identical rows."""
+    h = np.asarray(h)
+    n = h.shape[0]
+    if not np.any(h < 0):
+        seen, labels = {}, []
+        for row in h:
+            key = row.tobytes()
+            labels.append(seen.setdefault(key, len(seen)))
+        return labels
+    reps, labels = [0], [0]
+    for i in range(1, n):
+        for c, r in enumerate(reps):
+            both = (h[i] >= 0) & (h[r] >= 0)
+            if np.all(h[i][both] == h[r][both]):
+                labels.append(c)
+                break
+        else:
+            reps.append(i)
+            labels.append(len(reps) - 1)
+    return labels
+
+
+def mu_ld(hap, missing_data="include"):
+    """Exclusivity of the haplotype patterns of the left and right halves of
+    the variants (RAiSD's mu_LD)."""
+    h = np.asarray(hap)
+    if missing_data == "exclude":
+        h = h[:, ~np.any(h < 0, axis=0)]
+    if h.shape[1] < 2:
+        return 0.0
+    mid = h.shape[1] // 2
+    lab_l = cluster_haplotypes(h[:, :mid])
+    lab_r = cluster_haplotypes(h[:, mid:])
+    l2r, r2l = {}, {}
+    for a, b in zip(lab_l, lab_r):
+        l2r.setdefault(a, set()).add(b)
+        r2l.setdefault(b, set()).add(a)
+    if not l2r or not r2l:
+        return 0.0
+    el = sum(1 for v in l2r.values() if len(v) == 1)
+    er = sum(1 for v in r2l.values() if len(v) == 1)
+    return float((el / len(l2r) + er / len(r2l)) / 2.0)

@@ -17,7 +17,7 @@ from . import _lib as L
 from . import _ops
 from .ld_pipeline import case_of
 
-__all__ = ["dd", "dz", "pi2", "dd_within", "dd_between", "r", "r_squared", "d_prime",
+__all__ = ["mu_ld", "dd", "dz", "pi2", "dd_within", "dd_between", "r", "r_squared", "d_prime",
            "compute_ld_statistics", "rogers_huff_r", "rogers_huff_r_squared", "zns",
            "windowed_zns", "omega", "windowed_omega", "zns_diploid", "omega_diploid"]
 
@@ -266,6 +266,56 @@ def zns(r2_matrix_or_matrix, missing_data="include", estimator="auto"):
 # --------------------------------------------------------------------------
 # diploid dosage r^2 of a GenotypeMatrix (ld_statistics.py:973-1020)
 # --------------------------------------------------------------------------
+def _cluster_labels(h):
+    """Cluster labels of the rows of an int8 host matrix: identical rows
+    without missing data; with missing data each row joins the first cluster
+    whose representative (first member) matches it wherever both are called
+    (diversity.py:1310-1360), compared against all representatives at once."""
+    if not np.any(h < 0):
+        _, inv = np.unique(h, axis=0, return_inverse=True)
+        return inv.reshape(-1)
+    n = h.shape[0]
+    reps = np.empty((n, h.shape[1]), dtype=h.dtype)
+    reps[0] = h[0]
+    k = 1
+    labels = np.zeros(n, dtype=np.int64)
+    for i in range(1, n):
+        r = reps[:k]
+        ok = np.all((r == h[i]) | (r < 0) | (h[i] < 0), axis=1)
+        j = int(np.argmax(ok)) if ok.any() else -1
+        if j < 0:
+            reps[k] = h[i]
+            labels[i] = k
+            k += 1
+        else:
+            labels[i] = j
+    return labels
+
+
+def mu_ld(haplotype_matrix, missing_data="include"):
+    """mu_LD: how exclusively the haplotype patterns of the left half of the
+    variants pair with those of the right half (RAiSD; ld_statistics.py:
+    865-918).  A host computation over the haplotype patterns, as in the
+    reference."""
+    h = haplotype_matrix.haplotypes
+    h = np.asarray(h.cpu().numpy() if hasattr(h, "cpu") else h).astype(np.int8, copy=False)
+    if missing_data == "exclude":
+        h = h[:, ~np.any(h < 0, axis=0)]
+    n_hap, n_var = h.shape
+    if n_var < 2:
+        return 0.0
+    mid = n_var // 2
+    left = _cluster_labels(np.ascontiguousarray(h[:, :mid]))
+    right = _cluster_labels(np.ascontiguousarray(h[:, mid:]))
+    pairs = np.unique(np.stack([left, right], axis=1), axis=0)
+    if pairs.size == 0:
+        return 0.0
+    # a left pattern is exclusive when it pairs with one right pattern only
+    _, n_right_per_left = np.unique(pairs[:, 0], return_counts=True)
+    _, n_left_per_right = np.unique(pairs[:, 1], return_counts=True)
+    return float((np.mean(n_right_per_left == 1) + np.mean(n_left_per_right == 1)) / 2.0)
+
+
 def _is_genotype_matrix(x):
     from .genotype_matrix import GenotypeMatrix
     return isinstance(x, GenotypeMatrix)

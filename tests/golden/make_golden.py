@@ -23,6 +23,8 @@ host C++), or read from data the reference ships:
   rows of im_pop.txt, and the moments binned sums cached by the reference in
   tests/cache/moments_ld_test_im_4bins_deme0-deme1.pkl (read with a
   restricted unpickler that only accepts numpy array reconstruction).
+* ``mu_ld.npz``       -- ld_statistics.mu_ld (ld_statistics.py:865-918) with
+  the reference's haplotype clustering (diversity.py:1310-1360).
 * ``geno.npz``        -- 9-way genotype counts from the reference counting
   kernel (ld_pipeline.py:183-217), single-population genotype DD from
   _DD_GENO_SINGLE_KERN (genotype_kernels.py:27-71), sigma_D^2 from
@@ -442,6 +444,39 @@ def gen_diploid_ld(M):
     np.savez_compressed(os.path.join(HERE, "diploid_ld.npz"), **out)
 
 
+def gen_mu_ld(M):
+    """mu_LD (ld_statistics.mu_ld, ld_statistics.py:865-918) from the
+    reference, with its haplotype clustering (diversity.py:1310-1360, loaded
+    through the shim): matrices without missing data, with missing data (the
+    wildcard clustering), missing_data 'exclude', and one- / two-variant
+    edges."""
+    import importlib.util
+    ls = M["ld_statistics"]
+    HM = S.load_haplotype_matrix()
+    pkg = sys.modules["pg_gpu"]
+    for mod in ("_utils", "diversity"):
+        if hasattr(pkg, mod):
+            continue
+        path = os.path.join(S.REF_ROOT, "pg_gpu", mod + ".py")
+        spec = importlib.util.spec_from_file_location("pg_gpu." + mod, path)
+        m = importlib.util.module_from_spec(spec)
+        sys.modules["pg_gpu." + mod] = m
+        spec.loader.exec_module(m)
+        setattr(pkg, mod, m)
+    out = {}
+    cases = [(40, 30, 4, 0.05, 0.0), (64, 51, 6, 0.02, 0.0), (50, 40, 3, 0.1, 0.04),
+             (32, 25, 5, 0.05, 0.1), (20, 1, 2, 0.0, 0.0), (20, 2, 2, 0.5, 0.0),
+             (200, 120, 10, 0.01, 0.01)]
+    for k, (H, m, F, sw, miss) in enumerate(cases):
+        rng = np.random.default_rng(20261220 + k)
+        hap = copying_model(rng, H, m, F, sw, missing=miss)
+        pos = np.arange(1, m + 1, dtype=np.int64) * 100
+        out[f"hap{k}"] = hap
+        out[f"mu_{k}"] = ls.mu_ld(HM(hap.copy(), pos.copy()))
+        out[f"mu_excl_{k}"] = ls.mu_ld(HM(hap.copy(), pos.copy()), missing_data="exclude")
+    np.savez_compressed(os.path.join(HERE, "mu_ld.npz"), **out)
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -455,6 +490,7 @@ def main():
     gen_omega(M)
     gen_unlinked(M)
     gen_diploid_ld(M)
+    gen_mu_ld(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

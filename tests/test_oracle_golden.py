@@ -264,3 +264,23 @@ def test_diploid_zns_omega_match_reference(golden):
                                    atol=1e-15)
         np.testing.assert_allclose(O.omega_diploid(g, "exclude"), z[f"omega_excl_{k}"],
                                    rtol=1e-12)
+
+
+def test_mu_ld_matches_reference(golden):
+    """mu_LD (ld_statistics.py:865-918) of the reference, with and without
+    missing data and with missing_data='exclude': oracle and package."""
+    from pg_gpu_gb300 import ld_statistics as LS
+    from pg_gpu_gb300.haplotype_matrix import HaplotypeMatrix
+    z = golden("mu_ld")
+    k = 0
+    while f"hap{k}" in z.files:
+        hap = z[f"hap{k}"]
+        pos = np.arange(1, hap.shape[1] + 1, dtype=np.int64) * 100
+        assert O.mu_ld(hap) == pytest.approx(float(z[f"mu_{k}"]), abs=1e-15)
+        assert O.mu_ld(hap, "exclude") == pytest.approx(float(z[f"mu_excl_{k}"]), abs=1e-15)
+        hm = HaplotypeMatrix(hap.copy(), pos)
+        assert LS.mu_ld(hm) == pytest.approx(float(z[f"mu_{k}"]), abs=1e-15)
+        assert LS.mu_ld(hm, missing_data="exclude") == pytest.approx(float(z[f"mu_excl_{k}"]),
+                                                                     abs=1e-15)
+        k += 1
+    assert k >= 7
