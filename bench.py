@@ -28,15 +28,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LD SNP-pairs/s at 2k haps, int8-TC vs plain popcount; % INT8 TC peak; 1×GB300"
 
+from pg_gpu_gb300 import synthetic  # noqa: E402
+
 WORKLOADS = {
     # two-population binned moments statistics (the headline)
-    "binned2pop": dict(pops=2, hap_per_pop=1000, n_snp=200_000, length=20_000_000, founders=40,
-                       switch=1e-3, pop_flip=0.10, flip=1e-3, missing=0.02,
-                       bins=np.logspace(3, 6, 21), seed=20261503),
+    "binned2pop": synthetic.BINNED2POP,
     # reduced size of the same workload, for profiling captures
-    "binned2pop_small": dict(pops=2, hap_per_pop=1000, n_snp=20_000, length=2_000_000,
-                             founders=40, switch=1e-3, pop_flip=0.10, flip=1e-3, missing=0.02,
-                             bins=np.logspace(3, 6, 21), seed=20261503),
+    "binned2pop_small": synthetic.BINNED2POP_SMALL,
 }
 
 
@@ -47,37 +45,9 @@ def rank_info():
     return r, w, lr
 
 
-# --------------------------------------------------------------------------
-# synthetic panel
-# --------------------------------------------------------------------------
 def make_panel(cfg, device):
     """int8 (2*H, M) panel on the device, sorted int64 positions (host)."""
-    import torch
-    rng = np.random.default_rng(cfg["seed"])
-    M, F, H = cfg["n_snp"], cfg["founders"], cfg["hap_per_pop"]
-    pos = np.sort(rng.choice(cfg["length"], M, replace=False)).astype(np.int64)
-    p = torch.as_tensor(rng.beta(0.3, 0.3, size=M), dtype=torch.float32, device=device)
-    g = torch.Generator(device=device)
-    g.manual_seed(cfg["seed"])
-    founders = (torch.rand((F, M), generator=g, device=device) < p).to(torch.int8)
-    pops = []
-    for _ in range(cfg["pops"]):
-        fp = founders ^ (torch.rand((F, M), generator=g, device=device) < cfg["pop_flip"]).to(torch.int8)
-        sw = torch.rand((H, M), generator=g, device=device) < cfg["switch"]
-        seg = torch.cumsum(sw, dim=1, dtype=torch.int32)
-        del sw
-        choice = torch.randint(0, F, (H, int(seg.max()) + 1), generator=g, device=device,
-                               dtype=torch.int64)
-        idx = torch.gather(choice, 1, seg.to(torch.int64))
-        del seg, choice
-        hap = torch.gather(fp, 0, idx)
-        del idx
-        hap ^= (torch.rand((H, M), generator=g, device=device) < cfg["flip"]).to(torch.int8)
-        hap[torch.rand((H, M), generator=g, device=device) < cfg["missing"]] = -1
-        pops.append(hap)
-    panel = torch.cat(pops, 0).contiguous()
-    torch.cuda.synchronize()
-    return panel, pos
+    return synthetic.shared_founder_panel(cfg, device)
 
 
 # --------------------------------------------------------------------------
@@ -151,16 +121,119 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def tc_roofline(pairs_per_s, ops_per_pair, basis):
+# --------------------------------------------------------------------------
+# the tensor-pipe peak: tcgen05 E4M3 MMA throughput measured on this device
+# --------------------------------------------------------------------------
+_PEAK = {}
+
+
+def tc_mma_peak(gpu_index, launch_ms=20.0, sustained_s=3.0):
+    """E4M3 tcgen05.mma (M = 128, N = 128, K = 32) rate of this GPU, TFLOP/s:
+    every SM issues MMAs back to back from operands resident in shared memory
+    (pgld_tc_mma_rate), in launches of about launch_ms; "burst" = ten
+    launches, "sustained" = sustained_s seconds of them, each with the SM
+    clocks sampled while it ran.  Measured once per process."""
+    if "burst" in _PEAK:
+        return _PEAK
+    import ctypes
+    from pg_gpu_gb300 import _lib as L
+    h = L.handle()
+    ms, fl = ctypes.c_float(), ctypes.c_double()
+
+    def run(n_cols, mmas, launches):
+        L.check(L.lib().pgld_tc_mma_rate(h, n_cols, int(mmas), int(launches), ctypes.byref(ms),
+                                         ctypes.byref(fl), L.stream_ptr()), h)
+        return fl.value / (ms.value / 1e3) / 1e12, ms.value
+
+    run(128, 1 << 16, 3)
+    _, m = run(128, 1 << 18, 1)
+    mmas = int(min(1 << 24, max(1 << 12, (1 << 18) * launch_ms / max(m, 1e-3))))
+    run(128, mmas, 3)
+    with ClockSampler(gpu_index) as c1:
+        burst, bms = run(128, mmas, 10)
+    with ClockSampler(gpu_index) as c2:
+        sust, sms = run(128, mmas, max(10, int(sustained_s * 1e3 / launch_ms)))
+    n256, _ = run(256, mmas // 2, 10)
+    _PEAK.update({"burst": burst, "burst_clocks": c1.summary(), "sustained": sust,
+                  "sustained_clocks": c2.summary(), "n256_burst": n256,
+                  "mmas_per_sm_per_launch": mmas, "launch_ms": bms / 10})
+    return _PEAK
+
+
+def tc_roofline(pairs_per_s, ops_per_pair, basis, gpu_index=0, sm_mhz=None):
     """Tensor-pipe roofline of a tensor-core workload: ops_per_pair int8-
-    equivalent operations per pair (the algorithmic contraction), against 2 x
-    the measured bf16 dense rate (the E4M3 rate); basis names the timed region."""
-    peaks, src = measured_peaks()
-    peak = 2.0 * float(peaks["bf16_tflops"])
+    equivalent operations per pair (the algorithmic contraction) per second,
+    against the measured E4M3 tcgen05 burst rate of this GPU; basis names the
+    timed region.  frac_clock_normalised divides each rate by the median SM
+    clock it ran at."""
+    pk = tc_mma_peak(gpu_index)
+    peak = pk["burst"]
     achieved = pairs_per_s * ops_per_pair / 1e12
-    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None, "ops_per_pair": ops_per_pair,
-            "peak_source": f"2 x {src} bf16_tflops (dense fp8 rate)", "timed": basis}
+    out = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+           "frac": achieved / peak, "traffic": None, "ops_per_pair": ops_per_pair,
+           "peak_source": "measured on this GPU: tcgen05 kind::f8f6f4 M128 N128 K32 from "
+                          "shared memory on every SM (pgld_tc_mma_rate), burst of ten ~20 ms "
+                          "launches",
+           "peak_sm_mhz": pk["burst_clocks"].get("sm_mhz"),
+           "peak_sustained": pk["sustained"],
+           "peak_sustained_sm_mhz": pk["sustained_clocks"].get("sm_mhz"),
+           "timed": basis}
+    pm = pk["burst_clocks"].get("sm_mhz")
+    if sm_mhz and pm:
+        out["frac_clock_normalised"] = (achieved / sm_mhz) / (peak / pm)
+    return out
+
+
+def kernel_times(enable):
+    """Turn per-launch timing of the library's dominant kernels on (and clear
+    it) or read and clear the times (ms) timed since."""
+    import ctypes
+    from pg_gpu_gb300 import _lib as L
+    h = L.handle()
+    if enable:
+        L.check(L.lib().pgld_set_kernel_timing(h, 1), h)
+        return []
+    buf = (ctypes.c_float * 4096)()
+    n = ctypes.c_int32()
+    L.check(L.lib().pgld_kernel_times(h, buf, 4096, ctypes.byref(n)), h)
+    L.check(L.lib().pgld_set_kernel_timing(h, 0), h)
+    return [float(buf[k]) for k in range(min(n.value, 4096))]
+
+
+# --------------------------------------------------------------------------
+# parity of the timed configuration: one anchor block against the oracle
+# --------------------------------------------------------------------------
+def _oracle_block(args):
+    hap, pos, rows, bins, n_anchor = args
+    from oracle import ld_oracle as O
+    sums, cnt, asum = O.binned_sums(hap, pos, rows, bins, abs_sums=True, anchor_stop=n_anchor,
+                                    pair_block=100_000)
+    return sums, cnt, asum
+
+
+def parity_block(pool, panel, pos, cfg, pops, pos_d, form, first, n_pairs):
+    """The binned sums of the pairs anchored in one block of the panel (from
+    SNP `first`, about n_pairs pairs), this library against the oracle: exact
+    pair counts, and the largest error of every statistic relative to its bin
+    value and to the bin's sum of |x|."""
+    from pg_gpu_gb300 import _ops
+    bins = cfg["bins"]
+    md = float(bins[-1])
+    a1, npairs = synthetic.anchors_per_pairs(pos, md, first, n_pairs)
+    sums, cnt = _ops.binned_sums(pops, pos_d, bins, form=form, anchors=(first, a1))
+    halo = int(np.searchsorted(pos, pos[a1 - 1] + md, side="right"))
+    H = cfg["hap_per_pop"]
+    rows = [np.arange(q * H, (q + 1) * H) for q in range(cfg["pops"])]
+    args = (panel[:, first:halo].cpu().numpy(), pos[first:halo], rows, bins, a1 - first)
+    ref, ref_cnt, ref_abs = pool.apply(_oracle_block, (args,)) if pool else _oracle_block(args)
+    got = sums.cpu().numpy()
+    err = np.abs(got - ref)
+    nz = np.abs(ref) > 0
+    rel = np.where(nz, err / np.where(nz, np.abs(ref), 1.0), 0.0)
+    return {"anchors": [int(first), int(a1)], "pairs": int(npairs),
+            "counts_equal": bool(np.array_equal(cnt.cpu().numpy(), ref_cnt)),
+            "max_rel_err_of_value_by_stat": [float(x) for x in rel.max(axis=0)],
+            "max_err_of_sum_abs": float((err / np.maximum(ref_abs, 1e-300)).max())}
 
 
 def profile_traffic(form, workload):
@@ -279,10 +352,14 @@ def run_gpu(args, pool, cores):
         step()
     torch.cuda.synchronize()
 
-    # correctness guard on the timed configuration: pair counts per bin
-    _, cnt = step()
-    d = np.diff(bins)
-    assert int(cnt.sum()) <= n_pairs
+    # parity of the timed configuration (outside the timed region): the pairs
+    # anchored in one block in the middle of the chromosome against the oracle
+    parity = None
+    if rank == 0 and not args.no_parity:
+        packs = [_ops.pack(panel, r) for r in rows]
+        parity = parity_block(pool, panel, pos, cfg, packs, pos_d, args.form,
+                              len(pos) // 2, args.parity_pairs)
+        del packs
 
     # ---- timed region: device-resident inputs ----
     def timed(form):
@@ -296,6 +373,7 @@ def run_gpu(args, pool, cores):
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
+        kernel_times(True)
         with ClockSampler(lrank) as clk:
             for s in range(args.steps):
                 flush.fill_(s & 0x7F)  # L2 flush between steps (outside the events)
@@ -307,7 +385,11 @@ def run_gpu(args, pool, cores):
                 ev[s][1].record(stream)
             torch.cuda.synchronize()
         step_ms = [a.elapsed_time(b) for a, b in ev]
-        kern_ms = [a.elapsed_time(b) for a, b in kev]
+        # the binned-sum call (operand expansion, work list, band kernel) and,
+        # timed inside the library on the same stream, the band kernel alone
+        call_ms = [a.elapsed_time(b) for a, b in kev]
+        band_ms = kernel_times(False)
+        kern_ms = (call_ms, band_ms)
         total = sum(step_ms) / 1e3
         if world > 1:
             t = torch.tensor([total], device=dev, dtype=torch.float64)
@@ -321,7 +403,8 @@ def run_gpu(args, pool, cores):
         other = "plain" if args.form == "tc" else "tc"
         v2, s2, k2, c2 = timed(other)
         compare = {"form": other, "value": v2, "unit": "pairs/s",
-                   "ms_per_step": float(np.mean(s2)), "kernel_ms": float(np.mean(k2)),
+                   "ms_per_step": float(np.mean(s2)), "call_ms": float(np.mean(k2[0])),
+                   "band_kernel_ms": float(np.mean(k2[1])) if k2[1] else None,
                    "clocks": c2.summary(), "ratio_this_over_other": value / v2}
 
     # ---- end to end through the public API, host buffers ----
@@ -348,30 +431,30 @@ def run_gpu(args, pool, cores):
     h2d = host.numel() * host.element_size() + pos.nbytes
     d2h = (len(bins) - 1) * (15 + 1) * 8
 
-    # ---- roofline of the binned-sum kernel ----
+    # ---- roofline of the band kernel (its launches timed on the call's stream) ----
     peaks, peak_src = measured_peaks()
-    k_s = float(np.mean(kern_ms)) / 1e3
+    call_ms, band_ms = kern_ms
+    k_s = float(np.mean(band_ms if band_ms else call_ms)) / 1e3
     W = (H + 31) // 32
     plane_bytes = cfg["n_snp"] * cfg["pops"] * 2 * W * 4
     traffic = profile_traffic(args.form, args.workload)
+    basis = ("band kernel launches, CUDA events on the call's stream" if band_ms else
+             "whole binned-sum call")
     if args.form == "plain":
         achieved = plane_bytes / k_s / 1e9
         peak = float(peaks.get("hbm_gbs", 6800.0))
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "peak_source": f"{peak_src} hbm_gbs",
+                "peak_source": f"{peak_src} hbm_gbs", "timed": basis,
                 "algorithmic_bytes_per_launch": plane_bytes,
                 "note": "the plain form is bound by the integer (AND/POPC) pipe, not HBM; "
                         "int_ops_per_launch / time is reported as int_tops"}
         roof["int_tops"] = n_pairs * cfg["pops"] * 4 * W * 3 / k_s / 1e12
     else:
-        ops = n_pairs * 8 * H * cfg["pops"]
-        achieved = ops / k_s / 1e12
-        peak = 2.0 * float(peaks.get("bf16_tflops", 1900.0))
-        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "peak_source": f"2 x {peak_src} bf16_tflops (dense fp8 rate)",
-                "algorithmic_ops_per_launch": ops}
+        ops_per_pair = 8 * H * cfg["pops"]
+        roof = tc_roofline(n_pairs / k_s, ops_per_pair, basis, lrank, clk.summary().get("sm_mhz"))
+        roof["traffic"] = traffic
+        roof["algorithmic_ops_per_launch"] = n_pairs * ops_per_pair
 
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
@@ -390,9 +473,15 @@ def run_gpu(args, pool, cores):
                 "api": "HaplotypeMatrix(host int8).compute_ld_statistics_gpu_two_pops(raw=True)"},
         # per step: one pack per population, then the binned call: (tc: one operand
         # expansion per population) + tile counts + 3 scan launches + the band kernel
-        "gpu_launches": args.steps * (cfg["pops"] * (2 if args.form == "tc" else 1) + 5),
-        "kernel_ms": float(np.mean(kern_ms)),
+        # per step: one pack per population, then the binned call: tile counts, 3 scan
+        # launches and the band kernel (tc: also one operand expansion per
+        # population and the integer-position copy)
+        "gpu_launches": args.steps * (cfg["pops"] * (2 if args.form == "tc" else 1) +
+                                      (6 if args.form == "tc" else 5)),
+        "call_ms": float(np.mean(call_ms)),
+        "kernel_ms": k_s * 1e3,
         "roofline": roof,
+        "parity": parity,
         "compare": compare,
     }
     if pool is not None and rank == 0:
@@ -445,20 +534,6 @@ def run_reference(args, pool, cores):
 # --------------------------------------------------------------------------
 # secondary workloads (measurement of the other paths; not the headline line)
 # --------------------------------------------------------------------------
-def _copying_panel(gen, H, M, F, switch, flip, missing, device):
-    import torch
-    p = torch.distributions.Beta(0.3, 0.3).sample((M,)).to(device)
-    founders = (torch.rand((F, M), generator=gen, device=device) < p).to(torch.int8)
-    sw = torch.rand((H, M), generator=gen, device=device) < switch
-    seg = torch.cumsum(sw, dim=1, dtype=torch.int32)
-    choice = torch.randint(0, F, (H, int(seg.max()) + 1), generator=gen, device=device)
-    hap = torch.gather(founders, 0, torch.gather(choice, 1, seg.to(torch.int64)))
-    hap ^= (torch.rand((H, M), generator=gen, device=device) < flip).to(torch.int8)
-    if missing:
-        hap[torch.rand((H, M), generator=gen, device=device) < missing] = -1
-    return hap
-
-
 def run_windows(args):
     """Batched uneven windows: 400 haplotypes, 512 windows of log-uniform
     500..20,000 SNPs (own seed each), every within-window pair; one launch over
@@ -474,7 +549,7 @@ def run_windows(args):
     for w, m in enumerate(sizes):
         g = torch.Generator(device=dev)
         g.manual_seed(20261504 + w)
-        parts.append(_copying_panel(g, 400, int(m), 20, 1e-3, 1e-3, 0.0, dev))
+        parts.append(synthetic.copying_panel(g, 400, int(m), 20, 1e-3, 1e-3, 0.0, dev))
     panel = torch.cat(parts, 1).contiguous()
     del parts
     ends = np.cumsum(sizes)
@@ -542,7 +617,7 @@ def run_geno_band(args):
     g = torch.Generator(device=dev)
     g.manual_seed(20261505)
     M = args.geno_snps
-    hap = _copying_panel(g, 2000, M, 60, 5e-4, 1e-3, 0.0, dev)
+    hap = synthetic.copying_panel(g, 2000, M, 60, 5e-4, 1e-3, 0.0, dev)
     geno = (hap[0::2] + hap[1::2]).to(torch.int8)
     del hap
     geno[torch.rand(geno.shape, generator=g, device=dev) < 0.03] = -1
@@ -600,7 +675,7 @@ def run_hap_band(args):
     g = torch.Generator(device=dev)
     g.manual_seed(20261502)
     M = 100_000
-    hap = _copying_panel(g, 2000, M, 50, 5e-4, 1e-3, 0.02, dev)
+    hap = synthetic.copying_panel(g, 2000, M, 50, 5e-4, 1e-3, 0.02, dev)
     rng = np.random.default_rng(20261502)
     pos = np.sort(rng.choice(10_000_000, M, replace=False)).astype(np.int64)
     pos_d = _ops.positions_f64(pos)
@@ -653,6 +728,8 @@ def main():
     ap.add_argument("--geno-counts", action="store_true", help="also write the 9-way counts")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-pairs-per-worker", type=int, default=400_000)
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of one block")
+    ap.add_argument("--parity-pairs", type=int, default=200_000)
     args = ap.parse_args()
     rank, world, _ = rank_info()
     cores = host_cores()

@@ -70,8 +70,25 @@ int pgld_destroy(pgld_handle h);
 /* Message of the last failed call on h (h may be NULL: last failure of any
  * call on this host thread).  Valid until the next call on the thread. */
 const char* pgld_last_error(pgld_handle h);
-/* Reads and clears the device-side error word of h (synchronises). */
+/* Reads and clears the device-side error word of h (synchronises).  0: no
+ * error.  Kernels record the first failure of a launch and skip the rest of
+ * its work: 2001 / 3001 corrupt tile work list; 3002 - 3005 a bounded
+ * mbarrier wait of a tensor-core kernel expired (TMA producer, MMA issuer,
+ * epilogue) -- the launch drained its copies and MMAs, freed its tensor
+ * memory and returned, and the handle stays usable (PGLD_DEVICE_WAIT_EXPIRED
+ * tells these codes apart); 3100 - 3102 a window or SNP index outside its
+ * panel. */
 int pgld_device_status(pgld_handle h, int32_t* code_out, void* stream);
+#define PGLD_DEVICE_WAIT_EXPIRED(code) ((code) >= 3002 && (code) <= 3005)
+
+/* Test hook (no counterpart in the reference): kind PGLD_TEST_FAULT_NO_COPIES
+ * makes the next tensor-core band launch on h issue no operand copies and
+ * shortens its bounded waits to ~10 ms, so that the MMA issuer's wait for
+ * the first stage expires and the launch ends through its error path (a
+ * wait-expiry code in the device status word).  The hook faults and hangs
+ * nothing; it is cleared by that launch.  kind 0 clears it. */
+#define PGLD_TEST_FAULT_NO_COPIES 1
+int pgld_set_test_fault(pgld_handle h, int32_t kind);
 
 /* Pack rows of an int8 (n_rows_total x n_snp) haplotype matrix (row stride
  * ld bytes, values 1 / 0 / -1) into the bit planes above.  rows: device
@@ -229,6 +246,19 @@ int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, const doubl
                          int32_t n_bins, double* sums, int64_t* pair_counts, int32_t form,
                          void* stream);
 
+/* pgld_hap_binned_sums over the pairs (i, j) whose first SNP i lies in
+ * [anchor_begin, anchor_end) (0 <= anchor_begin <= anchor_end <= n_snp):
+ * one rank's share when the anchors are split across devices, each pair
+ * computed once.  The kernels read only the SNPs from anchor_begin up to the
+ * last partner within max_dist of anchor_end - 1, found on the device
+ * (synchronises unless anchor_end == n_snp).  The partition hook of the
+ * binned sums; the reference has no multi-device path (its counterpart is
+ * the single-device moments_ld._compute_ld_sums, moments_ld.py:248-343). */
+int pgld_hap_binned_sums_range(pgld_handle h, const pgld_hap_panel* panel, const double* pos,
+                               double max_dist, const double* bin_coord, const double* bins,
+                               int32_t n_bins, int64_t anchor_begin, int64_t anchor_end,
+                               double* sums, int64_t* pair_counts, int32_t form, void* stream);
+
 /* ----------------------------------------------------------------------
  * Genotype (unphased diploid dosage) path.
  *
@@ -368,6 +398,26 @@ int pgld_vcf_scan(const char* text, int64_t len, int32_t* n_samples, int64_t* n_
 int pgld_vcf_parse_gt(const char* text, int64_t len, int32_t n_samples, int64_t n_records,
                       const int32_t* sample_cols, int32_t n_sel, int8_t* hap, int64_t* pos);
 
+/* ----------------------------------------------------------------------
+ * Measurement (no counterpart in the reference, which publishes no kernel
+ * timings).
+ * ---------------------------------------------------------------------- */
+/* Turn per-launch timing of each call's dominant kernel (the band, window
+ * or tensor-core kernel) on or off for h; turning it on clears the list. */
+int pgld_set_kernel_timing(pgld_handle h, int32_t on);
+/* Device times (ms, CUDA events on the call's stream) of the dominant-kernel
+ * launches timed since the last read, oldest first: up to capacity written
+ * to ms_out, the number timed in *n_out; clears the list (synchronises). */
+int pgld_kernel_times(pgld_handle h, float* ms_out, int32_t capacity, int32_t* n_out);
+/* Throughput of the tensor-core instruction of the tcgen05 kernels: every
+ * SM issues mmas_per_sm E4M3 tcgen05.mma (M = 128, N = n_cols in {64, 128,
+ * 256}, K = 32, float32 accumulators) from operands resident in shared
+ * memory, `launches` times back to back.  *ms_out = elapsed device time,
+ * *flops_out = 2 * 128 * n_cols * 32 * mmas_per_sm * SMs * launches
+ * (synchronises). */
+int pgld_tc_mma_rate(pgld_handle h, int32_t n_cols, int64_t mmas_per_sm, int32_t launches,
+                     float* ms_out, double* flops_out, void* stream);
+
 /* pgld_hap_binned_sums for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers of this library cannot call
  * cudaMalloc: a host application that hands every byte of the device to its
@@ -389,6 +439,12 @@ int pgld_hap_binned_sums_noalloc(int device, const pgld_hap_panel* panel, const 
                                  double max_dist, const double* bin_coord, const double* bins,
                                  int32_t n_bins, double* sums, int64_t* pair_counts,
                                  void* stream);
+/* Device error word of the last allocation-free call on `device` (each call
+ * clears it first; 0 = no error, a nonzero code means the call met a corrupt
+ * work list and skipped that work), read and cleared through symbol copies,
+ * without an allocation.  Waits for the device's earlier work.  No
+ * counterpart in the reference. */
+int pgld_noalloc_status(int device, int32_t* code_out);
 
 #ifdef __cplusplus
 }

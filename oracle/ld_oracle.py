@@ -548,7 +548,8 @@ def bin_index(distances, bins):
 
 
 def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
-                pair_block=2_000_000, abs_sums=False, anchor_stop=None):
+                pair_block=2_000_000, abs_sums=False, anchor_stop=None, anchor_start=None,
+                missing_flags=None):
     """(n_bins, n_stats) float64 sums of the per-pair statistics, plus pair counts.
 
     ``pop_rows``: list of row-index arrays, one per population (1..4).
@@ -556,8 +557,11 @@ def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
     a genetic map in Morgans for the recombination-distance mode).
     With ``abs_sums`` the sums of |stat| are returned as a third value
     (the scale that bounds the float32 rounding of the GPU sums).
-    ``anchor_stop``: only the pairs whose first SNP lies below it (a sample of
-    a large panel's pairs).
+    ``anchor_start`` / ``anchor_stop``: only the pairs whose first SNP lies in
+    [anchor_start, anchor_stop) (a sample of a large panel's pairs, or one
+    rank's share).  ``missing_flags``: per population, whether its whole
+    panel holds a -1 (the reference's n_valid switch, ld_pipeline.py:158);
+    by default it is read from the SNPs the call looks at.
     """
     pos = np.asarray(positions)
     coord = pos.astype(np.float64) if coords is None else np.asarray(coords, np.float64)
@@ -566,20 +570,24 @@ def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
     P = len(pop_rows)
     if max_dist is None:
         max_dist = float(bins[-1])
-    if anchor_stop is not None:
-        jend = np.searchsorted(pos, pos[:anchor_stop] + max_dist, side="right")
-        pos = pos[:int(jend.max()) if anchor_stop > 0 else 0]
+    n = len(pos)
+    a0 = 0 if anchor_start is None else int(anchor_start)
+    a1 = n if anchor_stop is None else min(int(anchor_stop), n)
+    # the SNP slice [a0, halo): the anchors and their partners within max_dist
+    halo = int(np.searchsorted(pos, pos[a1 - 1] + max_dist, side="right")) if a1 > a0 else a0
+    pos = pos[a0:halo]
+    coord = coord[a0:halo]
     ii, jj = pairs_within_distance(pos, max_dist)
-    if anchor_stop is not None:
-        keep = ii < anchor_stop
-        ii, jj = ii[keep], jj[keep]
+    keep = ii < a1 - a0
+    ii, jj = ii[keep], jj[keep]
     specs = stat_specs(P)
     sums = np.zeros((n_bins, len(specs)))
     asums = np.zeros((n_bins, len(specs)))
     npairs = np.zeros(n_bins, np.int64)
     h = np.asarray(hap)
-    subs = [h[np.asarray(r), :] for r in pop_rows]
-    miss = [bool(np.any(s == -1)) for s in subs]
+    subs = [h[np.asarray(r), a0:halo] for r in pop_rows]
+    miss = ([bool(np.any(s == -1)) for s in subs] if missing_flags is None
+            else [bool(m) for m in missing_flags])
     for s0 in range(0, len(ii), pair_block):
         ci, cj = ii[s0:s0 + pair_block], jj[s0:s0 + pair_block]
         d = np.abs(coord[cj] - coord[ci]) if coords is not None else (coord[cj] - coord[ci])
@@ -602,6 +610,31 @@ def binned_sums(hap, positions, pop_rows, bins, coords=None, max_dist=None,
     if abs_sums:
         return sums, npairs, asums
     return sums, npairs
+
+
+def bin_errors(got, ref, ref_abs=None, floor=0.0):
+    """Errors of binned sums relative to the value: |got - ref| / max(|ref|,
+    floor * ref_abs) per bin and statistic (0 where that scale is 0 and the
+    sums agree, inf where it is 0 and they differ).  With floor > 0 a bin whose
+    terms cancel to below floor * sum|x| is measured against that share of
+    sum|x| (ref_abs, the oracle's sums of |x|) instead of its small value."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = np.abs(ref)
+    if floor and ref_abs is not None:
+        scale = np.maximum(scale, floor * np.asarray(ref_abs, np.float64))
+    err = np.abs(got - ref)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = np.where(scale > 0, err / np.where(scale > 0, scale, 1.0),
+                       np.where(err > 0, np.inf, 0.0))
+    return rel
+
+
+def binned_sums_task(args):
+    """binned_sums(*args[0], **args[1]) with abs_sums; a picklable task for a
+    process pool."""
+    a, kw = args
+    return binned_sums(*a, abs_sums=True, **kw)
 
 
 def heterozygosity(hap, pop_rows):

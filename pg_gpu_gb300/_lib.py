@@ -91,6 +91,8 @@ _SIGS = {
                             ctypes.c_int),
     "pgld_hap_binned_sums": ([_P, ctypes.POINTER(HapPanel), _P, _D, _P, _P, _I32, _P, _P, _I32,
                               _P], ctypes.c_int),
+    "pgld_hap_binned_sums_range": ([_P, ctypes.POINTER(HapPanel), _P, _D, _P, _P, _I32, _I64,
+                                    _I64, _P, _P, _I32, _P], ctypes.c_int),
     "pgld_pack_genotypes": ([_P, _P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
     "pgld_geno_counts_pairs": ([_P, _P, _P, _P, _I32, _I64, _P, _P, _I64, _P, _I64, _P, _P],
                                ctypes.c_int),
@@ -108,10 +110,16 @@ _SIGS = {
                              ctypes.c_int),
     "pgld_hap_binned_sums_noalloc": ([ctypes.c_int, ctypes.POINTER(HapPanel), _P, _D, _P, _P, _I32,
                                       _P, _P, _P], ctypes.c_int),
+    "pgld_noalloc_status": ([ctypes.c_int, ctypes.POINTER(_I32)], ctypes.c_int),
     "pgld_hap_window_snp_sums": ([_P, ctypes.POINTER(HapPanel), _P, _I64, _P, _P, _I32, _P, _I32,
                                   _P, _P, _I64, _P],
                                  ctypes.c_int),
     "pgld_prune_unlinked": ([_P, _P, _P, _I64, _I32, _I32, _D, _P], ctypes.c_int),
+    "pgld_set_kernel_timing": ([_P, _I32], ctypes.c_int),
+    "pgld_set_test_fault": ([_P, _I32], ctypes.c_int),
+    "pgld_kernel_times": ([_P, _P, _I32, ctypes.POINTER(_I32)], ctypes.c_int),
+    "pgld_tc_mma_rate": ([_P, _I32, _I64, _I32, ctypes.POINTER(ctypes.c_float),
+                          ctypes.POINTER(_D), _P], ctypes.c_int),
     "pgld_vcf_scan": ([_P, _I64, _P, _P], ctypes.c_int),
     "pgld_vcf_parse_gt": ([_P, _I64, _I32, _I64, _P, _I32, _P, _P], ctypes.c_int),
 }

@@ -391,11 +391,12 @@ def tc_applies(pops):
     return len(pops) <= 2 and all(pk.n_words <= 64 and pk.valid_for_n is None for pk in pops)
 
 
-def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto"):
+def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto", anchors=None):
     """(sums (n_bins, n_stats) float64 tensor, pair counts (n_bins,) int64).
 
     form: "tc" (tcgen05 tensor cores), "plain" (AND + popcount) or "auto"
-    (tensor cores whenever they apply)."""
+    (tensor cores whenever they apply).  anchors: optional (begin, end) --
+    only the pairs whose first SNP lies in [begin, end) are summed."""
     if form == "auto":
         form = "tc" if tc_applies(pops) else "plain"
     torch = _torch()
@@ -414,10 +415,16 @@ def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto"):
     md = float(bins_np[-1]) if max_dist is None else float(max_dist)
     bc = None if bin_coord is None else L.as_device(bin_coord, np.float64)
     h = L.handle()
-    L.check(L.lib().pgld_hap_binned_sums(h, ctypes.byref(panel(pops)), L.ptr(pos_d), md, L.ptr(bc),
-                                         L.ptr(bins_d), n_bins, L.ptr(sums), L.ptr(cnt),
-                                         L.FORM_TC if form == "tc" else L.FORM_PLAIN,
-                                         L.stream_ptr()), h)
+    fm = L.FORM_TC if form == "tc" else L.FORM_PLAIN
+    if anchors is None:
+        L.check(L.lib().pgld_hap_binned_sums(h, ctypes.byref(panel(pops)), L.ptr(pos_d), md,
+                                             L.ptr(bc), L.ptr(bins_d), n_bins, L.ptr(sums),
+                                             L.ptr(cnt), fm, L.stream_ptr()), h)
+    else:
+        a0, a1 = (int(v) for v in anchors)
+        L.check(L.lib().pgld_hap_binned_sums_range(h, ctypes.byref(panel(pops)), L.ptr(pos_d), md,
+                                                   L.ptr(bc), L.ptr(bins_d), n_bins, a0, a1,
+                                                   L.ptr(sums), L.ptr(cnt), fm, L.stream_ptr()), h)
     return sums, cnt
 
 

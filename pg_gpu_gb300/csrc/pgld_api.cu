@@ -54,6 +54,77 @@ int pgld_workspace(pgld_context* h, size_t bytes, void** out) {
   return PGLD_OK;
 }
 
+// at most this many timed launches are kept between two reads
+constexpr int kMaxTimedLaunches = 4096;
+
+void pgld_time_begin(pgld_context* h, cudaStream_t st) {
+  if (!h || !h->timing) return;
+  if (h->tev_used + 2 > 2 * kMaxTimedLaunches) {
+    h->tev_overflow = true;
+    return;
+  }
+  while ((int)h->tev.size() < h->tev_used + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      h->tev_overflow = true;
+      return;
+    }
+    h->tev.push_back(e);
+  }
+  cudaEventRecord(h->tev[h->tev_used], st);
+}
+
+void pgld_time_end(pgld_context* h, cudaStream_t st) {
+  if (!h || !h->timing || h->tev_overflow || h->tev_used + 2 > (int)h->tev.size()) return;
+  cudaEventRecord(h->tev[h->tev_used + 1], st);
+  h->tev_used += 2;
+}
+
+extern "C" int pgld_set_test_fault(pgld_handle h, int32_t kind) {
+  if (!h) return pgld_fail(nullptr, PGLD_ERR_INVALID_ARG, "pgld_set_test_fault: NULL handle");
+  if (kind != 0 && kind != PGLD_TEST_FAULT_NO_COPIES)
+    return pgld_fail(h, PGLD_ERR_INVALID_ARG, "pgld_set_test_fault: kind %d", kind);
+  h->test_fault = kind;
+  return PGLD_OK;
+}
+
+extern "C" int pgld_set_kernel_timing(pgld_handle h, int32_t on) {
+  if (!h) return pgld_fail(nullptr, PGLD_ERR_INVALID_ARG, "pgld_set_kernel_timing: NULL handle");
+  h->timing = on != 0;
+  h->tev_used = 0;
+  h->tev_overflow = false;
+  return PGLD_OK;
+}
+
+extern "C" int pgld_kernel_times(pgld_handle h, float* ms_out, int32_t capacity, int32_t* n_out) {
+  if (!h || !n_out || capacity < 0 || (capacity > 0 && !ms_out))
+    return pgld_fail(h, PGLD_ERR_INVALID_ARG, "pgld_kernel_times: bad arguments");
+  const int n = h->tev_used / 2;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(h->device);
+  int rc = PGLD_OK;
+  for (int k = 0; k < n && k < capacity; ++k) {
+    cudaError_t e = cudaEventSynchronize(h->tev[2 * k + 1]);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->tev[2 * k], h->tev[2 * k + 1]);
+    if (e != cudaSuccess) {
+      rc = pgld_cuda_fail(h, e, "pgld_kernel_times");
+      break;
+    }
+    ms_out[k] = ms;
+  }
+  cudaSetDevice(prev);
+  *n_out = n;
+  if (rc == PGLD_OK && h->tev_overflow)
+    rc = pgld_fail(h, PGLD_ERR_TOO_LARGE, "pgld_kernel_times: more than %d launches since the last read",
+                   kMaxTimedLaunches);
+  h->tev_used = 0;
+  h->tev_overflow = false;
+  return rc;
+}
+
 // ---------------------------------------------------------------------------
 // moments statistic table (ld_pipeline.py:357-457) as case terms
 // ---------------------------------------------------------------------------
@@ -320,6 +391,7 @@ extern "C" int pgld_destroy(pgld_handle h) {
   cudaDeviceSynchronize();
   if (h->ws) cudaFree(h->ws);
   if (h->dev_status) cudaFree(h->dev_status);
+  for (cudaEvent_t e : h->tev) cudaEventDestroy(e);
   for (int P = 0; P <= PGLD_MAX_POPS; ++P)
     if (h->spec_terms[P]) cudaFree(h->spec_terms[P]);
   for (int P = 0; P <= PGLD_MAX_POPS; ++P)

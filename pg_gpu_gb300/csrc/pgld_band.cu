@@ -114,6 +114,9 @@ __global__ void __launch_bounds__(kThreads) band_plain_kernel(BandArgs a) {
     if (threadIdx.x == 0 && a.status) atomicCAS(a.status, 0, 2001);
     n_items = 0;
   }
+  // binned mode over an anchor range: the row blocks holding anchors only
+  const i64 n_anchor = MODE == kModeBinned ? anchors_of(a) : a.n_snp;
+  if (n_items > 0 && n_anchor < a.n_snp) n_items = a.item_off[(n_anchor + kTile - 1) / kTile];
 
   for (i64 item = blockIdx.x; item < n_items; item += gridDim.x) {
     const i64 bi = item_block(a.item_off, a.n_blocks, item);
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(kThreads) band_plain_kernel(BandArgs a) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const i64 i = i0 + wid + 8 * q, j = j0 + lane;
-      bool ok = (i < j) && (j < a.n_snp);
+      bool ok = (i < j) && (j < a.n_snp) && (i < n_anchor);
       double dpos = 0.0;
       if (ok) {
         dpos = a.pos[j] - a.pos[i];
@@ -266,7 +269,9 @@ static int launch_p(pgld_context* h, const BandArgs& a, cudaStream_t st) {
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_plain occupancy");
   per_sm = std::max(1, per_sm);
   unsigned grid = (unsigned)(h->n_sm * per_sm);
+  pgld_time_begin(h, st);
   kern<<<grid, kThreads, smem, st>>>(a);
+  pgld_time_end(h, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_plain_kernel");
   return PGLD_OK;
@@ -377,27 +382,84 @@ extern "C" int pgld_hap_band_pairs(pgld_handle h, const pgld_hap_panel* panel, c
   return pgld::launch_band_plain(h, a, pgld::kModePairs, st);
 }
 
-extern "C" int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, const double* pos,
-                                    double max_dist, const double* bin_coord, const double* bins,
-                                    int32_t n_bins, double* sums, int64_t* pair_counts,
-                                    int32_t form, void* stream) {
-  PGLD_REQUIRE(h, h != nullptr, "pgld_hap_binned_sums: NULL handle");
-  int rc = check_panel(h, panel, "pgld_hap_binned_sums");
+namespace pgld {
+// one past the last SNP within max_dist of SNP last (positions sorted): the
+// halo of an anchor range ending at last + 1
+__global__ void halo_end_kernel(const double* __restrict__ pos, i64 n, i64 last, double max_dist,
+                                i64* __restrict__ out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const double lim = pos[last] + max_dist;
+  i64 lo = last + 1, hi = n;
+  while (lo < hi) {
+    const i64 mid = (lo + hi) >> 1;
+    if (pos[mid] <= lim) lo = mid + 1; else hi = mid;
+  }
+  *out = lo;
+}
+}  // namespace pgld
+
+// binned sums over the pairs (i, j) whose first SNP i lies in [a0, a1)
+static int binned_sums_range(pgld_context* h, const pgld_hap_panel* panel, const double* pos,
+                             double max_dist, const double* bin_coord, const double* bins,
+                             int32_t n_bins, i64 a0, i64 a1, double* sums, int64_t* pair_counts,
+                             int32_t form, void* stream, const char* fn) {
+  PGLD_REQUIRE(h, h != nullptr, "%s: NULL handle", fn);
+  int rc = check_panel(h, panel, fn);
   if (rc) return rc;
-  PGLD_REQUIRE(h, n_bins >= 1 && n_bins <= pgld::kMaxBins,
-               "pgld_hap_binned_sums: n_bins %d not in [1, %d]", n_bins, pgld::kMaxBins);
-  PGLD_REQUIRE(h, bins && sums, "pgld_hap_binned_sums: NULL bins/sums");
-  PGLD_REQUIRE(h, max_dist >= 0, "pgld_hap_binned_sums: negative max_dist");
-  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC, "pgld_hap_binned_sums: form");
+  PGLD_REQUIRE(h, n_bins >= 1 && n_bins <= pgld::kMaxBins, "%s: n_bins %d not in [1, %d]", fn,
+               n_bins, pgld::kMaxBins);
+  PGLD_REQUIRE(h, bins && sums, "%s: NULL bins/sums", fn);
+  PGLD_REQUIRE(h, max_dist >= 0, "%s: negative max_dist", fn);
+  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC, "%s: form", fn);
+  PGLD_REQUIRE(h, 0 <= a0 && a0 <= a1 && a1 <= panel->n_snp,
+               "%s: anchor range [%lld, %lld) outside [0, %lld)", fn, (long long)a0,
+               (long long)a1, (long long)panel->n_snp);
+  if (form == PGLD_FORM_TC && !pgld_tc_supported(h, panel))
+    return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "%s: tensor-core form needs "
+                     "1 or 2 populations and no separate validity plane", fn);
   PGLD_CHECK_CUDA(h, cudaSetDevice(h->device));
   cudaStream_t st = (cudaStream_t)stream;
   const int P = panel->n_pops;
   const int S = h->spec_n_stats[P];
   PGLD_CHECK_CUDA(h, cudaMemsetAsync(sums, 0, (size_t)n_bins * S * 8, st));
   if (pair_counts) PGLD_CHECK_CUDA(h, cudaMemsetAsync(pair_counts, 0, (size_t)n_bins * 8, st));
-  const i64 n = panel->n_snp;
+  if (panel->n_snp < 2 || a1 <= a0) return PGLD_OK;
+  PGLD_REQUIRE(h, pos != nullptr, "%s: NULL pos", fn);
+  // the SNP slice [a0, halo): the anchors and every partner within max_dist
+  i64 halo = panel->n_snp;
+  if (a1 < panel->n_snp) {
+    i64* dev_halo = reinterpret_cast<i64*>(h->dev_status) + 1;
+    pgld::halo_end_kernel<<<1, 32, 0, st>>>(pos, panel->n_snp, a1 - 1, max_dist, dev_halo);
+    PGLD_CHECK_CUDA(h, cudaGetLastError());
+    PGLD_CHECK_CUDA(h, cudaMemcpyAsync(&halo, dev_halo, 8, cudaMemcpyDeviceToHost, st));
+    PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));
+  }
+  pgld_hap_panel sub = *panel;
+  for (int p = 0; p < P; ++p) {
+    sub.planes[p] = panel->planes[p] + a0 * 2 * panel->n_words[p];
+    if (panel->valid[p]) sub.valid[p] = panel->valid[p] + a0 * panel->n_words[p];
+  }
+  sub.n_snp = halo - a0;
+  pos += a0;
+  if (bin_coord) bin_coord += a0;
+  const i64 n = sub.n_snp;
   if (n < 2) return PGLD_OK;
-  PGLD_REQUIRE(h, pos != nullptr, "pgld_hap_binned_sums: NULL pos");
+  pgld::BandArgs a{};
+  a.status = h->dev_status;
+  fill_panel(a, &sub);
+  a.n_anchor = a1 - a0;
+  a.pos = pos;
+  a.max_dist = max_dist;
+  a.bcoord = bin_coord;
+  a.bins = bins;
+  a.n_bins = n_bins;
+  a.sums = sums;
+  a.pair_counts = pair_counts;
+  a.terms = h->spec_terms[P];
+  a.n_terms = h->spec_n_terms[P];
+  a.n_stats = S;
+  // the tensor-core form schedules its own 64-SNP tiles
+  if (form == PGLD_FORM_TC) return pgld_tc_binned(h, &sub, a, st);
   const i64 nb = (n + pgld::kTile - 1) / pgld::kTile;
   size_t sb = pgld::scan_scratch_bytes(nb);
   void* ws = nullptr;
@@ -407,26 +469,27 @@ extern "C" int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, 
   char* scratch = (char*)ws + ((((size_t)(nb + 1) * 8) + 255) & ~size_t(255));
   rc = pgld::band_schedule(h, pos, n, max_dist, items, scratch, sb, st);
   if (rc) return rc;
-  pgld::BandArgs a{};
-  a.status = h->dev_status;
-  fill_panel(a, panel);
-  a.pos = pos;
-  a.max_dist = max_dist;
-  a.bcoord = bin_coord;
-  a.bins = bins;
-  a.n_bins = n_bins;
   a.item_off = items;
   a.n_blocks = nb;
-  a.sums = sums;
-  a.pair_counts = pair_counts;
-  a.terms = h->spec_terms[P];
-  a.n_terms = h->spec_n_terms[P];
-  a.n_stats = S;
-  if (form == PGLD_FORM_TC) {
-    if (!pgld_tc_supported(h, panel))
-      return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "pgld_hap_binned_sums: tensor-core form needs "
-                       "1 or 2 populations and no separate validity plane");
-    return pgld_tc_binned(h, panel, a, st);
-  }
   return pgld::launch_band_plain(h, a, pgld::kModeBinned, st);
+}
+
+extern "C" int pgld_hap_binned_sums(pgld_handle h, const pgld_hap_panel* panel, const double* pos,
+                                    double max_dist, const double* bin_coord, const double* bins,
+                                    int32_t n_bins, double* sums, int64_t* pair_counts,
+                                    int32_t form, void* stream) {
+  const i64 n = panel ? panel->n_snp : 0;
+  return binned_sums_range(h, panel, pos, max_dist, bin_coord, bins, n_bins, 0, n < 0 ? 0 : n, sums,
+                           pair_counts, form, stream, "pgld_hap_binned_sums");
+}
+
+extern "C" int pgld_hap_binned_sums_range(pgld_handle h, const pgld_hap_panel* panel,
+                                          const double* pos, double max_dist,
+                                          const double* bin_coord, const double* bins,
+                                          int32_t n_bins, int64_t anchor_begin, int64_t anchor_end,
+                                          double* sums, int64_t* pair_counts, int32_t form,
+                                          void* stream) {
+  return binned_sums_range(h, panel, pos, max_dist, bin_coord, bins, n_bins, anchor_begin,
+                           anchor_end, sums, pair_counts, form, stream,
+                           "pgld_hap_binned_sums_range");
 }

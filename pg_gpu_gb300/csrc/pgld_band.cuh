@@ -23,6 +23,9 @@ struct BandArgs {
   const uint32_t* valid[PGLD_MAX_POPS];
   const uint32_t* gext[PGLD_MAX_POPS];  // genotype planes of the values 3..8 (or NULL)
   long long n_snp;
+  // binned mode: only pairs whose first SNP lies below n_anchor count
+  // (<= 0: every SNP is an anchor)
+  long long n_anchor;
   const double* pos;
   double max_dist;
   const double* bcoord;  // binning coordinate (NULL: pos)
@@ -45,6 +48,11 @@ struct BandArgs {
   int nmax;         // largest per-population sample size (32 * max words)
   int stat_mask;    // genotype pairs mode: columns to compute (bit k = column k)
 };
+
+// number of anchors of a binned call (every SNP unless n_anchor limits it)
+__host__ __device__ __forceinline__ long long anchors_of(const BandArgs& a) {
+  return (a.n_anchor > 0 && a.n_anchor < a.n_snp) ? a.n_anchor : a.n_snp;
+}
 
 // tile work list of `tile`-SNP blocks: items[b] = tiles of row block b, then
 // exclusively scanned in place (items[n_blocks] = total)

@@ -137,6 +137,9 @@ __global__ void __launch_bounds__(kThreads) band_fast_kernel(BandArgs a) {
     if (threadIdx.x == 0 && a.status) atomicCAS(a.status, 0, 2001);
     n_items = 0;
   }
+  // binned mode over an anchor range: the row blocks holding anchors only
+  const long long n_anchor = MODE == kModeBinned ? anchors_of(a) : a.n_snp;
+  if (n_items > 0 && n_anchor < a.n_snp) n_items = a.item_off[(n_anchor + kTile - 1) / kTile];
   const double maxd = a.max_dist;
   const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
 
@@ -167,7 +170,8 @@ __global__ void __launch_bounds__(kThreads) band_fast_kernel(BandArgs a) {
     if (threadIdx.x == 0) {
       sm.tile_int = all_int;
       int tb = -1;
-      if (MODE == kModeBinned && all_int && bj > bi && j0 + kTile <= a.n_snp) {
+      if (MODE == kModeBinned && all_int && bj > bi && j0 + kTile <= a.n_snp &&
+          i0 + kTile <= n_anchor) {
         const int dmin = sm.relj[0] - sm.reli[kTile - 1];
         const int dmax = sm.relj[kTile - 1] - sm.reli[0];
         if (dmax <= maxd_int) {
@@ -245,7 +249,7 @@ __global__ void __launch_bounds__(kThreads) band_fast_kernel(BandArgs a) {
     for (int q = 0; q < 4; ++q) {
       const int il = wid * 4 + q;
       const long long i = i0 + il, j = j0 + lane;
-      bool ok = (i < j) && (j < a.n_snp);
+      bool ok = (i < j) && (j < a.n_snp) && (i < n_anchor);
       int b = -1;
       if (tint) {
         const int d = sm.relj[lane] - sm.reli[il];
@@ -331,7 +335,9 @@ int launch_fast_p(pgld_context* h, const BandArgs& a, cudaStream_t st) {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_fast occupancy");
   per_sm = std::max(1, per_sm);
+  pgld_time_begin(h, st);
   kern<<<(unsigned)(h->n_sm * per_sm), kThreads, smem, st>>>(a);
+  pgld_time_end(h, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_fast_kernel");
   return PGLD_OK;

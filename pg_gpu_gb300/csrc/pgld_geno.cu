@@ -506,7 +506,9 @@ int launch_geno_band(pgld_context* h, const BandArgs& a, cudaStream_t st) {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "geno_band occupancy");
   per_sm = std::max(1, per_sm);
+  pgld_time_begin(h, st);
   kern<<<(unsigned)(h->n_sm * per_sm), kThreads, smem, st>>>(a);
+  pgld_time_end(h, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "geno_band_kernel");
   return PGLD_OK;

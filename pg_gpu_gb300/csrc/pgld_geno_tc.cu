@@ -583,7 +583,9 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
                              : gtc_pairs_kernel<-1, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "gtc smem attribute");
+  pgld_time_begin(h, st);
   kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map, prm);
+  pgld_time_end(h, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "gtc_pairs_kernel");
   return PGLD_OK;

@@ -26,6 +26,13 @@ struct pgld_context {
   // the same tables with the genotype case kinds
   pgld_term* gspec_terms[PGLD_MAX_POPS + 1] = {nullptr};
   int gspec_n_terms[PGLD_MAX_POPS + 1] = {0};
+  // per-launch timing of the dominant kernel of each call (off by default):
+  // event pairs recorded around the launch on the call's stream
+  int test_fault = 0;  // pgld_set_test_fault: one-shot hook of the next tensor-core launch
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;
+  int tev_used = 0;
+  bool tev_overflow = false;
 };
 
 // --------------------------------------------------------------------------
@@ -34,6 +41,10 @@ struct pgld_context {
 int pgld_fail(pgld_context* h, int code, const char* fmt, ...);
 int pgld_cuda_fail(pgld_context* h, cudaError_t e, const char* what);
 int pgld_workspace(pgld_context* h, size_t bytes, void** out);
+// event marks around the dominant kernel launch of a call (no-ops unless
+// pgld_set_kernel_timing enabled timing on h)
+void pgld_time_begin(pgld_context* h, cudaStream_t st);
+void pgld_time_end(pgld_context* h, cudaStream_t st);
 
 #define PGLD_CHECK_CUDA(h, expr)                              \
   do {                                                        \

@@ -194,3 +194,34 @@ extern "C" int pgld_hap_binned_sums_noalloc(int device, const pgld_hap_panel* pa
   if (prev != device) cudaSetDevice(prev);
   return rc;
 }
+
+extern "C" int pgld_noalloc_status(int device, int32_t* code_out) {
+  if (!code_out)
+    return pgld_fail(nullptr, PGLD_ERR_INVALID_ARG, "pgld_noalloc_status: NULL code_out");
+  int n_dev = 0;
+  cudaError_t e = cudaGetDeviceCount(&n_dev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return pgld_cuda_fail(nullptr, e, "pgld_noalloc_status: cudaGetDeviceCount");
+  }
+  if (device < 0 || device >= n_dev || device >= kMaxDevices)
+    return pgld_fail(nullptr, PGLD_ERR_INVALID_ARG, "pgld_noalloc_status: device %d", device);
+  *code_out = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_setup[device].ready) return PGLD_OK;  // no call has run on the device
+  }
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess)
+    return pgld_cuda_fail(nullptr, e, "cudaSetDevice");
+  int32_t v = 0;
+  const int32_t zero = 0;
+  // symbol copies: no allocation; they wait for the device's earlier work
+  e = cudaMemcpyFromSymbol(&v, g_noalloc_status, sizeof(v));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_noalloc_status, &zero, sizeof(zero));
+  if (prev != device) cudaSetDevice(prev);
+  if (e != cudaSuccess) return pgld_cuda_fail(nullptr, e, "pgld_noalloc_status");
+  *code_out = v;
+  return PGLD_OK;
+}

@@ -46,6 +46,7 @@ struct Params {
   int n_pops;
   int kchunks[2];
   long long n_snp;
+  long long n_anchor;  // binned mode: pairs whose first SNP lies below n_anchor
   const double* pos;
   double max_dist;
   const double* bcoord;
@@ -58,6 +59,8 @@ struct Params {
   int32_t* status;
   int stages;
   int nmax;  // largest per-population sample size (reciprocal table length - 1)
+  long long wait_cycles;  // limit of every bounded mbarrier wait (SM clock cycles)
+  int no_copies;          // test hook: the TMA producer issues nothing
   const int* ipos;     // integer positions (valid when *ipos_bad == 0)
   const int* ipos_bad;
   // per-pair outputs (pairs mode, one population)
@@ -178,15 +181,6 @@ __device__ __forceinline__ int bin_of_f64(const double* sb, int n_bins, double d
   return lo;
 }
 
-// compensated (Neumaier) float32 accumulation: slot.x = sum, slot.y = correction
-__device__ __forceinline__ void kahan_add(float2* slot, float v) {
-  const float s = slot->x;
-  const float t = __fadd_rn(s, v);
-  const float bp = __fsub_rn(t, s);
-  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(v, bp));
-  slot->x = t;
-  slot->y = __fadd_rn(slot->y, err);
-}
 
 // warp totals of S <= 16 values by recursive halving (16 shuffles for S = 15
 // where a butterfly per value takes 75): each step sends the half of the values
@@ -224,13 +218,14 @@ __device__ __forceinline__ float warp_totals(const float (&v)[S], int lane) {
   for (; off >= 1; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
   return t;
 }
-// the warp's totals of v added to slot[0..S) (one lane per value)
+// the warp's totals of v added to the float64 bin slots slot[0..S) (one lane
+// per value)
 template <int S>
-__device__ __forceinline__ void warp_totals_add(const float (&v)[S], int lane, float2* slot) {
+__device__ __forceinline__ void warp_totals_add(const float (&v)[S], int lane, double* slot) {
   const float tot = warp_totals<S>(v, lane);
   constexpr int sh = totals_shift<S>();
   const int k = lane >> sh;
-  if ((lane & ((1 << sh) - 1)) == 0 && k < S) kahan_add(slot + k, tot);
+  if ((lane & ((1 << sh) - 1)) == 0 && k < S) slot[k] += (double)tot;
 }
 
 // MODE kModeBinned: distance-binned moments sums of P populations;
@@ -249,7 +244,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kStageBytes);
   double* sbins = reinterpret_cast<double*>(ctrl + 1);
   int* thr = reinterpret_cast<int*>(sbins + (kMaxBins + 1));
-  float2* kacc = reinterpret_cast<float2*>(thr + (kMaxBins + 2));  // [kEpiWarps][n_bins][S]
+  // per-warp float64 bin sums [kEpiWarps][n_bins][S] (8-byte aligned: thr holds an even count)
+  double* kacc = reinterpret_cast<double*>(thr + (kMaxBins + 2));
   unsigned long long* kcnt =
       reinterpret_cast<unsigned long long*>(kacc + kEpiWarps * a.n_bins * S);  // [kEpiWarps][n_bins]
   // reciprocal tables by n, 4 x (nmax + 1) floats: four arrays (1/n,
@@ -294,7 +290,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (warp >= 4) {
     const int t = threadIdx.x - 128;
-    for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) kacc[x] = make_float2(0.f, 0.f);
+    for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) kacc[x] = 0.0;
     for (int x = t; x < kEpiWarps * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
     for (int x = t; x <= a.nmax; x += kEpiThreads)
       if constexpr (MODE == kModeBinned)
@@ -320,6 +316,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (threadIdx.x == 0) set_abort(ctrl, a.status, 3001);
     n_items = 0;
   }
+  // binned mode over an anchor range: the row blocks holding anchors only
+  if (MODE == kModeBinned && n_items > 0 && a.n_anchor < a.n_snp)
+    n_items = a.item_off[(a.n_anchor + kTileSnp - 1) / kTileSnp];
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
@@ -328,13 +327,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t phase = 0;
       int issued = 0;
       long long row_hint = 0;
-      for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x) {
+      // (with no_copies the MMA warp's wait for the first stage expires)
+      const long long n_copy_items = a.no_copies ? 0 : n_items;
+      for (long long item = blockIdx.x; item < n_copy_items && !*abort_flag; item += gridDim.x) {
         const TileRef tr = decode_item<MODE>(a, item, row_hint);
         const int yi = (int)(2 * tr.i0), yj = (int)(2 * tr.j0);
         for (int p = 0; p < P && !*abort_flag; ++p) {
           const CUtensorMap* map = p == 0 ? &map0 : &map1;
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+            if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
               set_abort(ctrl, a.status, 3002);
               break;
             }
@@ -375,7 +376,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
+        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && ok; ++p) {
           const uint32_t d = tmem_base + (uint32_t)(acc * 256 + p * 128);
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait(&ctrl->full[stage], phase, abort_flag)) {
+            if (!mbar_wait(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
               set_abort(ctrl, a.status, 3004);
               ok = false;
               break;
@@ -423,7 +424,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
     const bool use_int = MODE != kModeWindows && (a.bcoord == nullptr) && (*a.ipos_bad == 0);
-    float2* my_acc = kacc + (size_t)e * n_bins * S;
+    double* my_acc = kacc + (size_t)e * n_bins * S;
     unsigned long long* my_cnt = kcnt + (size_t)e * n_bins;
     int t = 0;
     long long row_hint = 0;
@@ -437,7 +438,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 
       // classify the warp's sub-tile: 0 one bin, 1 two adjacent bins, 2 general
       int mode = 2, b0 = -1, thr_mid = 0;
-      if (MODE == kModeBinned && use_int && bj > bi && sj0 + 31 < a.n_snp) {
+      if (MODE == kModeBinned && use_int && bj > bi && sj0 + 31 < a.n_snp &&
+          si0 + 15 < a.n_anchor) {
         const int dmin = a.ipos[sj0] - a.ipos[si0 + 15];
         const int dmax = a.ipos[sj0 + 31] - a.ipos[si0];
         if (dmax <= maxd_int) {
@@ -507,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
 
       bool ready = true;
-      if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag);
+      if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag, a.wait_cycles);
       ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
       if (!ready) {
         if (lane == 0) set_abort(ctrl, a.status, 3005);
@@ -770,7 +772,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           key = -1;
         };
         auto bin_of = [&](long long is, int ipi, long long j, int jp) -> int {
-          if (!(is < j && j < a.n_snp)) return -1;
+          if (!(is < j && j < a.n_snp && is < a.n_anchor)) return -1;
           if (use_int) {
             const int d = jp - ipi;
             return d <= maxd_int ? bin_of_int(thr, n_bins, d) : -1;
@@ -840,10 +842,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x < n_bins * S; x += kEpiThreads) {
       double v = 0.0;
 #pragma unroll
-      for (int w = 0; w < kEpiWarps; ++w) {
-        const float2 k = kacc[w * n_bins * S + x];
-        v += (double)k.x + (double)k.y;
-      }
+      for (int w = 0; w < kEpiWarps; ++w) v += kacc[w * n_bins * S + x];
       if (v != 0.0) atomicAdd(a.sums + x, v);
     }
     if (a.pair_counts)
@@ -1023,6 +1022,7 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
   prm.n_pops = P;
   for (int p = 0; p < P; ++p) prm.kchunks[p] = k_pad[p] / kKChunk;
   prm.n_snp = n;
+  prm.n_anchor = pgld::anchors_of(a);
   prm.pos = a.pos;
   prm.max_dist = a.max_dist;
   prm.bcoord = a.bcoord;
@@ -1041,6 +1041,14 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
   prm.stats = a.stats;
   prm.nmax = 0;
   for (int p = 0; p < P; ++p) prm.nmax = std::max(prm.nmax, 32 * panel->n_words[p]);
+  prm.wait_cycles = kWaitCycles;
+  if (h->test_fault == PGLD_TEST_FAULT_NO_COPIES) {
+    // one-shot test hook: no operand copies, the bounded waits expire after
+    // ~10 ms and the launch reports it in the device status word
+    prm.no_copies = 1;
+    prm.wait_cycles = 20000000ll;
+    h->test_fault = 0;
+  }
 
   const size_t fixed = sizeof(Ctrl) + (pgld::kMaxBins + 1) * 8 + (pgld::kMaxBins + 2) * 4 +
                        (size_t)kEpiWarps * a.n_bins * (S + 1) * 8 +
@@ -1057,7 +1065,9 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
   if (mode == pgld::kModeWindows) kern = band_tc_kernel<1, pgld::kModeWindows>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc smem attribute");
+  pgld_time_begin(h, st);
   kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(maps[0], maps[1], prm);
+  pgld_time_end(h, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc_kernel");
   return PGLD_OK;
@@ -1153,6 +1163,7 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
   prm.n_bins = 0;
   prm.status = h->dev_status;
   prm.nmax = 32 * W;
+  prm.wait_cycles = kWaitCycles;
   prm.win_begin = wb;
   prm.win_end = we;
   prm.n_win = n_win;
@@ -1175,7 +1186,9 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
   auto kern = band_tc_kernel<1, pgld::kModeWindows>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "tc windows smem attribute");
+  pgld_time_begin(h, st);
   kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map, map, prm);
+  pgld_time_end(h, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc_kernel (windows)");
   return PGLD_OK;

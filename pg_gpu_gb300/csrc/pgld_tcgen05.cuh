@@ -59,11 +59,14 @@ __device__ __forceinline__ bool mbar_try_for(uint64_t* b, uint32_t parity, uint3
 // Each poll may suspend the thread until the phase completes (or 20 us pass).
 constexpr long long kWaitCycles = 4000000000ll;
 constexpr uint32_t kSuspendNs = 20000;
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
+// (limit: SM clock cycles before giving up; kWaitCycles unless a launch
+// shortens it)
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag,
+                                          long long limit = kWaitCycles) {
   const long long t0 = clock64();
   for (long long k = 0; k < kSpinLimit; ++k) {
     if (mbar_try_for(b, parity, kSuspendNs)) return true;
-    if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
+    if (*abort_flag || clock64() - t0 > limit) return false;
   }
   return false;
 }

@@ -326,7 +326,9 @@ static int window_run(pgld_context* h, const pgld_hap_panel* panel, const int32_
   int per_sm = 0;
   PGLD_CHECK_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern,
                                                                    pgld::win::kThreads, tab_b));
+  pgld_time_begin(h, st);
   kern<<<(unsigned)(h->n_sm * std::max(1, per_sm)), pgld::win::kThreads, tab_b, st>>>(a);
+  pgld_time_end(h, st);
   PGLD_CHECK_CUDA(h, cudaGetLastError());
   // the tile offsets and site counts live in the workspace: finish before reuse
   PGLD_CHECK_CUDA(h, cudaStreamSynchronize(st));

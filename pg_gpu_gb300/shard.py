@@ -3,16 +3,16 @@
 The binned sums of moments_ld._compute_ld_sums (moments_ld.py:248-343) are a
 sum over SNP pairs (i < j, pos[j] - pos[i] <= max_dist), so they partition by
 the first SNP of a pair: rank r takes the anchors [start, stop) -- contiguous
-ranges balanced by their pair counts -- and needs the SNPs up to the halo end
+ranges balanced by their pair counts -- and reads the SNPs up to the halo end
 (the last SNP within max_dist of stop - 1).  Its partial is the binned sum
-over [start, halo) minus the binned sum over [stop, halo) (the pairs whose
-first SNP belongs to the next ranks); the one exchange is a sum of the
+over the pairs whose first SNP lies in [start, stop), computed once
+(pgld_hap_binned_sums_range); the one exchange is a sum of the
 (n_bins x n_stats) float64 partials and the pair counts over the ranks.
 
 The packed panel is replicated on every rank (at 2,000 haplotypes a SNP packs
 to 504 bytes).  The planning and combination here are host code; the per-shard
-compute is any callable (s, e) -> (sums, counts) over the SNP slice [s, e),
-normally ``slice_binned_sums`` on the device.
+compute is any callable (start, stop) -> (sums, counts) over the pairs
+anchored in [start, stop), normally ``range_binned_sums`` on the device.
 """
 from __future__ import annotations
 
@@ -65,18 +65,12 @@ def plan_shards(positions, max_dist, world):
 
 
 def shard_partial(compute, shard):
-    """(sums, counts) of the pairs whose first SNP lies in the shard.
-
-    compute(s, e) -> (sums, counts) over the pairs inside the SNP slice [s, e);
-    the pairs of [stop, halo) belong to later ranks and are subtracted."""
+    """(sums, counts) of the pairs whose first SNP lies in the shard:
+    compute(start, stop) over the shard's anchor range, or None for an empty
+    shard."""
     if shard.stop <= shard.start:
         return None
-    sums, cnt = compute(shard.start, shard.halo)
-    if shard.halo > shard.stop:
-        s2, c2 = compute(shard.stop, shard.halo)
-        sums = sums - s2
-        cnt = cnt - c2
-    return sums, cnt
+    return compute(shard.start, shard.stop)
 
 
 def reduce_partials(sums, counts, group=None):
@@ -95,16 +89,15 @@ def reduce_partials(sums, counts, group=None):
     return sums, counts
 
 
-def slice_binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto"):
-    """The device compute of one SNP slice: compute(s, e) over views of the
-    packed populations, positions and bin coordinates (no copies)."""
+def range_binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto"):
+    """The device compute of one anchor range: compute(start, stop) -> the
+    binned sums of the pairs whose first SNP lies in [start, stop), on the
+    whole replicated panel (the kernels read the anchors and their halo)."""
     from . import _ops
 
     def compute(s, e):
-        sub = [_ops.PackedPop(pk.planes[s:e], pk.valid[s:e], pk.n_words, pk.n_rows, e - s,
-                              pk.has_missing, pk.has_other) for pk in pops]
-        bc = None if bin_coord is None else bin_coord[s:e]
-        return _ops.binned_sums(sub, pos_d[s:e], bins, max_dist=max_dist, bin_coord=bc, form=form)
+        return _ops.binned_sums(pops, pos_d, bins, max_dist=max_dist, bin_coord=bin_coord,
+                                form=form, anchors=(s, e))
     return compute
 
 
@@ -118,7 +111,7 @@ def binned_sums_distributed(pops, pos_d, bins, positions_host, max_dist=None, bi
     bins_np = np.asarray(bins, dtype=np.float64)
     md = float(bins_np[-1]) if max_dist is None else float(max_dist)
     shards = plan_shards(positions_host, md, world)
-    part = shard_partial(slice_binned_sums(pops, pos_d, bins, md, bin_coord, form), shards[rank])
+    part = shard_partial(range_binned_sums(pops, pos_d, bins, md, bin_coord, form), shards[rank])
     n_bins = len(bins_np) - 1
     n_stats = {1: 3, 2: 15, 3: 45, 4: 105}[len(pops)]
     if part is None:

@@ -1,11 +1,16 @@
 """GPU parity of the tcgen05 tensor-core binned-sum form.
 
-Same bar as the plain form: pair counts per bin equal the oracle's exactly,
-and every bin sum is within 2e-6 * sum|x| of the float64 oracle.  Cases cover
-one and two populations, SNP counts that leave partial 64-SNP tiles, sample
-sizes that are not multiples of 128 (K padding), 1,000 haplotypes per
-population, genetic-map distances and non-integer positions.
+Pair counts per bin equal the oracle's exactly.  Every bin sum is within
+1e-6 of its float64 oracle value (RTOL); a bin whose terms cancel to below
+5 % of their sum of |x| (FLOOR) is held to 1e-6 of that share instead.  The
+moments golden sums are held to the reference's own criterion, 1e-6 of each
+value.  Cases cover one and two populations, SNP counts that leave partial
+64-SNP tiles, sample sizes that are not multiples of 128 (K padding), 1,000
+haplotypes per population, genetic-map distances, non-integer positions,
+anchor ranges and the full-size benchmark panel.
 """
+import multiprocessing as mp
+
 import numpy as np
 import pytest
 
@@ -17,9 +22,10 @@ torch = pytest.importorskip("torch")
 if not torch.cuda.is_available():
     pytest.skip("needs a CUDA device", allow_module_level=True)
 
-from pg_gpu_gb300 import _ops  # noqa: E402
+from pg_gpu_gb300 import _ops, synthetic  # noqa: E402
 
-SUM_TOL = 2e-6
+RTOL = 1e-6
+FLOOR = 0.05
 
 
 def copying_model(rng, H, M, F, switch, missing=0.0, flip=1e-3):
@@ -35,7 +41,7 @@ def copying_model(rng, H, M, F, switch, missing=0.0, flip=1e-3):
     return hap.astype(np.int8)
 
 
-def check(hap, pos, rows, bins, **kw):
+def check(hap, pos, rows, bins, floor=FLOOR, **kw):
     hap_d = torch.as_tensor(hap, device="cuda")
     pops = [_ops.pack(hap_d, r) for r in rows]
     sums, cnt = _ops.binned_sums(pops, _ops.positions_f64(pos), bins, form="tc", **kw)
@@ -46,9 +52,10 @@ def check(hap, pos, rows, bins, **kw):
         okw["max_dist"] = kw["max_dist"]
     ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True, **okw)
     assert np.array_equal(cnt.cpu().numpy(), ref_cnt)
-    err = np.abs(sums.cpu().numpy() - ref)
-    worst = float((err / np.maximum(ref_abs, 1e-300)).max())
-    assert np.all(err <= SUM_TOL * ref_abs + 1e-300), worst
+    rel = O.bin_errors(sums.cpu().numpy(), ref, ref_abs, floor)
+    worst = float(rel.max())
+    print(f"max error relative to the bin value: {worst:.3g}")
+    assert worst <= RTOL, worst
     return worst
 
 
@@ -61,7 +68,8 @@ def test_tc_matches_reference_fixture(golden, P):
 def test_tc_matches_moments_golden(golden):
     z = golden("moments_im")
     keep = O.biallelic_keep(z["hap"])
-    check(z["hap"][:, keep], z["pos"][keep], [z["rows0"], z["rows1"]], z["bins"])
+    # the reference's criterion for moments' sums: 1e-6 of each value
+    check(z["hap"][:, keep], z["pos"][keep], [z["rows0"], z["rows1"]], z["bins"], floor=0.0)
 
 
 @pytest.mark.parametrize("H,M", [(40, 65), (130, 129), (300, 191), (257, 640)])
@@ -121,8 +129,9 @@ def test_tc_band_pairs_match_oracle(H, M):
 
 @pytest.mark.parametrize("form", ["tc", "plain"])
 def test_sharded_binned_sums_add_up(form):
-    # the multi-rank partition (pg_gpu_gb300/shard.py) run as three shards on
-    # one device: the partials' sum is the oracle's whole-panel result
+    # the multi-rank partition (pg_gpu_gb300/shard.py) run as three anchor
+    # ranges on one device: each range matches the oracle's sums over its
+    # anchors, and the ranges add up to the whole panel
     from pg_gpu_gb300 import shard as S
     rng = np.random.default_rng(77)
     H, M = 300, 2_500
@@ -133,49 +142,124 @@ def test_sharded_binned_sums_add_up(form):
     hap_d = torch.as_tensor(hap, device="cuda")
     pops = [_ops.pack(hap_d, r) for r in rows]
     pos_d = _ops.positions_f64(pos)
-    compute = S.slice_binned_sums(pops, pos_d, bins, form=form)
+    compute = S.range_binned_sums(pops, pos_d, bins, form=form)
     acc_s, acc_c = 0.0, 0
     for sh in S.plan_shards(pos, bins[-1], 3):
         part = S.shard_partial(compute, sh)
+        ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True,
+                                              anchor_start=sh.start, anchor_stop=sh.stop)
+        assert np.array_equal(part[1].cpu().numpy(), ref_cnt)
+        assert O.bin_errors(part[0].cpu().numpy(), ref, ref_abs, FLOOR).max() <= RTOL
         acc_s = acc_s + part[0].cpu().numpy()
         acc_c = acc_c + part[1].cpu().numpy()
     ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True)
     assert np.array_equal(acc_c, ref_cnt)
-    # each shard's sums carry the float32 per-pair error of the halo pairs twice
-    assert np.all(np.abs(acc_s - ref) <= 3 * SUM_TOL * ref_abs + 1e-300)
+    assert O.bin_errors(acc_s, ref, ref_abs, FLOOR).max() <= RTOL
+
+
+@pytest.mark.parametrize("form", ["tc", "plain"])
+def test_anchor_ranges_edge_cases(form):
+    # empty, single-anchor, last-anchor and whole-panel ranges, and a range
+    # outside the panel (rejected)
+    rng = np.random.default_rng(78)
+    hap = copying_model(rng, 160, 700, 8, 3e-3, missing=0.02)
+    pos = np.sort(rng.choice(300_000, 700, replace=False)).astype(np.int64)
+    bins = np.logspace(2, 4.7, 7)
+    rows = [np.arange(80), np.arange(80, 160)]
+    hap_d = torch.as_tensor(hap, device="cuda")
+    pops = [_ops.pack(hap_d, r) for r in rows]
+    pos_d = _ops.positions_f64(pos)
+    for a0, a1 in [(5, 5), (0, 1), (350, 351), (699, 700), (0, 700), (63, 129), (640, 700)]:
+        sums, cnt = _ops.binned_sums(pops, pos_d, bins, form=form, anchors=(a0, a1))
+        ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True,
+                                              anchor_start=a0, anchor_stop=a1)
+        assert np.array_equal(cnt.cpu().numpy(), ref_cnt), (a0, a1)
+        assert O.bin_errors(sums.cpu().numpy(), ref, ref_abs, FLOOR).max() <= RTOL, (a0, a1)
+    from pg_gpu_gb300._lib import PgldError
+    with pytest.raises(PgldError):
+        _ops.binned_sums(pops, pos_d, bins, form=form, anchors=(10, 701))
+    with pytest.raises(PgldError):
+        _ops.binned_sums(pops, pos_d, bins, form=form, anchors=(20, 10))
 
 
 def test_full_size_headline_panel():
-    # the binned two-population workload at full size (2 x 1,000 haplotypes,
-    # 200,000 SNPs over 20 Mb, 20 log bins up to 1 Mb; ~1.9e9 pairs):
-    # per-bin pair counts equal the exact counts from the positions alone, the
-    # tensor-core and popcount forms agree on them, and a 300-anchor sample of
-    # the pairs (~1e6, computed as a shard) matches the oracle
-    from pg_gpu_gb300 import shard as S
-    rng = np.random.default_rng(20261203)
-    M, H = 200_000, 1000
-    hap = np.concatenate([copying_model(rng, H, M, 40, 1e-3, missing=0.0) for _ in range(2)])
-    pos = np.sort(rng.choice(20_000_000, M, replace=False)).astype(np.int64)
-    bins = np.concatenate([[0.0], np.logspace(3, 6, 20)])
-    rows = [np.arange(0, H), np.arange(H, 2 * H)]
-    hap_d = torch.as_tensor(hap, device="cuda")
-    pops = [_ops.pack(hap_d, r) for r in rows]
+    # the benchmark's binned two-population panel itself (2 x 1,000
+    # haplotypes sharing 40 founders, 10 % founder alleles flipped per
+    # population, 2 % missing, 200,000 SNPs over 20 Mb, 20 log bins from 1 kb
+    # to 1 Mb; ~1.9e9 pairs): per-bin pair counts of both forms equal the
+    # exact counts from the positions alone, and twelve anchor blocks spread
+    # over the chromosome (>= 1e7 pairs) match the oracle -- counts exactly,
+    # every statistic within RTOL of its bin value (FLOOR for cancelling bins)
+    cfg = synthetic.BINNED2POP
+    panel, pos = synthetic.shared_founder_panel(cfg, torch.device("cuda", 0))
+    M, H = cfg["n_snp"], cfg["hap_per_pop"]
+    bins = cfg["bins"]
+    md = float(bins[-1])
+    rows_d = [torch.arange(q * H, (q + 1) * H, dtype=torch.int32, device="cuda") for q in range(2)]
+    pops = [_ops.pack(panel, r) for r in rows_d]
     pos_d = _ops.positions_f64(pos)
     sums_tc, cnt_tc = _ops.binned_sums(pops, pos_d, bins, form="tc")
     _, cnt_pl = _ops.binned_sums(pops, pos_d, bins, form="plain")
     pf = pos.astype(np.float64)
-    # pairs (i, j > i) with pos[j] - pos[i] < e, for every bin edge e
     below = [int(np.maximum(np.searchsorted(pf, pf + e, side="left") - np.arange(M) - 1, 0).sum())
              for e in bins]
     exact = np.diff(np.asarray(below, np.int64))
     assert np.array_equal(cnt_tc.cpu().numpy(), exact)
     assert np.array_equal(cnt_pl.cpu().numpy(), exact)
     assert np.all(np.isfinite(sums_tc.cpu().numpy()))
-    A = 100
-    sh = S.Shard(0, 0, A, int(np.searchsorted(pf, pf[A - 1] + bins[-1], side="right")))
-    part_s, part_c = S.shard_partial(S.slice_binned_sums(pops, pos_d, bins, form="tc"), sh)
-    ref, ref_cnt, ref_abs = O.binned_sums(hap, pos, rows, bins, abs_sums=True,
-                                          anchor_stop=A, pair_block=100_000)
-    assert np.array_equal(part_c.cpu().numpy(), ref_cnt)
-    err = np.abs(part_s.cpu().numpy() - ref)
-    assert np.all(err <= 3 * SUM_TOL * ref_abs + 1e-300)
+    # twelve anchor blocks of ~9e5 pairs each, spread over the chromosome
+    blocks, tasks, gpu = [], [], []
+    rows = [np.arange(0, H), np.arange(H, 2 * H)]
+    for k in range(12):
+        a0 = k * M // 12 + M // 40
+        a1, _ = synthetic.anchors_per_pairs(pos, md, a0, 900_000)
+        halo = int(np.searchsorted(pf, pf[a1 - 1] + md, side="right"))
+        blocks.append((a0, a1))
+        gpu.append(_ops.binned_sums(pops, pos_d, bins, form="tc", anchors=(a0, a1)))
+        tasks.append(((panel[:, a0:halo].cpu().numpy(), pos[a0:halo], rows, bins),
+                      dict(anchor_stop=a1 - a0, pair_block=100_000)))
+    with mp.get_context("spawn").Pool(min(12, mp.cpu_count())) as pool:
+        refs = pool.map(O.binned_sums_task, tasks)
+    n_checked = 0
+    worst = np.zeros(15)
+    for (a0, a1), (s_g, c_g), (ref, ref_cnt, ref_abs) in zip(blocks, gpu, refs):
+        assert np.array_equal(c_g.cpu().numpy(), ref_cnt), (a0, a1)
+        n_checked += int(ref_cnt.sum())
+        rel = O.bin_errors(s_g.cpu().numpy(), ref, ref_abs, FLOOR)
+        worst = np.maximum(worst, rel.max(axis=0))
+    from pg_gpu_gb300.ld_pipeline import ld_names
+    names = ld_names(2)
+    print(f"{n_checked} pairs checked; max error relative to the bin value per statistic: " +
+          ", ".join(f"{n}={w:.2e}" for n, w in zip(names, worst)))
+    assert n_checked >= 10_000_000
+    assert worst.max() <= RTOL, worst
+
+
+def test_bounded_wait_expiry_reports_and_recovers():
+    # failure detection without a fault: the one-shot test hook makes the
+    # next tensor-core launch issue no operand copies, so the MMA issuer's
+    # bounded wait for the first stage expires (~10 ms); the launch drains,
+    # frees its tensor memory and returns, the handle's status word holds a
+    # wait-expiry code, and the next calls on the same handle are correct
+    import ctypes
+    from pg_gpu_gb300 import _lib as L
+    rng = np.random.default_rng(31)
+    hap = copying_model(rng, 200, 500, 8, 3e-3, missing=0.02)
+    pos = np.sort(rng.choice(250_000, 500, replace=False)).astype(np.int64)
+    bins = np.logspace(2, 4.7, 7)
+    rows = [np.arange(100), np.arange(100, 200)]
+    hap_d = torch.as_tensor(hap, device="cuda")
+    pops = [_ops.pack(hap_d, r) for r in rows]
+    pos_d = _ops.positions_f64(pos)
+    h = L.handle()
+    code = ctypes.c_int32(-1)
+    L.check(L.lib().pgld_device_status(h, ctypes.byref(code), L.stream_ptr()), h)
+    assert code.value == 0
+    L.check(L.lib().pgld_set_test_fault(h, 1), h)
+    _ops.binned_sums(pops, pos_d, bins, form="tc")
+    L.check(L.lib().pgld_device_status(h, ctypes.byref(code), L.stream_ptr()), h)
+    assert 3002 <= code.value <= 3005, code.value
+    for _ in range(2):
+        check(hap, pos, rows, bins)
+        L.check(L.lib().pgld_device_status(h, ctypes.byref(code), L.stream_ptr()), h)
+        assert code.value == 0

@@ -1,7 +1,7 @@
 """The multi-rank path of the binned sums (pg_gpu_gb300/shard.py) on the CPU:
-shard planning, the halo subtraction and the sum of partials over a gloo
-process group of two ranks, with the oracle as each rank's compute (the
-device compute of a shard is checked against the unsharded call in
+shard planning, the per-rank anchor ranges and the sum of partials over a
+gloo process group of two ranks, with the oracle as each rank's compute (the
+device compute of an anchor range is checked against the oracle in
 tests/test_gpu_tc.py)."""
 import os
 import socket
@@ -25,7 +25,7 @@ def _panel(seed, H=24, M=300):
 
 def _oracle_compute(hap, pos, rows, bins):
     def compute(s, e):
-        sums, cnt = O.binned_sums(hap[:, s:e], pos[s:e], rows, bins)
+        sums, cnt = O.binned_sums(hap, pos, rows, bins, anchor_start=s, anchor_stop=e)
         return torch.as_tensor(np.asarray(sums, np.float64)), torch.as_tensor(np.asarray(cnt, np.int64))
     return compute
 
