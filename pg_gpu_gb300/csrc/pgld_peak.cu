@@ -106,7 +106,8 @@ extern "C" int pgld_tc_mma_rate(pgld_handle h, int32_t n_cols, int64_t mmas_per_
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
-  const size_t smem = 1024 + 16384 + (size_t)n_cols * 128;
+  // operands take at most 49 KB; 120 KB keeps one CTA (one MMA issuer) per SM
+  const size_t smem = 120 * 1024;
   auto kern = pgld::peak::mma_rate_kernel;
   int rc = PGLD_OK;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
