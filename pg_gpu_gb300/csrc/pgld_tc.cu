@@ -40,6 +40,9 @@ constexpr int kEpiWarps = 8;
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kThreads = (4 + kEpiWarps) * 32;
 constexpr uint32_t kTmemCols = 512;
+#ifndef PGLD_TC_MAXNREG
+#define PGLD_TC_MAXNREG 0
+#endif
 
 
 struct Params {
@@ -218,14 +221,36 @@ __device__ __forceinline__ float warp_totals(const float (&v)[S], int lane) {
   for (; off >= 1; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
   return t;
 }
-// the warp's totals of v added to the float64 bin slots slot[0..S) (one lane
-// per value)
+#ifndef PGLD_TC_SLOTS_F64
+#define PGLD_TC_SLOTS_F64 0
+#endif
+#if PGLD_TC_SLOTS_F64
+typedef double Slot;
+__device__ __forceinline__ void slot_add(Slot* s, float v) { *s += (double)v; }
+__device__ __forceinline__ double slot_value(const Slot& s) { return s; }
+__device__ __forceinline__ Slot slot_zero() { return 0.0; }
+#else
+// compensated (Neumaier) float32 slot: x = sum, y = running correction
+typedef float2 Slot;
+__device__ __forceinline__ void slot_add(Slot* slot, float v) {
+  const float s = slot->x;
+  const float t = __fadd_rn(s, v);
+  const float bp = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(v, bp));
+  slot->x = t;
+  slot->y = __fadd_rn(slot->y, err);
+}
+__device__ __forceinline__ double slot_value(const Slot& s) { return (double)s.x + (double)s.y; }
+__device__ __forceinline__ Slot slot_zero() { return make_float2(0.f, 0.f); }
+#endif
+
+// the warp's totals of v added to the bin slots slot[0..S) (one lane per value)
 template <int S>
-__device__ __forceinline__ void warp_totals_add(const float (&v)[S], int lane, double* slot) {
+__device__ __forceinline__ void warp_totals_add(const float (&v)[S], int lane, Slot* slot) {
   const float tot = warp_totals<S>(v, lane);
   constexpr int sh = totals_shift<S>();
   const int k = lane >> sh;
-  if ((lane & ((1 << sh) - 1)) == 0 && k < S) slot[k] += (double)tot;
+  if ((lane & ((1 << sh) - 1)) == 0 && k < S) slot_add(slot + k, tot);
 }
 
 // MODE kModeBinned: distance-binned moments sums of P populations;
@@ -244,8 +269,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kStageBytes);
   double* sbins = reinterpret_cast<double*>(ctrl + 1);
   int* thr = reinterpret_cast<int*>(sbins + (kMaxBins + 1));
-  // per-warp float64 bin sums [kEpiWarps][n_bins][S] (8-byte aligned: thr holds an even count)
-  double* kacc = reinterpret_cast<double*>(thr + (kMaxBins + 2));
+  // per-warp bin sums [kEpiWarps][n_bins][S] (8-byte aligned: thr holds an even count)
+  Slot* kacc = reinterpret_cast<Slot*>(thr + (kMaxBins + 2));
   unsigned long long* kcnt =
       reinterpret_cast<unsigned long long*>(kacc + kEpiWarps * a.n_bins * S);  // [kEpiWarps][n_bins]
   // reciprocal tables by n, 4 x (nmax + 1) floats: four arrays (1/n,
@@ -290,7 +315,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (warp >= 4) {
     const int t = threadIdx.x - 128;
-    for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) kacc[x] = 0.0;
+    for (int x = t; x < kEpiWarps * n_bins * S; x += kEpiThreads) kacc[x] = slot_zero();
     for (int x = t; x < kEpiWarps * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
     for (int x = t; x <= a.nmax; x += kEpiThreads)
       if constexpr (MODE == kModeBinned)
@@ -320,6 +345,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (MODE == kModeBinned && n_items > 0 && a.n_anchor < a.n_snp)
     n_items = a.item_off[(a.n_anchor + kTileSnp - 1) / kTileSnp];
 
+  // Registers move from the producer / MMA warpgroup (warps 0-3) to the two
+  // epilogue warpgroups: 128 x 56 + 256 x 224 = 384 x 168, the launch's total
+  // (the host launches this kernel only when it was built with 168 registers).
+  if (warp < 4) {
+#if PGLD_TC_MAXNREG
+  asm volatile("setmaxnreg.dec.sync.aligned.u32 56;" ::: "memory");
+#endif
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
@@ -414,7 +446,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_wait_drain(&ctrl->drain, 0);
       }
     }
-  } else if (warp >= 4) {
+  }
+  } else {
+#if PGLD_TC_MAXNREG
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 224;" ::: "memory");
+#endif
     // ---------------- epilogue ----------------
     // Warp e reads TMEM lane quarter (warp & 3) and column half (e >> 2): the
     // 16 x 32 sub-tile i in i0 + 16*quarter + [0,16), j in j0 + 32*half + [0,32).
@@ -424,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
     const bool use_int = MODE != kModeWindows && (a.bcoord == nullptr) && (*a.ipos_bad == 0);
-    double* my_acc = kacc + (size_t)e * n_bins * S;
+    Slot* my_acc = kacc + (size_t)e * n_bins * S;
     unsigned long long* my_cnt = kcnt + (size_t)e * n_bins;
     int t = 0;
     long long row_hint = 0;
@@ -842,7 +878,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x < n_bins * S; x += kEpiThreads) {
       double v = 0.0;
 #pragma unroll
-      for (int w = 0; w < kEpiWarps; ++w) v += kacc[w * n_bins * S + x];
+      for (int w = 0; w < kEpiWarps; ++w) v += slot_value(kacc[w * n_bins * S + x]);
       if (v != 0.0) atomicAdd(a.sums + x, v);
     }
     if (a.pair_counts)
@@ -934,6 +970,25 @@ __global__ void __launch_bounds__(256) pack_tc_kernel(const uint32_t* __restrict
 // ---------------------------------------------------------------------------
 using pgld::tchost::get_encode;
 using pgld::tchost::make_map;
+
+// The register split of the band kernel (setmaxnreg) needs the launch's
+// total: 384 threads x 168 registers.  A build that allocated fewer would
+// make the epilogue warps' increase wait forever, so it is never launched.
+static int check_launch_regs(pgld_context* h, const void* kern) {
+#if PGLD_TC_MAXNREG
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kern);
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc attributes");
+  if (fa.numRegs != 168)
+    return pgld_fail(h, PGLD_ERR_UNSUPPORTED,
+                     "band_tc_kernel built with %d registers per thread; its register split "
+                     "needs 168", fa.numRegs);
+#else
+  (void)h;
+  (void)kern;
+#endif
+  return PGLD_OK;
+}
 
 int pgld_tc_supported(pgld_context* h, const pgld_hap_panel* panel) {
   if (panel->n_pops < 1 || panel->n_pops > 2) return 0;
@@ -1063,6 +1118,8 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
                   ? band_tc_kernel<1, pgld::kModePairs>
                   : (P == 1 ? band_tc_kernel<1, pgld::kModeBinned> : band_tc_kernel<2, pgld::kModeBinned>);
   if (mode == pgld::kModeWindows) kern = band_tc_kernel<1, pgld::kModeWindows>;
+  rc = check_launch_regs(h, (const void*)kern);
+  if (rc) return rc;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_tc smem attribute");
   pgld_time_begin(h, st);
@@ -1184,6 +1241,8 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
   prm.stages = stages;
   const size_t smem = (size_t)stages * kStageBytes + fixed;
   auto kern = band_tc_kernel<1, pgld::kModeWindows>;
+  rc = check_launch_regs(h, (const void*)kern);
+  if (rc) return rc;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "tc windows smem attribute");
   pgld_time_begin(h, st);
