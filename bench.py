@@ -398,6 +398,14 @@ def run_gpu(args, pool, cores):
         return world * n_pairs * args.steps / total, step_ms, kern_ms, clk
 
     value, step_ms, kern_ms, clk = timed(args.form)
+    if args.kernel_only:
+        # profiling runs: the timed steps only (no peak probe, comparison,
+        # end-to-end leg or CPU baseline around the captured launches)
+        if rank == 0:
+            print(json.dumps({"workload": args.workload, "form": args.form, "value": value,
+                              "unit": "pairs/s", "ms_per_step": float(np.mean(step_ms)),
+                              "kernel_ms": float(np.mean(kern_ms[1] or kern_ms[0]))}), flush=True)
+        return
     compare = None
     if not args.no_compare:
         other = "plain" if args.form == "tc" else "tc"
@@ -729,8 +737,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-pairs-per-worker", type=int, default=400_000)
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of one block")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="time the steps only (for profiler captures); implies --no-cpu --no-parity")
     ap.add_argument("--parity-pairs", type=int, default=200_000)
     args = ap.parse_args()
+    if args.kernel_only:
+        args.no_cpu = args.no_parity = args.no_compare = True
     rank, world, _ = rank_info()
     cores = host_cores()
     # the oracle's process pool starts before the first GPU call (spawn)
