@@ -222,7 +222,7 @@ __device__ __forceinline__ float warp_totals(const float (&v)[S], int lane) {
   return t;
 }
 #ifndef PGLD_TC_SLOTS_F64
-#define PGLD_TC_SLOTS_F64 0
+#define PGLD_TC_SLOTS_F64 1
 #endif
 #if PGLD_TC_SLOTS_F64
 typedef double Slot;
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && !*abort_flag; ++p) {
           const CUtensorMap* map = p == 0 ? &map0 : &map1;
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
+            if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
               set_abort(ctrl, a.status, 3002);
               break;
             }
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
+        if (!mbar_wait_poll(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && ok; ++p) {
           const uint32_t d = tmem_base + (uint32_t)(acc * 256 + p * 128);
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
+            if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
               set_abort(ctrl, a.status, 3004);
               ok = false;
               break;

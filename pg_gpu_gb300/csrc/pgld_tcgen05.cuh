@@ -83,13 +83,14 @@ __device__ __forceinline__ bool mbar_test(uint64_t* b, uint32_t parity) {
 }
 // bounded polling wait for the single producer / MMA threads, whose stages
 // are short: reacts to a completed phase within a few cycles (no suspension);
-// false once ~2 s of SM clock passed or another role aborted
+// false once `limit` cycles of SM clock passed or another role aborted
 __device__ __forceinline__ bool mbar_wait_poll(uint64_t* b, uint32_t parity,
-                                               volatile int* abort_flag) {
+                                               volatile int* abort_flag,
+                                               long long limit = kWaitCycles) {
   const long long t0 = clock64();
   for (long long k = 0; k < kSpinLimit; ++k) {
     if (mbar_test(b, parity)) return true;
-    if ((k & 63) == 63 && (*abort_flag || clock64() - t0 > kWaitCycles)) return false;
+    if ((k & 63) == 63 && (*abort_flag || clock64() - t0 > limit)) return false;
   }
   return false;
 }
