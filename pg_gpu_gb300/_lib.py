@@ -117,6 +117,7 @@ _SIGS = {
     "pgld_prune_unlinked": ([_P, _P, _P, _I64, _I32, _I32, _D, _P], ctypes.c_int),
     "pgld_set_kernel_timing": ([_P, _I32], ctypes.c_int),
     "pgld_set_test_fault": ([_P, _I32], ctypes.c_int),
+    "pgld_set_tc_config": ([_P, _I32, _I32], ctypes.c_int),
     "pgld_kernel_times": ([_P, _P, _I32, ctypes.POINTER(_I32)], ctypes.c_int),
     "pgld_tc_mma_rate": ([_P, _I32, _I64, _I32, ctypes.POINTER(ctypes.c_float),
                           ctypes.POINTER(_D), _P], ctypes.c_int),

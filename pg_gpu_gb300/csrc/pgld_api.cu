@@ -89,6 +89,16 @@ extern "C" int pgld_set_test_fault(pgld_handle h, int32_t kind) {
   return PGLD_OK;
 }
 
+extern "C" int pgld_set_tc_config(pgld_handle h, int32_t layout, int32_t max_stages) {
+  if (!h) return pgld_fail(nullptr, PGLD_ERR_INVALID_ARG, "pgld_set_tc_config: NULL handle");
+  if (layout < 0 || layout > 2 || max_stages < 0)
+    return pgld_fail(h, PGLD_ERR_INVALID_ARG, "pgld_set_tc_config: layout %d, max_stages %d", layout,
+                     max_stages);
+  h->tc_layout = layout;
+  h->tc_stages_cap = max_stages;
+  return PGLD_OK;
+}
+
 extern "C" int pgld_set_kernel_timing(pgld_handle h, int32_t on) {
   if (!h) return pgld_fail(nullptr, PGLD_ERR_INVALID_ARG, "pgld_set_kernel_timing: NULL handle");
   h->timing = on != 0;

@@ -19,8 +19,11 @@ using pgld::i64;
 
 namespace pgld {
 
+// tiles of `tile` SNPs (rows) x `col_tile` SNPs (columns; a multiple of
+// `tile`): row block b owns the column blocks from the one holding its first
+// SNP to the one holding the last j paired with its last SNP
 __global__ void band_items_kernel(const double* __restrict__ pos, i64 n_snp, double max_dist,
-                                  i64 n_blocks, int tile, i64* __restrict__ items) {
+                                  i64 n_blocks, int tile, int col_tile, i64* __restrict__ items) {
   for (i64 b = (i64)blockIdx.x * blockDim.x + threadIdx.x; b < n_blocks;
        b += (i64)gridDim.x * blockDim.x) {
     i64 last = min(n_snp - 1, b * tile + tile - 1);
@@ -31,16 +34,18 @@ __global__ void band_items_kernel(const double* __restrict__ pos, i64 n_snp, dou
       if (pos[mid] <= lim) lo = mid + 1; else hi = mid;
     }
     i64 jhi = lo - 1;  // last j paired with `last` (>= last)
-    i64 bj_hi = max(b, jhi / tile);
-    items[b] = bj_hi - b + 1;
+    const i64 bj_lo = (b * tile) / col_tile;
+    i64 bj_hi = max(bj_lo, jhi / col_tile);
+    items[b] = bj_hi - bj_lo + 1;
   }
 }
 
 int band_schedule(pgld_context* h, const double* pos, i64 n_snp, double max_dist, i64* items,
-                  void* scratch, size_t scratch_bytes, cudaStream_t st, int tile) {
+                  void* scratch, size_t scratch_bytes, cudaStream_t st, int tile, int col_tile) {
   i64 nb = (n_snp + tile - 1) / tile;
+  if (col_tile <= 0) col_tile = tile;
   unsigned blocks = (unsigned)std::max<i64>(1, std::min<i64>((nb + 255) / 256, h->n_sm * 4));
-  band_items_kernel<<<blocks, 256, 0, st>>>(pos, n_snp, max_dist, nb, tile, items);
+  band_items_kernel<<<blocks, 256, 0, st>>>(pos, n_snp, max_dist, nb, tile, col_tile, items);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_items_kernel");
   return exclusive_scan_i64(h, items, nb, scratch, scratch_bytes, st);

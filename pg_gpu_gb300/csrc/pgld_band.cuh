@@ -58,7 +58,7 @@ __host__ __device__ __forceinline__ long long anchors_of(const BandArgs& a) {
 // exclusively scanned in place (items[n_blocks] = total)
 int band_schedule(pgld_context* h, const double* pos, long long n_snp, double max_dist,
                   long long* items, void* scratch, size_t scratch_bytes, cudaStream_t st,
-                  int tile = kTile);
+                  int tile = kTile, int col_tile = 0);
 int launch_band_plain(pgld_context* h, const BandArgs& a, int mode, cudaStream_t st);
 // the one/two-population kernel with the float32 epilogue (pgld_band_fast.cu)
 bool band_fast_applies(const BandArgs& a, int mode);

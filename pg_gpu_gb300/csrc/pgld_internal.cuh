@@ -29,6 +29,12 @@ struct pgld_context {
   // per-launch timing of the dominant kernel of each call (off by default):
   // event pairs recorded around the launch on the call's stream
   int test_fault = 0;  // pgld_set_test_fault: one-shot hook of the next tensor-core launch
+  // tensor-core configuration (pgld_set_tc_config): layout of the binned
+  // two-population form (0 automatic, 1 64 x 64 tiles with one accumulator
+  // per population, 2 64 x 128 tiles with one combined accumulator) and a cap
+  // on the pipeline stages (0 = as many as shared memory holds)
+  int tc_layout = 0;
+  int tc_stages_cap = 0;
   bool timing = false;
   std::vector<cudaEvent_t> tev;
   int tev_used = 0;

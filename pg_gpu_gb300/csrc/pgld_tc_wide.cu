@@ -1,0 +1,725 @@
+// Tensor-core binned sums of two populations in one contraction (sm_103a).
+//
+// Both populations share one E4M3 operand row per SNP plane: its first K0
+// bytes hold population 0's haplotypes as 1.0 (0x38), the next K1 bytes
+// population 1's as 64.0 (0x68).  The dot product of two such rows is
+// v = c0 + 4096 c1, c_p the joint count of population p; with at most 2,047
+// haplotypes per population v < 2^23 is an exact float32 integer and
+//   c1 = round-to-nearest(v / 4096)  (c0 / 4096 < 0.5),  c0 = v - 4096 c1.
+// One accumulator therefore holds both populations' counts, and a tile of
+// 64 SNPs i x 128 SNPs j -- an M = 128 (64 SNPs x carrier / reference
+// plane) by N = 256 (128 SNPs x 2 planes) MMA -- takes 256 TMEM columns,
+// so two accumulator buffers fit in the 512 columns.  Against the 64 x 64
+// two-accumulator form this moves 96 instead of 128 operand bytes through
+// shared memory per pair, and each 48 KB pipeline stage carries twice the
+// tensor work (four M128 N256 K32 MMAs), which keeps the tensor pipe fed
+// across the latency of the stage hand-offs.
+//
+// Roles (one CTA per SM, 384 threads):
+//   warp 0      TMA producer: A box 128 rows x 128 B, B box 256 rows x 128 B
+//               (SWIZZLE_128B) per K chunk into a ring of 48 KB stages
+//   warp 1      allocates TMEM; one lane issues tcgen05.mma M128 N256 K32
+//               (kind::f8f6f4) into accumulator buffer t % 2
+//   warps 4-11  epilogue: warp e owns TMEM lane quarter e % 4 (16 SNPs i)
+//               and column half e / 4 (64 SNPs j) as two 16 x 32 sub-tiles;
+//               decode, float32 statistics, float64 bin slots
+// Every mbarrier wait is bounded; on expiry the kernel records an error code
+// in the status word, drains its own copies and MMAs, frees TMEM and returns.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+
+#include "pgld_band.cuh"
+#include "pgld_epilogue.cuh"
+#include "pgld_epilogue2.cuh"
+#include "pgld_internal.cuh"
+#include "pgld_scan.cuh"
+#include "pgld_tc_common.cuh"
+#include "pgld_tcgen05.cuh"
+
+namespace pgld {
+namespace tcw {
+
+using namespace pgld::tc;
+
+constexpr int kRowSnp = 64;    // SNPs i per tile (A: 128 operand rows)
+constexpr int kColSnp = 128;   // SNPs j per tile (B: 256 operand rows)
+constexpr int kBoxA = 128 * kKChunk;           // 16 KB
+constexpr int kBoxB = 256 * kKChunk;           // 32 KB
+constexpr int kStage = kBoxA + kBoxB;          // 48 KB
+constexpr int kEpiWarps = 8;
+constexpr int kEpiThreads = kEpiWarps * 32;
+constexpr int kThreads = (4 + kEpiWarps) * 32;
+constexpr int kSlotSets = 4;   // bin slot sets, each shared by two epilogue warps
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kOne64 = 0x68;  // E4M3 64.0
+// instruction descriptor: D f32, A/B E4M3, both K-major, N = 256, M = 128
+constexpr uint32_t kIdescW = (1u << 4) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr int kS = 15;         // statistics of two populations
+
+struct Params {
+  int kchunks;                 // K chunks of 128 bytes (both populations)
+  long long n_snp;
+  long long n_anchor;          // pairs whose first SNP lies below n_anchor
+  const double* pos;
+  double max_dist;
+  const double* bcoord;
+  const double* bins;
+  int n_bins;
+  const long long* item_off;   // [n_rb + 1] tiles of each 64-SNP row block
+  long long n_rb, n_cb;        // 64-SNP row blocks, 128-SNP column blocks
+  double* sums;
+  int64_t* pair_counts;
+  int32_t* status;
+  int stages;
+  int nmax;
+  const int* ipos;
+  const int* ipos_bad;
+  long long wait_cycles;
+  int no_copies;               // test hook: the TMA producer issues nothing
+};
+
+__device__ __forceinline__ void mma_w(uint32_t d, uint64_t a, uint64_t b, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+      "l"(a), "l"(b), "r"(kIdescW), "r"(accum)
+      : "memory");
+}
+
+// row block of a work item, stepping forward from the previous one
+__device__ __forceinline__ long long row_of(const Params& a, long long item, long long& hint) {
+  long long lo = hint;
+  int steps = 0;
+  while (lo + 1 < a.n_rb && a.item_off[lo + 1] <= item && steps < 4) {
+    ++lo;
+    ++steps;
+  }
+  if (steps == 4) {
+    long long hi = a.n_rb;
+    while (hi - lo > 1) {
+      const long long mid = (lo + hi) >> 1;
+      if (a.item_off[mid] <= item) lo = mid; else hi = mid;
+    }
+  }
+  hint = lo;
+  return lo;
+}
+
+// the decoded counts of one population, two pairs (.x, .y)
+struct Counts2 {
+  float2 c1, c2, c3, c4;
+};
+
+// v = c0 + 4096 c1 (exact) -> (c0, c1)
+__device__ __forceinline__ void split2(float2 v, float2& lo, float2& hi) {
+  const float2 u = fast2::vfma(v, fast2::vs(1.0f / 4096.0f), fast2::vs(12582912.0f));
+  hi = fast2::vsub(u, fast2::vs(12582912.0f));
+  lo = fast2::vfma(hi, fast2::vs(-4096.0f), v);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    band_wide_kernel(const __grid_constant__ CUtensorMap map_a,
+                     const __grid_constant__ CUtensorMap map_b, Params a) {
+  extern __shared__ unsigned char smem_dyn[];
+  unsigned char* base = smem_dyn + ((1024 - (smem_u32(smem_dyn) & 1023)) & 1023);
+  const int stages = a.stages;
+  unsigned char* ring = base;
+  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ring + (size_t)stages * kStage);
+  double* sbins = reinterpret_cast<double*>(ctrl + 1);
+  int* thr = reinterpret_cast<int*>(sbins + (kMaxBins + 1));
+  double* kacc = reinterpret_cast<double*>(thr + (kMaxBins + 2));  // [kSlotSets][n_bins][kS]
+  unsigned long long* kcnt =
+      reinterpret_cast<unsigned long long*>(kacc + kSlotSets * a.n_bins * kS);  // [sets][n_bins]
+  unsigned char* tables_u8 = reinterpret_cast<unsigned char*>(kcnt + kSlotSets * a.n_bins);
+  tables_u8 += (16 - (smem_u32(tables_u8) & 15)) & 15;
+  float* tables = reinterpret_cast<float*>(tables_u8);
+  const float4* T4 = reinterpret_cast<const float4*>(tables);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n_bins = a.n_bins;
+  volatile int* abort_flag = &ctrl->abort_flag;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&ctrl->full[s], 1);
+      mbar_init(&ctrl->empty[s], 1);
+    }
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&ctrl->tfull[s], 1);
+      mbar_init(&ctrl->tempty[s], kEpiWarps);
+    }
+    mbar_init(&ctrl->drain, 1);
+    ctrl->abort_flag = 0;
+    ctrl->produced = 0;
+    ctrl->consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ctrl->tmem_base)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (warp >= 4) {
+    const int t = threadIdx.x - 128;
+    for (int x = t; x < kSlotSets * n_bins * kS; x += kEpiThreads) kacc[x] = 0.0;
+    for (int x = t; x < kSlotSets * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
+    for (int x = t; x <= a.nmax; x += kEpiThreads)
+      fast::recip_entry(x, tables + 4 * x, tables + 4 * x + 1, tables + 4 * x + 2,
+                        tables + 4 * x + 3);
+    for (int x = t; x <= n_bins; x += kEpiThreads) {
+      const double b = a.bins[x];
+      sbins[x] = b;
+      const double cb = ceil(b);
+      thr[x] = cb > 2147483647.0 ? 2147483647 : (cb < -2147483647.0 ? -2147483647 : (int)cb);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = ctrl->tmem_base;
+
+  long long n_items = a.item_off[a.n_rb];
+  if (n_items < 0 || n_items > a.n_rb * a.n_cb) {
+    if (threadIdx.x == 0) set_abort(ctrl, a.status, 3001);
+    n_items = 0;
+  }
+  if (n_items > 0 && a.n_anchor < a.n_snp) n_items = a.item_off[(a.n_anchor + kRowSnp - 1) / kRowSnp];
+
+  if (warp < 4) {
+    if (warp == 0 && lane == 0) {
+      // ---------------- TMA producer ----------------
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued = 0;
+      long long hint = 0;
+      const long long n_copy_items = a.no_copies ? 0 : n_items;
+      for (long long item = blockIdx.x; item < n_copy_items && !*abort_flag; item += gridDim.x) {
+        const long long bi = row_of(a, item, hint);
+        const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
+        const int yi = (int)(2 * bi * kRowSnp), yj = (int)(2 * bj * kColSnp);
+        for (int kc = 0; kc < a.kchunks; ++kc) {
+          if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
+            set_abort(ctrl, a.status, 3002);
+            break;
+          }
+          mbar_expect_tx(&ctrl->full[stage], kStage);
+          unsigned char* sa = ring + (size_t)stage * kStage;
+          tma_load_2d(sa, &map_a, &ctrl->full[stage], kc * kKChunk, yi);
+          tma_load_2d(sa + kBoxA, &map_b, &ctrl->full[stage], kc * kKChunk, yj);
+          ++issued;
+          if (++stage == stages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      if (*abort_flag) {
+        // drain: every issued copy lands before the CTA may exit
+        const int consumed = *(volatile int*)&ctrl->consumed;
+        int st2 = consumed % stages;
+        uint32_t ph2 = (uint32_t)((consumed / stages) & 1);
+        for (int k = consumed; k < issued; ++k) {
+          mbar_wait_drain(&ctrl->full[st2], ph2);
+          if (++st2 == stages) {
+            st2 = 0;
+            ph2 ^= 1;
+          }
+        }
+      }
+    } else if (warp == 1 && lane == 0) {
+      // ---------------- MMA issuer ----------------
+      int stage = 0;
+      uint32_t phase = 0;
+      int t = 0;
+      int consumed = 0;
+      bool any = false;
+      for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
+        const int acc = t & 1;
+        const uint32_t aph = (uint32_t)((t >> 1) & 1);
+        if (!mbar_wait_poll(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
+          set_abort(ctrl, a.status, 3003);
+          break;
+        }
+        tc_fence_after();
+        bool ok = true;
+        const uint32_t d = tmem_base + (uint32_t)(acc * 256);
+        for (int kc = 0; kc < a.kchunks; ++kc) {
+          if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
+            set_abort(ctrl, a.status, 3004);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = smem_u32(ring + (size_t)stage * kStage);
+          const uint64_t da = smem_desc(sa), db = smem_desc(sa + kBoxA);
+#pragma unroll
+          for (int k = 0; k < kKChunk / 32; ++k)
+            mma_w(d, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), (kc | k) != 0);
+          mma_commit(&ctrl->empty[stage]);
+          any = true;
+          *(volatile int*)&ctrl->consumed = ++consumed;
+          if (++stage == stages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (!ok) break;
+        mma_commit(&ctrl->tfull[acc]);
+      }
+      if (*abort_flag && any) {
+        // drain: every issued MMA completes before TMEM is freed
+        mma_commit(&ctrl->drain);
+        mbar_wait_drain(&ctrl->drain, 0);
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int e = warp - 4;
+    const int quarter = warp & 3;
+    const int half = e >> 2;
+    const double maxd = a.max_dist;
+    const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
+    const bool use_int = (a.bcoord == nullptr) && (*a.ipos_bad == 0);
+    double* my_acc = kacc + (size_t)(e & (kSlotSets - 1)) * n_bins * kS;
+    unsigned long long* my_cnt = kcnt + (size_t)(e & (kSlotSets - 1)) * n_bins;
+    auto slot_add = [&](int bin, int k, float v) { atomicAdd(my_acc + bin * kS + k, (double)v); };
+    auto cnt_add = [&](int bin, unsigned long long v) { atomicAdd(my_cnt + bin, v); };
+    int t = 0;
+    long long hint = 0;
+    for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
+      const int acc = t & 1;
+      const uint32_t aph = (uint32_t)((t >> 1) & 1);
+      const long long bi = row_of(a, item, hint);
+      const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
+      const long long i0 = bi * kRowSnp, j0 = bj * kColSnp;
+      const long long si0 = i0 + 16 * quarter;
+      const long long ib = si0 + (lane >> 2);  // the lane's SNP i of row half 0 (half 1: + 8)
+      bool waited = false;
+
+#pragma unroll 1
+      for (int sh = 0; sh < 2; ++sh) {
+        // the warp's 16 x 32 sub-tile: i in si0 + [0, 16), j in sj0 + [0, 32)
+        const long long sj0 = j0 + 64 * half + 32 * sh;
+        const uint32_t colb = (uint32_t)(acc * 256 + half * 128 + sh * 64);
+        // classify: 0 one bin, 1 two adjacent bins, 2 general
+        int mode = 2, b0 = -1, thr_mid = 0;
+        if (use_int && sj0 >= si0 + 16 && sj0 + 31 < a.n_snp && si0 + 15 < a.n_anchor) {
+          const int dmin = a.ipos[sj0] - a.ipos[si0 + 15];
+          const int dmax = a.ipos[sj0 + 31] - a.ipos[si0];
+          if (dmax <= maxd_int) {
+            const int blo = bin_of_int(thr, n_bins, dmin);
+            const int bhi = bin_of_int(thr, n_bins, dmax);
+            if (blo >= 0 && bhi == blo) {
+              mode = 0;
+              b0 = blo;
+            } else if (blo >= 0 && bhi == blo + 1) {
+              mode = 1;
+              b0 = blo;
+              thr_mid = thr[bhi];
+            }
+          }
+        }
+        // positions of the lane's SNPs for the sub-tiles that bin per pair
+        // (rows ib, ib + 8; columns sj0 + 8 g + 2 (lane % 4) + y)
+        int bp_i0 = 0, bp_i1 = 0, bp_j[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) bp_j[q] = 0;
+        if (use_int && mode != 0) {
+          bp_i0 = ib < a.n_snp ? a.ipos[ib] : 0;
+          bp_i1 = ib + 8 < a.n_snp ? a.ipos[ib + 8] : 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const long long jq = sj0 + 8 * (q >> 1) + 2 * (lane & 3) + (q & 1);
+            bp_j[q] = jq < a.n_snp ? a.ipos[jq] : 0;
+          }
+        }
+        if (!waited) {
+          bool ready = true;
+          if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag, a.wait_cycles);
+          ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
+          if (!ready) {
+            if (lane == 0) set_abort(ctrl, a.status, 3005);
+            break;
+          }
+          tc_fence_after();
+          waited = true;
+        }
+
+        // four steps (row half hh, column pair gp) of 8 x 16 SNPs: one
+        // 16x256b TMEM load gives thread t both planes of SNP i = t / 4 of
+        // its 8-SNP row group against SNPs 2 (t % 4), 2 (t % 4) + 1 of two
+        // 8-SNP column groups, each value both populations' count
+        auto steps = [&](auto&& body) {
+#pragma unroll 1
+          for (int c = 0; c < 4; ++c) {
+            const int hh = c & 1, gp = c >> 1;
+            uint32_t r[16];
+            tmem_ld16x256_x4(tmem_base + ((uint32_t)(quarter * 32 + hh * 16) << 16) + colb +
+                                 (uint32_t)(gp * 32),
+                             r);
+            tmem_wait_ld();
+            if (sh == 1 && c == 3) {
+              tc_fence_before();
+              __syncwarp();
+              if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
+            }
+            auto u2 = [](uint32_t x, uint32_t y) {
+              return make_float2(__uint_as_float(x), __uint_as_float(y));
+            };
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+              const int o = 8 * g;
+              float2 n11[2], n10[2], n01[2], n00[2];
+              split2(u2(r[o], r[o + 1]), n11[0], n11[1]);
+              split2(u2(r[o + 4], r[o + 5]), n10[0], n10[1]);
+              split2(u2(r[o + 2], r[o + 3]), n01[0], n01[1]);
+              split2(u2(r[o + 6], r[o + 7]), n00[0], n00[1]);
+              const fast2::Pop p0 = fast2::make(n11[0], n10[0], n01[0], n00[0]);
+              const fast2::Pop p1 = fast2::make(n11[1], n10[1], n01[1], n00[1]);
+              body(hh, 2 * gp + g, p0, p1);
+            }
+          }
+        };
+        auto jx_of = [&](int g) { return sj0 + 8 * g + 2 * (lane & 3); };
+        auto jpos = [&](int g, int y) {
+          const int a0 = y ? bp_j[1] : bp_j[0], a1 = y ? bp_j[3] : bp_j[2];
+          const int a2 = y ? bp_j[5] : bp_j[4], a3 = y ? bp_j[7] : bp_j[6];
+          return g == 0 ? a0 : g == 1 ? a1 : g == 2 ? a2 : a3;
+        };
+
+        if (mode == 0) {
+          // one bin: packed sums, each statistic's reciprocal factor fused
+          float2 acc2[kS];
+#pragma unroll
+          for (int s = 0; s < kS; ++s) acc2[s] = make_float2(0.f, 0.f);
+          steps([&](int, int, const fast2::Pop& p0, const fast2::Pop& p1) {
+            fast2::stats2_to(p0, p1, T4,
+                             [&](int k, float2 num, float2 sc) { acc2[k] = fast2::vfma(num, sc, acc2[k]); });
+          });
+          float v[kS];
+#pragma unroll
+          for (int s = 0; s < kS; ++s) v[s] = acc2[s].x + acc2[s].y;
+          const float tot = warp_totals<kS>(v, lane);
+          constexpr int sh_t = totals_shift<kS>();
+          const int k = lane >> sh_t;
+          if ((lane & ((1 << sh_t) - 1)) == 0 && k < kS) slot_add(b0, k, tot);
+          if (lane == 31) cnt_add(b0, 512ull);
+        } else if (mode == 1) {
+          // two adjacent bins split at thr_mid
+          float acc_lo[kS], acc_hi[kS];
+#pragma unroll
+          for (int s = 0; s < kS; ++s) acc_lo[s] = acc_hi[s] = 0.f;
+          int n_hi = 0;
+          steps([&](int hh, int g, const fast2::Pop& p0, const fast2::Pop& p1) {
+            const int ipi = hh ? bp_i1 : bp_i0;
+            const bool up0 = (jpos(g, 0) - ipi) >= thr_mid;
+            const bool up1 = (jpos(g, 1) - ipi) >= thr_mid;
+            const float2 fu = make_float2(up0 ? 1.f : 0.f, up1 ? 1.f : 0.f);
+            const float2 fl = make_float2(up0 ? 0.f : 1.f, up1 ? 0.f : 1.f);
+            n_hi += (up0 ? 1 : 0) + (up1 ? 1 : 0);
+            fast2::stats2_to(p0, p1, T4, [&](int kk, float2 num, float2 sc) {
+              const float2 st = fast2::vmul(num, sc);
+              acc_hi[kk] = fmaf(fu.x, st.x, fmaf(fu.y, st.y, acc_hi[kk]));
+              acc_lo[kk] = fmaf(fl.x, st.x, fmaf(fl.y, st.y, acc_lo[kk]));
+            });
+          });
+          constexpr int sh_t = totals_shift<kS>();
+          const int k = lane >> sh_t;
+          const bool leader = (lane & ((1 << sh_t) - 1)) == 0 && k < kS;
+          const float tlo = warp_totals<kS>(acc_lo, lane);
+          if (leader) slot_add(b0, k, tlo);
+          const float thi = warp_totals<kS>(acc_hi, lane);
+          if (leader) slot_add(b0 + 1, k, thi);
+          const int hi_total = __reduce_add_sync(0xffffffffu, n_hi);
+          if (lane == 31) {
+            cnt_add(b0, (unsigned long long)(512 - hi_total));
+            cnt_add(b0 + 1, (unsigned long long)hi_total);
+          }
+        } else {
+          // general (diagonal and band-edge sub-tiles, short distances,
+          // non-integer positions): per step, the bins of the lane's two
+          // pairs; steps over at most two adjacent bins go to running sums
+          // of bins (key, key + 1), the others take one warp total per bin
+          float acc_lo[kS], acc_hi[kS];
+#pragma unroll
+          for (int s = 0; s < kS; ++s) acc_lo[s] = acc_hi[s] = 0.f;
+          int key = -1, n_lo = 0, n_hi = 0;
+          constexpr int sh_t = totals_shift<kS>();
+          const int kl = lane >> sh_t;
+          const bool leader = (lane & ((1 << sh_t) - 1)) == 0 && kl < kS;
+          auto flush = [&]() {
+            if (key < 0) return;
+            const float tlo = warp_totals<kS>(acc_lo, lane);
+            if (leader) slot_add(key, kl, tlo);
+            const int tl = __reduce_add_sync(0xffffffffu, n_lo);
+            const int th = __reduce_add_sync(0xffffffffu, n_hi);
+            if (th) {
+              const float thi = warp_totals<kS>(acc_hi, lane);
+              if (leader) slot_add(key + 1, kl, thi);
+            }
+            if (lane == 31) {
+              cnt_add(key, (unsigned long long)tl);
+              if (th) cnt_add(key + 1, (unsigned long long)th);
+            }
+#pragma unroll
+            for (int s = 0; s < kS; ++s) acc_lo[s] = acc_hi[s] = 0.f;
+            n_lo = n_hi = 0;
+            key = -1;
+          };
+          auto bin_of = [&](long long is, int ipi, long long j, int jp) -> int {
+            if (!(is < j && j < a.n_snp && is < a.n_anchor)) return -1;
+            if (use_int) {
+              const int d = jp - ipi;
+              return d <= maxd_int ? bin_of_int(thr, n_bins, d) : -1;
+            }
+            const double dp = a.pos[j] - a.pos[is];
+            if (!(dp <= maxd)) return -1;
+            const double d = a.bcoord ? fabs(a.bcoord[j] - a.bcoord[is]) : dp;
+            return bin_of_f64(sbins, n_bins, d);
+          };
+          steps([&](int hh, int g, const fast2::Pop& p0, const fast2::Pop& p1) {
+            const long long jx = jx_of(g);
+            const long long is = ib + 8 * hh;
+            const int ipi = hh ? bp_i1 : bp_i0;
+            const int bx = bin_of(is, ipi, jx, jpos(g, 0)), by = bin_of(is, ipi, jx + 1, jpos(g, 1));
+            const int lo = min(bx < 0 ? 0x7fffffff : bx, by < 0 ? 0x7fffffff : by);
+            const int mn = __reduce_min_sync(0xffffffffu, lo);
+            const int mx = __reduce_max_sync(0xffffffffu, max(bx, by));
+            if (mx < 0) return;
+            if (mx - mn <= 1) {
+              if (mn != key) {
+                flush();
+                key = mn;
+              }
+              const float2 fl = make_float2(bx == key ? 1.f : 0.f, by == key ? 1.f : 0.f);
+              const float2 fu = make_float2(bx == key + 1 ? 1.f : 0.f, by == key + 1 ? 1.f : 0.f);
+              n_lo += (bx == key ? 1 : 0) + (by == key ? 1 : 0);
+              n_hi += (bx == key + 1 ? 1 : 0) + (by == key + 1 ? 1 : 0);
+              fast2::stats2_to(p0, p1, T4, [&](int kk, float2 num, float2 sc) {
+                const float2 st = fast2::vmul(num, sc);
+                acc_hi[kk] = fmaf(fu.x, st.x, fmaf(fu.y, st.y, acc_hi[kk]));
+                acc_lo[kk] = fmaf(fl.x, st.x, fmaf(fl.y, st.y, acc_lo[kk]));
+              });
+              return;
+            }
+            flush();
+            float2 st[kS];
+            fast2::stats2(p0, p1, T4, st);
+#pragma unroll 1
+            for (int hsel = 0; hsel < 2; ++hsel) {
+              const int b = hsel ? by : bx;
+              unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
+              while (pending) {
+                const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
+                const bool mine = (b == bb);
+                const unsigned grp = __ballot_sync(0xffffffffu, mine);
+                float v[kS];
+#pragma unroll
+                for (int s = 0; s < kS; ++s) v[s] = mine ? (hsel ? st[s].y : st[s].x) : 0.f;
+                const float tot = warp_totals<kS>(v, lane);
+                if (leader) slot_add(bb, kl, tot);
+                if (lane == 31) cnt_add(bb, (unsigned long long)__popc(grp));
+                pending &= ~grp;
+              }
+            }
+          });
+          flush();
+        }
+      }
+      if (!waited) break;  // the accumulator wait ran out (recorded above)
+    }
+  }
+
+  // ---------------- teardown ----------------
+  tc_fence_before();
+  __syncthreads();
+  if (warp >= 4 && !ctrl->abort_flag) {
+    const int t = threadIdx.x - 128;
+    for (int x = t; x < n_bins * kS; x += kEpiThreads) {
+      double v = 0.0;
+#pragma unroll
+      for (int w = 0; w < kSlotSets; ++w) v += kacc[w * n_bins * kS + x];
+      if (v != 0.0) atomicAdd(a.sums + x, v);
+    }
+    if (a.pair_counts)
+      for (int x = t; x < n_bins; x += kEpiThreads) {
+        unsigned long long v = 0;
+#pragma unroll
+        for (int w = 0; w < kSlotSets; ++w) v += kcnt[w * n_bins + x];
+        if (v) atomicAdd(reinterpret_cast<unsigned long long*>(a.pair_counts) + x, v);
+      }
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// Both populations' bit planes -> one E4M3 operand (rows grouped by 8 SNPs:
+// row 16g + 8 plane + k is plane `plane` of SNP 8g + k; SNPs past n_snp are
+// zero rows).  Bytes [0, k0) of a row: population 0 (1.0), [k0, k0 + k1):
+// population 1 (64.0).  A block writes 8 rows, a warp one row in 16-byte
+// chunks.
+__global__ void __launch_bounds__(256) pack_wide_kernel(const uint32_t* __restrict__ pl0, int W0,
+                                                        const uint32_t* __restrict__ pl1, int W1,
+                                                        long long n_snp, long long rows_out, int k0,
+                                                        int k1, uint32_t* __restrict__ out) {
+  const long long rowi = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (rowi >= rows_out) return;
+  const int chunks0 = k0 / 16, chunks = (k0 + k1) / 16;
+  uint4* dst = reinterpret_cast<uint4*>(out) + rowi * chunks;
+  const long long r = (rowi >> 4) * 8 + (rowi & 7);
+  const int plane = (int)((rowi >> 3) & 1);
+  const bool live = r < n_snp;
+  const uint32_t* src0 = pl0 + (live ? r : 0) * 2 * W0 + plane * W0;
+  const uint32_t* src1 = pl1 + (live ? r : 0) * 2 * W1 + plane * W1;
+  for (int c = lane; c < chunks; c += 32) {
+    const bool p1 = c >= chunks0;
+    const int h0 = 16 * (p1 ? c - chunks0 : c);
+    const int w = h0 >> 5;
+    const uint32_t one = p1 ? kOne64 : kOne;
+    uint32_t bits = 0u;
+    if (live) {
+      if (!p1 && w < W0) bits = (__ldg(src0 + w) >> (h0 & 31)) & 0xFFFFu;
+      if (p1 && w < W1) bits = (__ldg(src1 + w) >> (h0 & 31)) & 0xFFFFu;
+    }
+    uint32_t v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t nib = (bits >> (4 * q)) & 0xFu;
+      v[q] = (nib & 1u ? one : 0u) | (nib & 2u ? one << 8 : 0u) | (nib & 4u ? one << 16 : 0u) |
+             (nib & 8u ? one << 24 : 0u);
+    }
+    dst[c] = make_uint4(v[0], v[1], v[2], v[3]);
+  }
+}
+
+__global__ void pos_to_int_kernel_w(const double* __restrict__ pos, long long n, int* __restrict__ ipos,
+                                    int* __restrict__ bad) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    const double v = pos[k];
+    const bool ok = (v == rint(v)) && fabs(v) < 1073741824.0;
+    ipos[k] = ok ? (int)v : 0;
+    if (!ok) atomicOr(bad, 1);
+  }
+}
+
+}  // namespace tcw
+}  // namespace pgld
+
+using pgld::tchost::get_encode;
+using pgld::tchost::make_map;
+
+// The combined-population form applies to two populations of at most 2,016
+// haplotypes each (63 words: c0 / 4096 < 0.5) without a validity plane.
+int pgld_tc_wide_supported(const pgld_hap_panel* panel) {
+  if (panel->n_pops != 2) return 0;
+  for (int p = 0; p < 2; ++p)
+    if (panel->valid[p] != nullptr || panel->n_words[p] > 63) return 0;
+  return 1;
+}
+
+int pgld_tc_wide_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
+                        cudaStream_t st) {
+  using namespace pgld::tcw;
+  int rc = get_encode(h);
+  if (rc) return rc;
+  const long long n = panel->n_snp;
+  const long long n_rb = (n + kRowSnp - 1) / kRowSnp;
+  const long long n_cb = (n + kColSnp - 1) / kColSnp;
+  // operand rows: SNPs rounded up to whole 128-SNP column blocks (B boxes
+  // stay inside the matrix), two planes each, grouped by 8 SNPs
+  const long long n_op = n_cb * kColSnp;
+  if (2 * n_op > 2147483647LL) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: too many SNPs");
+  const int k0 = ((panel->n_words[0] * 32 + pgld::tc::kKChunk - 1) / pgld::tc::kKChunk) * pgld::tc::kKChunk;
+  const int k1 = ((panel->n_words[1] * 32 + pgld::tc::kKChunk - 1) / pgld::tc::kKChunk) * pgld::tc::kKChunk;
+  const size_t op_bytes = (size_t)2 * n_op * (k0 + k1);
+  const size_t sb = pgld::scan_scratch_bytes(n_rb);
+  auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+  const size_t off_items = 0, off_scan = al((n_rb + 1) * 8), off_op = off_scan + al(sb),
+               off_ipos = off_op + al(op_bytes), off_bad = off_ipos + al((size_t)n * 4),
+               total = off_bad + 1024;
+  void* ws = nullptr;
+  rc = pgld_workspace(h, total, &ws);
+  if (rc) return rc;
+  char* w = (char*)ws;
+  long long* items = (long long*)(w + off_items);
+  unsigned char* op = (unsigned char*)(w + off_op);
+  {
+    const unsigned blocks = (unsigned)((2 * n_op + 7) / 8);
+    pack_wide_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], panel->n_words[0], panel->planes[1],
+                                             panel->n_words[1], n, 2 * n_op, k0, k1, (uint32_t*)op);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_wide_kernel");
+  }
+  rc = pgld::band_schedule(h, a.pos, n, a.max_dist, items, w + off_scan, sb, st, kRowSnp, kColSnp);
+  if (rc) return rc;
+  int* ipos = (int*)(w + off_ipos);
+  int* ipos_bad = (int*)(w + off_bad);
+  {
+    cudaError_t e = cudaMemsetAsync(ipos_bad, 0, 4, st);
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "memset");
+    unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, h->n_sm * 8));
+    pos_to_int_kernel_w<<<blocks, 256, 0, st>>>(a.pos, n, ipos, ipos_bad);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pos_to_int_kernel");
+  }
+  CUtensorMap map_a, map_b;
+  rc = make_map(h, &map_a, op, 2 * n_op, k0 + k1, 128);
+  if (rc) return rc;
+  rc = make_map(h, &map_b, op, 2 * n_op, k0 + k1, 256);
+  if (rc) return rc;
+
+  Params prm{};
+  prm.kchunks = (k0 + k1) / pgld::tc::kKChunk;
+  prm.n_snp = n;
+  prm.n_anchor = pgld::anchors_of(a);
+  prm.pos = a.pos;
+  prm.max_dist = a.max_dist;
+  prm.bcoord = a.bcoord;
+  prm.bins = a.bins;
+  prm.n_bins = a.n_bins;
+  prm.item_off = items;
+  prm.n_rb = n_rb;
+  prm.n_cb = n_cb;
+  prm.sums = a.sums;
+  prm.pair_counts = a.pair_counts;
+  prm.status = h->dev_status;
+  prm.nmax = 32 * std::max(panel->n_words[0], panel->n_words[1]);
+  prm.ipos = ipos;
+  prm.ipos_bad = ipos_bad;
+  prm.wait_cycles = pgld::tc::kWaitCycles;
+  if (h->test_fault == PGLD_TEST_FAULT_NO_COPIES) {
+    prm.no_copies = 1;
+    prm.wait_cycles = 20000000ll;
+    h->test_fault = 0;
+  }
+  const size_t fixed = sizeof(pgld::tc::Ctrl) + (pgld::kMaxBins + 1) * 8 + (pgld::kMaxBins + 2) * 4 +
+                       (size_t)kSlotSets * a.n_bins * (kS + 1) * 8 +
+                       (size_t)4 * (prm.nmax + 1) * sizeof(float) + 16 + 1024;
+  int max_smem = 0;
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStage);
+  if (h->tc_stages_cap > 0) stages = std::min(stages, h->tc_stages_cap);
+  if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: shared memory");
+  prm.stages = stages;
+  const size_t smem = (size_t)stages * kStage + fixed;
+  auto kern = band_wide_kernel;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_wide smem attribute");
+  pgld_time_begin(h, st);
+  kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map_a, map_b, prm);
+  pgld_time_end(h, st);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_wide_kernel");
+  return PGLD_OK;
+}
