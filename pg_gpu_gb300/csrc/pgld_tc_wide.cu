@@ -39,6 +39,13 @@
 #include "pgld_tc_common.cuh"
 #include "pgld_tcgen05.cuh"
 
+#ifndef PGLD_TCW_MAXNREG
+#define PGLD_TCW_MAXNREG 1
+#endif
+#ifndef PGLD_TCW_CUNROLL
+#define PGLD_TCW_CUNROLL 1
+#endif
+
 namespace pgld {
 namespace tcw {
 
@@ -58,6 +65,7 @@ constexpr uint32_t kOne64 = 0x68;  // E4M3 64.0
 // instruction descriptor: D f32, A/B E4M3, both K-major, N = 256, M = 128
 constexpr uint32_t kIdescW = (1u << 4) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
 constexpr int kS = 15;         // statistics of two populations
+constexpr int kCUnroll = PGLD_TCW_CUNROLL;
 
 struct Params {
   int kchunks;                 // K chunks of 128 bytes (both populations)
@@ -190,7 +198,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (n_items > 0 && a.n_anchor < a.n_snp) n_items = a.item_off[(a.n_anchor + kRowSnp - 1) / kRowSnp];
 
+  // Registers move from the producer / MMA warpgroup (warps 0-3) to the two
+  // epilogue warpgroups: 128 x 56 + 256 x 224 = 384 x 168, the launch's total
+  // (the host launches this kernel only when it was built with 168 registers).
   if (warp < 4) {
+#if PGLD_TCW_MAXNREG
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 56;" ::: "memory");
+#endif
     if (warp == 0 && lane == 0) {
       // ---------------- TMA producer ----------------
       int stage = 0;
@@ -203,7 +217,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
         const int yi = (int)(2 * bi * kRowSnp), yj = (int)(2 * bj * kColSnp);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
+          if (!mbar_wait_nap(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
             set_abort(ctrl, a.status, 3002);
             break;
           }
@@ -241,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait_poll(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
+        if (!mbar_wait_nap(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }
@@ -249,7 +263,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         const uint32_t d = tmem_base + (uint32_t)(acc * 256);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
+          if (!mbar_wait_nap(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
             set_abort(ctrl, a.status, 3004);
             ok = false;
             break;
@@ -278,6 +292,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
+#if PGLD_TCW_MAXNREG
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 224;" ::: "memory");
+#endif
     // ---------------- epilogue ----------------
     const int e = warp - 4;
     const int quarter = warp & 3;
@@ -339,9 +356,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
         if (!waited) {
-          bool ready = true;
-          if (lane == 0) ready = mbar_wait(&ctrl->tfull[acc], aph, abort_flag, a.wait_cycles);
-          ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
+          // every lane waits (no divergent branch around the wait)
+          const bool ready =
+              __all_sync(0xffffffffu, mbar_wait(&ctrl->tfull[acc], aph, abort_flag, a.wait_cycles));
           if (!ready) {
             if (lane == 0) set_abort(ctrl, a.status, 3005);
             break;
@@ -355,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // its 8-SNP row group against SNPs 2 (t % 4), 2 (t % 4) + 1 of two
         // 8-SNP column groups, each value both populations' count
         auto steps = [&](auto&& body) {
-#pragma unroll 1
+#pragma unroll kCUnroll
           for (int c = 0; c < 4; ++c) {
             const int hh = c & 1, gp = c >> 1;
             uint32_t r[16];
@@ -714,6 +731,18 @@ int pgld_tc_wide_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::Band
   prm.stages = stages;
   const size_t smem = (size_t)stages * kStage + fixed;
   auto kern = band_wide_kernel;
+#if PGLD_TCW_MAXNREG
+  {
+    // the register split needs the launch's total (384 x 168): a build that
+    // allocated fewer would make the epilogue's increase wait forever
+    cudaFuncAttributes fa;
+    cudaError_t e0 = cudaFuncGetAttributes(&fa, (const void*)kern);
+    if (e0 != cudaSuccess) return pgld_cuda_fail(h, e0, "band_wide attributes");
+    if (fa.numRegs != 168)
+      return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "band_wide_kernel built with %d registers; its "
+                       "register split needs 168", fa.numRegs);
+  }
+#endif
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_wide smem attribute");
   pgld_time_begin(h, st);

@@ -94,6 +94,21 @@ __device__ __forceinline__ bool mbar_wait_poll(uint64_t* b, uint32_t parity,
   }
   return false;
 }
+// bounded polling wait that naps ~32 ns between probes, so that a waiting
+// producer / MMA thread leaves the issue slots of its sub-partition to the
+// epilogue warps there; false once `limit` cycles passed or another role
+// aborted
+__device__ __forceinline__ bool mbar_wait_nap(uint64_t* b, uint32_t parity,
+                                              volatile int* abort_flag,
+                                              long long limit = kWaitCycles) {
+  const long long t0 = clock64();
+  for (long long k = 0; k < kSpinLimit; ++k) {
+    if (mbar_test(b, parity)) return true;
+    __nanosleep(32);
+    if ((k & 15) == 15 && (*abort_flag || clock64() - t0 > limit)) return false;
+  }
+  return false;
+}
 // drain wait: bounded by time only
 __device__ __forceinline__ void mbar_wait_drain(uint64_t* b, uint32_t parity) {
   const long long t0 = clock64();
