@@ -342,6 +342,12 @@ def run_gpu(args, pool, cores):
     pos_d = _ops.positions_f64(pos)
     _, n_pairs = _ops.band_offsets(pos_d, float(bins[-1]))
     stream = torch.cuda.current_stream()
+    # the tensor-core tile layout and pipeline depth for these sample sizes
+    tuned = None
+    if args.form == "tc" and not args.kernel_only:
+        from pg_gpu_gb300 import autotune
+        W = (H + 31) // 32
+        tuned = autotune.tune("binned2" if cfg["pops"] == 2 else "binned1", [W] * cfg["pops"])
     flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
 
     def step():
@@ -490,6 +496,9 @@ def run_gpu(args, pool, cores):
         "kernel_ms": k_s * 1e3,
         "roofline": roof,
         "parity": parity,
+        "autotune": None if tuned is None else {
+            "choice": {"layout": tuned["choice"][0], "stages": tuned["choice"][1]},
+            "kernel_ms_by_layout_stages": tuned["ms"], "key": tuned["key"]},
         "compare": compare,
     }
     if pool is not None and rank == 0:

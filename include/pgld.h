@@ -259,6 +259,43 @@ int pgld_hap_binned_sums_range(pgld_handle h, const pgld_hap_panel* panel, const
                                int32_t n_bins, int64_t anchor_begin, int64_t anchor_end,
                                double* sums, int64_t* pair_counts, int32_t form, void* stream);
 
+/* Dense all-pairs LD of one population (planes: carrier / reference words
+ * as above, n_words per plane): D_out[i][j] = pAB - p_i p_j and r2_out[i][j]
+ * = D^2 / (p_i (1 - p_i) p_j (1 - p_j)) (0 where that is not positive) with
+ * pAB = n11 / n over the pair's valid haplotypes (0 where n = 0) and p per
+ * site over its valid haplotypes, each rounded operation by operation as the
+ * reference's float64 matrix expressions; zero diagonal; row stride ld
+ * (float64 elements); either output may be NULL.  Replaces
+ * HaplotypeMatrix._pairwise_ld_core / pairwise_LD_v / pairwise_r2
+ * (haplotype_matrix.py:1092-1170) for 0/1/-1 panels. */
+int pgld_hap_pairwise_ld(pgld_handle h, const uint32_t* planes, int32_t n_words, int64_t n_snp,
+                         double* D_out, double* r2_out, int64_t ld, void* stream);
+
+/* Every pair i < j grouped by distance bin (pos[j] - pos[i] in [bins[b],
+ * bins[b + 1]), right-open): its value is the pair's r^2 from the joint
+ * counts of planes (ld_statistics.r_squared, NaN where undefined) or, with
+ * pair_values non-NULL, pair_values[k] of the condensed upper triangle (k =
+ * i (2 n - i - 1) / 2 + j - i - 1); NaN values are skipped.  With values_out
+ * NULL the call counts the pairs of each bin into HOST bin_counts
+ * (synchronises); with values_out non-NULL (device, sum of bin_counts
+ * doubles) it writes the values bin after bin, bin_counts being the counts of
+ * the previous call on the same inputs.  The binning of
+ * HaplotypeMatrix.windowed_r_squared (haplotype_matrix.py:1282-1296). */
+int pgld_pairs_by_bin(pgld_handle h, const uint32_t* planes, int32_t n_words,
+                      const double* pair_values, int64_t n_snp, const double* pos,
+                      const double* bins, int32_t n_bins, int64_t* bin_counts,
+                      double* values_out, void* stream);
+
+/* Order statistics of segments of a device array of non-negative doubles:
+ * segment s is values[seg_offsets[s] .. seg_offsets[s + 1]) (HOST offsets,
+ * n_seg + 1 of them), targets (HOST int64 pairs) name (segment, rank), and
+ * out[t] (HOST) receives the rank-th smallest value (0-based) of the
+ * segment, by radix selection on the device (synchronises).  The per-bin
+ * percentiles of windowed_r_squared (haplotype_matrix.py:1302-1312) are the
+ * linear interpolation of two such order statistics. */
+int pgld_segment_kth(pgld_handle h, const double* values, const int64_t* seg_offsets, int32_t n_seg,
+                     const int64_t* targets, int32_t n_targets, double* out, void* stream);
+
 /* ----------------------------------------------------------------------
  * Genotype (unphased diploid dosage) path.
  *

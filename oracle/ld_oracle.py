@@ -1375,3 +1375,67 @@ def mu_ld(hap, missing_data="include"):
     el = sum(1 for v in l2r.values() if len(v) == 1)
     er = sum(1 for v in r2l.values() if len(v) == 1)
     return float((el / len(l2r) + er / len(r2l)) / 2.0)
+
+
+# --------------------------------------------------------------------------
+# dense all-pairs outputs (HaplotypeMatrix, haplotype_matrix.py:1092-1317)
+# --------------------------------------------------------------------------
+def pairwise_ld_core(hap):
+    """(D, p): D = pAB - p_i p_j with pAB = joint_11 / joint_n over the pair's
+    valid haplotypes and p per site (haplotype_matrix.py:1092-1128)."""
+    h = np.asarray(hap)
+    valid = (h >= 0).astype(np.float64)
+    clean = np.where(h >= 0, h, 0).astype(np.float64)
+    n_valid = valid.sum(axis=0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        p = np.where(n_valid > 0, clean.sum(axis=0) / n_valid, 0.0)
+        joint_n = valid.T @ valid
+        joint_11 = clean.T @ clean
+        p_ab = np.where(joint_n > 0, joint_11 / joint_n, 0.0)
+    return p_ab - np.outer(p, p), p
+
+
+def pairwise_ld_v(hap):
+    """pairwise_LD_v (haplotype_matrix.py:1130-1136): D, zero diagonal."""
+    D, _ = pairwise_ld_core(hap)
+    np.fill_diagonal(D, 0)
+    return D
+
+
+def pairwise_r2(hap):
+    """pairwise_r2, estimator 'r2' (haplotype_matrix.py:1138-1170)."""
+    D, p = pairwise_ld_core(hap)
+    den = np.outer(p * (1 - p), p * (1 - p))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r2 = np.where(den > 0, (D ** 2) / den, 0)
+    np.fill_diagonal(r2, 0)
+    return r2
+
+
+def windowed_r_squared(hap, positions, bins, percentile=50):
+    """windowed_r_squared, estimator 'r2' (haplotype_matrix.py:1235-1317):
+    r^2 of every pair i < j from its joint counts (NaN where undefined),
+    binned by pos[j] - pos[i] (digitize, right-open), numpy percentiles per
+    bin; (result, counts)."""
+    h = np.asarray(hap)
+    m = h.shape[1]
+    ii, jj = np.triu_indices(m, k=1)
+    c, nv = counts_for_pairs(h, ii, jj)
+    r2 = r_squared(c, nv)
+    pos = np.asarray(positions)
+    d = pos[jj] - pos[ii]
+    bins = np.asarray(bins, np.float64)
+    nb = len(bins) - 1
+    b = np.digitize(d, bins) - 1
+    ok = (b >= 0) & (b < nb) & ~np.isnan(r2)
+    pct = np.atleast_1d(percentile)
+    res = np.full((nb, len(pct)), np.nan)
+    cnt = np.zeros(nb, dtype=int)
+    for k in range(nb):
+        sel = r2[ok & (b == k)]
+        cnt[k] = sel.size
+        if sel.size:
+            for q, pc in enumerate(pct):
+                res[k, q] = np.percentile(sel, pc)
+    return (res[:, 0] if res.shape[1] == 1 else res), cnt
+

@@ -93,6 +93,9 @@ _SIGS = {
                               _P], ctypes.c_int),
     "pgld_hap_binned_sums_range": ([_P, ctypes.POINTER(HapPanel), _P, _D, _P, _P, _I32, _I64,
                                     _I64, _P, _P, _I32, _P], ctypes.c_int),
+    "pgld_hap_pairwise_ld": ([_P, _P, _I32, _I64, _P, _P, _I64, _P], ctypes.c_int),
+    "pgld_pairs_by_bin": ([_P, _P, _I32, _P, _I64, _P, _P, _I32, _P, _P, _P], ctypes.c_int),
+    "pgld_segment_kth": ([_P, _P, _P, _I32, _P, _I32, _P, _P], ctypes.c_int),
     "pgld_pack_genotypes": ([_P, _P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
     "pgld_geno_counts_pairs": ([_P, _P, _P, _P, _I32, _I64, _P, _P, _I64, _P, _I64, _P, _P],
                                ctypes.c_int),

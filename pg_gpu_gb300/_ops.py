@@ -260,7 +260,7 @@ def positions_f64(positions):
     return L.as_device(positions, np.float64)
 
 
-def band_pairs(pk, pos_d, max_dist, with_stats=True, form="auto"):
+def band_pairs(pk, pos_d, max_dist, with_stats=True, form="auto", _tuning=False):
     """Fused per-pair outputs of one population over the distance band.
 
     Returns (counts (N,4) int32, n_valid (N,) int32, stats (N,4) float32 =
@@ -269,6 +269,9 @@ def band_pairs(pk, pos_d, max_dist, with_stats=True, form="auto"):
     """
     if form == "auto":
         form = "tc" if tc_applies([pk]) else "plain"
+    if form == "tc" and not _tuning:
+        from . import autotune
+        autotune.apply("pairs", [pk.n_words])
     torch = _torch()
     _, n = band_offsets(pos_d, max_dist)
     dev = pos_d.device
@@ -286,7 +289,7 @@ def band_pairs(pk, pos_d, max_dist, with_stats=True, form="auto"):
 WINDOW_COLUMNS = ("r2", "sigma_d2", "dd", "dz", "pi2", "r2_naive")
 
 
-def window_sums(pk, idx, win_begin, win_end, form="auto"):
+def window_sums(pk, idx, win_begin, win_end, form="auto", _tuning=False):
     """Per-window sums (n_win, 6) float64 and counts (n_win, 3) int64 over
     every pair inside each window (one launch for all windows).
 
@@ -296,6 +299,9 @@ def window_sums(pk, idx, win_begin, win_end, form="auto"):
     "auto" (tensor cores whenever they apply)."""
     if form == "auto":
         form = "tc" if tc_applies([pk]) else "plain"
+    if form == "tc" and not _tuning:
+        from . import autotune
+        autotune.apply("windows", [pk.n_words])
     torch = _torch()
     dev = pk.planes.device
     wb = L.as_device(win_begin, np.int64)
@@ -391,7 +397,8 @@ def tc_applies(pops):
     return len(pops) <= 2 and all(pk.n_words <= 64 and pk.valid_for_n is None for pk in pops)
 
 
-def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto", anchors=None):
+def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto", anchors=None,
+                _tuning=False):
     """(sums (n_bins, n_stats) float64 tensor, pair counts (n_bins,) int64).
 
     form: "tc" (tcgen05 tensor cores), "plain" (AND + popcount) or "auto"
@@ -399,6 +406,9 @@ def binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto", a
     only the pairs whose first SNP lies in [begin, end) are summed."""
     if form == "auto":
         form = "tc" if tc_applies(pops) else "plain"
+    if form == "tc" and not _tuning:
+        from . import autotune
+        autotune.apply("binned2" if len(pops) == 2 else "binned1", [pk.n_words for pk in pops])
     torch = _torch()
     bins_np = np.asarray(bins, dtype=np.float64)
     if bins_np.ndim != 1 or len(bins_np) < 2:
@@ -606,3 +616,111 @@ def geno_binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None):
                                           L.ptr(bc), L.ptr(bins_d), n_bins, L.ptr(sums),
                                           L.ptr(cnt), L.stream_ptr()), h)
     return sums, cnt
+
+
+# --------------------------------------------------------------------------
+# dense all-pairs outputs and distance-binned percentiles
+# --------------------------------------------------------------------------
+def pairwise_ld(pk, want_D=True, want_r2=True):
+    """(D, r2) float64 (m, m) device matrices of one population (either None
+    when not wanted): pgld_hap_pairwise_ld."""
+    torch = _torch()
+    m = pk.n_snp
+    dev = pk.planes.device
+    D = torch.empty((m, m), dtype=torch.float64, device=dev) if want_D else None
+    r2 = torch.empty((m, m), dtype=torch.float64, device=dev) if want_r2 else None
+    if m:
+        h = L.handle()
+        L.check(L.lib().pgld_hap_pairwise_ld(h, L.ptr(pk.planes), pk.n_words, m, L.ptr(D),
+                                             L.ptr(r2), m, L.stream_ptr()), h)
+    return D, r2
+
+
+def pairs_by_bin(pos_d, bins, pk=None, pair_values=None):
+    """(values grouped by bin: float64 device tensor, counts: host int64
+    (n_bins,)) of every pair i < j with a non-NaN value -- its r^2 from the
+    packed population pk, or pair_values (condensed upper triangle, device
+    float64) -- binned by pos[j] - pos[i] (right-open bins)."""
+    torch = _torch()
+    bins_np = np.asarray(bins, dtype=np.float64)
+    if bins_np.ndim != 1 or len(bins_np) < 2:
+        raise ValueError("bins must hold at least two edges")
+    n_bins = len(bins_np) - 1
+    m = pos_d.numel()
+    dev = pos_d.device
+    bins_d = torch.as_tensor(bins_np, device=dev)
+    pv = None if pair_values is None else L.as_device(pair_values, np.float64)
+    if pv is not None and pv.numel() != m * (m - 1) // 2:
+        raise ValueError("pair_values must hold the m (m - 1) / 2 pairs of the upper triangle")
+    counts = np.zeros(n_bins, np.int64)
+    h = L.handle()
+    planes = None if pk is None else pk.planes
+    W = 1 if pk is None else pk.n_words
+    c_ptr = counts.ctypes.data_as(ctypes.c_void_p)
+    L.check(L.lib().pgld_pairs_by_bin(h, L.ptr(planes), W, L.ptr(pv), m, L.ptr(pos_d),
+                                      L.ptr(bins_d), n_bins, c_ptr, None, L.stream_ptr()), h)
+    vals = torch.empty(max(int(counts.sum()), 1), dtype=torch.float64, device=dev)
+    if counts.sum():
+        L.check(L.lib().pgld_pairs_by_bin(h, L.ptr(planes), W, L.ptr(pv), m, L.ptr(pos_d),
+                                          L.ptr(bins_d), n_bins, c_ptr, L.ptr(vals),
+                                          L.stream_ptr()), h)
+        st = torch.zeros(1, dtype=torch.int32)
+        L.check(L.lib().pgld_device_status(h, ctypes.cast(st.data_ptr(), ctypes.POINTER(
+            ctypes.c_int32)), L.stream_ptr()), h)
+        if int(st[0]):
+            raise RuntimeError(f"pairs changed between counting and filling (status {int(st[0])})")
+    return vals[:int(counts.sum())], counts
+
+
+def segment_kth(values, counts, targets):
+    """Host float64 order statistics: targets = [(segment, rank), ...] of the
+    segments of `values` whose lengths are `counts` (pgld_segment_kth)."""
+    off = np.concatenate([[0], np.cumsum(np.asarray(counts, np.int64))]).astype(np.int64)
+    tg = np.ascontiguousarray(np.asarray(targets, np.int64).reshape(-1, 2))
+    out = np.zeros(len(tg), np.float64)
+    if len(tg):
+        h = L.handle()
+        L.check(L.lib().pgld_segment_kth(h, L.ptr(values), off.ctypes.data_as(ctypes.c_void_p),
+                                         len(off) - 1, tg.ctypes.data_as(ctypes.c_void_p),
+                                         len(tg), out.ctypes.data_as(ctypes.c_void_p),
+                                         L.stream_ptr()), h)
+    return out
+
+
+def percentiles_from_order_stats(counts, percentile, kth):
+    """numpy.percentile (method 'linear') of segments of sizes `counts`,
+    computed from the order statistics kth([(segment, rank), ...]) -> values,
+    with numpy's own float64 steps: virtual index (n - 1) q, its floor and the
+    next rank (both the last one at or above n - 1), and the interpolation
+    a + (b - a) g, or b - (b - a)(1 - g) where g >= 0.5.  NaN where a segment
+    is empty.  Returns (n_seg, n_pct)."""
+    counts = np.asarray(counts, np.int64)
+    q = np.true_divide(np.atleast_1d(np.asarray(percentile, np.float64)), 100)
+    res = np.full((len(counts), len(q)), np.nan)
+    plan, targets = [], {}
+    for s, n in enumerate(counts):
+        if n <= 0:
+            continue
+        for k, qq in enumerate(q):
+            v = np.float64(n - 1) * qq
+            prev = np.floor(v)
+            if v >= n - 1:
+                lo = hi = int(n - 1)
+                g = v - np.float64(-1.0)
+            elif v < 0:
+                lo = hi = 0
+                g = v - prev
+            else:
+                lo, hi = int(prev), int(prev) + 1
+                g = v - prev
+            plan.append((s, k, lo, hi, g))
+            targets.setdefault((s, lo), None)
+            targets.setdefault((s, hi), None)
+    keys = list(targets)
+    vals = kth(keys) if keys else []
+    got = dict(zip(keys, vals))
+    for s, k, lo, hi, g in plan:
+        a, b = np.float64(got[(s, lo)]), np.float64(got[(s, hi)])
+        d = b - a
+        res[s, k] = (b - d * (1 - g)) if g >= 0.5 else (a + d * g)
+    return res

@@ -1150,7 +1150,8 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
                        (size_t)4 * (prm.nmax + 1) * sizeof(float) + 1024;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-  const int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStageBytes);
+  int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStageBytes);
+  if (h->tc_stages_cap > 0) stages = std::min(stages, h->tc_stages_cap);
   if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core windows: shared memory");
   prm.stages = stages;
   const size_t smem = (size_t)stages * kStageBytes + fixed;

@@ -386,44 +386,50 @@ class HaplotypeMatrix:
         return out
 
     def windowed_r_squared(self, bp_bins, percentile=50, pop=None, estimator="r2"):
-        """Percentiles of r^2 per distance bin and pair counts (haplotype_matrix.py:1235-1317)."""
-        import torch
+        """Percentiles of r^2 per distance bin and pair counts
+        (haplotype_matrix.py:1235-1317).  The pairs' r^2 are grouped by bin on
+        the device (pgld_pairs_by_bin) and each percentile is interpolated, as
+        numpy.percentile does, between two order statistics found on the
+        device (pgld_segment_kth); nothing per pair reaches the host."""
         if estimator == "rogers_huff":
-            raise NotImplementedError("estimator='rogers_huff' goes through GenotypeMatrix")
-        if estimator != "r2":
+            if pop is not None:
+                raise NotImplementedError(
+                    "windowed_r_squared(estimator='rogers_huff', pop=...) is not implemented; "
+                    "subset the haplotypes first")
+            from .ld_statistics import rogers_huff_r
+            r = rogers_huff_r(self)
+            vals, cnt = _ops.pairs_by_bin(_ops.positions_f64(self._positions), bp_bins,
+                                          pair_values=r * r)
+        elif estimator == "r2":
+            pk = self.packed(pop)
+            if pk.has_other:
+                raise NotImplementedError("windowed_r_squared of non-biallelic codes")
+            vals, cnt = _ops.pairs_by_bin(_ops.positions_f64(self._positions), bp_bins, pk=pk)
+        else:
             raise ValueError(f"Unknown estimator: {estimator!r} (expected 'r2' or 'rogers_huff')")
-        from .ld_statistics import r_squared
-        counts, nv = self.tally_gpu_haplotypes(pop=pop)
-        r2 = r_squared(counts, nv)
-        m = self.num_variants
-        ii, jj = torch.triu_indices(m, m, 1, device=r2.device)
-        pos = _ops.positions_f64(self._positions)
-        d = (pos[jj] - pos[ii]).cpu().numpy()
-        bins = np.asarray(bp_bins, dtype=np.float64)
-        nb = len(bins) - 1
-        b = np.digitize(d, bins) - 1
-        r2c = r2.cpu().numpy()
-        ok = (b >= 0) & (b < nb) & ~np.isnan(r2c)
-        percentile = np.atleast_1d(percentile)
-        res = np.full((nb, len(percentile)), np.nan)
-        pc = np.zeros(nb, dtype=int)
-        for i in range(nb):
-            sel = r2c[ok & (b == i)]
-            pc[i] = sel.size
-            if sel.size:
-                res[i] = np.percentile(sel, percentile)
-        return (res[:, 0] if res.shape[1] == 1 else res), pc
+        res = _ops.percentiles_from_order_stats(
+            cnt, percentile, lambda keys: _ops.segment_kth(vals, cnt, keys))
+        return (res[:, 0] if res.shape[1] == 1 else res), cnt.astype(int)
 
     def pairwise_r2(self, estimator="r2"):
-        """(m, m) r^2 from joint frequencies, zero diagonal (haplotype_matrix.py:1138-1170)."""
+        """(m, m) float64 r^2 with a zero diagonal (haplotype_matrix.py:1138-1170):
+        'r2' from the joint and per-site frequencies on the device
+        (pgld_hap_pairwise_ld); 'rogers_huff' the squared Rogers-Huff r of
+        adjacent-haplotype dosages, NaN set to 0."""
         import torch
+        if estimator == "rogers_huff":
+            from .ld_statistics import rogers_huff_r
+            r = rogers_huff_r(self)
+            m = self.num_variants
+            out = torch.zeros((m, m), dtype=torch.float64, device=r.device)
+            ii, jj = torch.triu_indices(m, m, 1, device=r.device)
+            r2 = torch.nan_to_num(r * r, nan=0.0)
+            out[ii, jj] = r2
+            out[jj, ii] = r2
+            return out
         if estimator != "r2":
             raise ValueError(f"Unknown estimator: {estimator!r} (expected 'r2' or 'rogers_huff')")
-        D, p = self._pairwise_ld_core()
-        pq = p * (1 - p)
-        den = torch.outer(pq, pq)
-        r2 = torch.where(den > 0, D * D / torch.where(den > 0, den, 1.0), 0.0)
-        r2.fill_diagonal_(0)
+        _, r2 = _ops.pairwise_ld(self._dense_packed(), want_D=False, want_r2=True)
         return r2
 
     def locate_unlinked(self, size=100, step=20, threshold=0.1):
@@ -471,31 +477,14 @@ class HaplotypeMatrix:
         return loc.astype(bool)
 
     def pairwise_LD_v(self):
-        D, _ = self._pairwise_ld_core()
-        D.fill_diagonal_(0)
+        """(m, m) float64 D = pAB - pA pB with a zero diagonal
+        (haplotype_matrix.py:1092-1136), on the device (pgld_hap_pairwise_ld)."""
+        D, _ = _ops.pairwise_ld(self._dense_packed(), want_D=True, want_r2=False)
         return D
 
-    def _pairwise_ld_core(self):
-        """D = pAB - pA pB and per-site p from all-pairs counts (haplotype_matrix.py:1092-1130)."""
-        import torch
-        m = self.num_variants
-        counts, nv = self.tally_gpu_haplotypes()
+    def _dense_packed(self):
         pk = self.packed(None)
-        h = self._haplotypes
-        valid = (h >= 0).sum(0).to(torch.float64)
-        p = torch.where(valid > 0, h.clamp(min=0).sum(0).to(torch.float64) /
-                        torch.where(valid > 0, valid, 1.0), 0.0)
-        c = counts.to(torch.float64)
-        n = c.sum(1) if nv is None else nv.to(torch.float64)
-        # joint_n counts hap >= 0 at both sites; with only 0/1/-1 data that is n
         if pk.has_other:
-            raise NotImplementedError("pairwise LD of non-biallelic codes")
-        pab = torch.where(n > 0, c[:, 0] / torch.where(n > 0, n, 1.0), 0.0)
-        ii, jj = torch.triu_indices(m, m, 1, device=c.device)
-        P = torch.zeros((m, m), dtype=torch.float64, device=c.device)
-        P[ii, jj] = pab
-        P[jj, ii] = pab
-        diag = torch.where(valid > 0, h.clamp(min=0).sum(0).to(torch.float64) /
-                           torch.where(valid > 0, valid, 1.0), 0.0)
-        P[torch.arange(m), torch.arange(m)] = diag
-        return P - torch.outer(p, p), p
+            raise NotImplementedError("pairwise LD of non-biallelic codes (apply the biallelic "
+                                      "filter first)")
+        return pk

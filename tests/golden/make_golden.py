@@ -477,6 +477,89 @@ def gen_mu_ld(M):
     np.savez_compressed(os.path.join(HERE, "mu_ld.npz"), **out)
 
 
+def _load_ref_module(mod):
+    """A further reference module under the stub package (after
+    load_haplotype_matrix)."""
+    import importlib.util
+    pkg = sys.modules["pg_gpu"]
+    if hasattr(pkg, mod):
+        return getattr(pkg, mod)
+    path = os.path.join(S.REF_ROOT, "pg_gpu", mod + ".py")
+    spec = importlib.util.spec_from_file_location("pg_gpu." + mod, path)
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["pg_gpu." + mod] = m
+    spec.loader.exec_module(m)
+    setattr(pkg, mod, m)
+    return m
+
+
+def gen_dense(M):
+    """The dense M x M outputs of the reference's HaplotypeMatrix:
+    pairwise_LD_v, pairwise_r2 (estimators 'r2' and 'rogers_huff') and
+    windowed_r_squared (haplotype_matrix.py:1092-1170, 1235-1317), on
+    copying-model panels with and without missing data."""
+    HM = S.load_haplotype_matrix()
+    out = {}
+    cases = [(40, 90, 6, 0.03, 0.0), (64, 150, 8, 0.02, 0.03), (33, 70, 4, 0.05, 0.05),
+             (130, 200, 10, 0.01, 0.0)]
+    for k, (H, m, F, sw, miss) in enumerate(cases):
+        rng = np.random.default_rng(20261230 + k)
+        hap = copying_model(rng, H, m, F, sw, missing=miss)
+        pos = np.sort(rng.choice(50_000, m, replace=False)).astype(np.int64) + 1
+        hm = HM(hap.copy(), pos.copy())
+        out[f"hap{k}"] = hap
+        out[f"pos{k}"] = pos
+        out[f"ldv{k}"] = np.asarray(hm.pairwise_LD_v())
+        out[f"r2_{k}"] = np.asarray(HM(hap.copy(), pos.copy()).pairwise_r2())
+        if H % 2 == 0 and not miss:
+            out[f"rh_{k}"] = np.asarray(HM(hap.copy(), pos.copy()).pairwise_r2(estimator="rogers_huff"))
+        bins = np.array([0.0, 500.0, 2_000.0, 5_000.0, 15_000.0, 40_000.0])
+        res, cnt = HM(hap.copy(), pos.copy()).windowed_r_squared(bins, percentile=[5, 50, 95])
+        out[f"wbins{k}"] = bins
+        out[f"wr2_{k}"] = np.asarray(res)
+        out[f"wcnt{k}"] = np.asarray(cnt)
+        res1, cnt1 = HM(hap.copy(), pos.copy()).windowed_r_squared(bins, percentile=50)
+        out[f"wr2med_{k}"] = np.asarray(res1)
+        if H % 2 == 0 and not miss:
+            resr, cntr = HM(hap.copy(), pos.copy()).windowed_r_squared(
+                bins, percentile=[25, 75], estimator="rogers_huff")
+            out[f"wrh_{k}"] = np.asarray(resr)
+            out[f"wrhcnt{k}"] = np.asarray(cntr)
+    np.savez_compressed(os.path.join(HERE, "dense.npz"), **out)
+
+
+def gen_rbins(M):
+    """moments_ld.compute_ld_statistics with recombination-distance bins
+    (r_bins and rec_map_file, moments_ld.py:164-175, 211-245) from the
+    reference, haplotype and genotype paths, on the IM example panel with a
+    piecewise-linear genetic map (tests/golden/rec_map_im.txt, written here)."""
+    HM = S.load_haplotype_matrix()
+    mld = _load_ref_module("moments_ld")
+    z = np.load(os.path.join(HERE, "moments_im.npz"))
+    hap, pos = z["hap"], z["pos"]
+    rng = np.random.default_rng(20261231)
+    knots = np.arange(0, 1_050_001, 50_000)
+    rates = rng.uniform(0.3, 3.0, len(knots) - 1)  # cM per Mb
+    cm = np.concatenate([[0.0], np.cumsum(rates * np.diff(knots) / 1e6)])
+    path = os.path.join(HERE, "rec_map_im.txt")
+    with open(path, "w") as f:
+        f.write("pos\tMap(cM)\n")
+        for p_, c in zip(knots, cm):
+            f.write(f"{int(p_)}\t{c:.10f}\n")
+    r_bins = np.array([0.0, 1e-6, 3e-6, 1e-5, 3e-5, 1e-4, 3e-4])
+    sets = {"deme0": list(map(int, z["rows0"])), "deme1": list(map(int, z["rows1"]))}
+    out = {"r_bins": r_bins}
+    for tag, geno in (("hap", False), ("geno", True)):
+        hm = HM(hap.copy(), pos.copy(), sample_sets={k: list(v) for k, v in sets.items()})
+        res = mld.compute_ld_statistics(haplotype_matrix=hm, rec_map_file=path,
+                                        pops=["deme0", "deme1"], r_bins=r_bins,
+                                        use_genotypes=geno, report=False)
+        out[f"{tag}_ld"] = np.stack([np.asarray(x, np.float64) for x in res["sums"][:-1]])
+        out[f"{tag}_het"] = np.asarray(res["sums"][-1], np.float64)
+        out[f"{tag}_bins"] = np.asarray(res["bins"], np.float64)
+    np.savez_compressed(os.path.join(HERE, "rbins.npz"), **out)
+
+
 def main():
     M = S.load_reference_modules()
     gen_hap_counts(M)
@@ -491,6 +574,8 @@ def main():
     gen_unlinked(M)
     gen_diploid_ld(M)
     gen_mu_ld(M)
+    gen_dense(M)
+    gen_rbins(M)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz") or f.endswith(".txt"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

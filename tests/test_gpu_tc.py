@@ -263,3 +263,31 @@ def test_bounded_wait_expiry_reports_and_recovers():
         check(hap, pos, rows, bins)
         L.check(L.lib().pgld_device_status(h, ctypes.byref(code), L.stream_ptr()), h)
         assert code.value == 0
+
+
+def test_autotuner_choice_is_cached_and_applied(tmp_path, monkeypatch):
+    # the tuner times every (layout, stages) candidate on a synthetic panel of
+    # the given sample sizes, stores the fastest keyed by (kind, words, GPU),
+    # and calls of that kind then run with it; results do not depend on it
+    import json
+    from pg_gpu_gb300 import autotune
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_cache", None)
+    monkeypatch.setattr(autotune, "_applied", {})
+    r = autotune.tune("binned2", [4, 4], n_snp=3_000, max_dist=2e5)
+    assert r["choice"] in autotune.BINNED2_CANDIDATES
+    assert set(r["ms"]) == {f"{a},{b}" for a, b in autotune.BINNED2_CANDIDATES}
+    saved = json.load(open(tmp_path / "tune.json"))
+    assert saved[r["key"]]["layout"] == r["choice"][0]
+    assert autotune.lookup("binned2", [4, 4]) == r["choice"]
+    # every candidate gives the oracle's sums
+    rng = np.random.default_rng(5)
+    hap = copying_model(rng, 256, 500, 8, 5e-3, missing=0.02)
+    pos = np.sort(rng.choice(300_000, 500, replace=False)).astype(np.int64)
+    rows = [np.arange(128), np.arange(128, 256)]
+    from pg_gpu_gb300 import _lib as L
+    for layout, stages in autotune.BINNED2_CANDIDATES:
+        monkeypatch.setattr(autotune, "lookup", lambda kind, words: (layout, stages))
+        monkeypatch.setattr(autotune, "_applied", {})
+        check(hap, pos, rows, np.logspace(2, 5, 9))
+    L.check(L.lib().pgld_set_tc_config(L.handle(), 0, 0), L.handle())
