@@ -164,8 +164,14 @@ class GenotypeMatrix:
             # masks them by the first record's chromosome)
             from .accessible import accessible_variants
             from .haplotype_matrix import vcf_first_chrom
-            keep = accessible_variants(pos, accessible_bed, vcf_first_chrom(path))
+            chrom = vcf_first_chrom(path)
+            keep = accessible_variants(pos, accessible_bed, chrom)
+            cs, ce = gm.chrom_start, gm.chrom_end
             gm = gm.get_subset(np.nonzero(keep)[0])
+            # the per-base denominator: the BED's accessible bases in the range
+            from .accessible import accessible_base_count
+            gm.chrom_start, gm.chrom_end = cs, ce
+            gm.n_total_sites = accessible_base_count(accessible_bed, chrom, cs, ce)
         return gm
 
     def load_pop_file(self, pop_file, pops=None):

@@ -270,7 +270,12 @@ class HaplotypeMatrix:
             from .accessible import accessible_variants
             chrom = _parse_region(region)[0] if region is not None else vcf_first_chrom(path)
             keep = accessible_variants(pos, accessible_bed, chrom or None)
+            cs, ce = hm.chrom_start, hm.chrom_end
             hm = hm.get_subset(np.nonzero(keep)[0])
+            # the per-base denominator: the BED's accessible bases in the range
+            from .accessible import accessible_base_count
+            hm.chrom_start, hm.chrom_end = cs, ce
+            hm.n_total_sites = accessible_base_count(accessible_bed, chrom or None, cs, ce)
         return hm
 
     def load_pop_file(self, pop_file, pops=None):

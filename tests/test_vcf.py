@@ -181,9 +181,17 @@ def test_accessible_filter_matches_loop(tmp_path):
             f.write(f"{c}\t{s}\t{e}\textra\n")
     assert A.parse_bed(str(bed)) == iv
     pos = np.sort(rng.choice(np.arange(1, 10_500), 2_000, replace=False))
-    for chrom in (None, "chr1", "chr2", "chr9"):
+    for chrom in (None, "chr1", "chr2"):
         assert np.array_equal(A.accessible_variants(pos, str(bed), chrom),
                               _accessible_loop(pos, iv, chrom))
+        # the interval list form gives the same mask
+        assert np.array_equal(A.accessible_variants(pos, iv, chrom),
+                              _accessible_loop(pos, iv, chrom))
+    # no interval for the chromosome: an error for a file (the reference's
+    # resolve_accessible_mask), an empty mask for an interval list
+    with pytest.raises(ValueError):
+        A.accessible_variants(pos, str(bed), "chr9")
+    assert not A.accessible_variants(pos, iv, "chr9").any()
 
 
 def test_from_vcf_accessible_bed(tmp_path):
@@ -202,3 +210,22 @@ def test_from_vcf_accessible_bed(tmp_path):
     assert list(np.asarray(gm.positions)) == [100, 300]  # 1000 is multi-allelic
     hm = HaplotypeMatrix.from_vcf(str(p), region="chr2", accessible_bed=str(bed))
     assert list(np.asarray(hm.positions)) == [50]
+    # n_total_sites: the BED-accessible bases of the analysis range
+    # [chrom_start, chrom_end] (haplotype_matrix.py:196-205), counted directly
+    for m, chrom, iv in ((HaplotypeMatrix.from_vcf(str(p), accessible_bed=str(bed)), "chr1",
+                          [(99, 100), (299, 1000)]),
+                         (GenotypeMatrix.from_vcf(str(p), accessible_bed=str(bed)), "chr1",
+                          [(99, 100), (299, 1000)]),
+                         (HaplotypeMatrix.from_vcf(str(p), region="chr2",
+                                                   accessible_bed=str(bed)), "chr2", [(0, 60)])):
+        cs, ce = m.chrom_start, m.chrom_end
+        want = sum(1 for x in range(cs, ce + 1) if any(s < x <= e for s, e in iv))
+        assert m.n_total_sites == want, (chrom, cs, ce)
+    # a BED without intervals for the chromosome is an error, as in the
+    # reference (accessible.py:232-235), not an empty mask
+    other = tmp_path / "b.bed"
+    other.write_text("chr3\t0\t1000\n")
+    with pytest.raises(ValueError, match="No BED intervals"):
+        HaplotypeMatrix.from_vcf(str(p), accessible_bed=str(other))
+    with pytest.raises(ValueError, match="No BED intervals"):
+        GenotypeMatrix.from_vcf(str(p), accessible_bed=str(other))
