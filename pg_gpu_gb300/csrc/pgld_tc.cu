@@ -1,11 +1,15 @@
 // tcgen05 tensor-core form of the binned band kernel (sm_103a).
 //
 // The joint counts of a SNP pair are dot products of 0/1 vectors over the
-// haplotypes: with A = the carrier / reference rows of 64 SNPs i (rows 2i,
-// 2i+1) and B the same for 64 SNPs j, D = A B^T holds n11, n10, n01, n00 of
-// all 4096 pairs of the tile.  Operands are E4M3 bytes (0x38 = 1.0, 0x00 = 0)
-// in K-major rows padded to 128 bytes; products are exact and the float32
-// accumulators hold integers below 2^24, so the counts are exact.
+// haplotypes: with A = the carrier / reference rows of 64 SNPs i and B the
+// same for 64 SNPs j, D = A B^T holds n11, n10, n01, n00 of all 4096 pairs of
+// the tile.  Operand rows are grouped by 8 SNPs (row 16g + k: carrier plane
+// of SNP 8g + k, row 16g + 8 + k: its reference plane).  Operands are E4M3
+// bytes (0x38 = 1.0, 0x00 = 0) in K-major rows padded to 128 bytes; products
+// are exact and the float32 accumulators hold integers below 2^24, so the
+// counts are exact.  This kernel serves one population (binned, per-pair and
+// window modes) and two populations with one accumulator each (the 64 x 64
+// layout); pgld_tc_wide.cu holds the combined two-population layout.
 //
 // One CTA per SM (it owns all 512 TMEM columns):
 //   warp 0      TMA producer: 128-row x 128-byte A and B boxes (SWIZZLE_128B)
@@ -13,8 +17,9 @@
 //   warp 1      allocates TMEM; one lane issues tcgen05.mma M=128 N=128 K=32
 //               (kind::f8f6f4) into accumulator stage t%2 (population p at
 //               columns 256*(t%2) + 128*p), commits stages and tiles
-//   warps 4-11  epilogue: tcgen05.ld the counts, exchange C/Z rows with a lane
-//               shuffle, float32 statistics (pgld_epilogue.cuh), bin sums
+//   warps 4-11  epilogue: 16x256b tcgen05.ld of the grouped rows gives each
+//               lane all four counts of two pairs as the float2 operands of
+//               the packed float32 statistics (pgld_epilogue2.cuh), bin sums
 // Every mbarrier wait is bounded; on expiry the kernel records an error code
 // in the status word, drains its own copies and MMAs, frees TMEM and returns.
 #include <cuda.h>

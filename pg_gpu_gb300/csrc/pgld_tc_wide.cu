@@ -15,13 +15,14 @@
 // tensor work (four M128 N256 K32 MMAs), which keeps the tensor pipe fed
 // across the latency of the stage hand-offs.
 //
-// Roles (one CTA per SM, 384 threads):
+// Roles (one CTA per SM, 512 threads):
 //   warp 0      TMA producer: A box 128 rows x 128 B, B box 256 rows x 128 B
 //               (SWIZZLE_128B) per K chunk into a ring of 48 KB stages
 //   warp 1      allocates TMEM; one lane issues tcgen05.mma M128 N256 K32
 //               (kind::f8f6f4) into accumulator buffer t % 2
-//   warps 4-11  epilogue: warp e owns TMEM lane quarter e % 4 (16 SNPs i)
-//               and column half e / 4 (64 SNPs j) as two 16 x 32 sub-tiles;
+//   warps 4..   epilogue (8 or 12 warps): warp e owns TMEM lane quarter
+//               e % 4 (16 SNPs i); the quarter's warps take its 32-SNP column
+//               chunks of the CTA's tiles in turn (16 x 32 sub-tiles);
 //               decode, float32 statistics, float64 bin slots
 // Every mbarrier wait is bounded; on expiry the kernel records an error code
 // in the status word, drains its own copies and MMAs, frees TMEM and returns.
@@ -45,6 +46,9 @@
 #ifndef PGLD_TCW_CUNROLL
 #define PGLD_TCW_CUNROLL 1
 #endif
+#ifndef PGLD_TCW_EPI
+#define PGLD_TCW_EPI 12
+#endif
 
 namespace pgld {
 namespace tcw {
@@ -56,9 +60,18 @@ constexpr int kColSnp = 128;   // SNPs j per tile (B: 256 operand rows)
 constexpr int kBoxA = 128 * kKChunk;           // 16 KB
 constexpr int kBoxB = 256 * kKChunk;           // 32 KB
 constexpr int kStage = kBoxA + kBoxB;          // 48 KB
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = PGLD_TCW_EPI;   // 8 or 12 epilogue warps (2 or 3 per sub-partition)
+static_assert(kEpiWarps == 8 || kEpiWarps == 12, "8 or 12 epilogue warps");
+constexpr int kUnitsPerTile = 16;          // 4 lane quarters x 4 column chunks of 32 SNPs
+// registers per thread at launch, and the split between the producer / MMA
+// warpgroup and the epilogue warpgroups: 128 lo + 32 kEpiWarps hi <= kThreads x launch
+constexpr int kRegLaunch = kEpiWarps == 8 ? 168 : 128;
+constexpr int kRegLo = kEpiWarps == 8 ? 56 : 32;
+constexpr int kRegHi = kEpiWarps == 8 ? 224 : 160;
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kThreads = (4 + kEpiWarps) * 32;
+static_assert(128 * kRegLo + 32 * kEpiWarps * kRegHi <= kThreads * kRegLaunch,
+              "register split above the launch's total");
 constexpr int kSlotSets = 4;   // bin slot sets, each shared by two epilogue warps
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kOne64 = 0x68;  // E4M3 64.0
@@ -157,7 +170,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&ctrl->tfull[s], 1);
-      mbar_init(&ctrl->tempty[s], kEpiWarps);
+      mbar_init(&ctrl->tempty[s], kUnitsPerTile);
     }
     mbar_init(&ctrl->drain, 1);
     ctrl->abort_flag = 0;
@@ -203,7 +216,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   // (the host launches this kernel only when it was built with 168 registers).
   if (warp < 4) {
 #if PGLD_TCW_MAXNREG
-    asm volatile("setmaxnreg.dec.sync.aligned.u32 56;" ::: "memory");
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegLo) : "memory");
 #endif
     if (warp == 0 && lane == 0) {
       // ---------------- TMA producer ----------------
@@ -293,12 +306,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else {
 #if PGLD_TCW_MAXNREG
-    asm volatile("setmaxnreg.inc.sync.aligned.u32 224;" ::: "memory");
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegHi) : "memory");
 #endif
     // ---------------- epilogue ----------------
     const int e = warp - 4;
     const int quarter = warp & 3;
-    const int half = e >> 2;
+    // the warps of a lane quarter take its 32-SNP column chunks ("units") of
+    // the CTA's tiles in turn: unit U = 4 t + u (tile t, chunk u) goes to the
+    // quarter's warp U mod (kEpiWarps / 4)
+    constexpr int kPerQuarter = kEpiWarps / 4;
+    const int k_in_q = e >> 2;
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
     const bool use_int = (a.bcoord == nullptr) && (*a.ipos_bad == 0);
@@ -306,10 +323,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     unsigned long long* my_cnt = kcnt + (size_t)(e & (kSlotSets - 1)) * n_bins;
     auto slot_add = [&](int bin, int k, float v) { atomicAdd(my_acc + bin * kS + k, (double)v); };
     auto cnt_add = [&](int bin, unsigned long long v) { atomicAdd(my_cnt + bin, v); };
-    int t = 0;
     long long hint = 0;
-    for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
-      const int acc = t & 1;
+    bool aborted = false;
+#pragma unroll 1
+    for (long long U = k_in_q;; U += kPerQuarter) {
+      const long long t = U >> 2;
+      const int u = (int)(U & 3);
+      const long long item = blockIdx.x + t * gridDim.x;
+      if (item >= n_items) break;
+      const int acc = (int)(t & 1);
       const uint32_t aph = (uint32_t)((t >> 1) & 1);
       const long long bi = row_of(a, item, hint);
       const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
@@ -317,12 +339,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       const long long si0 = i0 + 16 * quarter;
       const long long ib = si0 + (lane >> 2);  // the lane's SNP i of row half 0 (half 1: + 8)
       bool waited = false;
-
-#pragma unroll 1
-      for (int sh = 0; sh < 2; ++sh) {
-        // the warp's 16 x 32 sub-tile: i in si0 + [0, 16), j in sj0 + [0, 32)
-        const long long sj0 = j0 + 64 * half + 32 * sh;
-        const uint32_t colb = (uint32_t)(acc * 256 + half * 128 + sh * 64);
+      {
+        // the unit's 16 x 32 sub-tile: i in si0 + [0, 16), j in sj0 + [0, 32)
+        const long long sj0 = j0 + 32 * u;
+        const uint32_t colb = (uint32_t)(acc * 256 + u * 64);
         // classify: 0 one bin, 1 two adjacent bins, 2 general
         int mode = 2, b0 = -1, thr_mid = 0;
         if (use_int && sj0 >= si0 + 16 && sj0 + 31 < a.n_snp && si0 + 15 < a.n_anchor) {
@@ -361,11 +381,12 @@ __global__ void __launch_bounds__(kThreads, 1)
               __all_sync(0xffffffffu, mbar_wait(&ctrl->tfull[acc], aph, abort_flag, a.wait_cycles));
           if (!ready) {
             if (lane == 0) set_abort(ctrl, a.status, 3005);
-            break;
+            aborted = true;
           }
           tc_fence_after();
           waited = true;
         }
+        if (aborted) break;
 
         // four steps (row half hh, column pair gp) of 8 x 16 SNPs: one
         // 16x256b TMEM load gives thread t both planes of SNP i = t / 4 of
@@ -380,7 +401,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                                  (uint32_t)(gp * 32),
                              r);
             tmem_wait_ld();
-            if (sh == 1 && c == 3) {
+            if (c == 3) {
+              // the unit's last TMEM load: release its share of the buffer
               tc_fence_before();
               __syncwarp();
               if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
@@ -738,9 +760,9 @@ int pgld_tc_wide_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::Band
     cudaFuncAttributes fa;
     cudaError_t e0 = cudaFuncGetAttributes(&fa, (const void*)kern);
     if (e0 != cudaSuccess) return pgld_cuda_fail(h, e0, "band_wide attributes");
-    if (fa.numRegs != 168)
+    if (fa.numRegs != kRegLaunch)
       return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "band_wide_kernel built with %d registers; its "
-                       "register split needs 168", fa.numRegs);
+                       "register split needs %d", fa.numRegs, kRegLaunch);
   }
 #endif
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
