@@ -16,6 +16,7 @@ inline float2 make_float2(float x, float y) { return {x, y}; }
 struct alignas(16) float4 {
   float x, y, z, w;
 };
+inline float4 make_float4(float x, float y, float z, float w) { return {x, y, z, w}; }
 #endif
 
 namespace pgld {
@@ -52,6 +53,7 @@ struct Pop {
   V a, b, x;
   V dA, dB, e;
   V s, t, ns;
+  V m1;        // ns - 1
   int n0, n1;  // valid n of each lane
 };
 
@@ -65,6 +67,7 @@ PGLD_HD Pop make(V c1, V c2, V c3, V c4) {
   p.dA = vsub(p.qA, p.pA); p.dB = vsub(p.qB, p.pB);
   p.s = vadd(c2, c3); p.t = vadd(c1, c4); p.e = vsub(p.s, p.t);
   p.ns = vadd(p.pA, p.qA);
+  p.m1 = vsub(p.ns, vs(1.0f));
   p.n0 = f2i(p.ns.x);
   p.n1 = f2i(p.ns.y);
   return p;
@@ -82,7 +85,7 @@ PGLD_HD V dz_num(const Pop& p, V w) {
 }
 PGLD_HD V pi2_num(const Pop& p) {
   const V pn = vfma(p.ns, vsub(p.ns, vs(4.0f)), vs(2.0f));
-  const V w = vfma(vsub(vs(2.0f), p.ns), p.t, vadd(p.x, vsub(p.ns, vs(1.0f))));
+  const V w = vfma(vsub(vs(2.0f), p.ns), p.t, vadd(p.x, p.m1));
   return dot2(p.a, pn, p.x, w);
 }
 // uA = pA qA of population t
@@ -92,7 +95,7 @@ PGLD_HD V triple_num2(const Pop& t, const Pop& s, V uA) {
 }
 PGLD_HD V ijij_num4(const Pop& A, const Pop& B) {
   const V K = vfma(A.c1, B.c4, vfma(A.c2, B.c3, vfma(A.c3, B.c2, vmul(A.c4, B.c1))));
-  const V mA = vsub(A.ns, vs(1.0f)), mB = vsub(B.ns, vs(1.0f));
+  const V mA = A.m1, mB = B.m1;
   const V x2 = vadd(B.x, B.x);
   const V y1 = vmul(mA, A.e), y2 = vfma(mB, B.e, vadd(x2, x2));
   const V p1 = vmul(B.x, y1), e1 = vfma(B.x, y1, vneg(p1));
@@ -104,10 +107,21 @@ PGLD_HD V ijij_num4(const Pop& A, const Pop& B) {
 }
 
 // the reciprocal factors of the valid n of two lanes: 1/n, 1/(n(n-1)),
-// 1/(n(n-1)(n-2)), 1/(n(n-1)(n-2)(n-3)), from one interleaved table of float4
+// 1/(2 n(n-1)(n-2)) (half the scalar table's r3: exact, and the factor the
+// triple statistics need), 1/(n(n-1)(n-2)(n-3)), from one interleaved table
+// of float4 (recip_entry4)
 struct R2 {
-  V inv, r2, r3, r4;
+  V inv, r2, r3h, r4;
 };
+PGLD_HD void recip_entry4(int n, float4* e) {
+  float inv, r2, r3, r4;
+  fast::recip_entry(n, &inv, &r2, &r3, &r4);
+  *e = make_float4(inv, r2, 0.5f * r3, r4);
+}
+// statistics 11 (pi2_0_0_1_1) and 12 (pi2_0_1_0_1) leave stats2_to with the
+// scale r22; their values are the num * r22 products (or sums of them) times
+// these exact powers of two
+constexpr float kPost11 = 0.5f, kPost12 = 0.25f;
 PGLD_HD R2 recip(const float4* T4, int n0, int n1) {
   const float4 a = T4[n0], b = T4[n1];
   return {make_float2(a.x, b.x), make_float2(a.y, b.y), make_float2(a.z, b.z),
@@ -132,20 +146,29 @@ PGLD_HD void stats2_to(const Pop& p, const Pop& q, const float4* T4, Sink&& sink
   sink(5, vmul(p.x, wq), r22);
   sink(6, vmul(q.x, wp), r22);
   const V uAp = vmul(p.pA, p.qA), uAq = vmul(q.pA, q.qA);
-  sink(11, vfma(uAp, vmul(q.pB, q.qB), vmul(uAq, vmul(p.pB, p.qB))), vmul(vs(0.5f), r22));
-  sink(12, ijij_num4(p, q), vmul(vs(0.25f), r22));
+  sink(11, vfma(uAp, vmul(q.pB, q.qB), vmul(uAq, vmul(p.pB, p.qB))), r22);  // x kPost11
+  sink(12, ijij_num4(p, q), r22);                                            // x kPost12
   const V dc = vfma(p.dA, q.dB, vmul(p.dB, q.dA));
-  const V h31p = vmul(vs(0.5f), vmul(rp.r3, rq.inv));
+  const V h31p = vmul(rp.r3h, rq.inv);
   sink(4, vmul(p.x, dc), h31p);
   sink(10, triple_num2(p, q, uAp), h31p);
-  const V h31q = vmul(vs(0.5f), vmul(rq.r3, rp.inv));
+  const V h31q = vmul(rq.r3h, rp.inv);
   sink(7, vmul(q.x, dc), h31q);
   sink(13, triple_num2(q, p, uAq), h31q);
 }
 
-PGLD_HD void stats2(const Pop& p, const Pop& q, const float4* T4, V o[15]) {
+// the sink's products, statistics 11 and 12 still without their post factors
+PGLD_HD void stats2_raw(const Pop& p, const Pop& q, const float4* T4, V o[15]) {
   stats2_to(p, q, T4, [&](int k, V num, V sc) { o[k] = vmul(num, sc); });
 }
+PGLD_HD void stats2(const Pop& p, const Pop& q, const float4* T4, V o[15]) {
+  stats2_raw(p, q, T4, o);
+  o[11] = vmul(o[11], vs(kPost11));
+  o[12] = vmul(o[12], vs(kPost12));
+}
+// the post factor of statistic k of the two-population list (scaling by a
+// power of two commutes with every rounding of a sum of the sink's products)
+PGLD_HD constexpr double post2(int k) { return k == 11 ? kPost11 : k == 12 ? kPost12 : 1.0; }
 
 template <class Sink>
 PGLD_HD void stats1_to(const Pop& p, const float4* T4, Sink&& sink) {

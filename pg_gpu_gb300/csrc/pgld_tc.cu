@@ -231,8 +231,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x < kEpiWarps * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
     for (int x = t; x <= a.nmax; x += kEpiThreads)
       if constexpr (MODE == kModeBinned)
-        fast::recip_entry(x, tables + 4 * x, tables + 4 * x + 1, tables + 4 * x + 2,
-                          tables + 4 * x + 3);
+        fast2::recip_entry4(x, reinterpret_cast<float4*>(tables) + x);
       else
         fast::recip_entry(x, tables + x, tables + (a.nmax + 1) + x, tables + 2 * (a.nmax + 1) + x,
                           tables + 3 * (a.nmax + 1) + x);
@@ -646,7 +645,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       };
       auto stats_of = [&](const fast2::Pop& p0, const fast2::Pop& p1, float2 (&st)[S]) {
         if constexpr (P == 1) fast2::stats1(p0, T4, st);
-        else fast2::stats2(p0, p1, T4, st);
+        else fast2::stats2_raw(p0, p1, T4, st);
       };
 
       if (mode == 0) {
@@ -791,6 +790,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       double v = 0.0;
 #pragma unroll
       for (int w = 0; w < kEpiWarps; ++w) v += slot_value(kacc[w * n_bins * S + x]);
+      if constexpr (P == 2) v *= fast2::post2(x % S);
       if (v != 0.0) atomicAdd(a.sums + x, v);
     }
     if (a.pair_counts)

@@ -190,8 +190,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x < kSlotSets * n_bins * kS; x += kEpiThreads) kacc[x] = 0.0;
     for (int x = t; x < kSlotSets * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
     for (int x = t; x <= a.nmax; x += kEpiThreads)
-      fast::recip_entry(x, tables + 4 * x, tables + 4 * x + 1, tables + 4 * x + 2,
-                        tables + 4 * x + 3);
+      fast2::recip_entry4(x, reinterpret_cast<float4*>(tables) + x);
     for (int x = t; x <= n_bins; x += kEpiThreads) {
       const double b = a.bins[x];
       sbins[x] = b;
@@ -548,7 +547,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             flush();
             float2 st[kS];
-            fast2::stats2(p0, p1, T4, st);
+            fast2::stats2_raw(p0, p1, T4, st);
 #pragma unroll 1
             for (int hsel = 0; hsel < 2; ++hsel) {
               const int b = hsel ? by : bx;
@@ -583,6 +582,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       double v = 0.0;
 #pragma unroll
       for (int w = 0; w < kSlotSets; ++w) v += kacc[w * n_bins * kS + x];
+      v *= fast2::post2(x % kS);
       if (v != 0.0) atomicAdd(a.sums + x, v);
     }
     if (a.pair_counts)

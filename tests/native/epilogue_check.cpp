@@ -34,7 +34,7 @@ extern "C" void pgld_check_stats2(const int* counts, const int* n, int N, int P,
   int nmax = 0;
   for (int k = 0; k < N * 2; ++k) nmax = n[k] > nmax ? n[k] : nmax;
   std::vector<float4> tab(nmax + 1);
-  for (int v = 0; v <= nmax; ++v) recip_entry(v, &tab[v].x, &tab[v].y, &tab[v].z, &tab[v].w);
+  for (int v = 0; v <= nmax; ++v) f2::recip_entry4(v, &tab[v]);
   const float4* T = tab.data();
   const int S = P == 1 ? 3 : 15;
   for (int k = 0; k < N; ++k) {
