@@ -22,7 +22,8 @@
 //               (kind::f8f6f4) into accumulator buffer t % 2
 //   warps 4..   epilogue (8 or 12 warps): warp e owns TMEM lane quarter
 //               e % 4 (16 SNPs i); the quarter's warps take its 32-SNP column
-//               chunks of the CTA's tiles in turn (16 x 32 sub-tiles);
+//               chunks of the CTA's tiles in order, each the next one when
+//               it is free (16 x 32 sub-tiles);
 //               decode, float32 statistics, float64 bin slots
 // Every mbarrier wait is bounded; on expiry the kernel records an error code
 // in the status word, drains its own copies and MMAs, frees TMEM and returns.
@@ -45,6 +46,17 @@
 #endif
 #ifndef PGLD_TCW_CUNROLL
 #define PGLD_TCW_CUNROLL 1
+#endif
+// producer / MMA waits: 1 try_wait suspending up to PGLD_TCW_SUSPEND ns per
+// probe (no issue slots taken while waiting), 0 probes with ~32 ns naps
+#ifndef PGLD_TCW_PWAIT
+#define PGLD_TCW_PWAIT 1
+#endif
+#ifndef PGLD_TCW_SUSPEND
+#define PGLD_TCW_SUSPEND 20000
+#endif
+#ifndef PGLD_TCW_DYN
+#define PGLD_TCW_DYN 1
 #endif
 #ifndef PGLD_TCW_EPI
 #define PGLD_TCW_EPI 12
@@ -141,6 +153,21 @@ __device__ __forceinline__ void split2(float2 v, float2& lo, float2& hi) {
   lo = fast2::vfma(hi, fast2::vs(-4096.0f), v);
 }
 
+// the producer's and MMA issuer's waits
+__device__ __forceinline__ bool role_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag,
+                                          long long limit) {
+#if PGLD_TCW_PWAIT == 1
+  const long long t0 = clock64();
+  for (long long k = 0; k < kSpinLimit; ++k) {
+    if (mbar_try_for(b, parity, PGLD_TCW_SUSPEND)) return true;
+    if (*abort_flag || clock64() - t0 > limit) return false;
+  }
+  return false;
+#else
+  return mbar_wait_nap(b, parity, abort_flag, limit);
+#endif
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
     band_wide_kernel(const __grid_constant__ CUtensorMap map_a,
                      const __grid_constant__ CUtensorMap map_b, Params a) {
@@ -176,6 +203,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     ctrl->abort_flag = 0;
     ctrl->produced = 0;
     ctrl->consumed = 0;
+    for (int q = 0; q < 4; ++q) ctrl->unit_next[q] = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -229,7 +257,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
         const int yi = (int)(2 * bi * kRowSnp), yj = (int)(2 * bj * kColSnp);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait_nap(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
+          if (!role_wait(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
             set_abort(ctrl, a.status, 3002);
             break;
           }
@@ -267,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait_nap(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
+        if (!role_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }
@@ -275,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         const uint32_t d = tmem_base + (uint32_t)(acc * 256);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait_nap(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
+          if (!role_wait(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
             set_abort(ctrl, a.status, 3004);
             ok = false;
             break;
@@ -311,12 +339,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int e = warp - 4;
     const int quarter = warp & 3;
     // the warps of a lane quarter take its 32-SNP column chunks ("units") of
-    // the CTA's tiles in turn: unit U = 4 t + u (tile t, chunk u) goes to the
-    // quarter's warp U mod (kEpiWarps / 4)
+    // the CTA's tiles, unit U = 4 t + u (tile t, chunk u), in order: each
+    // takes the quarter's next unit when it is free (a shared counter), or,
+    // without PGLD_TCW_DYN, unit U goes to the quarter's warp U mod (kEpiWarps / 4)
     constexpr int kPerQuarter = kEpiWarps / 4;
     const int k_in_q = e >> 2;
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
+    // the largest distance in a bin (below INT_MAX, so top + 1 does not wrap)
+    const int top = thr[n_bins] > maxd_int ? maxd_int : thr[n_bins] - 1;
     const bool use_int = (a.bcoord == nullptr) && (*a.ipos_bad == 0);
     double* my_acc = kacc + (size_t)(e & (kSlotSets - 1)) * n_bins * kS;
     unsigned long long* my_cnt = kcnt + (size_t)(e & (kSlotSets - 1)) * n_bins;
@@ -325,7 +356,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     long long hint = 0;
     bool aborted = false;
 #pragma unroll 1
-    for (long long U = k_in_q;; U += kPerQuarter) {
+    for (long long Us = k_in_q;; Us += kPerQuarter) {
+#if PGLD_TCW_DYN
+      // the quarter's next unit, whichever of its warps is free first
+      uint32_t un = 0;
+      if (lane == 0) un = atomicAdd(&ctrl->unit_next[quarter], 1u);
+      const long long U = (long long)__shfl_sync(0xffffffffu, un, 0);
+#else
+      const long long U = Us;
+#endif
       const long long t = U >> 2;
       const int u = (int)(U & 3);
       const long long item = blockIdx.x + t * gridDim.x;
@@ -342,21 +381,30 @@ __global__ void __launch_bounds__(kThreads, 1)
         // the unit's 16 x 32 sub-tile: i in si0 + [0, 16), j in sj0 + [0, 32)
         const long long sj0 = j0 + 32 * u;
         const uint32_t colb = (uint32_t)(acc * 256 + u * 64);
-        // classify: 0 one bin, 1 two adjacent bins, 2 general
-        int mode = 2, b0 = -1, thr_mid = 0;
-        if (use_int && sj0 >= si0 + 16 && sj0 + 31 < a.n_snp && si0 + 15 < a.n_anchor) {
-          const int dmin = a.ipos[sj0] - a.ipos[si0 + 15];
-          const int dmax = a.ipos[sj0 + 31] - a.ipos[si0];
-          if (dmax <= maxd_int) {
-            const int blo = bin_of_int(thr, n_bins, dmin);
-            const int bhi = bin_of_int(thr, n_bins, dmax);
-            if (blo >= 0 && bhi == blo) {
-              mode = 0;
-              b0 = blo;
-            } else if (blo >= 0 && bhi == blo + 1) {
-              mode = 1;
-              b0 = blo;
-              thr_mid = thr[bhi];
+        // classify: 0 one bin; 1 bin b0 below distance thr_mid, bin b0 + 1
+        // from thr_mid below thr_hi, nothing from thr_hi; 2 general; 3 no
+        // pair in a bin (the unit only releases its share of the buffer)
+        int mode = 2, b0 = -1, thr_mid = 0, thr_hi = 0;
+        if (use_int) {
+          if (sj0 + 31 <= si0 || si0 >= a.n_anchor || sj0 >= a.n_snp) {
+            mode = 3;
+          } else if (sj0 >= si0 + 16 && sj0 + 31 < a.n_snp && si0 + 15 < a.n_anchor) {
+            const int dmin = a.ipos[sj0] - a.ipos[si0 + 15];
+            const int dmax = a.ipos[sj0 + 31] - a.ipos[si0];
+            if (dmax < thr[0] || dmin > top) {
+              mode = 3;
+            } else {
+              const int blo = bin_of_int(thr, n_bins, dmin);
+              const int bhi = bin_of_int(thr, n_bins, min(dmax, top));
+              if (blo >= 0 && bhi == blo && dmax <= top) {
+                mode = 0;
+                b0 = blo;
+              } else if (blo >= 0 && bhi >= blo && bhi <= blo + 1) {
+                mode = 1;
+                b0 = blo;
+                thr_mid = min(thr[blo + 1], top + 1);
+                thr_hi = max(thr_mid, blo + 2 <= n_bins ? min(thr[blo + 2], top + 1) : top + 1);
+              }
             }
           }
         }
@@ -365,7 +413,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         int bp_i0 = 0, bp_i1 = 0, bp_j[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) bp_j[q] = 0;
-        if (use_int && mode != 0) {
+        if (use_int && (mode == 1 || mode == 2)) {
           bp_i0 = ib < a.n_snp ? a.ipos[ib] : 0;
           bp_i1 = ib + 8 < a.n_snp ? a.ipos[ib + 8] : 0;
 #pragma unroll
@@ -386,6 +434,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           waited = true;
         }
         if (aborted) break;
+        if (mode == 3) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
+          continue;
+        }
 
         // four steps (row half hh, column pair gp) of 8 x 16 SNPs: one
         // 16x256b TMEM load gives thread t both planes of SNP i = t / 4 of
@@ -448,18 +502,20 @@ __global__ void __launch_bounds__(kThreads, 1)
           if ((lane & ((1 << sh_t) - 1)) == 0 && k < kS) slot_add(b0, k, tot);
           if (lane == 31) cnt_add(b0, 512ull);
         } else if (mode == 1) {
-          // two adjacent bins split at thr_mid
+          // bins b0 (d < thr_mid) and b0 + 1 (thr_mid <= d < thr_hi)
           float acc_lo[kS], acc_hi[kS];
+          int n_lo = 0, n_hi = 0;
 #pragma unroll
           for (int s = 0; s < kS; ++s) acc_lo[s] = acc_hi[s] = 0.f;
-          int n_hi = 0;
           steps([&](int hh, int g, const fast2::Pop& p0, const fast2::Pop& p1) {
             const int ipi = hh ? bp_i1 : bp_i0;
-            const bool up0 = (jpos(g, 0) - ipi) >= thr_mid;
-            const bool up1 = (jpos(g, 1) - ipi) >= thr_mid;
-            const float2 fu = make_float2(up0 ? 1.f : 0.f, up1 ? 1.f : 0.f);
-            const float2 fl = make_float2(up0 ? 0.f : 1.f, up1 ? 0.f : 1.f);
-            n_hi += (up0 ? 1 : 0) + (up1 ? 1 : 0);
+            const int d0 = jpos(g, 0) - ipi, d1 = jpos(g, 1) - ipi;
+            const bool lo0 = d0 < thr_mid, lo1 = d1 < thr_mid;
+            const bool hi0 = !lo0 && d0 < thr_hi, hi1 = !lo1 && d1 < thr_hi;
+            const float2 fu = make_float2(hi0 ? 1.f : 0.f, hi1 ? 1.f : 0.f);
+            const float2 fl = make_float2(lo0 ? 1.f : 0.f, lo1 ? 1.f : 0.f);
+            n_lo += (lo0 ? 1 : 0) + (lo1 ? 1 : 0);
+            n_hi += (hi0 ? 1 : 0) + (hi1 ? 1 : 0);
             fast2::stats2_to(p0, p1, T4, [&](int kk, float2 num, float2 sc) {
               const float2 st = fast2::vmul(num, sc);
               acc_hi[kk] = fmaf(fu.x, st.x, fmaf(fu.y, st.y, acc_hi[kk]));
@@ -469,14 +525,19 @@ __global__ void __launch_bounds__(kThreads, 1)
           constexpr int sh_t = totals_shift<kS>();
           const int k = lane >> sh_t;
           const bool leader = (lane & ((1 << sh_t) - 1)) == 0 && k < kS;
-          const float tlo = warp_totals<kS>(acc_lo, lane);
-          if (leader) slot_add(b0, k, tlo);
-          const float thi = warp_totals<kS>(acc_hi, lane);
-          if (leader) slot_add(b0 + 1, k, thi);
+          const int lo_total = __reduce_add_sync(0xffffffffu, n_lo);
           const int hi_total = __reduce_add_sync(0xffffffffu, n_hi);
+          if (lo_total) {
+            const float tlo = warp_totals<kS>(acc_lo, lane);
+            if (leader) slot_add(b0, k, tlo);
+          }
+          if (hi_total) {
+            const float thi = warp_totals<kS>(acc_hi, lane);
+            if (leader) slot_add(b0 + 1, k, thi);
+          }
           if (lane == 31) {
-            cnt_add(b0, (unsigned long long)(512 - hi_total));
-            cnt_add(b0 + 1, (unsigned long long)hi_total);
+            if (lo_total) cnt_add(b0, (unsigned long long)lo_total);
+            if (hi_total) cnt_add(b0 + 1, (unsigned long long)hi_total);
           }
         } else {
           // general (diagonal and band-edge sub-tiles, short distances,

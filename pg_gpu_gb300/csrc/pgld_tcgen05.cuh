@@ -98,13 +98,16 @@ __device__ __forceinline__ bool mbar_wait_poll(uint64_t* b, uint32_t parity,
 // producer / MMA thread leaves the issue slots of its sub-partition to the
 // epilogue warps there; false once `limit` cycles passed or another role
 // aborted
+#ifndef PGLD_NAP_NS
+#define PGLD_NAP_NS 32
+#endif
 __device__ __forceinline__ bool mbar_wait_nap(uint64_t* b, uint32_t parity,
                                               volatile int* abort_flag,
                                               long long limit = kWaitCycles) {
   const long long t0 = clock64();
   for (long long k = 0; k < kSpinLimit; ++k) {
     if (mbar_test(b, parity)) return true;
-    __nanosleep(32);
+    __nanosleep(PGLD_NAP_NS);
     if ((k & 15) == 15 && (*abort_flag || clock64() - t0 > limit)) return false;
   }
   return false;
@@ -207,6 +210,7 @@ struct Ctrl {
   uint32_t tmem_base;
   int abort_flag;
   int produced, consumed;
+  uint32_t unit_next[4];  // the next work unit of each lane quarter (dynamic epilogue order)
 };
 
 __device__ __forceinline__ void set_abort(Ctrl* c, int32_t* status, int code) {
