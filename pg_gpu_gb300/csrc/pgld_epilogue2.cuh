@@ -35,6 +35,29 @@ PGLD_HD V vmul(V a, V b) { return make_float2(a.x * b.x, a.y * b.y); }
 PGLD_HD V vfma(V a, V b, V c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)); }
 #endif
 PGLD_HD V vneg(V a) { return make_float2(-a.x, -a.y); }
+// one rounded product / fused multiply-add per lane, kept scalar (not paired
+// into one packed instruction), for operands that live in unpaired registers
+#if defined(__CUDA_ARCH__)
+PGLD_HD float smul(float a, float b) {
+  float r;
+  asm("mul.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+PGLD_HD float sfma(float a, float b, float c) {
+  float r;
+  asm("fma.rn.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+#else
+PGLD_HD float smul(float a, float b) { return a * b; }
+PGLD_HD float sfma(float a, float b, float c) { return fmaf(a, b, c); }
+#endif
+PGLD_HD V vmul_s(V a, V b) { return make_float2(smul(a.x, b.x), smul(a.y, b.y)); }
+PGLD_HD V vfma_s(V a, V b, V c) { return make_float2(sfma(a.x, b.x, c.x), sfma(a.y, b.y, c.y)); }
+// the scale products r22, h31 from unpaired table loads: scalar (1) or packed
+#ifndef PGLD_F2_SSCALE
+#define PGLD_F2_SSCALE 1
+#endif
 PGLD_HD V vs(float a) { return make_float2(a, a); }
 // a - b: the negation is exact, so the sum rounds once, exactly like a
 // correctly rounded subtraction
@@ -134,7 +157,11 @@ PGLD_HD R2 recip(const float4* T4, int n0, int n1) {
 template <class Sink>
 PGLD_HD void stats2_to(const Pop& p, const Pop& q, const float4* T4, Sink&& sink) {
   const R2 rp = recip(T4, p.n0, p.n1), rq = recip(T4, q.n0, q.n1);
+#if PGLD_F2_SSCALE
+  const V r22 = vmul_s(rp.r2, rq.r2);
+#else
   const V r22 = vmul(rp.r2, rq.r2);
+#endif
   const V wp = vfma(p.dA, p.dB, p.e), wq = vfma(q.dA, q.dB, q.e);
   sink(0, dd_num(p), rp.r4);
   sink(1, vmul(p.x, q.x), r22);
@@ -149,10 +176,18 @@ PGLD_HD void stats2_to(const Pop& p, const Pop& q, const float4* T4, Sink&& sink
   sink(11, vfma(uAp, vmul(q.pB, q.qB), vmul(uAq, vmul(p.pB, p.qB))), r22);  // x kPost11
   sink(12, ijij_num4(p, q), r22);                                            // x kPost12
   const V dc = vfma(p.dA, q.dB, vmul(p.dB, q.dA));
+#if PGLD_F2_SSCALE
+  const V h31p = vmul_s(rp.r3h, rq.inv);
+#else
   const V h31p = vmul(rp.r3h, rq.inv);
+#endif
   sink(4, vmul(p.x, dc), h31p);
   sink(10, triple_num2(p, q, uAp), h31p);
+#if PGLD_F2_SSCALE
+  const V h31q = vmul_s(rq.r3h, rp.inv);
+#else
   const V h31q = vmul(rq.r3h, rp.inv);
+#endif
   sink(7, vmul(q.x, dc), h31q);
   sink(13, triple_num2(q, p, uAq), h31q);
 }

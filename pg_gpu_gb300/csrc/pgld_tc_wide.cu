@@ -52,8 +52,14 @@
 #ifndef PGLD_TCW_PWAIT
 #define PGLD_TCW_PWAIT 1
 #endif
+#ifndef PGLD_TCW_NAP_LONG
+#define PGLD_TCW_NAP_LONG 0
+#endif
 #ifndef PGLD_TCW_SUSPEND
 #define PGLD_TCW_SUSPEND 20000
+#endif
+#ifndef PGLD_TCW_SSINK
+#define PGLD_TCW_SSINK 0
 #endif
 #ifndef PGLD_TCW_DYN
 #define PGLD_TCW_DYN 1
@@ -153,14 +159,20 @@ __device__ __forceinline__ void split2(float2 v, float2& lo, float2& hi) {
   lo = fast2::vfma(hi, fast2::vs(-4096.0f), v);
 }
 
-// the producer's and MMA issuer's waits
+// the producer's and MMA issuer's waits.  try_wait suspends the thread until
+// the phase completes or a hardware time limit passes; waits that usually
+// outlast that limit (kNapNs > 0: a free accumulator buffer, a free stage)
+// nap between probes, so that the waiting thread takes few issue slots from
+// the epilogue warps of its sub-partition
+template <int kNapNs>
 __device__ __forceinline__ bool role_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag,
                                           long long limit) {
 #if PGLD_TCW_PWAIT == 1
   const long long t0 = clock64();
   for (long long k = 0; k < kSpinLimit; ++k) {
     if (mbar_try_for(b, parity, PGLD_TCW_SUSPEND)) return true;
-    if (*abort_flag || clock64() - t0 > limit) return false;
+    if (kNapNs > 0) __nanosleep(kNapNs);
+    if ((k & 7) == 7 && (*abort_flag || clock64() - t0 > limit)) return false;
   }
   return false;
 #else
@@ -257,7 +269,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
         const int yi = (int)(2 * bi * kRowSnp), yj = (int)(2 * bj * kColSnp);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!role_wait(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
+          if (!role_wait<PGLD_TCW_NAP_LONG>(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
             set_abort(ctrl, a.status, 3002);
             break;
           }
@@ -295,7 +307,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!role_wait(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
+        if (!role_wait<PGLD_TCW_NAP_LONG>(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }
@@ -303,7 +315,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         const uint32_t d = tmem_base + (uint32_t)(acc * 256);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!role_wait(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
+          if (!role_wait<0>(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
             set_abort(ctrl, a.status, 3004);
             ok = false;
             break;
@@ -490,8 +502,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int s = 0; s < kS; ++s) acc2[s] = make_float2(0.f, 0.f);
           steps([&](int, int, const fast2::Pop& p0, const fast2::Pop& p1) {
+#if PGLD_TCW_SSINK
+            fast2::stats2_to(p0, p1, T4,
+                             [&](int k, float2 num, float2 sc) { acc2[k] = fast2::vfma_s(num, sc, acc2[k]); });
+#else
             fast2::stats2_to(p0, p1, T4,
                              [&](int k, float2 num, float2 sc) { acc2[k] = fast2::vfma(num, sc, acc2[k]); });
+#endif
           });
           float v[kS];
 #pragma unroll
