@@ -435,6 +435,26 @@ int pgld_vcf_scan(const char* text, int64_t len, int32_t* n_samples, int64_t* n_
 int pgld_vcf_parse_gt(const char* text, int64_t len, int32_t n_samples, int64_t n_records,
                       const int32_t* sample_cols, int32_t n_sel, int8_t* hap, int64_t* pos);
 
+/* The GT alleles of a VCF text packed straight into the bit planes of
+ * pgld_pack_haplotypes for n_pops populations, with no int8 haplotype matrix
+ * (the path HaplotypeMatrix.from_vcf -> load_pop_file -> per-call gathers of
+ * haplotype_matrix.py:293-404 and ld_pipeline.py:150-158 takes).  hap_rows:
+ * HOST int32 VCF haplotype indices (h < n_samples: first allele of VCF
+ * sample h, else the second allele of sample h - n_samples), population p
+ * owning hap_rows[pop_offsets[p] .. pop_offsets[p + 1]) in bit order.
+ * planes: HOST uint32; population p (W_p = max(1, ceil(n_p / 32)) words)
+ * starts at word 2 n_records sum_{q<p} W_q, record r's row is [carrier W_p |
+ * reference W_p]; valid: HOST uint32, population p at n_records sum_{q<p}
+ * W_q, record r's row W_p words (allele >= 0).  site_flags (nullable): HOST
+ * uint8 [n_records] over every haplotype of the VCF: bit 0 an allele 0, bit
+ * 1 an allele 1, bit 2 an allele >= 2, bit 3 a missing allele.  pop_flags
+ * (nullable): HOST uint8 [n_records][n_pops]: bit 0 a missing allele, bit 1
+ * an allele outside {0, 1} in the population's rows.  pos: int64 POS. */
+int pgld_vcf_pack_gt(const char* text, int64_t len, int32_t n_samples, int64_t n_records,
+                     const int32_t* hap_rows, const int32_t* pop_offsets, int32_t n_pops,
+                     uint32_t* planes, uint32_t* valid, uint8_t* site_flags, uint8_t* pop_flags,
+                     int64_t* pos);
+
 /* ----------------------------------------------------------------------
  * Measurement (no counterpart in the reference, which publishes no kernel
  * timings).

@@ -126,6 +126,7 @@ _SIGS = {
                           ctypes.POINTER(_D), _P], ctypes.c_int),
     "pgld_vcf_scan": ([_P, _I64, _P, _P], ctypes.c_int),
     "pgld_vcf_parse_gt": ([_P, _I64, _I32, _I64, _P, _I32, _P, _P], ctypes.c_int),
+    "pgld_vcf_pack_gt": ([_P, _I64, _I32, _I64, _P, _P, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
 }
 
 _lib = None

@@ -80,12 +80,7 @@ def read_vcf_gt(path, region=None, samples=None):
     pgld_vcf_parse_gt): row k = first allele of sample k, row n + k its
     second, -1 = missing (the calldata/GT layout of allel.read_vcf that
     haplotype_matrix.py:317-328 reshapes)."""
-    with open(path, "rb") as f:
-        data = f.read()
-    if data[:2] == b"\x1f\x8b":
-        data = gzip.decompress(data)
-    if region is not None:
-        data = _vcf_region(data, region)
+    data = _read_vcf_text(path, region)
     ns, nr = ctypes.c_int32(0), ctypes.c_int64(0)
     L.check(L.lib().pgld_vcf_scan(data, len(data), ctypes.byref(ns), ctypes.byref(nr)))
     names = _vcf_sample_names(data)
@@ -107,6 +102,138 @@ def read_vcf_gt(path, region=None, samples=None):
         None if cols is None else cols.ctypes.data_as(ctypes.c_void_p), n_sel,
         hap.ctypes.data_as(ctypes.c_void_p), pos.ctypes.data_as(ctypes.c_void_p)))
     return names, hap, pos
+
+
+def _read_vcf_text(path, region=None):
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:2] == b"\x1f\x8b":
+        data = gzip.decompress(data)
+    if region is not None:
+        data = _vcf_region(data, region)
+    return data
+
+
+def pop_file_sets(pop_file, names, pops=None):
+    """{pop: haplotype rows} of a sample / pop file over the VCF samples
+    `names`: sample i owns rows i and i + len(names), in the order of
+    HaplotypeMatrix.load_pop_file (haplotype_matrix.py:475-512)."""
+    n = len(names)
+    pop_map = {}
+    with open(pop_file) as f:
+        for line in f:
+            parts = line.strip().split()
+            if len(parts) >= 2 and parts[0] != "sample":
+                pop_map[parts[0]] = parts[1]
+    if pops is None:
+        pops = sorted(set(pop_map.values()))
+    sets = {p: [] for p in pops}
+    for i, name in enumerate(names):
+        p = pop_map.get(name)
+        if p in sets:
+            sets[p].append(i)
+            sets[p].append(i + n)
+    return sets
+
+
+class PackedVcf:
+    """Populations of a VCF packed straight from the GT text into bit planes
+    (pgld_vcf_pack_gt), without the int8 haplotype matrix.
+
+    ``packs``: {pop: PackedPop} on the device; ``positions``: int64 POS;
+    ``site_flags``: uint8 per site over every haplotype of the VCF (bit 0 an
+    allele 0, bit 1 an allele 1, bit 2 an allele >= 2, bit 3 missing);
+    ``pop_flags``: uint8 (n_sites, n_pops) (bit 0 missing, bit 1 an allele
+    outside {0, 1}); ``sample_sets``: {pop: rows}."""
+
+    def __init__(self, names, sample_sets, packs, positions, site_flags, pop_flags):
+        self.samples = names
+        self.sample_sets = sample_sets
+        self.packs = packs
+        self.positions = positions
+        self.site_flags = site_flags
+        self.pop_flags = pop_flags
+
+    @property
+    def num_variants(self):
+        return len(self.positions)
+
+    def biallelic_sites(self):
+        """Sites with an allele 0, an allele 1 and no allele >= 2 over every
+        haplotype (HaplotypeMatrix.apply_biallelic_filter,
+        haplotype_matrix.py:724-789)."""
+        f = self.site_flags
+        return ((f & 4) == 0) & ((f & 1) != 0) & ((f & 2) != 0)
+
+    def subset(self, keep):
+        """The sites where the boolean mask keep is True (planes gathered on
+        the device; population flags recomputed over the kept sites)."""
+        import torch
+        idx = np.nonzero(np.asarray(keep, bool))[0]
+        idx_d = torch.as_tensor(idx, dtype=torch.int64, device="cuda")
+        packs = {}
+        pf = self.pop_flags[idx]
+        for k, (p, pk) in enumerate(self.packs.items()):
+            f = np.bitwise_or.reduce(pf[:, k]) if len(idx) else 0
+            packs[p] = _ops.PackedPop(pk.planes.index_select(0, idx_d).contiguous(),
+                                      pk.valid.index_select(0, idx_d).contiguous(), pk.n_words,
+                                      pk.n_rows, len(idx), bool(f & 1), bool(f & 2))
+        return PackedVcf(self.samples, self.sample_sets, packs, self.positions[idx],
+                         self.site_flags[idx], pf)
+
+    def alt_counts(self, pop):
+        """float64 device (n_sites,): carriers of allele 1 among the
+        population's haplotypes (popcount of its carrier plane)."""
+        import torch
+        pk = self.packs[pop]
+        words = pk.planes[:, :pk.n_words].contiguous()
+        b = words.view(torch.uint8).to(torch.int64)
+        table = torch.tensor([bin(v).count("1") for v in range(256)], dtype=torch.int64,
+                             device=b.device)
+        return table[b].sum(1).to(torch.float64)
+
+
+def read_vcf_packed(path, pop_file, pops=None, region=None):
+    """PackedVcf of a plain or gzipped VCF: the populations of pop_file
+    (rows as load_pop_file gives them) packed on the host threads straight
+    from the GT text into carrier / reference / validity planes (no int8
+    haplotype matrix), then copied to the device."""
+    import torch
+    data = _read_vcf_text(path, region)
+    ns, nr = ctypes.c_int32(0), ctypes.c_int64(0)
+    L.check(L.lib().pgld_vcf_scan(data, len(data), ctypes.byref(ns), ctypes.byref(nr)))
+    if nr.value == 0:
+        raise ValueError(f"No variants found in {path}"
+                         + (f" for region {region}" if region else ""))
+    names = _vcf_sample_names(data)
+    sets = pop_file_sets(pop_file, names, pops)
+    order = list(sets)
+    rows = np.ascontiguousarray(np.concatenate(
+        [np.asarray(sets[p], np.int32) for p in order] or [np.zeros(0, np.int32)]), np.int32)
+    off = np.zeros(len(order) + 1, np.int32)
+    off[1:] = np.cumsum([len(sets[p]) for p in order])
+    Ws = [max(1, (len(sets[p]) + 31) // 32) for p in order]
+    n_rec = nr.value
+    planes = np.empty(2 * n_rec * max(1, sum(Ws)), np.uint32)
+    valid = np.empty(n_rec * max(1, sum(Ws)), np.uint32)
+    site = np.empty(n_rec, np.uint8)
+    popf = np.empty((n_rec, max(1, len(order))), np.uint8)
+    pos = np.empty(n_rec, np.int64)
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    L.check(L.lib().pgld_vcf_pack_gt(data, len(data), ns.value, n_rec, vp(rows), vp(off),
+                                     len(order), vp(planes), vp(valid), vp(site), vp(popf),
+                                     vp(pos)))
+    packs = OrderedDict()
+    wb = 0
+    for k, p in enumerate(order):
+        W = Ws[k]
+        pl = torch.from_numpy(planes[2 * n_rec * wb:2 * n_rec * (wb + W)].view(np.int32))
+        va = torch.from_numpy(valid[n_rec * wb:n_rec * (wb + W)].view(np.int32))
+        f = np.bitwise_or.reduce(popf[:, k])
+        packs[p] = _ops.PackedPop(pl.view(n_rec, 2 * W).to("cuda"), va.view(n_rec, W).to("cuda"),
+                                  W, len(sets[p]), n_rec, bool(f & 1), bool(f & 2))
+        wb += W
+    return PackedVcf(names, sets, packs, pos, site, popf[:, :len(order)])
 
 
 class HaplotypeMatrix:
@@ -283,22 +410,7 @@ class HaplotypeMatrix:
         i + n_samples (haplotype_matrix.py:475-512)."""
         if self.samples is None:
             raise ValueError("No sample names stored. Use from_vcf() to load data.")
-        n = len(self.samples)
-        pop_map = {}
-        with open(pop_file) as f:
-            for line in f:
-                parts = line.strip().split()
-                if len(parts) >= 2 and parts[0] != "sample":
-                    pop_map[parts[0]] = parts[1]
-        if pops is None:
-            pops = sorted(set(pop_map.values()))
-        sets = {p: [] for p in pops}
-        for i, name in enumerate(self.samples):
-            p = pop_map.get(name)
-            if p in sets:
-                sets[p].append(i)
-                sets[p].append(i + n)
-        self.sample_sets = sets
+        self.sample_sets = pop_file_sets(pop_file, self.samples, pops)
 
     # ------------------------------------------------------------- packing
     def _pop_rows(self, pop):

@@ -13,7 +13,7 @@ import numpy as np
 from . import _lib as L
 from . import _ops
 from .genotype_matrix import GenotypeMatrix
-from .haplotype_matrix import HaplotypeMatrix
+from .haplotype_matrix import HaplotypeMatrix, PackedVcf, read_vcf_packed
 from .ld_pipeline import het_names as _het_names
 from .ld_pipeline import ld_names as _ld_names
 
@@ -25,8 +25,23 @@ def _accessible(mat, accessible_bed):
     if accessible_bed is None:
         return mat
     from .accessible import accessible_variants
+    if isinstance(mat, PackedVcf):
+        return mat.subset(accessible_variants(mat.positions, accessible_bed))
     keep = accessible_variants(mat._pos_np(), accessible_bed)
     return mat.get_subset(np.nonzero(keep)[0])
+
+
+def _packed_vcf(vcf_file, pop_file, pops, ac_filter):
+    """The populations packed straight from the VCF's GT text (no int8
+    haplotype matrix), biallelic sites only with ac_filter; None when a
+    population holds alleles >= 2 that are kept (ac_filter False), whose
+    values the heterozygosity sums need."""
+    pv = read_vcf_packed(vcf_file, pop_file, pops)
+    if ac_filter:
+        return pv.subset(pv.biallelic_sites())
+    if any(pk.has_other for pk in pv.packs.values()):
+        return None
+    return pv
 
 
 def compute_ld_statistics(vcf_file=None, rec_map_file=None, pop_file=None, pops=None,
@@ -73,16 +88,22 @@ def compute_ld_statistics(vcf_file=None, rec_map_file=None, pop_file=None, pops=
                 raise ValueError("pop_file is required when loading from VCF")
             if report:
                 print(f"Loading {vcf_file} ...")
-            mat = HaplotypeMatrix.from_vcf(vcf_file)
-            mat.load_pop_file(pop_file, pops=pops)
-            if ac_filter:
-                mat = mat.apply_biallelic_filter()
+            mat = _packed_vcf(vcf_file, pop_file, pops, ac_filter)
+            if mat is None:
+                mat = HaplotypeMatrix.from_vcf(vcf_file)
+                mat.load_pop_file(pop_file, pops=pops)
+                if ac_filter:
+                    mat = mat.apply_biallelic_filter()
         mat = _accessible(mat, accessible_bed)
-        mat.transfer_to_gpu()
-        if report:
-            print(f"  {mat.num_haplotypes} hap, {mat.num_variants:,} variants")
+        if isinstance(mat, HaplotypeMatrix):
+            mat.transfer_to_gpu()
+            if report:
+                print(f"  {mat.num_haplotypes} hap, {mat.num_variants:,} variants")
+        elif report:
+            print(f"  {sum(len(r) for r in mat.sample_sets.values())} hap, "
+                  f"{mat.num_variants:,} variants")
 
-    pos_np = mat._pos_np().astype(np.float64)
+    pos_np = (mat.positions if isinstance(mat, PackedVcf) else mat._pos_np()).astype(np.float64)
     if r_bins is not None:
         if rec_map_file is None:
             raise ValueError("rec_map_file required with r_bins")
@@ -157,7 +178,7 @@ def _compute_ld_sums(mat, pops, bins, gen_dists, max_bp, use_genotypes=False):
     else:
         pos_d = L.as_device(mat.positions, np.float64)
         bc = None if gen_dists is None else L.as_device(gen_dists, np.float64)
-        packs = [mat.packed(p) for p in pops]
+        packs = [mat.packs[p] if isinstance(mat, PackedVcf) else mat.packed(p) for p in pops]
         sums, _ = _ops.binned_sums(packs, pos_d, bins, max_dist=max_bp, bin_coord=bc)
     return sums.cpu().numpy()
 
@@ -173,6 +194,10 @@ def _compute_heterozygosity(mat, pops, use_genotypes=False):
             v = d >= 0
             a = torch.where(v, d, torch.zeros_like(d)).to(torch.float64).sum(0)
             n = 2.0 * v.to(torch.float64).sum(0)
+        elif isinstance(mat, PackedVcf):
+            # biallelic alleles: the carriers of allele 1
+            a = mat.alt_counts(p)
+            n = torch.full_like(a, float(len(mat.sample_sets[p])))
         else:
             a = mat.haplotypes[rows].clamp(min=0).to(torch.float64).sum(0)
             n = torch.full_like(a, float(len(mat.sample_sets[p])))

@@ -359,3 +359,57 @@ def test_full_size_band_pairs():
     assert np.array_equal(np.isnan(got), np.isnan(ref))
     m = ~np.isnan(ref) & (np.abs(ref) > 1e-30)
     assert (np.abs(got[m] - ref[m]) / np.abs(ref[m])).max() <= 1e-6
+
+
+def test_moments_ld_vcf_packs_straight_from_the_gt_text(golden, tmp_path):
+    """moments_ld.compute_ld_statistics(vcf_file, pop_file): the populations
+    are packed from the GT text into bit planes (no int8 haplotype matrix);
+    the sums equal the matrix path's (from_vcf, load_pop_file,
+    apply_biallelic_filter) and the moments golden within 1e-6 of each
+    value; heterozygosity from the carrier planes."""
+    from pg_gpu_gb300 import moments_ld
+    from pg_gpu_gb300.haplotype_matrix import HaplotypeMatrix, PackedVcf
+    z = golden("moments_im")
+    hap, pos = z["hap"], z["pos"]
+    n = hap.shape[0] // 2
+    names = [f"tsk_{k}" for k in range(n)]
+    r0 = set(int(r) for r in z["rows0"])
+    al = lambda a: "." if a < 0 else str(int(a))  # noqa: E731
+    lines = ["##fileformat=VCFv4.2",
+             "#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO\tFORMAT\t" + "\t".join(names)]
+    for j in range(hap.shape[1]):
+        lines.append("\t".join(["1", str(int(pos[j])), ".", "A", "T", ".", "PASS", ".", "GT"]
+                               + [al(hap[k, j]) + "|" + al(hap[n + k, j]) for k in range(n)]))
+    vcf = tmp_path / "im.vcf"
+    vcf.write_text("\n".join(lines) + "\n")
+    popf = tmp_path / "pops.txt"
+    popf.write_text("sample\tpop\n" + "".join(f"{names[k]}\t{'deme0' if k in r0 else 'deme1'}\n"
+                                              for k in range(n)))
+    pops = ["deme0", "deme1"]
+    assert isinstance(moments_ld._packed_vcf(str(vcf), str(popf), pops, True), PackedVcf)
+    res = moments_ld.compute_ld_statistics(vcf_file=str(vcf), pop_file=str(popf), pops=pops,
+                                           bp_bins=z["bins"], report=False)
+    hm = HaplotypeMatrix.from_vcf(str(vcf))
+    hm.load_pop_file(str(popf), pops=pops)
+    ref = moments_ld.compute_ld_statistics(haplotype_matrix=hm.apply_biallelic_filter(),
+                                           pops=pops, bp_bins=z["bins"], report=False)
+    np.testing.assert_allclose(np.array(res["sums"][:-1]), np.array(ref["sums"][:-1]),
+                               rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(res["sums"][-1], ref["sums"][-1], rtol=1e-14)
+    np.testing.assert_allclose(res["sums"][-1], z["het_sums"], rtol=1e-12)
+    keep = O.biallelic_keep(hap)
+    _, _, a = O.binned_sums(hap[:, keep], pos[keep], [z["rows0"], z["rows1"]], z["bins"],
+                            abs_sums=True)
+    _near(np.array(res["sums"][:-1]), z["ld_sums"], a, floor=0.0)
+    # with an accessible mask (sites subset on the device) as the matrix path
+    lo, hi = int(pos[len(pos) // 4]), int(pos[3 * len(pos) // 4])
+    bed = tmp_path / "acc.bed"
+    bed.write_text(f"1\t{lo}\t{hi}\n")
+    res_b = moments_ld.compute_ld_statistics(vcf_file=str(vcf), pop_file=str(popf), pops=pops,
+                                             bp_bins=z["bins"], report=False,
+                                             accessible_bed=str(bed))
+    ref_b = moments_ld.compute_ld_statistics(haplotype_matrix=hm.apply_biallelic_filter(),
+                                             pops=pops, bp_bins=z["bins"], report=False,
+                                             accessible_bed=str(bed))
+    np.testing.assert_allclose(np.array(res_b["sums"]), np.array(ref_b["sums"]), rtol=1e-12,
+                               atol=1e-300)

@@ -229,3 +229,106 @@ def test_from_vcf_accessible_bed(tmp_path):
         HaplotypeMatrix.from_vcf(str(p), accessible_bed=str(other))
     with pytest.raises(ValueError, match="No BED intervals"):
         GenotypeMatrix.from_vcf(str(p), accessible_bed=str(other))
+
+
+def _pack_native(text, sets):
+    """pgld_vcf_pack_gt of text for the row lists sets (list of lists)."""
+    import ctypes
+    data = text.encode()
+    ns, nr = ctypes.c_int32(0), ctypes.c_int64(0)
+    L.check(L.lib().pgld_vcf_scan(data, len(data), ctypes.byref(ns), ctypes.byref(nr)))
+    rows = np.ascontiguousarray(np.concatenate([np.asarray(r, np.int32) for r in sets]
+                                               or [np.zeros(0, np.int32)]), np.int32)
+    off = np.zeros(len(sets) + 1, np.int32)
+    off[1:] = np.cumsum([len(r) for r in sets])
+    Ws = [max(1, (len(r) + 31) // 32) for r in sets]
+    n = nr.value
+    planes = np.full(2 * n * sum(Ws), 0xDEADBEEF, np.uint32)
+    valid = np.full(n * sum(Ws), 0xDEADBEEF, np.uint32)
+    site = np.zeros(n, np.uint8)
+    popf = np.zeros((n, len(sets)), np.uint8)
+    pos = np.zeros(n, np.int64)
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    rc = L.lib().pgld_vcf_pack_gt(data, len(data), ns.value, n, vp(rows), vp(off), len(sets),
+                                  vp(planes), vp(valid), vp(site), vp(popf), vp(pos))
+    L.check(rc)
+    out, wb = [], 0
+    for k, W in enumerate(Ws):
+        out.append((planes[2 * n * wb:2 * n * (wb + W)].reshape(n, 2 * W),
+                    valid[n * wb:n * (wb + W)].reshape(n, W)))
+        wb += W
+    return out, site, popf, pos
+
+
+def _planes_of(hap, rows):
+    """Carrier / reference / validity words of hap's rows (bit k of word w: row 32 w + k)."""
+    sub = hap[np.asarray(rows, np.int64)] if len(rows) else np.zeros((0, hap.shape[1]), np.int8)
+    M = hap.shape[1]
+    W = max(1, (len(rows) + 31) // 32)
+    c, z, v = (np.zeros((M, W), np.uint32) for _ in range(3))
+    for k in range(len(rows)):
+        w, b = divmod(k, 32)
+        c[:, w] |= (sub[k] == 1).astype(np.uint32) << np.uint32(b)
+        z[:, w] |= (sub[k] == 0).astype(np.uint32) << np.uint32(b)
+        v[:, w] |= (sub[k] >= 0).astype(np.uint32) << np.uint32(b)
+    flags = (np.any(sub == -1, 0).astype(np.uint8)
+             | (np.any((sub != -1) & (sub != 0) & (sub != 1), 0).astype(np.uint8) << 1))
+    return np.concatenate([c, z], 1), v, flags
+
+
+def _random_vcf(rng, n_samples, n_records):
+    names = [f"ind{k}" for k in range(n_samples)]
+    alle = lambda: rng.choice(["0", "1", ".", "2", "13"], p=[0.45, 0.4, 0.08, 0.05, 0.02])  # noqa: E731
+    recs = []
+    for j in range(n_records):
+        gts = []
+        for _ in range(n_samples):
+            u = rng.random()
+            if u < 0.03:
+                gts.append(alle())                       # haploid call
+            else:
+                gts.append(alle() + ("|" if u < 0.6 else "/") + alle() + (":7" if u > 0.9 else ""))
+        recs.append(("chr1", 10 * j + 5, "GT:DP" if j % 3 == 0 else "GT", gts))
+    return names, _vcf(names, recs)
+
+
+@pytest.mark.parametrize("case", ["edge", "random"])
+def test_pack_gt_matches_packing_of_the_int8_matrix(case):
+    """Packing straight from the GT text equals packing the int8 matrix the
+    text parses to: carrier / reference / validity words of every population
+    (overlapping, empty, more than 32 rows, any row order), the per-site and
+    per-population flags and POS."""
+    rng = np.random.default_rng(11)
+    if case == "edge":
+        names, text = _edge_text()
+    else:
+        names, text = _random_vcf(rng, 45, 70)
+    n = len(names)
+    hap, pos = _native(text)
+    sets = [list(range(0, 2 * n, 2)), [], list(rng.permutation(2 * n)[:37]), [2 * n - 1, 0, n],
+            list(range(2 * n))]
+    got, site, popf, gpos = _pack_native(text, sets)
+    assert np.array_equal(gpos, pos)
+    for k, rows in enumerate(sets):
+        pl, va, fl = _planes_of(hap, rows)
+        assert np.array_equal(got[k][0], pl), k
+        assert np.array_equal(got[k][1], va), k
+        assert np.array_equal(popf[:, k], fl), k
+    want_site = ((np.any(hap == 0, 0).astype(np.uint8)) | (np.any(hap == 1, 0).astype(np.uint8) << 1)
+                 | (np.any(hap >= 2, 0).astype(np.uint8) << 2)
+                 | (np.any(hap < 0, 0).astype(np.uint8) << 3))
+    assert np.array_equal(site, want_site)
+
+
+def test_pack_gt_rejects_bad_rows_and_records():
+    import ctypes
+    names, text = _edge_text()
+    with pytest.raises(Exception):
+        _pack_native(text, [[0, 2 * len(names)]])      # a haplotype index past the samples
+    bad = text.replace("0|1\t1|1\t0|0\t1|0", "0|1\t1|1", 1)  # a record with too few fields
+    with pytest.raises(Exception):
+        _pack_native(bad, [[0, 1]])
+    data = text.encode()
+    z = np.zeros(4, np.int32)
+    assert L.lib().pgld_vcf_pack_gt(data, len(data), 4, 5, None, None, 1, None, None, None,
+                                    None, z.ctypes.data_as(ctypes.c_void_p)) != 0
