@@ -680,6 +680,67 @@ def run_geno_band(args):
                     "ratio_tc_over_plain": res["plain"] / ms}}), flush=True)
 
 
+def run_geno_binned(args):
+    """Genotype moments LD in distance bins (moments_ld with use_genotypes):
+    the 1,000 diploids x 500,000 SNPs over 50 Mb of the genotype band
+    workload split into --geno-pops equal populations; the 3 / 15 / 45 / 105
+    statistics of every pair within 200 kb summed in 12 log bins from 100 bp
+    to 200 kb; the tensor-core form against the popcount form."""
+    import torch
+    from pg_gpu_gb300 import _ops
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(20261505)
+    M = args.geno_snps
+    hap = synthetic.copying_panel(g, 2000, M, 60, 5e-4, 1e-3, 0.0, dev)
+    geno = (hap[0::2] + hap[1::2]).to(torch.int8)
+    del hap
+    geno[torch.rand(geno.shape, generator=g, device=dev) < 0.03] = -1
+    rng = np.random.default_rng(20261505)
+    pos = np.sort(rng.choice(int(50_000_000 * M / 500_000), M, replace=False)).astype(np.int64)
+    pos_d = _ops.positions_f64(pos)
+    P = args.geno_pops
+    bins = np.logspace(2, np.log10(200_000), 13)
+    _, n_pairs = _ops.band_offsets(pos_d, float(bins[-1]))
+    per = 1000 // P
+    rows = [torch.arange(q * per, (q + 1) * per, dtype=torch.int32, device=dev) for q in range(P)]
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
+    res = {}
+    for form in ("tc", "plain"):
+        def step():
+            pops = [_ops.pack_geno(geno, r) for r in rows]
+            return _ops.geno_binned_sums(pops, pos_d, bins, form=form)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        ev = []
+        for s_ in range(args.steps):
+            flush.fill_(s_ & 0x7F)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            out = step()
+            b.record()
+            ev.append((a, b))
+            del out
+        torch.cuda.synchronize()
+        res[form] = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    ms = res["tc"]
+    print(json.dumps({
+        "metric": "genotype binned moments LD SNP-pairs/s",
+        "value": n_pairs / (ms / 1e3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "e4m3",
+        "data": "synthetic (copying-model dosages, 3 % missing)",
+        "config": {"workload": "geno_binned", "pops": P, "individuals_per_pop": per,
+                   "n_snp": M, "max_dist_bp": 200_000, "bins": "12 log bins 1e2..2e5",
+                   "pairs": n_pairs, "form": "tc"},
+        "roofline": tc_roofline(n_pairs / (ms / 1e3), 9 * 2 * 1000, "whole call, wall clock"),
+        "compare": {"form": "plain", "ms_per_step": res["plain"],
+                    "value": n_pairs / (res["plain"] / 1e3),
+                    "ratio_tc_over_plain": res["plain"] / ms}}), flush=True)
+
+
 def run_hap_band(args):
     """Haplotype LD with missing data, per-pair outputs: 2,000 haplotypes x
     100,000 SNPs over 10 Mb (50 founders, switch 5e-4, 2 % missing), every pair
@@ -740,8 +801,10 @@ def main():
     ap.add_argument("--form", default="tc", choices=["plain", "tc"])
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other form")
     ap.add_argument("--workload", default="binned2pop",
-                    choices=sorted(WORKLOADS) + ["windows512", "geno_band", "hap_band"])
+                    choices=sorted(WORKLOADS) + ["windows512", "geno_band", "geno_binned",
+                                                 "hap_band"])
     ap.add_argument("--geno-snps", type=int, default=500_000)
+    ap.add_argument("--geno-pops", type=int, default=2, choices=[1, 2, 3, 4])
     ap.add_argument("--geno-counts", action="store_true", help="also write the 9-way counts")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-pairs-per-worker", type=int, default=400_000)
@@ -756,7 +819,7 @@ def main():
     cores = host_cores()
     # the oracle's process pool starts before the first GPU call (spawn)
     pool = None
-    if args.workload in ("windows512", "geno_band", "hap_band"):
+    if args.workload in ("windows512", "geno_band", "geno_binned", "hap_band"):
         args.no_cpu = True
     if rank == 0 and (args.impl == "reference" or not args.no_cpu):
         pool = make_pool(cores)
@@ -767,6 +830,8 @@ def main():
             run_windows(args)
         elif args.workload == "geno_band":
             run_geno_band(args)
+        elif args.workload == "geno_binned":
+            run_geno_binned(args)
         elif args.workload == "hap_band":
             run_hap_band(args)
         else:

@@ -374,6 +374,15 @@ int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel, const doub
 int pgld_geno_binned_sums(pgld_handle h, const pgld_geno_panel* panel, const double* pos,
                           double max_dist, const double* bin_coord, const double* bins,
                           int32_t n_bins, double* sums, int64_t* pair_counts, void* stream);
+/* The same sums with a choice of form: PGLD_FORM_PLAIN (pgld_geno_binned_sums)
+ * or PGLD_FORM_TC, the moments of each population's pairs from tcgen05 MMAs
+ * (dosages 0..2 and missing only: no ext planes) and the same exact-integer
+ * term table per pair, summed per bin in float32 warp partials and float64
+ * slots. */
+int pgld_geno_binned_sums_form(pgld_handle h, const pgld_geno_panel* panel, const double* pos,
+                               double max_dist, const double* bin_coord, const double* bins,
+                               int32_t n_bins, double* sums, int64_t* pair_counts, int32_t form,
+                               void* stream);
 
 /* Per-window sums over batched, uneven windows in one launch, one
  * population.  Window w holds the SNPs snp_idx[win_begin[w] .. win_end[w])

@@ -108,6 +108,8 @@ _SIGS = {
                              ctypes.c_int),
     "pgld_geno_binned_sums": ([_P, ctypes.POINTER(GenoPanel), _P, _D, _P, _P, _I32, _P, _P, _P],
                               ctypes.c_int),
+    "pgld_geno_binned_sums_form": ([_P, ctypes.POINTER(GenoPanel), _P, _D, _P, _P, _I32, _P, _P,
+                                    _I32, _P], ctypes.c_int),
     "pgld_hap_window_sums": ([_P, ctypes.POINTER(HapPanel), _P, _I64, _P, _P, _I32, _P, _P, _I32,
                               _P],
                              ctypes.c_int),

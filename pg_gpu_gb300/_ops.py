@@ -595,8 +595,23 @@ def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True,
     return counts, nv, st
 
 
-def geno_binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None):
-    """(sums (n_bins, n_stats) float64, pair counts (n_bins,) int64), genotype statistics."""
+def geno_tc_applies(pops):
+    """The genotype tensor-core forms take dosages 0/1/2 with missing data
+    (no values above 2) of 1-4 populations."""
+    return 1 <= len(pops) <= 4 and all(pk.ext_planes is None for pk in pops)
+
+
+def geno_binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None, form="auto"):
+    """(sums (n_bins, n_stats) float64, pair counts (n_bins,) int64), genotype statistics.
+
+    form: "tc" (moments from tcgen05 MMAs), "plain" (AND + popcount) or
+    "auto" (tensor cores whenever they apply)."""
+    if form == "auto":
+        # several populations: the exact per-pair term table dominates
+        # either form, and the popcount one measured slightly faster
+        form = "tc" if len(pops) == 1 and geno_tc_applies(pops) else "plain"
+    if form not in ("tc", "plain"):
+        raise ValueError("form must be 'tc', 'plain' or 'auto'")
     torch = _torch()
     bins_np = np.asarray(bins, dtype=np.float64)
     if bins_np.ndim != 1 or len(bins_np) < 2:
@@ -612,9 +627,10 @@ def geno_binned_sums(pops, pos_d, bins, max_dist=None, bin_coord=None):
     md = float(bins_np[-1]) if max_dist is None else float(max_dist)
     bc = None if bin_coord is None else L.as_device(bin_coord, np.float64)
     h = L.handle()
-    L.check(L.lib().pgld_geno_binned_sums(h, ctypes.byref(geno_panel(pops)), L.ptr(pos_d), md,
-                                          L.ptr(bc), L.ptr(bins_d), n_bins, L.ptr(sums),
-                                          L.ptr(cnt), L.stream_ptr()), h)
+    L.check(L.lib().pgld_geno_binned_sums_form(h, ctypes.byref(geno_panel(pops)), L.ptr(pos_d), md,
+                                               L.ptr(bc), L.ptr(bins_d), n_bins, L.ptr(sums),
+                                               L.ptr(cnt), 1 if form == "tc" else 0,
+                                               L.stream_ptr()), h)
     return sums, cnt
 
 

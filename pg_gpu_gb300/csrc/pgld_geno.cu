@@ -141,60 +141,6 @@ __global__ void __launch_bounds__(256) geno_counts_pairs_kernel(
   }
 }
 
-// ---------------------------------------------------------------------------
-// statistic terms
-// ---------------------------------------------------------------------------
-__host__ __device__ __forceinline__ GV term_gv(int kind, const int32_t* pp, const GPop* P) {
-  switch (kind) {
-    case PGLD_G_DD_II: return dd_single(P[pp[0]]);
-    case PGLD_G_DD_IJ: return dd_between(P[pp[0]], P[pp[1]]);
-    case PGLD_G_DZ_III: return dz_single(P[pp[0]]);
-    case PGLD_G_DZ_IIJ: return dz_iik(P[pp[0]], P[pp[1]]);
-    case PGLD_G_DZ_IJI: return dz_iji(P[pp[0]], P[pp[1]]);
-    case PGLD_G_DZ_IJJ: return dz_ijj(P[pp[0]], P[pp[1]]);
-    case PGLD_G_DZ_IJK: return dz_ijk(P[pp[0]], P[pp[1]], P[pp[2]]);
-    case PGLD_G_PI2_IIII: return pi2_single(P[pp[0]]);
-    case PGLD_G_PI2_IIIJ: return pi2_triple(P[pp[0]], P[pp[1]], true);
-    case PGLD_G_PI2_IJII: return pi2_triple(P[pp[0]], P[pp[1]], false);
-    case PGLD_G_PI2_IIKK: return pi2_iikk(P[pp[0]], P[pp[1]]);
-    case PGLD_G_PI2_IIKL: return pi2_iikl(P[pp[0]], P[pp[1]], P[pp[2]]);
-    case PGLD_G_PI2_IJKK: return pi2_ijkk(P[pp[0]], P[pp[1]], P[pp[2]]);
-    case PGLD_G_PI2_IJIJ: return pi2_ijij(P[pp[0]], P[pp[1]]);
-    case PGLD_G_PI2_SHARED: return pi2_shared(P[pp[0]], P[pp[1]], P[pp[2]]);
-    default: return pi2_alldiff(P[pp[0]], P[pp[1]], P[pp[2]], P[pp[3]]);
-  }
-}
-
-__device__ __forceinline__ double gv_f64(const GV& v) {
-  if (v.gated && !v.ok) return 0.0;
-  return __ll2double_rn(v.num) / __ll2double_rn(v.den);
-}
-
-// r or r^2 of Rogers-Huff, NaN where a SNP has no variance among the valid
-__device__ __forceinline__ double rh_f64(const int* c, bool square) {
-  const RH m = rh_moments(c);
-  const i64 den = m.vi * m.vj;
-  if (den <= 0) return __longlong_as_double(0x7ff8000000000000ll);
-  if (square) return __ll2double_rn(m.cov * m.cov) / __ll2double_rn(den);
-  return __ll2double_rn(m.cov) / sqrt(__ll2double_rn(den));
-}
-
-template <typename T>
-__device__ __forceinline__ T term_value(const pgld_term& tm, const GPop* P, const int* const* cc) {
-  if (tm.kind == PGLD_G_SIGMA_D2) {
-    const GV v = sigma_d2(P[tm.pops[0]]);
-    if (!v.ok) return (T)__longlong_as_double(0x7ff8000000000000ll);
-    return sizeof(T) == 8 ? (T)(__ll2double_rn(v.num) / __ll2double_rn(v.den))
-                          : (T)(ll2f(v.num) / ll2f(v.den));
-  }
-  if (tm.kind == PGLD_G_RH_R || tm.kind == PGLD_G_RH_R2) {
-    if (sizeof(T) == 4 && tm.kind == PGLD_G_RH_R2) return (T)rh2_f32(cc[tm.pops[0]]);
-    return (T)rh_f64(cc[tm.pops[0]], tm.kind == PGLD_G_RH_R2);
-  }
-  const GV v = term_gv(tm.kind, tm.pops, P);
-  return sizeof(T) == 8 ? (T)gv_f64(v) : (T)gv_f32(v);
-}
-
 struct GStatsArgs {
   const int32_t* counts[PGLD_MAX_POPS];
   i64 counts_ld[PGLD_MAX_POPS];
@@ -740,11 +686,25 @@ extern "C" int pgld_geno_band_pairs(pgld_handle h, const pgld_geno_panel* panel,
   return pgld::geno::launch_geno_band<pgld::kModePairs, 1>(h, a, st);
 }
 
+int pgld_geno_tc_binned(pgld_context* h, const pgld_geno_panel* panel, const pgld::BandArgs& ba,
+                        cudaStream_t st);
+
 extern "C" int pgld_geno_binned_sums(pgld_handle h, const pgld_geno_panel* panel,
                                      const double* pos, double max_dist, const double* bin_coord,
                                      const double* bins, int32_t n_bins, double* sums,
                                      int64_t* pair_counts, void* stream) {
+  return pgld_geno_binned_sums_form(h, panel, pos, max_dist, bin_coord, bins, n_bins, sums,
+                                    pair_counts, PGLD_FORM_PLAIN, stream);
+}
+
+extern "C" int pgld_geno_binned_sums_form(pgld_handle h, const pgld_geno_panel* panel,
+                                          const double* pos, double max_dist,
+                                          const double* bin_coord, const double* bins,
+                                          int32_t n_bins, double* sums, int64_t* pair_counts,
+                                          int32_t form, void* stream) {
   PGLD_REQUIRE(h, h != nullptr, "pgld_geno_binned_sums: NULL handle");
+  PGLD_REQUIRE(h, form == PGLD_FORM_PLAIN || form == PGLD_FORM_TC,
+               "pgld_geno_binned_sums: unknown form %d", form);
   int rc = check_geno_panel(h, panel, "pgld_geno_binned_sums");
   if (rc) return rc;
   PGLD_REQUIRE(h, n_bins >= 1 && n_bins <= pgld::kMaxBins,
@@ -784,6 +744,12 @@ extern "C" int pgld_geno_binned_sums(pgld_handle h, const pgld_geno_panel* panel
   a.terms = h->gspec_terms[P];
   a.n_terms = h->gspec_n_terms[P];
   a.n_stats = S;
+  if (form == PGLD_FORM_TC) {
+    for (int p = 0; p < P; ++p)
+      PGLD_REQUIRE(h, panel->ext[p] == nullptr,
+                   "pgld_geno_binned_sums: the tensor-core form takes dosages 0..2 only");
+    return pgld_geno_tc_binned(h, panel, a, st);
+  }
   if (P == 1) return pgld::geno::launch_geno_band<pgld::kModeBinned, 1>(h, a, st);
   return pgld::geno::launch_geno_band<pgld::kModeBinned, PGLD_MAX_POPS>(h, a, st);
 }

@@ -256,5 +256,59 @@ __device__ __forceinline__ float rh2_f32(const int* c) {
 }
 #endif
 
+// ---------------------------------------------------------------------------
+// statistic terms
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ GV term_gv(int kind, const int32_t* pp, const GPop* P) {
+  switch (kind) {
+    case PGLD_G_DD_II: return dd_single(P[pp[0]]);
+    case PGLD_G_DD_IJ: return dd_between(P[pp[0]], P[pp[1]]);
+    case PGLD_G_DZ_III: return dz_single(P[pp[0]]);
+    case PGLD_G_DZ_IIJ: return dz_iik(P[pp[0]], P[pp[1]]);
+    case PGLD_G_DZ_IJI: return dz_iji(P[pp[0]], P[pp[1]]);
+    case PGLD_G_DZ_IJJ: return dz_ijj(P[pp[0]], P[pp[1]]);
+    case PGLD_G_DZ_IJK: return dz_ijk(P[pp[0]], P[pp[1]], P[pp[2]]);
+    case PGLD_G_PI2_IIII: return pi2_single(P[pp[0]]);
+    case PGLD_G_PI2_IIIJ: return pi2_triple(P[pp[0]], P[pp[1]], true);
+    case PGLD_G_PI2_IJII: return pi2_triple(P[pp[0]], P[pp[1]], false);
+    case PGLD_G_PI2_IIKK: return pi2_iikk(P[pp[0]], P[pp[1]]);
+    case PGLD_G_PI2_IIKL: return pi2_iikl(P[pp[0]], P[pp[1]], P[pp[2]]);
+    case PGLD_G_PI2_IJKK: return pi2_ijkk(P[pp[0]], P[pp[1]], P[pp[2]]);
+    case PGLD_G_PI2_IJIJ: return pi2_ijij(P[pp[0]], P[pp[1]]);
+    case PGLD_G_PI2_SHARED: return pi2_shared(P[pp[0]], P[pp[1]], P[pp[2]]);
+    default: return pi2_alldiff(P[pp[0]], P[pp[1]], P[pp[2]], P[pp[3]]);
+  }
+}
+
+__device__ __forceinline__ double gv_f64(const GV& v) {
+  if (v.gated && !v.ok) return 0.0;
+  return __ll2double_rn(v.num) / __ll2double_rn(v.den);
+}
+
+// r or r^2 of Rogers-Huff, NaN where a SNP has no variance among the valid
+__device__ __forceinline__ double rh_f64(const int* c, bool square) {
+  const RH m = rh_moments(c);
+  const i64 den = m.vi * m.vj;
+  if (den <= 0) return __longlong_as_double(0x7ff8000000000000ll);
+  if (square) return __ll2double_rn(m.cov * m.cov) / __ll2double_rn(den);
+  return __ll2double_rn(m.cov) / sqrt(__ll2double_rn(den));
+}
+
+template <typename T>
+__device__ __forceinline__ T term_value(const pgld_term& tm, const GPop* P, const int* const* cc) {
+  if (tm.kind == PGLD_G_SIGMA_D2) {
+    const GV v = sigma_d2(P[tm.pops[0]]);
+    if (!v.ok) return (T)__longlong_as_double(0x7ff8000000000000ll);
+    return sizeof(T) == 8 ? (T)(__ll2double_rn(v.num) / __ll2double_rn(v.den))
+                          : (T)(ll2f(v.num) / ll2f(v.den));
+  }
+  if (tm.kind == PGLD_G_RH_R || tm.kind == PGLD_G_RH_R2) {
+    if (sizeof(T) == 4 && tm.kind == PGLD_G_RH_R2) return (T)rh2_f32(cc[tm.pops[0]]);
+    return (T)rh_f64(cc[tm.pops[0]], tm.kind == PGLD_G_RH_R2);
+  }
+  const GV v = term_gv(tm.kind, tm.pops, P);
+  return sizeof(T) == 8 ? (T)gv_f64(v) : (T)gv_f32(v);
+}
+
 }  // namespace geno
 }  // namespace pgld

@@ -36,7 +36,9 @@
 #include "pgld_epilogue.cuh"
 #include "pgld_geno_mom.cuh"
 #include "pgld_internal.cuh"
+#include "pgld_geno.cuh"
 #include "pgld_scan.cuh"
+#include "pgld_tc_common.cuh"
 #include "pgld_tcgen05.cuh"
 
 namespace pgld {
@@ -500,6 +502,358 @@ __global__ void __launch_bounds__(256) pack_gtc_kernel(const uint32_t* __restric
   }
 }
 
+// ---------------------------------------------------------------------------
+// Distance-binned sums of the genotype statistics of 1-4 populations.  The
+// tile of 32 x 32 SNPs takes one M = 128, N = 96 MMA chain per population
+// (the operand rows of population p start at row p * n_blocks * 96), each
+// into its own 96 TMEM columns of the tile's accumulator stage.  One
+// population: DD, Dz and pi2 in float32 straight from the moments
+// (gmom::stats_f32).  Several: the epilogue turns each population's moments
+// into 9-way counts and evaluates the term table of the statistics (the
+// exact 64-bit integer forms of the popcount kernel, pgld_geno.cuh) per pair,
+// which costs far more than the counting (the form is then as fast as the
+// popcount one).  Sums per distance bin in float64 slots of the CTA.  G epilogue groups take alternate tiles: G = 2 for at most two
+// populations (two accumulator stages of 256 columns), G = 1 for three or
+// four (one stage of 384 columns).
+// ---------------------------------------------------------------------------
+struct BParams {
+  int kchunks;
+  long long n_snp;
+  const long long* item_off;
+  long long n_blocks;
+  int n_pops;
+  int pop_rows;             // operand rows per population (n_blocks * 96)
+  const double* pos;
+  const double* bcoord;     // distances for binning (NULL: positions)
+  double max_dist;
+  const double* bins;
+  int n_bins;
+  const pgld_term* terms;
+  int n_terms, n_stats;
+  double* sums;             // [n_bins][n_stats]
+  unsigned long long* pair_counts;
+  int32_t* status;
+  int stages;
+};
+
+template <int G>
+__global__ void __launch_bounds__(kThreads, 1)
+    gtc_binned_kernel(const __grid_constant__ CUtensorMap map, BParams a) {
+  constexpr int kGW = kEpiWarps / G;   // warps per epilogue group
+  constexpr int kPMax = G == 2 ? 2 : 4;
+  constexpr uint32_t kStageCols = G == 2 ? 256u : 0u;
+  extern __shared__ unsigned char smem_dyn[];
+  unsigned char* base = smem_dyn + ((1024 - (smem_u32(smem_dyn) & 1023)) & 1023);
+  const int stages = a.stages;
+  unsigned char* ring = base;
+  GCtrl* ctrl = reinterpret_cast<GCtrl*>(ring + (size_t)stages * kGStageBytes);
+  int16_t* cnt = reinterpret_cast<int16_t*>(ctrl + 1);  // [G][kPMax][96][kCntPitch]
+  double* sbins = reinterpret_cast<double*>(cnt + (size_t)G * kPMax * 96 * kCntPitch);
+  double* acc = sbins + (kMaxBins + 1);                 // [n_bins][n_stats]
+  unsigned long long* bcnt =
+      reinterpret_cast<unsigned long long*>(acc + (size_t)a.n_bins * a.n_stats);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  volatile int* abort_flag = &ctrl->abort_flag;
+  const int P = a.n_pops;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&ctrl->full[s], 1);
+      mbar_init(&ctrl->empty[s], 1);
+    }
+    for (int s = 0; s < G; ++s) {
+      mbar_init(&ctrl->tfull[s], 1);
+      mbar_init(&ctrl->tempty[s], kGW);
+    }
+    mbar_init(&ctrl->drain, 1);
+    ctrl->abort_flag = 0;
+    ctrl->consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ctrl->tmem_base)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  for (int s = 0; s < stages; ++s) {
+    uint4* z = reinterpret_cast<uint4*>(ring + (size_t)s * kGStageBytes + kBlkRows * kKChunk);
+    for (int k = threadIdx.x; k < (kABytes - kBlkRows * kKChunk) / 16; k += blockDim.x)
+      z[k] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  for (int x = threadIdx.x; x < a.n_bins * a.n_stats; x += blockDim.x) acc[x] = 0.0;
+  for (int x = threadIdx.x; x < a.n_bins; x += blockDim.x) bcnt[x] = 0ull;
+  for (int x = threadIdx.x; x <= a.n_bins; x += blockDim.x) sbins[x] = a.bins[x];
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = ctrl->tmem_base;
+
+  long long n_items = a.item_off[a.n_blocks];
+  if (n_items < 0 || n_items > a.n_blocks * (a.n_blocks + 1) / 2) {
+    if (threadIdx.x == 0) set_abort(ctrl, a.status, 4101);
+    n_items = 0;
+  }
+
+  if (warp == 0) {
+    // ---------------- TMA producer: per tile, every population's K chunks ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued = 0;
+      long long lo = 0;
+      bool ok = true;
+      for (long long item = blockIdx.x; item < n_items && ok && !*abort_flag; item += gridDim.x) {
+        lo = advance_block(a.item_off, a.n_blocks, lo, item);
+        const long long jb = lo + (item - a.item_off[lo]);
+        for (int p = 0; p < P && ok; ++p)
+          for (int kc = 0; kc < a.kchunks; ++kc) {
+            if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+              set_abort(ctrl, a.status, 4102);
+              ok = false;
+              break;
+            }
+            unsigned char* sa = ring + (size_t)stage * kGStageBytes;
+            mbar_expect_tx(&ctrl->full[stage], 2 * kBBytes);
+            tma_load_2d(sa, &map, &ctrl->full[stage], kc * kKChunk,
+                        p * a.pop_rows + (int)(lo * kBlkRows));
+            tma_load_2d(sa + kABytes, &map, &ctrl->full[stage], kc * kKChunk,
+                        p * a.pop_rows + (int)(jb * kBlkRows));
+            ++issued;
+            if (++stage == stages) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+      }
+      if (*abort_flag) {
+        const int consumed = *(volatile int*)&ctrl->consumed;
+        int st2 = consumed % stages;
+        uint32_t ph2 = (uint32_t)((consumed / stages) & 1);
+        for (int k = consumed; k < issued; ++k) {
+          mbar_wait_drain(&ctrl->full[st2], ph2);
+          if (++st2 == stages) {
+            st2 = 0;
+            ph2 ^= 1;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int consumed = 0;
+      bool any = false, ok = true;
+      for (int t = 0; ok && !*abort_flag; ++t) {
+        if ((long long)blockIdx.x + (long long)t * gridDim.x >= n_items) break;
+        const int sg = t % G;
+        const uint32_t tph = (uint32_t)((t / G) & 1);
+        if (!mbar_wait_poll(&ctrl->tempty[sg], tph ^ 1, abort_flag)) {
+          set_abort(ctrl, a.status, 4103);
+          break;
+        }
+        tc_fence_after();
+        for (int p = 0; p < P && ok; ++p) {
+          const uint32_t d = tmem_base + (uint32_t)sg * kStageCols + (uint32_t)(p * 96);
+          for (int kc = 0; kc < a.kchunks; ++kc) {
+            if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag)) {
+              set_abort(ctrl, a.status, 4104);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(ring + (size_t)stage * kGStageBytes);
+            const uint64_t da = smem_desc(sa), db = smem_desc(sa + kABytes);
+#pragma unroll
+            for (int k = 0; k < kKChunk / 32; ++k)
+              mma_f8_n96(d, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), (kc | k) != 0);
+            mma_commit(&ctrl->empty[stage]);
+            any = true;
+            *(volatile int*)&ctrl->consumed = ++consumed;
+            if (++stage == stages) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+        if (!ok) break;
+        mma_commit(&ctrl->tfull[sg]);
+      }
+      if (*abort_flag && any) {
+        mma_commit(&ctrl->drain);
+        mbar_wait_drain(&ctrl->drain, 0);
+      }
+    }
+  } else if (warp >= 4) {
+    // ---------------- epilogue ----------------
+    const int e = warp - 4;
+    const int grp = e / kGW;
+    const int gi = e % kGW;                // warp within the group
+    const int wq = warp & 3;               // TMEM lane quarter: plane wq of the SNPs i
+    const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+    const uint32_t bar_id = 1u + (uint32_t)grp;
+    int16_t* gbuf = cnt + (size_t)grp * kPMax * 96 * kCntPitch;
+    long long lo = 0;
+    for (int t = grp, u = 0;; t += G, ++u) {
+      const long long item = (long long)blockIdx.x + (long long)t * gridDim.x;
+      if (item >= n_items) break;
+      bool ready = true;
+      if (lane == 0) ready = mbar_wait(&ctrl->tfull[grp], (uint32_t)(u & 1), abort_flag);
+      ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
+      if (!ready && lane == 0) set_abort(ctrl, a.status, 4105);
+      // the group meets before overwriting its moment buffers and takes one
+      // decision on aborting (bar.red.or over every thread's view)
+      uint32_t any_abort = 0;
+      const uint32_t mine = (ready ? 0u : 1u) | (uint32_t)(*abort_flag != 0);
+      asm volatile(
+          "{\n .reg .pred pin, pout;\n setp.ne.u32 pin, %1, 0;\n"
+          " bar.red.or.pred pout, %2, %3, pin;\n selp.u32 %0, 1, 0, pout;\n}"
+          : "=r"(any_abort)
+          : "r"(mine), "r"(bar_id), "r"(kGW * 32)
+          : "memory");
+      if (any_abort) break;
+      tc_fence_after();
+      // copy: the warps of lane quarters 0-2 copy plane wq's moments of the
+      // populations they own (with two warps per quarter, alternate ones)
+      if (wq < 3) {
+        const int half = gi >> 2;   // 0 with four warps per group
+        for (int p = half; p < P; p += kGW / 4) {
+          int16_t* row = gbuf + ((size_t)p * 96 + wq * 32 + lane) * kCntPitch;
+#pragma unroll 1
+          for (int h = 0; h < 2; ++h) {
+            uint32_t r[3][16];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              tmem_ld16(tmem_base + lane_base +
+                            ((uint32_t)grp * kStageCols + (uint32_t)(p * 96 + 48 * h + 16 * c)),
+                        r[c]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+              for (int v = 0; v < 16; ++v)
+                row[48 * h + 16 * c + v] = (int16_t)fast::f2i_small(__uint_as_float(r[c][v]));
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&ctrl->tempty[grp]);
+      asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(kGW * 32) : "memory");
+
+      lo = advance_block(a.item_off, a.n_blocks, lo, item);
+      const long long i0 = lo * kTileSnp, j0 = (lo + (item - a.item_off[lo])) * kTileSnp;
+      const long long j = j0 + lane;
+      const bool j_ok = j < a.n_snp;
+      const double pj = j_ok ? a.pos[j] : 0.0;
+      const double cj = (j_ok && a.bcoord) ? a.bcoord[j] : 0.0;
+#pragma unroll 1
+      for (int k = 0; k < 32 / kGW; ++k) {
+        const int il = gi + kGW * k;
+        const long long i = i0 + il;
+        bool ok = i < j && j_ok;
+        double dpos = 0.0;
+        if (ok) {
+          dpos = pj - a.pos[i];
+          ok = dpos <= a.max_dist;
+        }
+        int b = -1;
+        if (ok) {
+          const double d = a.bcoord ? fabs(cj - a.bcoord[i]) : dpos;
+          b = bin_of_f64(sbins, a.n_bins, d);
+        }
+        unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
+        if (!pending) continue;
+        if (P == 1) {
+          // one population: DD, Dz, pi2 in float32 from the moments
+          // (gmom::stats_f32, within 1e-6 relative of each exact value)
+          gmom::Mom mo;
+#pragma unroll
+          for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int y = 0; y < 3; ++y)
+              mo.m[3 * x + y] = gbuf[(x * 32 + il) * kCntPitch + y * 32 + lane];
+          const float4 o4 = gmom::stats_f32<14>(mo, 14);
+          while (pending) {
+            const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
+            const bool mine = (b == bb);
+            const unsigned grpm = __ballot_sync(0xffffffffu, mine);
+            float v[3] = {mine ? o4.y : 0.f, mine ? o4.z : 0.f, mine ? o4.w : 0.f};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+#pragma unroll
+              for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+            }
+            if (lane == 0) {
+#pragma unroll
+              for (int q = 0; q < 3; ++q) atomicAdd(&acc[bb * 3 + q], (double)v[q]);
+              atomicAdd(&bcnt[bb], (unsigned long long)__popc(grpm));
+            }
+            pending &= ~grpm;
+          }
+          continue;
+        }
+        int cc[kPMax][9];
+        geno::GPop gp[kPMax];
+        const int* cp[kPMax];
+#pragma unroll
+        for (int p = 0; p < kPMax; ++p) {
+          if (p < P) {
+            gmom::Mom mo;
+            const int16_t* bp = gbuf + (size_t)p * 96 * kCntPitch;
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+#pragma unroll
+              for (int y = 0; y < 3; ++y) mo.m[3 * x + y] = bp[(x * 32 + il) * kCntPitch + y * 32 + lane];
+            gmom::to_counts(mo, cc[p]);
+            gp[p] = geno::make_gpop(cc[p], -1);
+          }
+          cp[p] = cc[p];
+        }
+        while (pending) {
+          const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
+          const bool mine = (b == bb);
+          const unsigned grpm = __ballot_sync(0xffffffffu, mine);
+          int tt = 0;
+          for (int s = 0; s < a.n_stats; ++s) {
+            float v = 0.f;
+            for (; tt < a.n_terms && a.terms[tt].stat == s; ++tt) {
+              const pgld_term tm = a.terms[tt];
+              if (mine) v += (float)tm.weight * geno::term_value<float>(tm, gp, cp);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) atomicAdd(&acc[bb * a.n_stats + s], (double)v);
+          }
+          if (lane == 0) atomicAdd(&bcnt[bb], (unsigned long long)__popc(grpm));
+          pending &= ~grpm;
+        }
+      }
+    }
+  }
+
+  // ---------------- teardown ----------------
+  tc_fence_before();
+  __syncthreads();
+  if (!*abort_flag) {
+    for (int x = threadIdx.x; x < a.n_bins * a.n_stats; x += blockDim.x)
+      if (acc[x] != 0.0) atomicAdd(a.sums + x, acc[x]);
+    if (a.pair_counts)
+      for (int x = threadIdx.x; x < a.n_bins; x += blockDim.x)
+        if (bcnt[x]) atomicAdd(a.pair_counts + x, bcnt[x]);
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(512)
+                 : "memory");
+  }
+}
+
 }  // namespace gtc
 }  // namespace pgld
 
@@ -588,5 +942,87 @@ int pgld_geno_tc_pairs(pgld_context* h, const pgld_geno_panel* panel, const doub
   pgld_time_end(h, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "gtc_pairs_kernel");
+  return PGLD_OK;
+}
+
+// Genotype distance-binned sums on the tensor cores: 1-4 populations of
+// dosages 0/1/2 (missing allowed, no values above 2), at most kMaxGenoN
+// individuals each; ba carries the bins, term table and outputs (sums and
+// pair counts already zeroed).
+int pgld_geno_tc_binned(pgld_context* h, const pgld_geno_panel* panel, const pgld::BandArgs& ba,
+                        cudaStream_t st) {
+  using namespace pgld::gtc;
+  int rc = pgld::tchost::get_encode(h);
+  if (rc) return rc;
+  const int P = panel->n_pops;
+  const long long n = panel->n_snp;
+  const long long nb = (n + kTileSnp - 1) / kTileSnp;
+  int W = 0;
+  for (int p = 0; p < P; ++p) W = std::max(W, panel->n_words[p]);
+  if ((long long)P * nb * kBlkRows > 2147483647LL)
+    return pgld_fail(h, PGLD_ERR_TOO_LARGE, "genotype tensor-core binned form: too many SNPs");
+  const int k_pad = ((W * 32 + kKChunk - 1) / kKChunk) * kKChunk;
+  const size_t op_pop = (size_t)nb * kBlkRows * k_pad;
+  const size_t sb = pgld::scan_scratch_bytes(nb);
+  auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+  const size_t off_items = 0, off_scan = al((nb + 1) * 8), off_op = off_scan + al(sb),
+               total = off_op + al(op_pop * P);
+  void* ws = nullptr;
+  rc = pgld_workspace(h, total, &ws);
+  if (rc) return rc;
+  char* w = (char*)ws;
+  long long* items = (long long*)(w + off_items);
+  unsigned char* op = (unsigned char*)(w + off_op);
+  for (int p = 0; p < P; ++p) {
+    const unsigned blocks = (unsigned)std::max<long long>(1, (nb * kBlkRows + 7) / 8);
+    pack_gtc_kernel<<<blocks, 256, 0, st>>>(panel->planes[p], panel->n_words[p], n, nb, k_pad,
+                                            (uint32_t*)(op + op_pop * p));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_gtc_kernel");
+  }
+  rc = pgld::band_schedule(h, ba.pos, n, ba.max_dist, items, w + off_scan, sb, st, kTileSnp);
+  if (rc) return rc;
+  CUtensorMap map;
+  rc = pgld::tchost::make_map(h, &map, op, (long long)P * nb * kBlkRows, k_pad, kBlkRows);
+  if (rc) return rc;
+  BParams prm{};
+  prm.kchunks = k_pad / kKChunk;
+  prm.n_snp = n;
+  prm.item_off = items;
+  prm.n_blocks = nb;
+  prm.n_pops = P;
+  prm.pop_rows = (int)(nb * kBlkRows);
+  prm.pos = ba.pos;
+  prm.bcoord = ba.bcoord;
+  prm.max_dist = ba.max_dist;
+  prm.bins = ba.bins;
+  prm.n_bins = ba.n_bins;
+  prm.terms = ba.terms;
+  prm.n_terms = ba.n_terms;
+  prm.n_stats = ba.n_stats;
+  prm.sums = ba.sums;
+  prm.pair_counts = reinterpret_cast<unsigned long long*>(ba.pair_counts);
+  prm.status = h->dev_status;
+  const int G = P <= 2 ? 2 : 1;
+  const int pmax = G == 2 ? 2 : 4;
+  const size_t fixed = sizeof(GCtrl) + (size_t)G * pmax * 96 * kCntPitch * 2 +
+                       (size_t)(pgld::kMaxBins + 1) * 8 + (size_t)ba.n_bins * ba.n_stats * 8 +
+                       (size_t)ba.n_bins * 8 + 1024;
+  int max_smem = 0;
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  const int stages =
+      (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kGStageBytes);
+  if (stages < 2)
+    return pgld_fail(h, PGLD_ERR_TOO_LARGE, "genotype tensor-core binned form: shared memory");
+  prm.stages = stages;
+  const size_t smem = (size_t)stages * kGStageBytes + fixed;
+  void (*kern)(CUtensorMap, BParams) = G == 2 ? gtc_binned_kernel<2> : gtc_binned_kernel<1>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "gtc binned smem attribute");
+  pgld_time_begin(h, st);
+  kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map, prm);
+  pgld_time_end(h, st);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "gtc_binned_kernel");
   return PGLD_OK;
 }

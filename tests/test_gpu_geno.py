@@ -180,6 +180,58 @@ def test_binned_sums_match_reference(golden, P):
     assert np.all(np.abs(np_(sums) - z[f"sums_{P}"]) <= SUM_TOL * ref_abs + 1e-300)
 
 
+@pytest.mark.parametrize("sizes,missing,coords", [([300], 0.03, False), ([120, 77], 0.02, False),
+                                                  ([40, 33, 65], 0.0, True),
+                                                  ([20, 31, 50, 9], 0.05, False)])
+def test_tc_binned_sums_match_plain_and_oracle(sizes, missing, coords):
+    """The tensor-core genotype binned form (moments from tcgen05 MMAs, one
+    chain per population) against the popcount form and the oracle: 1-4
+    populations of uneven sizes, missing dosages, a partial last tile,
+    pairs below the first bin, binning by a second coordinate."""
+    P = len(sizes)
+    rng = np.random.default_rng(700 + P)
+    M = 1_037
+    g = dosages(rng, sum(sizes), M, 6, 0.01, missing)
+    edges = np.concatenate([[0], np.cumsum(sizes)])
+    rows = [np.arange(edges[q], edges[q + 1], dtype=np.int32) for q in range(P)]
+    pos = np.sort(rng.choice(2_000_000, M, replace=False)).astype(np.int64)
+    pos_d = _ops.positions_f64(pos)
+    gt = torch.as_tensor(g, device="cuda")
+    pops = [_ops.pack_geno(gt, r) for r in rows]
+    if coords:
+        rate = np.cumsum(rng.uniform(0.2, 2.0, M)) * 1e-6      # Morgans, uneven local rates
+        bins = np.linspace(0.0, rate[-1] / 8, 7)
+        max_dist = 400_000.0
+        bc = torch.as_tensor(rate, device="cuda")
+    else:
+        bins = np.logspace(2.5, 5.3, 9)
+        max_dist, bc, rate = None, None, None
+    s_tc, c_tc = _ops.geno_binned_sums(pops, pos_d, bins, max_dist=max_dist, bin_coord=bc,
+                                       form="tc")
+    s_pl, c_pl = _ops.geno_binned_sums(pops, pos_d, bins, max_dist=max_dist, bin_coord=bc,
+                                       form="plain")
+    ref, ref_cnt, ref_abs = O.geno_binned_sums(g, pos, rows, bins, coords=rate,
+                                               max_dist=max_dist, abs_sums=True)
+    assert np.array_equal(np_(c_tc), ref_cnt) and np.array_equal(np_(c_pl), ref_cnt)
+    assert ref_cnt.sum() > 10_000
+    assert np.all(np.abs(np_(s_tc) - ref) <= SUM_TOL * ref_abs + 1e-300)
+    assert np.all(np.abs(np_(s_tc) - np_(s_pl)) <= SUM_TOL * ref_abs + 1e-300)
+
+
+def test_tc_binned_rejects_dosages_above_two():
+    rng = np.random.default_rng(5)
+    g = dosages(rng, 40, 200, 4, 0.01)
+    g[3, 17] = 3
+    pos = np.sort(rng.choice(100_000, 200, replace=False)).astype(np.int64)
+    pk = _ops.pack_geno(torch.as_tensor(g, device="cuda"))
+    with pytest.raises(PgldError):
+        _ops.geno_binned_sums([pk], _ops.positions_f64(pos), np.logspace(2, 4, 5), form="tc")
+    # auto takes the popcount form for such panels
+    s, c = _ops.geno_binned_sums([pk], _ops.positions_f64(pos), np.logspace(2, 4, 5))
+    ref, ref_cnt = O.geno_binned_sums(g, pos, [np.arange(40)], np.logspace(2, 4, 5))
+    assert np.array_equal(np_(c), ref_cnt)
+
+
 def test_moments_ld_genotype_and_haplotype_paths(golden):
     z = golden("moments_im")
     sets = {"deme0": list(map(int, z["rows0"])), "deme1": list(map(int, z["rows1"]))}
