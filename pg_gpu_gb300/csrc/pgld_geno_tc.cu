@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (RES && first) {
           // a new strip: its row block replaces the resident B once the MMAs
           // of the previous strip are done with it
-          if (strips > 0 && !mbar_wait_poll(&ctrl->bempty, (uint32_t)((strips - 1) & 1),
+          if (strips > 0 && !mbar_wait_role(&ctrl->bempty, (uint32_t)((strips - 1) & 1),
                                             abort_flag)) {
             set_abort(ctrl, a.status, 4006);
             break;
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           ++strips;
         }
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+          if (!mbar_wait_role(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
             set_abort(ctrl, a.status, 4002);
             ok = false;
             break;
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (tile_item(t, chunk) >= n_items) break;
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait_poll(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
+        if (!mbar_wait_role(&ctrl->tempty[acc], aph ^ 1, abort_flag)) {
           set_abort(ctrl, a.status, 4003);
           break;
         }
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true, last = false;
         const uint32_t d = tmem_base + (uint32_t)(acc * 128);
         for (int kc = 0; kc < a.kchunks; ++kc) {
-          if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag)) {
+          if (!mbar_wait_role(&ctrl->full[stage], phase, abort_flag)) {
             set_abort(ctrl, a.status, 4004);
             ok = false;
             break;
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int m = ctrl->meta[stage];
             last = (m & 2) != 0;
             if (RES && (m & 1)) {
-              if (!mbar_wait_poll(&ctrl->bfull, (uint32_t)(strips & 1), abort_flag)) {
+              if (!mbar_wait_role(&ctrl->bfull, (uint32_t)(strips & 1), abort_flag)) {
                 set_abort(ctrl, a.status, 4007);
                 ok = false;
                 break;
@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const long long jb = lo + (item - a.item_off[lo]);
         for (int p = 0; p < P && ok; ++p)
           for (int kc = 0; kc < a.kchunks; ++kc) {
-            if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
+            if (!mbar_wait_role(&ctrl->empty[stage], phase ^ 1, abort_flag)) {
               set_abort(ctrl, a.status, 4102);
               ok = false;
               break;
@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if ((long long)blockIdx.x + (long long)t * gridDim.x >= n_items) break;
         const int sg = t % G;
         const uint32_t tph = (uint32_t)((t / G) & 1);
-        if (!mbar_wait_poll(&ctrl->tempty[sg], tph ^ 1, abort_flag)) {
+        if (!mbar_wait_role(&ctrl->tempty[sg], tph ^ 1, abort_flag)) {
           set_abort(ctrl, a.status, 4103);
           break;
         }
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && ok; ++p) {
           const uint32_t d = tmem_base + (uint32_t)sg * kStageCols + (uint32_t)(p * 96);
           for (int kc = 0; kc < a.kchunks; ++kc) {
-            if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag)) {
+            if (!mbar_wait_role(&ctrl->full[stage], phase, abort_flag)) {
               set_abort(ctrl, a.status, 4104);
               ok = false;
               break;

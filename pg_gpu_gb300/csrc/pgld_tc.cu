@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && !*abort_flag; ++p) {
           const CUtensorMap* map = p == 0 ? &map0 : &map1;
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait_poll(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
+            if (!mbar_wait_role(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
               set_abort(ctrl, a.status, 3002);
               break;
             }
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long item = blockIdx.x; item < n_items && !*abort_flag; item += gridDim.x, ++t) {
         const int acc = t & 1;
         const uint32_t aph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait_poll(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
+        if (!mbar_wait_role(&ctrl->tempty[acc], aph ^ 1, abort_flag, a.wait_cycles)) {
           set_abort(ctrl, a.status, 3003);
           break;
         }
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int p = 0; p < P && ok; ++p) {
           const uint32_t d = tmem_base + (uint32_t)(acc * 256 + p * 128);
           for (int kc = 0; kc < a.kchunks[p]; ++kc) {
-            if (!mbar_wait_poll(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
+            if (!mbar_wait_role(&ctrl->full[stage], phase, abort_flag, a.wait_cycles)) {
               set_abort(ctrl, a.status, 3004);
               ok = false;
               break;

@@ -626,22 +626,24 @@ __global__ void __launch_bounds__(kThreads, 1)
             flush();
             float2 st[kS];
             fast2::stats2_raw(p0, p1, T4, st);
+            // one warp total per distinct bin of the step's 64 pairs (both
+            // pairs of a lane at once), lowest bin first
+            int rx = bx, ry = by;
 #pragma unroll 1
-            for (int hsel = 0; hsel < 2; ++hsel) {
-              const int b = hsel ? by : bx;
-              unsigned pending = __ballot_sync(0xffffffffu, b >= 0);
-              while (pending) {
-                const int bb = __shfl_sync(0xffffffffu, b, __ffs(pending) - 1);
-                const bool mine = (b == bb);
-                const unsigned grp = __ballot_sync(0xffffffffu, mine);
-                float v[kS];
+            for (;;) {
+              const int lo2 = min(rx < 0 ? 0x7fffffff : rx, ry < 0 ? 0x7fffffff : ry);
+              const int bb = __reduce_min_sync(0xffffffffu, lo2);
+              if (bb == 0x7fffffff) break;
+              const bool mx = rx == bb, my = ry == bb;
+              float v[kS];
 #pragma unroll
-                for (int s = 0; s < kS; ++s) v[s] = mine ? (hsel ? st[s].y : st[s].x) : 0.f;
-                const float tot = warp_totals<kS>(v, lane);
-                if (leader) slot_add(bb, kl, tot);
-                if (lane == 31) cnt_add(bb, (unsigned long long)__popc(grp));
-                pending &= ~grp;
-              }
+              for (int s = 0; s < kS; ++s) v[s] = (mx ? st[s].x : 0.f) + (my ? st[s].y : 0.f);
+              const float tot = warp_totals<kS>(v, lane);
+              if (leader) slot_add(bb, kl, tot);
+              const int nb = __reduce_add_sync(0xffffffffu, (mx ? 1 : 0) + (my ? 1 : 0));
+              if (lane == 31) cnt_add(bb, (unsigned long long)nb);
+              if (mx) rx = -1;
+              if (my) ry = -1;
             }
           });
           flush();

@@ -112,6 +112,28 @@ __device__ __forceinline__ bool mbar_wait_nap(uint64_t* b, uint32_t parity,
   }
   return false;
 }
+// the wait of a single producer / MMA-issuer thread: try_wait suspends the
+// thread until the phase completes or a hardware time limit passes, so the
+// waiting thread takes few issue slots from the epilogue warps of its
+// sub-partition (PGLD_ROLE_WAIT 0: polling test_wait, mbar_wait_poll);
+// false once `limit` cycles passed or another role aborted
+#ifndef PGLD_ROLE_WAIT
+#define PGLD_ROLE_WAIT 1
+#endif
+__device__ __forceinline__ bool mbar_wait_role(uint64_t* b, uint32_t parity,
+                                               volatile int* abort_flag,
+                                               long long limit = kWaitCycles) {
+#if PGLD_ROLE_WAIT
+  const long long t0 = clock64();
+  for (long long k = 0; k < kSpinLimit; ++k) {
+    if (mbar_try_for(b, parity, kSuspendNs)) return true;
+    if ((k & 7) == 7 && (*abort_flag || clock64() - t0 > limit)) return false;
+  }
+  return false;
+#else
+  return mbar_wait_poll(b, parity, abort_flag, limit);
+#endif
+}
 // drain wait: bounded by time only
 __device__ __forceinline__ void mbar_wait_drain(uint64_t* b, uint32_t parity) {
   const long long t0 = clock64();
