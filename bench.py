@@ -561,6 +561,7 @@ def run_windows(args):
     torch.cuda.set_device(0)
     rng = np.random.default_rng(20261504)
     sizes = np.exp(rng.uniform(np.log(500), np.log(20_000), 512)).astype(np.int64)
+    sizes = sizes[:args.windows]  # a smaller case for profiler captures: the first windows
     torch.manual_seed(20261504)
     parts = []
     for w, m in enumerate(sizes):
@@ -609,11 +610,11 @@ def run_windows(args):
     s_pl, c_pl = one_plain()
     assert torch.equal(cnt, c_pl)
     print(json.dumps({
-        "metric": "within-window SNP-pairs/s, 512 uneven windows, 400 haplotypes",
+        "metric": f"within-window SNP-pairs/s, {len(sizes)} uneven windows, 400 haplotypes",
         "value": n_pairs / (t_one / 1e3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_one, "higher_is_better": True,
         "dtype": "e4m3", "data": "synthetic (copying model, seed per window)",
-        "config": {"workload": "windows512", "haplotypes": 400, "windows": 512,
+        "config": {"workload": "windows512", "haplotypes": 400, "windows": int(len(sizes)),
                    "n_snp": int(sizes.sum()), "pairs": n_pairs, "form": "tc"},
         "roofline": tc_roofline(n_pairs / (t_one / 1e3), 8 * 400, "whole call, wall clock"),
         "plain_one_launch": {"ms_per_step": t_plain, "value": n_pairs / (t_plain / 1e3)},
@@ -805,6 +806,8 @@ def main():
                                                  "hap_band"])
     ap.add_argument("--geno-snps", type=int, default=500_000)
     ap.add_argument("--geno-pops", type=int, default=2, choices=[1, 2, 3, 4])
+    ap.add_argument("--windows", type=int, default=512,
+                    help="windows512: time the first N of the 512 windows (profiler captures)")
     ap.add_argument("--geno-counts", action="store_true", help="also write the 9-way counts")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-pairs-per-worker", type=int, default=400_000)
