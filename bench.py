@@ -753,10 +753,11 @@ def run_hap_band(args):
     torch.cuda.set_device(0)
     g = torch.Generator(device=dev)
     g.manual_seed(20261502)
-    M = 100_000
+    M = args.hap_snps
     hap = synthetic.copying_panel(g, 2000, M, 50, 5e-4, 1e-3, 0.02, dev)
     rng = np.random.default_rng(20261502)
-    pos = np.sort(rng.choice(10_000_000, M, replace=False)).astype(np.int64)
+    # 100 bp per SNP on average (10 Mb for the 100,000 SNPs of the workload)
+    pos = np.sort(rng.choice(100 * M, M, replace=False)).astype(np.int64)
     pos_d = _ops.positions_f64(pos)
     _, n_pairs = _ops.band_offsets(pos_d, 100_000)
     flush = torch.empty(256 << 20, dtype=torch.int8, device=dev)
@@ -805,6 +806,8 @@ def main():
                     choices=sorted(WORKLOADS) + ["windows512", "geno_band", "geno_binned",
                                                  "hap_band"])
     ap.add_argument("--geno-snps", type=int, default=500_000)
+    ap.add_argument("--hap-snps", type=int, default=100_000,
+                    help="hap_band: SNPs (same density; smaller cases for profiler captures)")
     ap.add_argument("--geno-pops", type=int, default=2, choices=[1, 2, 3, 4])
     ap.add_argument("--windows", type=int, default=512,
                     help="windows512: time the first N of the 512 windows (profiler captures)")

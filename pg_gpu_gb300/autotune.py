@@ -10,6 +10,8 @@ call and the GPU:
 * layout of the binned two-population form: 1 = tiles of 64 x 64 SNPs with
   one accumulator per population (M = N = 128 MMAs), 2 = tiles of 64 x 128
   SNPs with both populations in one accumulator (M = 128, N = 256 MMAs);
+  of the one-population per-pair and window forms: 1 = 64 x 64 tiles with
+  eight epilogue warps, 2 = 64 x 128 tiles with twelve;
 * stages: pipeline stages of the TMA ring (0 = as many as shared memory
   holds).  A K chunk is one 128-byte swizzle row of the operand; it is not
   a knob.
@@ -37,6 +39,8 @@ _cache = None
 _applied = {}
 
 BINNED2_CANDIDATES = [(layout, stages) for layout in (2, 1) for stages in (0, 4, 3, 2)]
+# per-pair outputs and window sums of one population: 64 x 128 (2) or 64 x 64 (1) tiles
+ONE_POP_CANDIDATES = [(layout, stages) for layout in (2, 1) for stages in (0, 4, 3, 2)]
 OTHER_CANDIDATES = [(0, stages) for stages in (0, 4, 3, 2)]
 
 
@@ -140,7 +144,7 @@ def tune(kind, words, n_snp=24_000, max_dist=1e6, save=True):
 
         def call():
             _ops.band_pairs(pops[0], pos_d, md, form="tc", _tuning=True)
-        cands = OTHER_CANDIDATES
+        cands = ONE_POP_CANDIDATES
     elif kind == "windows":
         sizes = np.full(max(1, n_snp // 2_000), 2_000)
         ends = np.cumsum(sizes)
@@ -149,7 +153,7 @@ def tune(kind, words, n_snp=24_000, max_dist=1e6, save=True):
 
         def call():
             _ops.window_sums(pops[0], None, begins, ends, form="tc", _tuning=True)
-        cands = OTHER_CANDIDATES
+        cands = ONE_POP_CANDIDATES
     else:
         raise ValueError(f"unknown call kind {kind!r}")
     h = L.handle()

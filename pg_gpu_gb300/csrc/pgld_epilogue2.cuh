@@ -205,6 +205,27 @@ PGLD_HD void stats2(const Pop& p, const Pop& q, const float4* T4, V o[15]) {
 // power of two commutes with every rounding of a sum of the sink's products)
 PGLD_HD constexpr double post2(int k) { return k == 11 ? kPost11 : k == 12 ? kPost12 : 1.0; }
 
+// a / b with b > 0: the CUDA fast division (within 2 ulp for b below 2^126)
+PGLD_HD float fdiv(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// the per-pair outputs of two pairs: r^2 (NaN where p_A q_A p_B q_B = 0), and
+// DD, Dz, pi2 times r4 = 1/(n(n-1)(n-2)(n-3)) of each lane (0 below n = 4)
+PGLD_HD void pair_outputs(const Pop& p, V r4, float4 (&st)[2]) {
+  const V dd = vmul(dd_num(p), r4);
+  const V dz = vmul(dz_num(p, vfma(p.dA, p.dB, p.e)), r4);
+  const V pi = vmul(pi2_num(p), r4);
+  const V num = vmul(p.x, p.x);
+  const V den = vmul(vmul(p.pA, p.qA), vmul(p.pB, p.qB));
+  st[0] = make_float4(den.x > 0.f ? fdiv(num.x, den.x) : NAN, dd.x, dz.x, pi.x);
+  st[1] = make_float4(den.y > 0.f ? fdiv(num.y, den.y) : NAN, dd.y, dz.y, pi.y);
+}
+
 template <class Sink>
 PGLD_HD void stats1_to(const Pop& p, const float4* T4, Sink&& sink) {
   const V r4 = recip(T4, p.n0, p.n1).r4;

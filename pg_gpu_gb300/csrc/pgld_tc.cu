@@ -505,7 +505,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             const fast2::Pop p = fast2::make(u2(r[o], r[o + 1]), u2(r[o + 4], r[o + 5]),
                                              u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
             const int gg = 2 * gp + g;
-            win::window_pair2(p, u2(r[o], r[o + 1]), T, fi, l0 ? wfj[2 * gg] : zero4,
+            win::window_pair2(p, u2(r[o], r[o + 1]),
+                              [&](int n) { return make_float2(T.inv[n], T.r4[n]); }, fi,
+                              l0 ? wfj[2 * gg] : zero4,
                               l1 ? wfj[2 * gg + 1] : zero4, l0, l1, ws2, np, nr2, nfour);
           }
         }
@@ -568,16 +570,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                              u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
             const long long k = offh + (j - is - 1);  // row of (is, j); (is, j + 1) follows
             float4 st[2];
-            if (a.stats) {
-              const float2 r4 = make_float2(T.r4[p.n0], T.r4[p.n1]);
-              const float2 dd = fast2::vmul(fast2::dd_num(p), r4);
-              const float2 dz = fast2::vmul(fast2::dz_num(p, fast2::vfma(p.dA, p.dB, p.e)), r4);
-              const float2 pi = fast2::vmul(fast2::pi2_num(p), r4);
-              const float2 num = fast2::vmul(p.x, p.x);
-              const float2 den = fast2::vmul(fast2::vmul(p.pA, p.qA), fast2::vmul(p.pB, p.qB));
-              st[0] = make_float4(den.x > 0.f ? num.x / den.x : NAN, dd.x, dz.x, pi.x);
-              st[1] = make_float4(den.y > 0.f ? num.y / den.y : NAN, dd.y, dz.y, pi.y);
-            }
+            if (a.stats) fast2::pair_outputs(p, make_float2(T.r4[p.n0], T.r4[p.n1]), st);
 #pragma unroll
             for (int y = 0; y < 2; ++y) {
               const bool oky = y ? ok1 : ok0;
@@ -1054,9 +1047,33 @@ int pgld_tc_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs&
   return tc_launch(h, panel, a, pgld::kModeBinned, st);
 }
 
+int pgld_tc_wide_pairs(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
+                       cudaStream_t st);
+int pgld_tc_wide_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t* idx,
+                         long long n_idx, const long long* wb, const long long* we, int n_win,
+                         double* sums, unsigned long long* counts, cudaStream_t st);
+
+// per-pair outputs: 64 x 64 tiles unless the 64 x 128 layout (pgld_tc_wide.cu)
+// is configured (the output stores bound this form; at 2,000 haplotypes the
+// square tiles measured faster)
 int pgld_tc_pairs(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
                   cudaStream_t st) {
+  if (h->tc_layout == 2) return pgld_tc_wide_pairs(h, panel, a, st);
   return tc_launch(h, panel, a, pgld::kModePairs, st);
+}
+
+// the E4M3 operand rows of a population's bit planes over an index list
+// (pack_tc_kernel, rows grouped by 8 positions)
+int pgld_tc_pack_rows(pgld_context* h, const uint32_t* planes, int W, long long n_snp,
+                      long long n_rows, const int32_t* idx, int k_pad, unsigned char* out,
+                      cudaStream_t st) {
+  const long long rows_out = 2 * ((n_rows + 7) / 8 * 8);
+  const unsigned blocks = (unsigned)std::max<long long>(1, (rows_out + 7) / 8);
+  pgld::tc::pack_tc_kernel<<<blocks, 256, 0, st>>>(planes, W, n_snp, n_rows, idx, k_pad, 1,
+                                                   (uint32_t*)out, h->dev_status);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_tc_kernel");
+  return PGLD_OK;
 }
 
 namespace pgld {
@@ -1088,6 +1105,9 @@ int pgld_tc_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t*
                     long long n_idx, const long long* wb, const long long* we, int n_win,
                     double* sums, unsigned long long* counts, cudaStream_t st) {
   using namespace pgld::tc;
+  // 64 x 128 tiles (pgld_tc_wide.cu) unless the square layout is configured
+  if (h->tc_layout != 1)
+    return pgld_tc_wide_windows(h, panel, idx, n_idx, wb, we, n_win, sums, counts, st);
   int rc = get_encode(h);
   if (rc) return rc;
   const long long n = panel->n_snp;

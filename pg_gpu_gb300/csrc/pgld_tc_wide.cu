@@ -15,6 +15,12 @@
 // tensor work (four M128 N256 K32 MMAs), which keeps the tensor pipe fed
 // across the latency of the stage hand-offs.
 //
+// The same kernel serves one population in two more modes (a population's
+// counts straight from the accumulator, no split): per-pair outputs over the
+// distance band (counts, n, r^2, DD, Dz, pi2 in the reference's pair order)
+// and per-window sums over the 64 x 128 tiles of every window's upper
+// triangle (r^2, sigma_D^2, DD, Dz, pi2, naive r^2), all windows in one launch.
+//
 // Roles (one CTA per SM, 512 threads):
 //   warp 0      TMA producer: A box 128 rows x 128 B, B box 256 rows x 128 B
 //               (SWIZZLE_128B) per K chunk into a ring of 48 KB stages
@@ -32,6 +38,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "pgld_band.cuh"
 #include "pgld_epilogue.cuh"
@@ -40,6 +47,7 @@
 #include "pgld_scan.cuh"
 #include "pgld_tc_common.cuh"
 #include "pgld_tcgen05.cuh"
+#include "pgld_window.cuh"
 
 #ifndef PGLD_TCW_MAXNREG
 #define PGLD_TCW_MAXNREG 1
@@ -118,7 +126,71 @@ struct Params {
   const int* ipos_bad;
   long long wait_cycles;
   int no_copies;               // test hook: the TMA producer issues nothing
+  // per-pair outputs (pairs mode)
+  const long long* pair_off;   // [n_snp + 1] first output row of each SNP's pairs
+  int32_t* counts;             // [n_pairs][4]
+  int32_t* nvalid;             // [n_pairs] or NULL
+  float* stats;                // [n_pairs][4] r^2, DD, Dz, pi2, or NULL
+  // windows mode: operand rows are list positions; window w covers list
+  // positions [win_begin[w], win_end[w]), its tiles start at win_begin & ~7
+  const long long* win_begin;
+  const long long* win_end;
+  int n_win;
+  const long long* tile_off;   // [n_win + 1] prefix of the windows' tile counts
+  const int32_t* idx;          // list position -> SNP (NULL: identity)
+  const float4* site;          // per-SNP (dac, nv, 1 / nv, 1 / pq) of the naive r^2
+  long long n_panel;           // SNPs of the panel (bound of idx values)
+  double* wsums;               // [n_win][6]
+  unsigned long long* wcnt;    // [n_win][3]
 };
+
+// windows mode: row block b of a window of C column blocks holds the column
+// blocks b / 2 .. C - 1; the tiles before row block b
+__host__ __device__ __forceinline__ long long wtiles_before(long long b, long long C) {
+  const long long k = b >> 1;
+  return b * C - ((b & 1) ? k * k : k * (k - 1));
+}
+
+// a work item's tile: first list positions of its rows i0 and columns j0,
+// and (windows mode) its window [begin, end) and index
+struct WideTile {
+  long long i0, j0, begin, end;
+  int w;
+};
+
+// windows mode: the tile of an item, the window found by stepping forward
+// from the previous item's window (hint), then the row block by bisection
+__device__ __forceinline__ WideTile window_tile(const Params& a, long long item, long long& hint) {
+  int lo = (int)hint;
+  int steps = 0;
+  while (lo + 1 < a.n_win && a.tile_off[lo + 1] <= item && steps < 4) {
+    ++lo;
+    ++steps;
+  }
+  if (steps == 4) {
+    int hi = a.n_win;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (a.tile_off[mid] <= item) lo = mid; else hi = mid;
+    }
+  }
+  hint = lo;
+  const long long base = a.win_begin[lo] & ~7ll, m = a.win_end[lo] - base;
+  const long long R = (m + kRowSnp - 1) / kRowSnp, C = (m + kColSnp - 1) / kColSnp;
+  const long long t = item - a.tile_off[lo];
+  long long rlo = 0, rhi = R;
+  while (rhi - rlo > 1) {
+    const long long mid = (rlo + rhi) >> 1;
+    if (wtiles_before(mid, C) <= t) rlo = mid; else rhi = mid;
+  }
+  WideTile r;
+  r.i0 = base + rlo * kRowSnp;
+  r.j0 = base + ((rlo >> 1) + (t - wtiles_before(rlo, C))) * kColSnp;
+  r.begin = a.win_begin[lo];
+  r.end = a.win_end[lo];
+  r.w = lo;
+  return r;
+}
 
 __device__ __forceinline__ void mma_w(uint32_t d, uint64_t a, uint64_t b, uint32_t accum) {
   asm volatile(
@@ -180,6 +252,10 @@ __device__ __forceinline__ bool role_wait(uint64_t* b, uint32_t parity, volatile
 #endif
 }
 
+// MODE kModeBinned: distance-binned sums of two populations (combined
+// operand); kModePairs: per-pair outputs of one population; kModeWindows:
+// per-window sums of one population
+template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     band_wide_kernel(const __grid_constant__ CUtensorMap map_a,
                      const __grid_constant__ CUtensorMap map_b, Params a) {
@@ -231,7 +307,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int x = t; x < kSlotSets * n_bins; x += kEpiThreads) kcnt[x] = 0ull;
     for (int x = t; x <= a.nmax; x += kEpiThreads)
       fast2::recip_entry4(x, reinterpret_cast<float4*>(tables) + x);
-    for (int x = t; x <= n_bins; x += kEpiThreads) {
+    for (int x = t; MODE == kModeBinned && x <= n_bins; x += kEpiThreads) {
       const double b = a.bins[x];
       sbins[x] = b;
       const double cb = ceil(b);
@@ -243,12 +319,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tmem_base = ctrl->tmem_base;
 
-  long long n_items = a.item_off[a.n_rb];
-  if (n_items < 0 || n_items > a.n_rb * a.n_cb) {
+  long long n_items = MODE == kModeWindows ? a.tile_off[a.n_win] : a.item_off[a.n_rb];
+  if (n_items < 0 || (MODE != kModeWindows && n_items > a.n_rb * a.n_cb)) {
     if (threadIdx.x == 0) set_abort(ctrl, a.status, 3001);
     n_items = 0;
   }
-  if (n_items > 0 && a.n_anchor < a.n_snp) n_items = a.item_off[(a.n_anchor + kRowSnp - 1) / kRowSnp];
+  if (MODE == kModeBinned && n_items > 0 && a.n_anchor < a.n_snp)
+    n_items = a.item_off[(a.n_anchor + kRowSnp - 1) / kRowSnp];
 
   // Registers move from the producer / MMA warpgroup (warps 0-3) to the two
   // epilogue warpgroups: 128 x 56 + 256 x 224 = 384 x 168, the launch's total
@@ -265,9 +342,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       long long hint = 0;
       const long long n_copy_items = a.no_copies ? 0 : n_items;
       for (long long item = blockIdx.x; item < n_copy_items && !*abort_flag; item += gridDim.x) {
-        const long long bi = row_of(a, item, hint);
-        const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
-        const int yi = (int)(2 * bi * kRowSnp), yj = (int)(2 * bj * kColSnp);
+        int yi, yj;
+        if constexpr (MODE == kModeWindows) {
+          const WideTile tw = window_tile(a, item, hint);
+          yi = (int)(2 * tw.i0);
+          yj = (int)(2 * tw.j0);
+        } else {
+          const long long bi = row_of(a, item, hint);
+          const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
+          yi = (int)(2 * bi * kRowSnp);
+          yj = (int)(2 * bj * kColSnp);
+        }
         for (int kc = 0; kc < a.kchunks; ++kc) {
           if (!role_wait<PGLD_TCW_NAP_LONG>(&ctrl->empty[stage], phase ^ 1, abort_flag, a.wait_cycles)) {
             set_abort(ctrl, a.status, 3002);
@@ -359,14 +444,46 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double maxd = a.max_dist;
     const int maxd_int = maxd >= 2147483647.0 ? 2147483647 : (int)floor(maxd);
     // the largest distance in a bin (below INT_MAX, so top + 1 does not wrap)
-    const int top = thr[n_bins] > maxd_int ? maxd_int : thr[n_bins] - 1;
-    const bool use_int = (a.bcoord == nullptr) && (*a.ipos_bad == 0);
+    const int top = MODE != kModeBinned ? 0 : thr[n_bins] > maxd_int ? maxd_int : thr[n_bins] - 1;
+    const bool use_int = MODE == kModeBinned && (a.bcoord == nullptr) && (*a.ipos_bad == 0);
     double* my_acc = kacc + (size_t)(e & (kSlotSets - 1)) * n_bins * kS;
     unsigned long long* my_cnt = kcnt + (size_t)(e & (kSlotSets - 1)) * n_bins;
     auto slot_add = [&](int bin, int k, float v) { atomicAdd(my_acc + bin * kS + k, (double)v); };
     auto cnt_add = [&](int bin, unsigned long long v) { atomicAdd(my_cnt + bin, v); };
     long long hint = 0;
     bool aborted = false;
+    auto u2 = [](uint32_t x, uint32_t y) {
+      return make_float2(__uint_as_float(x), __uint_as_float(y));
+    };
+    // windows mode: the warp's running sums (per lane, compensated) and
+    // counts of its current window, added to the window's totals by win_emit
+    int cur_w = -1;
+    float run[6], comp[6];
+    int run_np = 0, run_r2 = 0, run_four = 0, run_units = 0;
+#pragma unroll
+    for (int s2 = 0; s2 < 6; ++s2) run[s2] = comp[s2] = 0.f;
+    auto win_emit = [&]() {
+      if (cur_w >= 0) {
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2) {
+          double v = (double)run[s2] + (double)comp[s2];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          if (lane == 0 && v != 0.0) atomicAdd(a.wsums + (long long)cur_w * 6 + s2, v);
+        }
+        const int tp = __reduce_add_sync(0xffffffffu, run_np);
+        const int tr2 = __reduce_add_sync(0xffffffffu, run_r2);
+        const int tf = __reduce_add_sync(0xffffffffu, run_four);
+        if (lane == 0) {
+          if (tp) atomicAdd(a.wcnt + (long long)cur_w * 3 + 0, (unsigned long long)tp);
+          if (tr2) atomicAdd(a.wcnt + (long long)cur_w * 3 + 1, (unsigned long long)tr2);
+          if (tf) atomicAdd(a.wcnt + (long long)cur_w * 3 + 2, (unsigned long long)tf);
+        }
+      }
+#pragma unroll
+      for (int s2 = 0; s2 < 6; ++s2) run[s2] = comp[s2] = 0.f;
+      run_np = run_r2 = run_four = run_units = 0;
+    };
 #pragma unroll 1
     for (long long Us = k_in_q;; Us += kPerQuarter) {
 #if PGLD_TCW_DYN
@@ -383,16 +500,200 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (item >= n_items) break;
       const int acc = (int)(t & 1);
       const uint32_t aph = (uint32_t)((t >> 1) & 1);
-      const long long bi = row_of(a, item, hint);
-      const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
-      const long long i0 = bi * kRowSnp, j0 = bj * kColSnp;
+      long long i0, j0;
+      WideTile tw{};
+      if constexpr (MODE == kModeWindows) {
+        tw = window_tile(a, item, hint);
+        i0 = tw.i0;
+        j0 = tw.j0;
+      } else {
+        const long long bi = row_of(a, item, hint);
+        const long long bj = (bi * kRowSnp) / kColSnp + (item - a.item_off[bi]);
+        i0 = bi * kRowSnp;
+        j0 = bj * kColSnp;
+      }
       const long long si0 = i0 + 16 * quarter;
       const long long ib = si0 + (lane >> 2);  // the lane's SNP i of row half 0 (half 1: + 8)
+      // the unit's 16 x 32 sub-tile: i in si0 + [0, 16), j in sj0 + [0, 32)
+      const long long sj0 = j0 + 32 * u;
+      const uint32_t colb = (uint32_t)(acc * 256 + u * 64);
+      auto release = [&]() {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ctrl->tempty[acc]);
+      };
+      auto wait_tile = [&]() {
+        // every lane waits (no divergent branch around the wait)
+        const bool ready =
+            __all_sync(0xffffffffu, mbar_wait(&ctrl->tfull[acc], aph, abort_flag, a.wait_cycles));
+        if (!ready && lane == 0) set_abort(ctrl, a.status, 3005);
+        tc_fence_after();
+        return ready;
+      };
+
+      if constexpr (MODE == kModePairs) {
+        // per-pair outputs.  A 16x256b TMEM load gives thread t all four
+        // counts of the pairs (i, j) and (i, j + 1), i = si0 + 8 hh + t / 4,
+        // j = sj0 + 8 g + 2 (t % 4); output rows k = pair_off[i] + (j - i - 1)
+        // in the reference's order, two consecutive rows per thread.  The band
+        // offsets of the lane's rows are loaded before the accumulator wait.
+        long long off0 = 0, np0 = 0, off1 = 0, np1 = 0;
+        if (ib < a.n_snp) {
+          off0 = a.pair_off[ib];
+          np0 = a.pair_off[ib + 1] - off0;
+        }
+        if (ib + 8 < a.n_snp) {
+          off1 = a.pair_off[ib + 8];
+          np1 = a.pair_off[ib + 9] - off1;
+        }
+        // no pair of the unit in the band: below the diagonal, past the last
+        // SNP, or past the band of each of its rows
+        const bool past = __all_sync(0xffffffffu, sj0 - ib - 1 >= np0 && sj0 - ib - 9 >= np1);
+        const bool none = past || sj0 + 31 <= si0 || si0 >= a.n_snp || sj0 >= a.n_snp;
+        if (!wait_tile()) {
+          aborted = true;
+          break;
+        }
+        if (none) {
+          release();
+          continue;
+        }
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+          const int hh = c & 1, gp = c >> 1;
+          uint32_t r[16];
+          tmem_ld16x256_x4(tmem_base + ((uint32_t)(quarter * 32 + hh * 16) << 16) + colb +
+                               (uint32_t)(gp * 32),
+                           r);
+          tmem_wait_ld();
+          if (c == 3) release();
+          const long long is = ib + 8 * hh;
+          const long long offh = hh ? off1 : off0, nph = hh ? np1 : np0;
+#pragma unroll
+          for (int g = 0; g < 2; ++g) {
+            const int o = 8 * g;
+            const long long j = sj0 + 8 * (2 * gp + g) + 2 * (lane & 3);
+            // a pair's row comes from the band offsets themselves, so a pair
+            // is written exactly when the offsets list it
+            const bool ok0 = is < j && j < a.n_snp && (j - is - 1) < nph;
+            const bool ok1 = is < j + 1 && j + 1 < a.n_snp && (j - is) < nph;
+            if (!ok0 && !ok1) continue;
+            const fast2::Pop p = fast2::make(u2(r[o], r[o + 1]), u2(r[o + 4], r[o + 5]),
+                                             u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
+            const long long k = offh + (j - is - 1);  // row of (is, j); (is, j + 1) follows
+            float4 st[2];
+            if (a.stats) fast2::pair_outputs(p, make_float2(T4[p.n0].w, T4[p.n1].w), st);
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+              const bool oky = y ? ok1 : ok0;
+              const int q = o + y;
+              st_cs_if(oky, reinterpret_cast<int4*>(a.counts) + (k + y),
+                       make_int4(fast::f2i_small(__uint_as_float(r[q])),
+                                 fast::f2i_small(__uint_as_float(r[q + 4])),
+                                 fast::f2i_small(__uint_as_float(r[q + 2])),
+                                 fast::f2i_small(__uint_as_float(r[q + 6]))));
+              if (a.nvalid) st_cs_if(oky, a.nvalid + (k + y), y ? p.n1 : p.n0);
+              if (a.stats) st_cs_if(oky, reinterpret_cast<float4*>(a.stats) + (k + y), st[y]);
+            }
+          }
+        }
+        continue;
+      }
+
+      if constexpr (MODE == kModeWindows) {
+        // per-window sums: every pair of list positions begin <= i < j < end
+        // of the tile's window; the unit's sums go to the warp's running sums
+        // of its current window (flushed when the window changes)
+        const long long wb_ = tw.begin, we_ = tw.end;
+        const long long il = si0 > wb_ ? si0 : wb_, ih = si0 + 15 < we_ - 1 ? si0 + 15 : we_ - 1;
+        const long long jl = sj0 > wb_ ? sj0 : wb_, jh = sj0 + 31 < we_ - 1 ? sj0 + 31 : we_ - 1;
+        const bool none = il > ih || jl > jh || il >= jh;
+        // every pair of the unit in the window
+        const bool full = si0 >= wb_ && si0 + 15 < sj0 && sj0 + 31 < we_;
+        // the naive-r^2 site terms of the lane's SNPs, loaded before the wait
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 wfi[2], wfj[8];
+        auto site_at = [&](long long pos) {
+          if (pos < wb_ || pos >= we_) return zero4;
+          const long long sp = a.idx ? (long long)a.idx[pos] : pos;
+          return (sp >= 0 && sp < a.n_panel) ? a.site[sp] : zero4;
+        };
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) wfi[hh] = none ? zero4 : site_at(ib + 8 * hh);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          wfj[q] = none ? zero4 : site_at(sj0 + 8 * (q >> 1) + 2 * (lane & 3) + (q & 1));
+        if (!wait_tile()) {
+          aborted = true;
+          break;
+        }
+        if (none) {
+          release();
+          continue;
+        }
+        if (tw.w != cur_w) {
+          win_emit();
+          cur_w = tw.w;
+        }
+        float2 ws2[6];
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2) ws2[s2] = make_float2(0.f, 0.f);
+        int np = 0, nr2 = 0, nfour = 0;
+        auto tab = [&](int n) {
+          const float4 e4 = T4[n];
+          return make_float2(e4.x, e4.w);
+        };
+        auto body = [&](auto full_c) {
+          constexpr bool F = decltype(full_c)::value;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int hh = c & 1, gp = c >> 1;
+            uint32_t r[16];
+            tmem_ld16x256_x4(tmem_base + ((uint32_t)(quarter * 32 + hh * 16) << 16) + colb +
+                                 (uint32_t)(gp * 32),
+                             r);
+            tmem_wait_ld();
+            if (c == 3) release();
+            const long long is = ib + 8 * hh;
+            const bool iok = F || (is >= wb_ && is < we_);
+            const float4 fi = wfi[hh];
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+              const int o = 8 * g;
+              const int gg = 2 * gp + g;
+              const long long j = sj0 + 8 * gg + 2 * (lane & 3);
+              const bool l0 = F || (iok && is < j && j < we_);
+              const bool l1 = F || (iok && is < j + 1 && j + 1 < we_);
+              if (!F && !(l0 || l1)) continue;
+              const fast2::Pop p = fast2::make(u2(r[o], r[o + 1]), u2(r[o + 4], r[o + 5]),
+                                               u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
+              win::window_pair2(p, u2(r[o], r[o + 1]), tab, fi, l0 ? wfj[2 * gg] : zero4,
+                                l1 ? wfj[2 * gg + 1] : zero4, l0, l1, ws2, np, nr2, nfour);
+            }
+          }
+        };
+        if (full) body(std::true_type{});
+        else body(std::false_type{});
+        // compensated (Neumaier) running sums of the lane's unit totals
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2) {
+          const float v = __fadd_rn(ws2[s2].x, ws2[s2].y);
+          const float sum = __fadd_rn(run[s2], v);
+          const float err = fabsf(run[s2]) >= fabsf(v) ? __fadd_rn(__fsub_rn(run[s2], sum), v)
+                                                       : __fadd_rn(__fsub_rn(v, sum), run[s2]);
+          comp[s2] = __fadd_rn(comp[s2], err);
+          run[s2] = sum;
+        }
+        run_np += np;
+        run_r2 += nr2;
+        run_four += nfour;
+        // bounded lane counts and compensated sums: flush every 4,096 units
+        if (++run_units == 4096) win_emit();
+        continue;
+      }
+
       bool waited = false;
       {
-        // the unit's 16 x 32 sub-tile: i in si0 + [0, 16), j in sj0 + [0, 32)
-        const long long sj0 = j0 + 32 * u;
-        const uint32_t colb = (uint32_t)(acc * 256 + u * 64);
         // classify: 0 one bin; 1 bin b0 below distance thr_mid, bin b0 + 1
         // from thr_mid below thr_hi, nothing from thr_hi; 2 general; 3 no
         // pair in a bin (the unit only releases its share of the buffer)
@@ -651,6 +952,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       if (!waited) break;  // the accumulator wait ran out (recorded above)
     }
+    if constexpr (MODE == kModeWindows)
+      if (!aborted) win_emit();
   }
 
   // ---------------- teardown ----------------
@@ -729,6 +1032,25 @@ __global__ void pos_to_int_kernel_w(const double* __restrict__ pos, long long n,
     const bool ok = (v == rint(v)) && fabs(v) < 1073741824.0;
     ipos[k] = ok ? (int)v : 0;
     if (!ok) atomicOr(bad, 1);
+  }
+}
+
+// 64 x 128 tiles of each window's upper triangle (list positions from
+// win_begin & ~7); bad ranges get none and set the status
+__global__ void wide_window_tiles_kernel(const long long* __restrict__ wb,
+                                         const long long* __restrict__ we, int n_win,
+                                         long long n_idx, long long* __restrict__ tiles,
+                                         int32_t* __restrict__ status) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_win; w += gridDim.x * blockDim.x) {
+    const long long lo = wb[w], hi = we[w];
+    long long T = 0;
+    if (lo < 0 || hi < lo || hi > n_idx) {
+      atomicCAS(status, 0, 3100);
+    } else if (hi > lo) {
+      const long long m = hi - (lo & ~7ll);
+      T = wtiles_before((m + kRowSnp - 1) / kRowSnp, (m + kColSnp - 1) / kColSnp);
+    }
+    tiles[w] = T;
   }
 }
 
@@ -832,7 +1154,7 @@ int pgld_tc_wide_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::Band
   if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: shared memory");
   prm.stages = stages;
   const size_t smem = (size_t)stages * kStage + fixed;
-  auto kern = band_wide_kernel;
+  auto kern = band_wide_kernel<pgld::kModeBinned>;
 #if PGLD_TCW_MAXNREG
   {
     // the register split needs the launch's total (384 x 168): a build that
@@ -853,4 +1175,193 @@ int pgld_tc_wide_binned(pgld_context* h, const pgld_hap_panel* panel, pgld::Band
   e = cudaGetLastError();
   if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_wide_kernel");
   return PGLD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// one population: per-pair outputs and per-window sums on 64 x 128 tiles
+// ---------------------------------------------------------------------------
+int pgld_tc_pack_rows(pgld_context* h, const uint32_t* planes, int W, long long n_snp,
+                      long long n_rows, const int32_t* idx, int k_pad, unsigned char* out,
+                      cudaStream_t st);
+int pgld_site_freqs(pgld_context* h, const uint32_t* planes, const uint32_t* valid, int W,
+                    long long n_snp, float4* site, cudaStream_t st);
+
+// shared memory, stages and the register check of a one-population launch
+template <int MODE>
+static int wide_one_pop_launch(pgld_context* h, pgld::tcw::Params& prm, const CUtensorMap& map_a,
+                               const CUtensorMap& map_b, cudaStream_t st, const char* what) {
+  using namespace pgld::tcw;
+  if (h->test_fault == PGLD_TEST_FAULT_NO_COPIES) {
+    prm.no_copies = 1;
+    prm.wait_cycles = 20000000ll;
+    h->test_fault = 0;
+  }
+  const size_t fixed = sizeof(pgld::tc::Ctrl) + (pgld::kMaxBins + 1) * 8 + (pgld::kMaxBins + 2) * 4 +
+                       (size_t)4 * (prm.nmax + 1) * sizeof(float) + 16 + 1024;
+  int max_smem = 0;
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStage);
+  if (h->tc_stages_cap > 0) stages = std::min(stages, h->tc_stages_cap);
+  if (stages < 2) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "%s: shared memory", what);
+  prm.stages = stages;
+  const size_t smem = (size_t)stages * kStage + fixed;
+  auto kern = band_wide_kernel<MODE>;
+#if PGLD_TCW_MAXNREG
+  {
+    cudaFuncAttributes fa;
+    cudaError_t e0 = cudaFuncGetAttributes(&fa, (const void*)kern);
+    if (e0 != cudaSuccess) return pgld_cuda_fail(h, e0, "band_wide attributes");
+    if (fa.numRegs != kRegLaunch)
+      return pgld_fail(h, PGLD_ERR_UNSUPPORTED, "band_wide_kernel built with %d registers; its "
+                       "register split needs %d", fa.numRegs, kRegLaunch);
+  }
+#endif
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, "band_wide smem attribute");
+  pgld_time_begin(h, st);
+  kern<<<(unsigned)h->n_sm, kThreads, smem, st>>>(map_a, map_b, prm);
+  pgld_time_end(h, st);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return pgld_cuda_fail(h, e, what);
+  return PGLD_OK;
+}
+
+// Per-pair outputs of one population (<= 2,048 haplotypes, no validity
+// plane) over the distance band: a's pair_off / counts / nvalid / stats as
+// for the square form; the band offsets are rebuilt in this call's workspace.
+int pgld_tc_wide_pairs(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArgs& a,
+                       cudaStream_t st) {
+  using namespace pgld::tcw;
+  int rc = get_encode(h);
+  if (rc) return rc;
+  const long long n = panel->n_snp;
+  const int W = panel->n_words[0];
+  const long long n_rb = (n + kRowSnp - 1) / kRowSnp;
+  const long long n_cb = (n + kColSnp - 1) / kColSnp;
+  const long long n_op = n_cb * kColSnp;
+  if (2 * n_op > 2147483647LL) return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core form: too many SNPs");
+  const int k0 = ((W * 32 + pgld::tc::kKChunk - 1) / pgld::tc::kKChunk) * pgld::tc::kKChunk;
+  const size_t op_bytes = (size_t)2 * n_op * k0;
+  const size_t sb = pgld::scan_scratch_bytes(std::max<long long>(n_rb, n));
+  auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+  const size_t off_items = 0, off_scan = al((n_rb + 1) * 8), off_op = off_scan + al(sb),
+               off_poff = off_op + al(op_bytes), total = off_poff + al((size_t)(n + 1) * 8);
+  void* ws = nullptr;
+  rc = pgld_workspace(h, total, &ws);
+  if (rc) return rc;
+  char* w = (char*)ws;
+  long long* items = (long long*)(w + off_items);
+  unsigned char* op = (unsigned char*)(w + off_op);
+  long long* poff = (long long*)(w + off_poff);
+  rc = pgld_band_offsets(h, a.pos, n, a.max_dist, poff, w + off_scan, sb, st);
+  if (rc) return rc;
+  {
+    const unsigned blocks = (unsigned)((2 * n_op + 7) / 8);
+    pack_wide_kernel<<<blocks, 256, 0, st>>>(panel->planes[0], W, panel->planes[0], 0, n, 2 * n_op,
+                                             k0, 0, (uint32_t*)op);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "pack_wide_kernel");
+  }
+  rc = pgld::band_schedule(h, a.pos, n, a.max_dist, items, w + off_scan, sb, st, kRowSnp, kColSnp);
+  if (rc) return rc;
+  CUtensorMap map_a, map_b;
+  rc = make_map(h, &map_a, op, 2 * n_op, k0, 128);
+  if (rc) return rc;
+  rc = make_map(h, &map_b, op, 2 * n_op, k0, 256);
+  if (rc) return rc;
+  Params prm{};
+  prm.kchunks = k0 / pgld::tc::kKChunk;
+  prm.n_snp = n;
+  prm.n_anchor = n;
+  prm.pos = a.pos;
+  prm.max_dist = a.max_dist;
+  prm.item_off = items;
+  prm.n_rb = n_rb;
+  prm.n_cb = n_cb;
+  prm.status = h->dev_status;
+  prm.nmax = 32 * W;
+  prm.wait_cycles = pgld::tc::kWaitCycles;
+  prm.pair_off = poff;
+  prm.counts = a.counts;
+  prm.nvalid = a.nvalid;
+  prm.stats = a.stats;
+  return wide_one_pop_launch<pgld::kModePairs>(h, prm, map_a, map_b, st, "band_wide_kernel (pairs)");
+}
+
+// Per-window sums of one population (<= 2,048 haplotypes, no validity plane):
+// the operand is built over the index list, so a window is a contiguous range
+// of operand rows; one launch over the tiles of every window.
+int pgld_tc_wide_windows(pgld_context* h, const pgld_hap_panel* panel, const int32_t* idx,
+                         long long n_idx, const long long* wb, const long long* we, int n_win,
+                         double* sums, unsigned long long* counts, cudaStream_t st) {
+  using namespace pgld::tcw;
+  int rc = get_encode(h);
+  if (rc) return rc;
+  const long long n = panel->n_snp;
+  const int W = panel->n_words[0];
+  const int k_pad = ((W * 32 + pgld::tc::kKChunk - 1) / pgld::tc::kKChunk) * pgld::tc::kKChunk;
+  // operand rows: list positions grouped by 8, then zero rows for the column
+  // blocks that reach past the last position (a tile's columns start at most
+  // 127 positions before its window's end)
+  const long long n_pk = (std::max<long long>(n_idx, 1) + 7) / 8 * 8;
+  const long long n_op = n_pk + kColSnp;
+  if (2 * n_op > 2147483647LL - 256)
+    return pgld_fail(h, PGLD_ERR_TOO_LARGE, "tensor-core windows: too many SNPs");
+  const size_t op_bytes = (size_t)2 * n_op * k_pad;
+  const size_t sb = pgld::scan_scratch_bytes(n_win);
+  auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+  const size_t off_tiles = 0, off_scan = al((size_t)(n_win + 1) * 8), off_op = off_scan + al(sb),
+               off_site = off_op + al(op_bytes),
+               total = off_site + al((size_t)std::max<long long>(n, 1) * 16);
+  void* ws = nullptr;
+  rc = pgld_workspace(h, total, &ws);
+  if (rc) return rc;
+  char* w = (char*)ws;
+  long long* tiles = (long long*)(w + off_tiles);
+  unsigned char* op = (unsigned char*)(w + off_op);
+  float4* site = (float4*)(w + off_site);
+  {
+    const unsigned gb = (unsigned)std::max<long long>(1, std::min<long long>((n_win + 255) / 256, h->n_sm * 4LL));
+    wide_window_tiles_kernel<<<gb, 256, 0, st>>>(wb, we, n_win, n_idx, tiles, h->dev_status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "wide_window_tiles_kernel");
+  }
+  rc = pgld::exclusive_scan_i64(h, tiles, n_win, w + off_scan, sb, st);
+  if (rc) return rc;
+  if (n > 0) {
+    rc = pgld_site_freqs(h, panel->planes[0], nullptr, W, n, site, st);
+    if (rc) return rc;
+  }
+  if (n_idx > 0) {
+    rc = pgld_tc_pack_rows(h, panel->planes[0], W, n, n_idx, idx, k_pad, op, st);
+    if (rc) return rc;
+  }
+  {
+    const size_t packed = n_idx > 0 ? (size_t)2 * n_pk * k_pad : 0;
+    cudaError_t e = cudaMemsetAsync(op + packed, 0, op_bytes - packed, st);
+    if (e != cudaSuccess) return pgld_cuda_fail(h, e, "memset");
+  }
+  CUtensorMap map_a, map_b;
+  rc = make_map(h, &map_a, op, 2 * n_op, k_pad, 128);
+  if (rc) return rc;
+  rc = make_map(h, &map_b, op, 2 * n_op, k_pad, 256);
+  if (rc) return rc;
+  Params prm{};
+  prm.kchunks = k_pad / pgld::tc::kKChunk;
+  prm.n_snp = n_idx;
+  prm.n_anchor = n_idx;
+  prm.status = h->dev_status;
+  prm.nmax = 32 * W;
+  prm.wait_cycles = pgld::tc::kWaitCycles;
+  prm.win_begin = wb;
+  prm.win_end = we;
+  prm.n_win = n_win;
+  prm.tile_off = tiles;
+  prm.idx = idx;
+  prm.site = site;
+  prm.n_panel = n;
+  prm.wsums = sums;
+  prm.wcnt = counts;
+  return wide_one_pop_launch<pgld::kModeWindows>(h, prm, map_a, map_b, st,
+                                                 "band_wide_kernel (windows)");
 }

@@ -59,14 +59,17 @@ __device__ __forceinline__ void window_pair(const fast::Pop& p, int n, float c1,
 }
 
 // window_pair for two pairs (i, j0) and (i, j1) at once on packed float2
-// features (the tensor-core window kernel): the same statistics, with the
+// features (the tensor-core window kernels): the same statistics, with the
 // naive-r^2 numerator c1 v_i v_j - n d_i d_j by Kahan's two-product
-// algorithm; live.x / live.y select the pairs that belong to the window
-__device__ __forceinline__ void window_pair2(const fast2::Pop& p, float2 c1, const fast::Recip& T,
+// algorithm; live.x / live.y select the pairs that belong to the window.
+// tab(n) gives (1/n, 1/(n(n-1)(n-2)(n-3))) of the reciprocal tables.
+template <class Tab>
+__device__ __forceinline__ void window_pair2(const fast2::Pop& p, float2 c1, Tab&& tab,
                                              float4 si, float4 sj0, float4 sj1, bool live0,
                                              bool live1, float2 (&acc)[6], int& n_pairs,
                                              int& n_r2, int& n_four) {
   using namespace fast2;
+  const float2 t0 = tab(p.n0), t1 = tab(p.n1);
   n_pairs += (live0 ? 1 : 0) + (live1 ? 1 : 0);
   const V rden = vmul(vmul(p.pA, p.qA), vmul(p.pB, p.qB));
   const V xx = vmul(p.x, p.x);
@@ -79,7 +82,7 @@ __device__ __forceinline__ void window_pair2(const fast2::Pop& p, float2 c1, con
   if (f0 || f1) {
     const V dd = dd_num(p), pi = pi2_num(p);
     const V dz = dz_num(p, vfma(p.dA, p.dB, p.e));
-    const V r4 = make_float2(f0 ? T.r4[p.n0] : 0.f, f1 ? T.r4[p.n1] : 0.f);
+    const V r4 = make_float2(f0 ? t0.y : 0.f, f1 ? t1.y : 0.f);
     acc[1] = vadd(acc[1], make_float2(f0 && pi.x != 0.f ? __fdividef(dd.x, pi.x) : 0.f,
                                       f1 && pi.y != 0.f ? __fdividef(dd.y, pi.y) : 0.f));
     acc[2] = vfma(dd, r4, acc[2]);
@@ -92,7 +95,7 @@ __device__ __forceinline__ void window_pair2(const fast2::Pop& p, float2 c1, con
     const V ns = p.ns;
     const V vv = make_float2(si.y * sj0.y, si.y * sj1.y), dd2 = make_float2(si.x * sj0.x, si.x * sj1.x);
     const V num = dot2(c1, vv, vneg(ns), dd2);
-    const V inv = make_float2(T.inv[p.n0], T.inv[p.n1]);
+    const V inv = make_float2(t0.x, t1.x);
     const V zz = make_float2(si.z * sj0.z, si.z * sj1.z);
     const V neg0 = make_float2(-(si.x * si.z) * (sj0.x * sj0.z), -(si.x * si.z) * (sj1.x * sj1.z));
     const V Dv = vmul(vmul(num, inv), zz);

@@ -249,13 +249,16 @@ def test_large_sample_statistics_are_exact():
     _close(got, ref, rtol=1e-15)
 
 
-def test_band_pairs_fp32_outputs():
+@pytest.mark.parametrize("layout", [1, 2])
+def test_band_pairs_fp32_outputs(layout, tc_layout):
+    # layout: 1 = 64 x 64 tiles, 2 = 64 x 128 tiles
     rng = np.random.default_rng(11)
     H, M = 2000, 600
     hap = copying_model(rng, H, M, 50, 5e-4, missing=0.02)
     pos = np.sort(rng.choice(200_000, M, replace=False)).astype(np.int64)
     pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
-    counts, nv, st = _ops.band_pairs(pk, _ops.positions_f64(pos), 20_000)
+    with tc_layout(layout):
+        counts, nv, st = _ops.band_pairs(pk, _ops.positions_f64(pos), 20_000)
     ii, jj = O.pairs_within_distance(pos, 20_000)
     rc, rnv = O.counts_for_pairs(hap, ii, jj)
     assert np.array_equal(np_(counts), rc) and np.array_equal(np_(nv), rnv)
@@ -322,6 +325,29 @@ def _block_copies(rng, n, M, F, block):
         s, e = b * block, min(M, (b + 1) * block)
         out[:, s:e] = f[pick[:, b], s:e]
     return out
+
+
+@pytest.mark.parametrize("H,M,D", [(33, 700, 3_000), (400, 1_300, 40_000), (2000, 900, 1e9),
+                                   (64, 129, 1e9), (96, 2, 1e9)])
+def test_band_pairs_layouts_agree(H, M, D, tc_layout):
+    # 64 x 64 tiles (eight epilogue warps) and 64 x 128 tiles (twelve) run the
+    # same per-pair arithmetic: equal outputs bit for bit, every band pair
+    # written once (including bands wider than the panel and ragged ends)
+    rng = np.random.default_rng(H + M)
+    hap = copying_model(rng, H, M, 12, 2e-3, missing=0.03)
+    pos = np.sort(rng.choice(100 * M, M, replace=False)).astype(np.int64)
+    pk = _ops.pack(torch.as_tensor(hap, device="cuda"))
+    pos_d = _ops.positions_f64(pos)
+    out = {}
+    for layout in (1, 2):
+        with tc_layout(layout):
+            c, nv, st = _ops.band_pairs(pk, pos_d, D, form="tc")
+        out[layout] = (np_(c), np_(nv), np_(st))
+    for a, b in zip(out[1], out[2]):
+        assert np.array_equal(a.view(np.int32), b.view(np.int32))
+    ii, jj = O.pairs_within_distance(pos, D)
+    rc, rnv = O.counts_for_pairs(hap, ii, jj)
+    assert np.array_equal(out[2][0], rc) and np.array_equal(out[2][1], rnv)
 
 
 def test_full_size_band_pairs():

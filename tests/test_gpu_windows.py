@@ -32,9 +32,16 @@ def copying_model(rng, H, M, F, switch, missing=0.0, flip=1e-3):
     return hap.astype(np.int8)
 
 
-@pytest.mark.parametrize("H,form", [(33, "plain"), (400, "plain"), (33, "tc"), (400, "tc"),
-                                    (2000, "tc")])
-def test_window_sums_match_oracle(H, form):
+@pytest.mark.parametrize("H,form,layout", [(33, "plain", 0), (400, "plain", 0), (33, "tc", 1),
+                                           (33, "tc", 2), (400, "tc", 1), (400, "tc", 2),
+                                           (2000, "tc", 1), (2000, "tc", 2)])
+def test_window_sums_match_oracle(H, form, layout, tc_layout):
+    # layout (tensor cores): 1 = 64 x 64 tiles, 2 = 64 x 128 tiles
+    with tc_layout(layout):
+        _window_sums_check(H, form)
+
+
+def _window_sums_check(H, form):
     rng = np.random.default_rng(H)
     M = 900
     hap = copying_model(rng, H, M, 12, 2e-3, missing=0.02)
