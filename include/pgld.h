@@ -468,13 +468,14 @@ int pgld_vcf_pack_gt(const char* text, int64_t len, int32_t n_samples, int64_t n
  * Measurement (no counterpart in the reference, which publishes no kernel
  * timings).
  * ---------------------------------------------------------------------- */
-/* Tensor-core configuration of h (the autotuner's knobs): layout of the
- * binned two-population form -- 0 automatic (the combined layout whenever
- * it applies), 1 tiles of 64 x 64 SNPs with one accumulator per population
- * (M = N = 128 MMAs), 2 tiles of 64 x 128 SNPs with both populations'
- * counts in one accumulator (M = 128, N = 256 MMAs; populations of at most
- * 2,016 haplotypes) -- and a cap on the pipeline stages of the tensor-core
- * kernels (0: as many as shared memory holds).  No counterpart in the
+/* Tensor-core configuration of h (the autotuner's knobs): tile layout -- 0
+ * automatic, 1 tiles of 64 x 64 SNPs (M = N = 128 MMAs; binned: one
+ * accumulator per population), 2 tiles of 64 x 128 SNPs (M = 128, N = 256
+ * MMAs; binned: both populations' counts in one accumulator, populations of
+ * at most 2,016 haplotypes).  Automatic: layout 2 for the binned
+ * two-population sums and the window sums, layout 1 for the per-pair
+ * outputs.  And a cap on the pipeline stages of the tensor-core kernels
+ * (0: as many as shared memory holds).  No counterpart in the
  * reference, whose chunk sizes come from free device memory
  * (ld_pipeline.py:16-49, _memutil.py:6-52). */
 int pgld_set_tc_config(pgld_handle h, int32_t layout, int32_t max_stages);

@@ -43,6 +43,13 @@ namespace tc {
 
 constexpr int kTileSnp = 64;
 constexpr int kEpiWarps = 8;
+// pairs mode: per epilogue warp two staging buffers of the counts and the
+// float32 statistics of one step (8 rows i x 16 columns j, rows padded to 17
+// entries of 16 bytes), written out by bulk copies of each row's band range
+constexpr int kStgRow = 17 * 16;
+constexpr int kStgArr = 8 * kStgRow;
+constexpr int kStgBuf = 2 * kStgArr;
+constexpr int kStgWarp = 2 * kStgBuf;
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kThreads = (4 + kEpiWarps) * 32;
 constexpr uint32_t kTmemCols = 512;
@@ -198,6 +205,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   T.r3 = tables + 2 * (a.nmax + 1);
   T.r4 = tables + 3 * (a.nmax + 1);
   const float4* T4 = reinterpret_cast<const float4*>(tables);
+  // pairs mode: the epilogue warps' staging buffers, after the tables
+  unsigned char* stg = reinterpret_cast<unsigned char*>(tables + 4 * (a.nmax + 1));
+  stg += (16 - (smem_u32(stg) & 15)) & 15;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_bins = a.n_bins;
@@ -375,6 +385,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     unsigned long long* my_cnt = kcnt + (size_t)e * n_bins;
     int t = 0;
     long long row_hint = 0;
+    int stg_step = 0;  // pairs mode: the warp's steps so far (staging buffer stg_step % 2)
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x, ++t) {
       const int acc = t & 1;
       const uint32_t aph = (uint32_t)((t >> 1) & 1);
@@ -535,9 +546,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         // binned mode), so a 16x256b TMEM load gives thread t all four counts
         // of the pairs (i, j) and (i, j + 1), i = i0 + 16 quarter + 8 hh + t/4,
         // j = j0 + 32 half + 8 g + 2 (t % 4); rows k = pair_off[i] + (j - i - 1)
-        // in the reference's order, two consecutive rows per thread
+        // in the reference's order.  A step's counts and statistics (8 rows i
+        // x 16 columns j) go through a shared-memory staging buffer: the lane
+        // of each row then writes the row's band range with one bulk copy per
+        // array (contiguous output rows, whole sectors); n goes out directly.
         const long long ib = i0 + 16 * quarter + (lane >> 2);
         const long long off0 = pf_off0, np0 = pf_np0, off1 = pf_off1, np1 = pf_np1;
+        unsigned char* wst = stg + (size_t)e * kStgWarp;
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
           const int hh = c & 1, gp = c >> 1;
@@ -553,6 +568,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           const long long is = ib + 8 * hh;
           const long long offh = hh ? off1 : off0, nph = hh ? np1 : np0;
+          // this step's buffer is free once the copies issued from it two
+          // steps ago have read it (one bulk group per row lane and step)
+          unsigned char* buf = wst + (size_t)(stg_step & 1) * kStgBuf;
+          bulk_wait_read<1>();
+          __syncwarp();
+          int4* cst = reinterpret_cast<int4*>(buf) + (lane >> 2) * 17;
+          float4* sst = reinterpret_cast<float4*>(buf + kStgArr) + (lane >> 2) * 17;
           auto u2 = [](uint32_t x, uint32_t y) {
             return make_float2(__uint_as_float(x), __uint_as_float(y));
           };
@@ -560,9 +582,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int g = 0; g < 2; ++g) {
             // the pairs (is, j) and (is, j + 1), two lanes of the packed epilogue
             const int o = 8 * g;
-            const long long j = j0 + 32 * half + 8 * (2 * gp + g) + 2 * (lane & 3);
-            // a pair's row comes from the band offsets themselves, so a pair
-            // is written exactly when the offsets list it
+            const int jj = 8 * g + 2 * (lane & 3);  // column in the step's 16
+            const long long j = j0 + 32 * half + 16 * gp + jj;
+            // a pair is written exactly when the band offsets list it
             const bool ok0 = is < j && j < a.n_snp && (j - is - 1) < nph;
             const bool ok1 = is < j + 1 && j + 1 < a.n_snp && (j - is) < nph;
             if (!ok0 && !ok1) continue;
@@ -573,17 +595,33 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (a.stats) fast2::pair_outputs(p, make_float2(T.r4[p.n0], T.r4[p.n1]), st);
 #pragma unroll
             for (int y = 0; y < 2; ++y) {
-              const bool oky = y ? ok1 : ok0;
               const int q = o + y;
-              st_cs_if(oky, reinterpret_cast<int4*>(a.counts) + (k + y),
-                       make_int4(fast::f2i_small(__uint_as_float(r[q])),
-                                 fast::f2i_small(__uint_as_float(r[q + 4])),
-                                 fast::f2i_small(__uint_as_float(r[q + 2])),
-                                 fast::f2i_small(__uint_as_float(r[q + 6]))));
-              if (a.nvalid) st_cs_if(oky, a.nvalid + (k + y), y ? p.n1 : p.n0);
-              if (a.stats) st_cs_if(oky, reinterpret_cast<float4*>(a.stats) + (k + y), st[y]);
+              cst[jj + y] = make_int4(fast::f2i_small(__uint_as_float(r[q])),
+                                      fast::f2i_small(__uint_as_float(r[q + 4])),
+                                      fast::f2i_small(__uint_as_float(r[q + 2])),
+                                      fast::f2i_small(__uint_as_float(r[q + 6])));
+              if (a.stats) sst[jj + y] = st[y];
+              if (a.nvalid) st_cs_if(y ? ok1 : ok0, a.nvalid + (k + y), y ? p.n1 : p.n0);
             }
           }
+          fence_proxy_async_smem();
+          __syncwarp();
+          if ((lane & 3) == 0) {
+            // the row's pairs in this step: columns jlo..jhi (j <= is + nph)
+            const long long jb = j0 + 32 * half + 16 * gp;
+            const long long jlo = jb > is + 1 ? jb : is + 1;
+            long long jhi = jb + 15 < a.n_snp - 1 ? jb + 15 : a.n_snp - 1;
+            if (is + nph < jhi) jhi = is + nph;
+            if (jlo <= jhi) {
+              const long long k0 = offh + (jlo - is - 1);
+              const uint32_t bytes = (uint32_t)(jhi - jlo + 1) * 16u;
+              const int q0 = (int)(jlo - jb);
+              bulk_store(reinterpret_cast<int4*>(a.counts) + k0, cst + q0, bytes);
+              if (a.stats) bulk_store(reinterpret_cast<float4*>(a.stats) + k0, sst + q0, bytes);
+            }
+            bulk_commit();
+          }
+          ++stg_step;
         }
         continue;
       }
@@ -772,6 +810,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         flush();
       }
     }
+    // pairs mode: every bulk copy of the warp has completed (its staging
+    // buffers stay valid until then)
+    if constexpr (MODE == kModePairs) bulk_wait_all();
   }
 
   // ---------------- teardown ----------------
@@ -1012,7 +1053,8 @@ static int tc_launch(pgld_context* h, const pgld_hap_panel* panel, pgld::BandArg
 
   const size_t fixed = sizeof(Ctrl) + (pgld::kMaxBins + 1) * 8 + (pgld::kMaxBins + 2) * 4 +
                        (size_t)kEpiWarps * a.n_bins * (S + 1) * 8 +
-                       (size_t)4 * (prm.nmax + 1) * sizeof(float) + 1024;
+                       (size_t)4 * (prm.nmax + 1) * sizeof(float) + 1024 +
+                       (mode == pgld::kModePairs ? (size_t)kEpiWarps * kStgWarp + 16 : 0);
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
   int stages = (int)std::min<long long>(8, ((long long)max_smem - (long long)fixed) / kStageBytes);

@@ -664,11 +664,21 @@ __global__ void __launch_bounds__(kThreads, 1)
               const long long j = sj0 + 8 * gg + 2 * (lane & 3);
               const bool l0 = F || (iok && is < j && j < we_);
               const bool l1 = F || (iok && is < j + 1 && j + 1 < we_);
-              if (!F && !(l0 || l1)) continue;
+              // a step without a live pair in any lane is skipped by the whole
+              // warp (the vote below needs every lane)
+              if (!F && !__any_sync(0xffffffffu, l0 || l1)) continue;
               const fast2::Pop p = fast2::make(u2(r[o], r[o + 1]), u2(r[o + 4], r[o + 5]),
                                                u2(r[o + 2], r[o + 3]), u2(r[o + 6], r[o + 7]));
-              win::window_pair2(p, u2(r[o], r[o + 1]), tab, fi, l0 ? wfj[2 * gg] : zero4,
-                                l1 ? wfj[2 * gg + 1] : zero4, l0, l1, ws2, np, nr2, nfour);
+              const float4 sj0 = l0 ? wfj[2 * gg] : zero4, sj1 = l1 ? wfj[2 * gg + 1] : zero4;
+              // both SNPs of each live pair with the same valid haplotypes
+              // (n = nv_i = nv_j), for every lane: the shorter form
+              const bool same = (!l0 || (p.ns.x == fi.y && p.ns.x == sj0.y)) &&
+                                (!l1 || (p.ns.y == fi.y && p.ns.y == sj1.y));
+              if (__all_sync(0xffffffffu, same))
+                win::window_pair2_same(p, tab, fi, sj0, sj1, l0, l1, ws2, np, nr2, nfour);
+              else
+                win::window_pair2(p, u2(r[o], r[o + 1]), tab, fi, sj0, sj1, l0, l1, ws2, np, nr2,
+                                  nfour);
             }
           }
         };

@@ -16,14 +16,16 @@
 namespace pgld {
 namespace win {
 
-// per-site (dac, nv, 1 / nv, 1 / (p (1 - p))) with p = dac / nv; the last
-// entry is 0 where the site is monomorphic among its valid haplotypes or has
-// none
+// per-site (dac, nv, 1 / nv, u) with u = 1 / (dac (nv - dac)); u is 0 where
+// the site is monomorphic among its valid haplotypes or has none.  The naive
+// r^2 of a pair is D^2 / (p_i q_i p_j q_j) with D = c1 / n - p_i p_j and
+// p = dac / nv, i.e. E^2 u_i u_j with E = D nv_i nv_j = (c1 nv_i nv_j -
+// n dac_i dac_j) / n (or -dac_i dac_j where n = 0)
 __device__ __forceinline__ float4 site_freq(int dac, int nv) {
   if (nv <= 0) return make_float4(0.f, 0.f, 0.f, 0.f);
   const float d = (float)dac, v = (float)nv;
   const float pq_num = d * (v - d);  // exact: below 2^24 for nv <= 4096
-  return make_float4(d, v, 1.0f / v, pq_num > 0.f ? (v * v) / pq_num : 0.f);
+  return make_float4(d, v, 1.0f / v, pq_num > 0.f ? 1.0f / pq_num : 0.f);
 }
 
 // accumulate one pair: acc = r^2, sigma_D^2, DD, Dz, pi2, naive r^2
@@ -44,17 +46,17 @@ __device__ __forceinline__ void window_pair(const fast::Pop& p, int n, float c1,
     acc[4] += pi * r4n;
   }
   if (si.w > 0.f && sj.w > 0.f) {
-    // D = c1 / n - p_i p_j from the exact integer c1 v_i v_j - n d_i d_j, so
-    // that the cancellation costs nothing (p_AB = 0 where n = 0)
-    float D;
+    // E = D v_i v_j from the exact integer c1 v_i v_j - n d_i d_j, so that
+    // the cancellation costs nothing (p_AB = 0 where n = 0)
+    float E;
     if (n > 0) {
       fast::X2 num = fast::x2_prod(c1, si.y * sj.y);
       fast::x2_add_prod(num, -(float)n, si.x * sj.x);
-      D = fast::x2_value(num) * inv_n * si.z * sj.z;
+      E = fast::x2_value(num) * inv_n;
     } else {
-      D = -(si.x * si.z) * (sj.x * sj.z);
+      E = -(si.x * sj.x);
     }
-    acc[5] += (D * D) * (si.w * sj.w);
+    acc[5] += (E * E) * (si.w * sj.w);
   }
 }
 
@@ -91,17 +93,47 @@ __device__ __forceinline__ void window_pair2(const fast2::Pop& p, float2 c1, Tab
   }
   const bool s0 = live0 && si.w > 0.f && sj0.w > 0.f, s1 = live1 && si.w > 0.f && sj1.w > 0.f;
   if (s0 || s1) {
-    // D = c1 / n - p_i p_j from the integer c1 v_i v_j - n d_i d_j
+    // E = D v_i v_j from the integer c1 v_i v_j - n d_i d_j
     const V ns = p.ns;
     const V vv = make_float2(si.y * sj0.y, si.y * sj1.y), dd2 = make_float2(si.x * sj0.x, si.x * sj1.x);
     const V num = dot2(c1, vv, vneg(ns), dd2);
-    const V inv = make_float2(t0.x, t1.x);
-    const V zz = make_float2(si.z * sj0.z, si.z * sj1.z);
-    const V neg0 = make_float2(-(si.x * si.z) * (sj0.x * sj0.z), -(si.x * si.z) * (sj1.x * sj1.z));
-    const V Dv = vmul(vmul(num, inv), zz);
-    const float D0 = p.n0 > 0 ? Dv.x : neg0.x, D1 = p.n1 > 0 ? Dv.y : neg0.y;
+    const V Ev = vmul(num, make_float2(t0.x, t1.x));
+    const float E0 = p.n0 > 0 ? Ev.x : -dd2.x, E1 = p.n1 > 0 ? Ev.y : -dd2.y;
     const V ww = make_float2(s0 ? si.w * sj0.w : 0.f, s1 ? si.w * sj1.w : 0.f);
-    acc[5] = vfma(vmul(make_float2(D0, D1), make_float2(D0, D1)), ww, acc[5]);
+    acc[5] = vfma(vmul(make_float2(E0, E1), make_float2(E0, E1)), ww, acc[5]);
+  }
+}
+
+// window_pair2 for pairs whose two SNPs have the same valid haplotypes (the
+// pair's n equals nv of both sites: every pair of a panel without missing
+// data).  Then p_A, q_A, p_B, q_B are the sites' own counts, r^2 =
+// x^2 / (p_A q_A p_B q_B) = x^2 u_i u_j, and the naive r^2 equals it
+// (E = x), so one product serves both; DD, Dz, pi2 and sigma_D^2 as above.
+template <class Tab>
+__device__ __forceinline__ void window_pair2_same(const fast2::Pop& p, Tab&& tab, float4 si,
+                                                  float4 sj0, float4 sj1, bool live0, bool live1,
+                                                  float2 (&acc)[6], int& n_pairs, int& n_r2,
+                                                  int& n_four) {
+  using namespace fast2;
+  n_pairs += (live0 ? 1 : 0) + (live1 ? 1 : 0);
+  const V uu = vmul(vs(si.w), make_float2(sj0.w, sj1.w));
+  const bool r0 = live0 && uu.x > 0.f, r1 = live1 && uu.y > 0.f;
+  n_r2 += (r0 ? 1 : 0) + (r1 ? 1 : 0);
+  const V r2 = vmul(vmul(p.x, p.x), make_float2(live0 ? uu.x : 0.f, live1 ? uu.y : 0.f));
+  acc[0] = vadd(acc[0], r2);
+  acc[5] = vadd(acc[5], r2);
+  const bool f0 = live0 && p.n0 >= 4, f1 = live1 && p.n1 >= 4;
+  n_four += (f0 ? 1 : 0) + (f1 ? 1 : 0);
+  if (f0 || f1) {
+    const float2 t0 = tab(p.n0), t1 = tab(p.n1);
+    const V dd = dd_num(p), pi = pi2_num(p);
+    const V dz = dz_num(p, vfma(p.dA, p.dB, p.e));
+    const V r4 = make_float2(f0 ? t0.y : 0.f, f1 ? t1.y : 0.f);
+    acc[1] = vadd(acc[1], make_float2(f0 && pi.x != 0.f ? __fdividef(dd.x, pi.x) : 0.f,
+                                      f1 && pi.y != 0.f ? __fdividef(dd.y, pi.y) : 0.f));
+    acc[2] = vfma(dd, r4, acc[2]);
+    acc[3] = vfma(dz, r4, acc[3]);
+    acc[4] = vfma(pi, r4, acc[4]);
   }
 }
 
@@ -124,15 +156,15 @@ __device__ __forceinline__ float pair_stat(int stat, const fast::Pop& p, int n, 
     return fast::pi2_num(p) * r4n;
   }
   if (!(si.w > 0.f && sj.w > 0.f)) return 0.f;
-  float D;
+  float E;
   if (n > 0) {
     fast::X2 num = fast::x2_prod(c1, si.y * sj.y);
     fast::x2_add_prod(num, -(float)n, si.x * sj.x);
-    D = fast::x2_value(num) * inv_n * si.z * sj.z;
+    E = fast::x2_value(num) * inv_n;
   } else {
-    D = -(si.x * si.z) * (sj.x * sj.z);
+    E = -(si.x * sj.x);
   }
-  return (D * D) * (si.w * sj.w);
+  return (E * E) * (si.w * sj.w);
 }
 
 }  // namespace win
