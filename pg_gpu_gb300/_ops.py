@@ -73,7 +73,14 @@ def _check_rows(rows, n_total):
     if isinstance(rows, torch.Tensor) and rows.is_cuda:
         rows_t = L.as_device(rows, np.int32)
         if rows_t.numel():
-            lo, hi = (int(v) for v in torch.aminmax(rows_t))
+            # a device tensor passed again unmodified (same version counter)
+            # keeps the range its last check found: no device read per call
+            seen = getattr(rows_t, "_pgld_range", None)
+            if seen is not None and seen[0] == rows_t._version:
+                lo, hi = seen[1], seen[2]
+            else:
+                lo, hi = (int(v) for v in torch.aminmax(rows_t))
+                rows_t._pgld_range = (rows_t._version, lo, hi)
             if lo < 0 or hi >= n_total:
                 raise IndexError("population row index out of range")
         return rows_t

@@ -657,6 +657,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             const long long is = ib + 8 * hh;
             const bool iok = F || (is >= wb_ && is < we_);
             const float4 fi = wfi[hh];
+            // the shorter form's n is the row SNP's nv: its r4 and n >= 4 once
+            const int nvi = fast::f2i_small(fi.y);
+            const float r4i = T4[nvi].w;
+            const bool four_i = nvi >= 4;
 #pragma unroll
             for (int g = 0; g < 2; ++g) {
               const int o = 8 * g;
@@ -675,7 +679,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               const bool same = (!l0 || (p.ns.x == fi.y && p.ns.x == sj0.y)) &&
                                 (!l1 || (p.ns.y == fi.y && p.ns.y == sj1.y));
               if (__all_sync(0xffffffffu, same))
-                win::window_pair2_same(p, tab, fi, sj0, sj1, l0, l1, ws2, np, nr2, nfour);
+                win::window_pair2_same(p, four_i, r4i, fi, sj0, sj1, l0, l1, ws2, np, nr2, nfour);
               else
                 win::window_pair2(p, u2(r[o], r[o + 1]), tab, fi, sj0, sj1, l0, l1, ws2, np, nr2,
                                   nfour);

@@ -109,11 +109,12 @@ __device__ __forceinline__ void window_pair2(const fast2::Pop& p, float2 c1, Tab
 // data).  Then p_A, q_A, p_B, q_B are the sites' own counts, r^2 =
 // x^2 / (p_A q_A p_B q_B) = x^2 u_i u_j, and the naive r^2 equals it
 // (E = x), so one product serves both; DD, Dz, pi2 and sigma_D^2 as above.
-template <class Tab>
-__device__ __forceinline__ void window_pair2_same(const fast2::Pop& p, Tab&& tab, float4 si,
-                                                  float4 sj0, float4 sj1, bool live0, bool live1,
-                                                  float2 (&acc)[6], int& n_pairs, int& n_r2,
-                                                  int& n_four) {
+// n is the row SNP's nv for both pairs: four = (nv_i >= 4) and r4 =
+// 1/(n(n-1)(n-2)(n-3)) come from the caller, once per row.
+__device__ __forceinline__ void window_pair2_same(const fast2::Pop& p, bool four, float r4n,
+                                                  float4 si, float4 sj0, float4 sj1, bool live0,
+                                                  bool live1, float2 (&acc)[6], int& n_pairs,
+                                                  int& n_r2, int& n_four) {
   using namespace fast2;
   n_pairs += (live0 ? 1 : 0) + (live1 ? 1 : 0);
   const V uu = vmul(vs(si.w), make_float2(sj0.w, sj1.w));
@@ -122,13 +123,12 @@ __device__ __forceinline__ void window_pair2_same(const fast2::Pop& p, Tab&& tab
   const V r2 = vmul(vmul(p.x, p.x), make_float2(live0 ? uu.x : 0.f, live1 ? uu.y : 0.f));
   acc[0] = vadd(acc[0], r2);
   acc[5] = vadd(acc[5], r2);
-  const bool f0 = live0 && p.n0 >= 4, f1 = live1 && p.n1 >= 4;
+  const bool f0 = live0 && four, f1 = live1 && four;
   n_four += (f0 ? 1 : 0) + (f1 ? 1 : 0);
   if (f0 || f1) {
-    const float2 t0 = tab(p.n0), t1 = tab(p.n1);
     const V dd = dd_num(p), pi = pi2_num(p);
     const V dz = dz_num(p, vfma(p.dA, p.dB, p.e));
-    const V r4 = make_float2(f0 ? t0.y : 0.f, f1 ? t1.y : 0.f);
+    const V r4 = make_float2(f0 ? r4n : 0.f, f1 ? r4n : 0.f);
     acc[1] = vadd(acc[1], make_float2(f0 && pi.x != 0.f ? __fdividef(dd.x, pi.x) : 0.f,
                                       f1 && pi.y != 0.f ? __fdividef(dd.y, pi.y) : 0.f));
     acc[2] = vfma(dd, r4, acc[2]);

@@ -313,6 +313,24 @@ def test_edge_cases_and_errors():
         _ops.binned_sums([pk], _ops.positions_f64([1.0]), np.linspace(0, 1, 200))
 
 
+def test_device_rows_checked_again_after_a_change():
+    # the range of a device row tensor is read once and kept with the tensor;
+    # an in-place change (a new version) is checked again before packing
+    hap = torch.zeros((8, 5), dtype=torch.int8, device="cuda")
+    rows = torch.arange(4, dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        pk = _ops.pack(hap, rows)
+        assert pk.n_rows == 4
+    rows[2] = 8
+    with pytest.raises(IndexError):
+        _ops.pack(hap, rows)
+    rows[2] = -1
+    with pytest.raises(IndexError):
+        _ops.pack(hap, rows)
+    rows[2] = 7
+    assert _ops.pack(hap, rows).n_rows == 4
+
+
 def _block_copies(rng, n, M, F, block):
     """n haplotypes copying one of F founders per block of SNPs (a coarse
     copying model that generates full-size panels quickly)."""
