@@ -253,6 +253,22 @@ def band_offsets(pos_d, max_dist):
     return off, int(tot.value)
 
 
+def band_pair_count(pos_d, max_dist):
+    """Pairs within max_dist of sorted device positions.  The count is kept
+    with the positions tensor (keyed by its version counter and max_dist), so
+    a call repeated on unchanged positions reads nothing from the device."""
+    key = float(max_dist)
+    cache = getattr(pos_d, "_pgld_npairs", None)
+    if cache is not None and cache[0] == pos_d._version and key in cache[1]:
+        return cache[1][key]
+    _, n = band_offsets(pos_d, max_dist)
+    if cache is None or cache[0] != pos_d._version:
+        cache = (pos_d._version, {})
+        pos_d._pgld_npairs = cache
+    cache[1][key] = n
+    return n
+
+
 def pairs_range(pos_d, max_dist, i_begin, i_end, n_pairs):
     torch = _torch()
     ii = torch.empty(n_pairs, dtype=torch.int32, device=pos_d.device)
@@ -280,7 +296,7 @@ def band_pairs(pk, pos_d, max_dist, with_stats=True, form="auto", _tuning=False)
         from . import autotune
         autotune.apply("pairs", [pk.n_words])
     torch = _torch()
-    _, n = band_offsets(pos_d, max_dist)
+    n = band_pair_count(pos_d, max_dist)
     dev = pos_d.device
     counts = torch.empty((n, 4), dtype=torch.int32, device=dev)
     nv = torch.empty(n, dtype=torch.int32, device=dev)
@@ -589,7 +605,7 @@ def geno_band_pairs(pk, pos_d, max_dist, with_counts=True, with_stats=True,
             raise ValueError(f"unknown column {c!r}")
         mask |= 1 << GENO_BAND_COLUMNS.index(c)
     torch = _torch()
-    _, n = band_offsets(pos_d, max_dist)
+    n = band_pair_count(pos_d, max_dist)
     dev = pos_d.device
     counts = torch.empty((n, 9), dtype=torch.int32, device=dev) if with_counts else None
     nv = torch.empty(n, dtype=torch.int32, device=dev)

@@ -331,6 +331,18 @@ def test_device_rows_checked_again_after_a_change():
     assert _ops.pack(hap, rows).n_rows == 4
 
 
+def test_band_pair_count_follows_position_changes():
+    # the pair count kept with a positions tensor is read again after an
+    # in-place change of the positions, and per distance
+    pos_d = _ops.positions_f64(np.arange(0, 1000, 10, dtype=np.float64))
+    assert _ops.band_pair_count(pos_d, 25) == 99 + 98
+    assert _ops.band_pair_count(pos_d, 25) == 99 + 98
+    assert _ops.band_pair_count(pos_d, 5) == 0
+    pos_d.mul_(0.5)  # spacing 5
+    assert _ops.band_pair_count(pos_d, 5) == 99
+    assert _ops.band_pair_count(pos_d, 25) == 99 + 98 + 97 + 96 + 95
+
+
 def _block_copies(rng, n, M, F, block):
     """n haplotypes copying one of F founders per block of SNPs (a coarse
     copying model that generates full-size panels quickly)."""
