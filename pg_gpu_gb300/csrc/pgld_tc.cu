@@ -401,8 +401,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int dmin = a.ipos[sj0] - a.ipos[si0 + 15];
         const int dmax = a.ipos[sj0 + 31] - a.ipos[si0];
         if (dmax <= maxd_int) {
-          const int blo = bin_of_int(thr, n_bins, dmin);
-          const int bhi = bin_of_int(thr, n_bins, dmax);
+          // (dmin, dmax are the same in every lane: one vote per lookup)
+          const int blo = bin_of_int_warp(thr, n_bins, dmin, lane);
+          const int bhi = bin_of_int_warp(thr, n_bins, dmax, lane);
           if (blo >= 0 && bhi == blo) {
             mode = 0;
             b0 = blo;

@@ -22,6 +22,16 @@ __device__ __forceinline__ int bin_of_int(const int* thr, int n_bins, int d) {
   }
   return lo;
 }
+// bin_of_int of a distance d that every lane of the warp passes alike: lane l
+// compares d with thresholds l and 32 + l, and the bin is the number of
+// thresholds at or below d, less one (n_bins <= 64)
+__device__ __forceinline__ int bin_of_int_warp(const int* thr, int n_bins, int d, int lane) {
+  const bool a = lane <= n_bins && thr[lane] <= d;
+  const bool b = 32 + lane <= n_bins && thr[32 + lane] <= d;
+  int c = __popc(__ballot_sync(0xffffffffu, a)) + __popc(__ballot_sync(0xffffffffu, b));
+  if (n_bins >= 64 && thr[64] <= d) ++c;
+  return (c == 0 || c > n_bins) ? -1 : c - 1;
+}
 __device__ __forceinline__ int bin_of_f64(const double* sb, int n_bins, double d) {
   if (!(d >= sb[0]) || !(d < sb[n_bins])) return -1;
   int lo = 0, hi = n_bins;

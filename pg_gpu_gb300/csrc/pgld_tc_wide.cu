@@ -721,8 +721,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (dmax < thr[0] || dmin > top) {
               mode = 3;
             } else {
-              const int blo = bin_of_int(thr, n_bins, dmin);
-              const int bhi = bin_of_int(thr, n_bins, min(dmax, top));
+              // (dmin, dmax are the same in every lane: one vote per lookup)
+              const int blo = bin_of_int_warp(thr, n_bins, dmin, lane);
+              const int bhi = bin_of_int_warp(thr, n_bins, min(dmax, top), lane);
               if (blo >= 0 && bhi == blo && dmax <= top) {
                 mode = 0;
                 b0 = blo;
