@@ -178,11 +178,16 @@ __device__ __forceinline__ WideTile window_tile(const Params& a, long long item,
   const long long base = a.win_begin[lo] & ~7ll, m = a.win_end[lo] - base;
   const long long R = (m + kRowSnp - 1) / kRowSnp, C = (m + kColSnp - 1) / kColSnp;
   const long long t = item - a.tile_off[lo];
-  long long rlo = 0, rhi = R;
-  while (rhi - rlo > 1) {
-    const long long mid = (rlo + rhi) >> 1;
-    if (wtiles_before(mid, C) <= t) rlo = mid; else rhi = mid;
-  }
+  // the row block: the largest b < R with wtiles_before(b, C) <= t.  For even
+  // b, wtiles_before = b C - b^2 / 4 + b / 2, whose root in b, (2C + 1) -
+  // sqrt((2C + 1)^2 - 4 t), starts the search; the steps below make it exact
+  // (wtiles_before rises by C - floor(b / 2) >= 1 per row block)
+  const long long c2 = 2 * C + 1;
+  const float disc = (float)(c2 * c2 - 4 * t);
+  long long rlo = (long long)((float)c2 - sqrtf(disc > 0.f ? disc : 0.f));
+  rlo = rlo < 0 ? 0 : (rlo > R - 1 ? R - 1 : rlo);
+  while (rlo > 0 && wtiles_before(rlo, C) > t) --rlo;
+  while (rlo + 1 < R && wtiles_before(rlo + 1, C) <= t) ++rlo;
   WideTile r;
   r.i0 = base + rlo * kRowSnp;
   r.j0 = base + ((rlo >> 1) + (t - wtiles_before(rlo, C))) * kColSnp;
