@@ -90,7 +90,7 @@ struct Params {
   int n_win;
   const long long* tile_off;   // [n_win + 1] prefix of 64-SNP tiles per window
   const int32_t* idx;          // list position -> SNP (NULL: identity)
-  const float4* site;          // per-SNP (dac, nv, 1 / nv, 1 / pq) of the naive r^2
+  const float4* site;          // per-SNP (dac, nv, 1 / nv, 1 / (dac (nv - dac))) of the naive r^2
   long long n_panel;           // SNPs of the panel (bound of idx values)
   double* wsums;               // [n_win][6]
   unsigned long long* wcnt;    // [n_win][3]

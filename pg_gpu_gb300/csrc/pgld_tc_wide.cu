@@ -138,7 +138,7 @@ struct Params {
   int n_win;
   const long long* tile_off;   // [n_win + 1] prefix of the windows' tile counts
   const int32_t* idx;          // list position -> SNP (NULL: identity)
-  const float4* site;          // per-SNP (dac, nv, 1 / nv, 1 / pq) of the naive r^2
+  const float4* site;          // per-SNP (dac, nv, 1 / nv, 1 / (dac (nv - dac))) of the naive r^2
   long long n_panel;           // SNPs of the panel (bound of idx values)
   double* wsums;               // [n_win][6]
   unsigned long long* wcnt;    // [n_win][3]
@@ -159,7 +159,8 @@ struct WideTile {
 };
 
 // windows mode: the tile of an item, the window found by stepping forward
-// from the previous item's window (hint), then the row block by bisection
+// from the previous item's window (hint), then the row block from the root of
+// the window's tile count
 __device__ __forceinline__ WideTile window_tile(const Params& a, long long item, long long& hint) {
   int lo = (int)hint;
   int steps = 0;

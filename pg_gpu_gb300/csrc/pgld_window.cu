@@ -43,7 +43,7 @@ struct Args {
   const i64* win_end;
   int n_win;
   const i64* tile_off;     // [n_win + 1] prefix of tiles per window
-  const float4* site;      // per-SNP (dac, nv, 1 / nv, 1 / pq) of site_freq
+  const float4* site;      // per-SNP (dac, nv, 1 / nv, 1 / (dac (nv - dac))) of site_freq
   int nmax;                // largest valid n (reciprocal tables 0..nmax)
   double* sums;            // [n_win][kCols]
   unsigned long long* cnt; // [n_win][kCnts]
