@@ -284,3 +284,57 @@ def test_mu_ld_matches_reference(golden):
                                                                      abs=1e-15)
         k += 1
     assert k >= 7
+
+
+def test_naive_r2_equals_r2_where_valid_sets_agree():
+    # the identity the tensor-core window kernel uses for pairs whose two SNPs
+    # have the same valid haplotypes (every pair of a panel without missing
+    # data): the naive r^2 from per-site frequencies equals the pairwise r^2,
+    # x^2 / (p_A q_A p_B q_B) = x^2 u_i u_j with u = 1 / (dac (nv - dac));
+    # with missing data the two differ
+    rng = np.random.default_rng(41)
+    H, M = 64, 300
+    hap = (rng.random((H, M)) < rng.beta(0.3, 0.3, M)).astype(np.int8)
+    idx = np.arange(M)
+    b, e = np.array([0, 17, 100]), np.array([M, 90, 300])
+    sums, cnt = O.window_sums(hap, idx, b, e)
+    np.testing.assert_allclose(sums[:, 5], sums[:, 0], rtol=1e-12)
+    assert np.array_equal(cnt[:, 0], cnt[:, 2])  # n = H >= 4 for every pair
+    hap[rng.random(hap.shape) < 0.05] = -1
+    sums2, _ = O.window_sums(hap, idx, b, e)
+    assert np.all(np.abs(sums2[:, 5] - sums2[:, 0]) > 1e-9 * np.abs(sums2[:, 0]))
+
+
+def test_bin_vote_equals_bisection():
+    # the warp-vote bin of a distance (thresholds at or below it, less one:
+    # the tensor-core kernels' unit classification) against a bisection over
+    # the same right-open integer thresholds (ceil of the bin edges, as the
+    # reference's np.digitize bins integer distances), with equal thresholds
+    # (bin edges closer than 1 bp) and the range ends
+    rng = np.random.default_rng(5)
+
+    def bisect(thr, d):
+        n = len(thr) - 1
+        if d < thr[0] or d >= thr[n]:
+            return -1
+        lo, hi = 0, n
+        while hi - lo > 1:
+            mid = (lo + hi) // 2
+            if thr[mid] <= d:
+                lo = mid
+            else:
+                hi = mid
+        return lo
+
+    def vote(thr, d):
+        n = len(thr) - 1
+        c = int(np.sum(thr[: n + 1] <= d))
+        return -1 if c == 0 or c > n else c - 1
+
+    for n_bins in (1, 2, 20, 31, 32, 33, 63, 64):
+        edges = np.sort(rng.uniform(0, 5_000, n_bins + 1))
+        edges[n_bins // 2] = edges[max(0, n_bins // 2 - 1)] + 0.3  # two edges within 1 bp
+        edges = np.sort(edges)
+        thr = np.ceil(edges).astype(np.int64)
+        for d in list(rng.integers(-10, 5_010, 400)) + list(thr) + list(thr - 1):
+            assert vote(thr, int(d)) == bisect(thr, int(d)), (n_bins, d)
