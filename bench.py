@@ -485,13 +485,14 @@ def run_gpu(args, pool, cores):
         "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "api": "HaplotypeMatrix(host int8).compute_ld_statistics_gpu_two_pops(raw=True)"},
-        # per step: one pack per population, then the binned call: (tc: one operand
-        # expansion per population) + tile counts + 3 scan launches + the band kernel
-        # per step: one pack per population, then the binned call: tile counts, 3 scan
-        # launches and the band kernel (tc: also one operand expansion per
-        # population and the integer-position copy)
-        "gpu_launches": args.steps * (cfg["pops"] * (2 if args.form == "tc" else 1) +
-                                      (6 if args.form == "tc" else 5)),
+        # per step: one pack per population, then the binned call: tile counts,
+        # 3 scan launches and the band kernel; tc: also the integer-position
+        # copy and the operand expansion -- one launch for both populations in
+        # the combined 64 x 128 layout, one per population in the 64 x 64 one
+        "gpu_launches": args.steps * (cfg["pops"] + 5 + (
+            0 if args.form != "tc" else
+            1 + (1 if (cfg["pops"] == 2 and (tuned is None or tuned["choice"][0] != 1))
+                 else cfg["pops"]))),
         "call_ms": float(np.mean(call_ms)),
         "kernel_ms": k_s * 1e3,
         "roofline": roof,
